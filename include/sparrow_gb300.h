@@ -1,0 +1,199 @@
+/*
+ * sparrow_gb300.h - C ABI of the GB300 (sm_103a) directional fast-radiosity
+ * library (libsparrow_gb300.so).
+ *
+ * The reference (sparrowpy 1.0.1) is pure Python + numba and has no foreign
+ * function interface; each entry point below replaces one of its numba or
+ * numpy routines, named in the comment as file:line inside the sparrowpy
+ * source tree.  The Python class sparrowpy_gb300.DirectionalRadiosityFast
+ * binds these symbols with ctypes; INTEGRATION.md shows the binding.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless stated otherwise.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *  - Work is enqueued on `stream`; functions return before it finishes,
+ *    except where a comment says the call synchronises.
+ *  - Return value: SP_OK (0) or a negative sp_status.  No exception, abort or
+ *    device trap crosses the ABI.
+ *  - Scratch memory is always caller-provided (`ws`, `ws_bytes`); the
+ *    matching *_workspace() function gives the size.  The library itself
+ *    calls no cudaMalloc.
+ *  - Arrays are C-contiguous, row-major, with the reference's shapes.
+ */
+#ifndef SPARROW_GB300_H
+#define SPARROW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SP_OK = 0,
+    SP_ERR_ARG = -1,       /* invalid size, null pointer, unsupported shape */
+    SP_ERR_CUDA = -2,      /* a CUDA launch or copy failed */
+    SP_ERR_WORKSPACE = -3, /* ws_bytes smaller than the *_workspace() size */
+    SP_ERR_RANGE = -4,     /* a delay falls outside the histogram (reference: IndexError) */
+    SP_ERR_TIMEOUT = -5,   /* a bounded device wait gave up */
+    SP_ERR_UNSUPPORTED = -6
+} sp_status;
+
+enum { SP_F32 = 0, SP_F64 = 1 };
+enum { SP_EXCHANGE_DENSE = 0, SP_EXCHANGE_STRUCTURED = 1 };
+
+/* Library version string (static storage). */
+const char* sp_version(void);
+
+/* ---------------------------------------------------------------- geometry */
+
+/* Patch centres (vertex mean) and areas (fan triangulation).
+ * Replaces geometry.py:412-413 `_calculate_center` and :420-448
+ * `_calculate_area`.  pts (n, nv, 3) -> centers (n, 3), areas (n). */
+int sp_patch_geometry(int n, int nv, const double* pts, double* centers, double* areas, void* stream);
+
+/* Patch-to-patch visibility, upper triangle (i < j) of vis (n, n) as 0/1.
+ * Replaces geometry.py:750-797 `_check_patch2patch_visibility` (predicate
+ * geometry.py:841-909 `_basic_visibility`); blockers are all n patches. */
+size_t sp_patch_visibility_workspace(int n);
+int sp_patch_visibility(int n, int nv, const double* centers, const double* normals, const double* pts,
+                        uint8_t* vis, void* ws, size_t ws_bytes, void* stream);
+
+/* Point-to-patch visibility; blockers are n_surf surfaces (walls).
+ * Replaces geometry.py:799-839 `_check_point2patch_visibility`.
+ * point (3) -> out (n) 0/1. */
+size_t sp_point_visibility_workspace(int n_surf);
+int sp_point_visibility(const double* point, int n, const double* centers, int n_surf, int nv,
+                        const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws, size_t ws_bytes,
+                        void* stream);
+
+/* Row-major list of visible pairs (i < j).  Replaces RadiosityFast.py:377-387.
+ * row_counts (n) and row_offset (n+1, int64) are outputs; pairs (n_vis, 2)
+ * must hold n*(n-1)/2 entries; pair_index (n, n) (optional) receives the
+ * pair number of (i, j) for visible i < j (other entries untouched). */
+int sp_visible_pairs(int n, const uint8_t* vis, int32_t* row_counts, int64_t* row_offset, int32_t* pairs,
+                     int32_t* pair_index, void* stream);
+
+/* Destination-major list of directed visible pairs (both directions of every
+ * visible pair, the loop of RadiosityFast.py:1124-1131).  First call
+ * sp_count_directed (sym (n, n) scratch, row_counts (n), row_offset (n+1)),
+ * then sp_directed_pairs fills src/dst (row_offset[n] entries, ascending src
+ * within each destination). */
+int sp_count_directed(int n, const uint8_t* vis, uint8_t* sym, int32_t* row_counts, int64_t* row_offset,
+                      void* stream);
+int sp_directed_pairs(int n, const uint8_t* sym, const int64_t* row_offset, int32_t* src, int32_t* dst, void* stream);
+
+/* Per directed pair (src -> dst): outgoing-direction index of src toward dst
+ * (RadiosityFast.py:402-414 / :1277-1312), incoming index of the BRDF row
+ * used by ff_tilde (:1264-1268 / :1359-1390), centre distance (:538-543),
+ * normalised-vector length (:1252-1258) and F' (:1255-1256).
+ * dirs_in (n_walls, n_in, 3), dirs_out (n_walls, n_out, 3); either may be
+ * NULL (index 0 is written). */
+int sp_pair_setup(long long n_dir, int n, const int32_t* src, const int32_t* dst, const double* centers,
+                  const double* areas, const int32_t* pair_index, const double* ff, const int32_t* wall_of, int n_in,
+                  const double* dirs_in, int n_out, const double* dirs_out, int32_t* out_dir, int32_t* in_dir,
+                  double* dist, double* unit_len, double* fprime, void* stream);
+
+/* Dense (n, n) int64 outgoing-direction map, `sentinel` where not visible:
+ * the reference attribute _patch_2_brdf_outgoing_index (RadiosityFast.py:403-414). */
+int sp_outgoing_index_map(long long n_dir, int n, const int32_t* src, const int32_t* dst, const int32_t* out_dir,
+                          int64_t sentinel, int64_t* out, void* stream);
+
+/* Dense (n, n) FP64 form-factor matrix from the per-pair values (zero
+ * elsewhere): the reference attribute _form_factors (universal.py:42-52). */
+int sp_dense_form_factors(long long n_pairs, int n, const int32_t* pairs, const double* ff, double* out, void* stream);
+
+/* Dense ff_tilde (n, n, nd, nb) FP64 from the directed-pair data: replaces
+ * RadiosityFast.py:1234-1272 `_form_factors_with_directivity_dim`.  brdf
+ * NULL: no BRDF (nd must be 1, factor 1); att NULL: no air attenuation. */
+int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, const int32_t* src, const int32_t* dst,
+                          const int32_t* in_dir, const double* fprime, const double* unit_len, const double* att,
+                          const int32_t* wall_of, const int32_t* brdf_index, const double* brdf, double* out,
+                          void* stream);
+
+/* ------------------------------------------------------------ form factors */
+
+/* Universal patch-to-patch form factor for each listed pair (i = source).
+ * Replaces universal.py:12-52 `patch2patch_ff_universal` (+ :54-96,
+ * integration.py:38-114 Stokes, :116-289 Nusselt).  Quadrilateral patches.
+ * precision SP_F64: FP64 throughout; SP_F32: Stokes in re-centred FP32 with
+ * FP64 for vertex-sharing and near-coincident pairs.  ff (n_pairs) FP64;
+ * method (optional, n_pairs): 0 Stokes FP32, 1 Stokes FP64, 2 Nusselt FP64. */
+int sp_form_factors(int precision, long long n_pairs, const int32_t* pairs, const double* pts, const double* normals,
+                    const double* areas, double* ff, uint8_t* method, void* stream);
+
+/* Source -> patch energy and directional initial energy.
+ * Replaces universal.py:98-147 `_source2patch_energy_universal` and
+ * RadiosityFast.py:988-1034 `_add_directional`.  src (3); vis (n) from
+ * sp_point_visibility; brdf (n_slots, n_in, n_out, nb); outputs e0 (n, nb),
+ * d0 (n), e0dir (n, n_out, nb). */
+int sp_source_energy(const double* src, int n, const double* centers, const double* pts, const uint8_t* vis, int nb,
+                     const double* att, const int32_t* wall_of, const int32_t* brdf_index, int n_in,
+                     const double* dirs_in, int n_out, const double* brdf, double* e0, double* d0, double* e0dir,
+                     void* stream);
+
+/* Patch -> receiver factors: point factor (universal.py:149-160), outgoing
+ * direction toward the receiver (RadiosityFast.py:728-730) and distance
+ * (:712, :745).  rcv (3) -> rfac (n), ridx (n), dist (n). */
+int sp_receiver_factors(const double* rcv, int n, const double* centers, const double* pts, const uint8_t* vis,
+                        const int32_t* wall_of, int n_out, const double* dirs_out, double* rfac, int32_t* ridx,
+                        double* dist, void* stream);
+
+/* ---------------------------------------------------------- energy exchange */
+
+/* Arguments of sp_energy_exchange (host struct; array members are device
+ * pointers).  Directed pairs are destination-major (sp_directed_pairs). */
+typedef struct sp_exchange_args {
+    int precision;          /* SP_F32 or SP_F64: type of etc_total and of the arithmetic */
+    int algorithm;          /* SP_EXCHANGE_DENSE or SP_EXCHANGE_STRUCTURED */
+    int n_patches, n_dirs, n_bins, n_samples, max_order;
+    const double* energy_0_dir; /* (N, D, B) */
+    const double* distance_0;   /* (N) */
+    long long n_dir_pairs;
+    const int64_t* dst_offset;  /* (N + 1) */
+    const int32_t* pair_src;    /* (P) */
+    const int32_t* pair_out_dir;/* (P) p2o[src, dst] */
+    const int32_t* pair_in_dir; /* (P) BRDF incoming row of the sender */
+    const double* pair_distance;/* (P) */
+    const double* pair_fprime;  /* (P) F' */
+    const double* pair_unit_len;/* (P) */
+    const double* air_attenuation; /* (B) or NULL (no attenuation) */
+    const int32_t* wall_of;     /* (N) */
+    const int32_t* brdf_index;  /* (n_walls) */
+    int n_slots, n_in_dirs;
+    const double* brdf;         /* (n_slots, n_in, D, B) */
+    double speed_of_sound, time_resolution;
+    void* etc_total;            /* (N, D, B, T) output, precision type */
+    /* structured algorithm only (from sp_brdf_structure): */
+    const int32_t* slot_group;  /* (n_slots) material group of each slot */
+    const double* slot_scale;   /* (n_slots, B) */
+    int n_groups;
+    const double* class_diff;   /* (n_groups * n_in, B) */
+    const double* class_spec;   /* (n_groups * n_in, B) */
+    const int32_t* class_target;/* (n_groups * n_in) mirror direction, -1 if none */
+} sp_exchange_args;
+
+/* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070
+ * `_energy_exchange_init_energy` (max_order < 1).  Synchronises `stream` once
+ * (to report SP_ERR_RANGE for a source delay outside the histogram). */
+size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins,
+                                    int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs);
+int sp_energy_exchange(const sp_exchange_args* args, void* ws, size_t ws_bytes, void* stream);
+
+/* --------------------------------------------------------------- collection */
+
+/* One receiver: patchwise (n, nb, nt) and/or mono (nb, nt) FP64 histograms.
+ * Replaces RadiosityFast.py:686-752 `_collect_energy_patches` with
+ * :1148-1185 `_collect_receiver_energy` (circular roll by ceil(d/c/dt)) and
+ * the patch sum of :592.  etot in `precision`. */
+size_t sp_collect_workspace(int n_patches, int n_bins);
+int sp_collect_receiver(int precision, int n, int nd, int nb, int nt, const void* etot, const int32_t* ridx,
+                        const double* rfac, const double* dist, double c, double dt, const double* att,
+                        double* patchwise, double* mono, void* ws, size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPARROW_GB300_H */

@@ -1,0 +1,15 @@
+"""GB300-native directional fast radiosity (sparrowpy's hot path on sm_103a).
+
+Drop-in for ``sparrowpy.DirectionalRadiosityFast``; see radiosity.py.
+"""
+from . import brdf, geometry
+from .coords import Coordinates, FrequencyData, TimeData
+from .geometry import Polygon, shoebox_room_stub
+from .radiosity import DirectionalRadiosityFast, analyse_brdf
+
+__version__ = "0.1.0"
+
+__all__ = [
+    "DirectionalRadiosityFast", "Polygon", "shoebox_room_stub", "Coordinates", "FrequencyData", "TimeData",
+    "brdf", "geometry", "analyse_brdf",
+]

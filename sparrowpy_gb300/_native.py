@@ -1,0 +1,125 @@
+"""ctypes binding of libsparrow_gb300.so (the C ABI in include/sparrow_gb300.h).
+
+The library must exist: there is no CPU fallback.  If it is missing the
+import raises with the command that builds it.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsparrow_gb300.so")
+
+SP_OK = 0
+SP_ERR_ARG = -1
+SP_ERR_CUDA = -2
+SP_ERR_WORKSPACE = -3
+SP_ERR_RANGE = -4
+SP_ERR_TIMEOUT = -5
+SP_ERR_UNSUPPORTED = -6
+SP_F32 = 0
+SP_F64 = 1
+SP_EXCHANGE_DENSE = 0
+SP_EXCHANGE_STRUCTURED = 1
+
+_ERRORS = {
+    SP_ERR_ARG: "invalid argument",
+    SP_ERR_CUDA: "CUDA launch or copy failed",
+    SP_ERR_WORKSPACE: "workspace too small",
+    SP_ERR_RANGE: "delay outside the histogram",
+    SP_ERR_TIMEOUT: "bounded device wait gave up",
+    SP_ERR_UNSUPPORTED: "unsupported configuration",
+}
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+LL = ctypes.c_longlong
+D = ctypes.c_double
+SZ = ctypes.c_size_t
+
+
+class ExchangeArgs(ctypes.Structure):
+    """Mirror of `sp_exchange_args`."""
+    _fields_ = [
+        ("precision", I), ("algorithm", I),
+        ("n_patches", I), ("n_dirs", I), ("n_bins", I), ("n_samples", I), ("max_order", I),
+        ("energy_0_dir", P), ("distance_0", P),
+        ("n_dir_pairs", LL),
+        ("dst_offset", P), ("pair_src", P), ("pair_out_dir", P), ("pair_in_dir", P),
+        ("pair_distance", P), ("pair_fprime", P), ("pair_unit_len", P),
+        ("air_attenuation", P), ("wall_of", P), ("brdf_index", P),
+        ("n_slots", I), ("n_in_dirs", I), ("brdf", P),
+        ("speed_of_sound", D), ("time_resolution", D),
+        ("etc_total", P),
+        ("slot_group", P), ("slot_scale", P), ("n_groups", I),
+        ("class_diff", P), ("class_spec", P), ("class_target", P),
+    ]
+
+
+# name: (restype, argtypes)
+_SIGS = {
+    "sp_version": (ctypes.c_char_p, []),
+    "sp_patch_geometry": (I, [I, I, P, P, P, P]),
+    "sp_patch_visibility_workspace": (SZ, [I]),
+    "sp_patch_visibility": (I, [I, I, P, P, P, P, P, SZ, P]),
+    "sp_point_visibility_workspace": (SZ, [I]),
+    "sp_point_visibility": (I, [P, I, P, I, I, P, P, P, P, SZ, P]),
+    "sp_visible_pairs": (I, [I, P, P, P, P, P, P]),
+    "sp_count_directed": (I, [I, P, P, P, P, P]),
+    "sp_directed_pairs": (I, [I, P, P, P, P, P]),
+    "sp_pair_setup": (I, [LL, I, P, P, P, P, P, P, P, I, P, I, P, P, P, P, P, P, P]),
+    "sp_outgoing_index_map": (I, [LL, I, P, P, P, ctypes.c_int64, P, P]),
+    "sp_form_factors": (I, [I, LL, P, P, P, P, P, P, P]),
+    "sp_dense_form_factors": (I, [LL, I, P, P, P, P]),
+    "sp_form_factors_tilde": (I, [LL, I, I, I, I, P, P, P, P, P, P, P, P, P, P, P]),
+    "sp_source_energy": (I, [P, I, P, P, P, I, P, P, P, I, P, I, P, P, P, P, P]),
+    "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
+    "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I]),
+    "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
+    "sp_collect_workspace": (SZ, [I, I]),
+    "sp_collect_receiver": (I, [I, I, I, I, I, P, P, P, P, D, D, P, P, P, P, SZ, P]),
+}
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call returned a negative status."""
+
+    def __init__(self, name, code):
+        super().__init__(f"{name} failed: {_ERRORS.get(code, 'unknown error')} (status {code})")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load (once) and return the ctypes library handle."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                "`python sparrowpy_gb300/build_lib.py` (there is no CPU fallback)")
+        h = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def call(name, *args):
+    """Call an int-returning entry point and raise NativeError on failure."""
+    rc = getattr(lib(), name)(*args)
+    if rc != SP_OK:
+        raise NativeError(name, rc)
+    return rc
+
+
+def size(name, *args):
+    return int(getattr(lib(), name)(*args))

@@ -1,0 +1,573 @@
+// Patch-to-patch form factors (universal method) and point-to-patch factors.
+//
+// * Pairs with a shared vertex (distance < 1e-6, geometry.py:719-748) use the
+//   Nusselt analogue in FP64 (integration.py:116-289), as the reference does.
+// * All other pairs use the Stokes boundary integral (integration.py:38-114):
+//   F = |sum_ab (u_a . v_b) ln|P_a - Q_b|| / (2 pi A_i), where P_a, Q_b are the
+//   16 Boole sample points of each boundary and u_a, v_b their Boole weight
+//   vectors (a segment whose |dx_dim| <= 1e-3 contributes nothing to dim).
+//   - FP64 mode evaluates the logarithms directly.
+//   - FP32 mode uses an exact re-centring: with D = c_i - c_j,
+//     ln r_ab = ln|D| + (1/2)(L_ab + Q_ab) + (1/2) phi(delta_ab), where
+//     delta = L + Q, L = 2 D.e/|D|^2, Q = |e|^2/|D|^2, e = (P_a - c_i) - (Q_b - c_j)
+//     and phi(x) = ln(1 + x) - x.  The ln|D|, L and Q sums reduce to 3x3 moments
+//     of the weights (computed in FP64), leaving only the well-conditioned phi
+//     sum for FP32.  Pairs whose sample points come closer than 0.3 |D| are
+//     recomputed in FP64 inside the same warp.
+#include "common.cuh"
+
+namespace {
+
+__device__ __forceinline__ double boole_coef(int k) {
+    return (k == 0 || k == 4) ? 7.0 : ((k == 2) ? 12.0 : 32.0);
+}
+
+// geometry.py:498-559 (n_out = z); same operation order as the reference.
+__device__ void rotation_matrix_ff(const double* n_in, double* m) {
+    if (n_in[0] == 0.0 && n_in[1] == 0.0 && n_in[2] == 1.0) {
+        for (int i = 0; i < 9; ++i) m[i] = (i % 4 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    double nn = xnorm3(n_in);
+    double a[3] = {xdiv(n_in[0], nn), xdiv(n_in[1], nn), xdiv(n_in[2], nn)};
+    double c = a[2];
+    if (c != -1.0) {
+        double v[3] = {a[1], -a[0], 0.0};  // a x (0,0,1)
+        double s = xnorm3(v);
+        double k[9] = {0.0, -v[2], v[1], v[2], 0.0, -v[0], -v[1], v[0], 0.0};
+        double f = xdiv(xsub(1.0, c), xmul(s, s));
+        for (int r = 0; r < 3; ++r)
+            for (int col = 0; col < 3; ++col) {
+                double kk = k[r * 3 + 0] * k[col] + k[r * 3 + 1] * k[3 + col] + k[r * 3 + 2] * k[6 + col];
+                m[r * 3 + col] = ((r == col) ? 1.0 : 0.0) + k[r * 3 + col] + kk * f;
+            }
+    } else {
+        const double flip[9] = {-1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, -1.0};
+        for (int i = 0; i < 9; ++i) m[i] = flip[i];
+    }
+}
+
+// Boundary sample point `a` (0..15) of a quadrilateral: integration.py:639-649
+// with npoints = 5 (segment a/4, position a%4).
+__device__ __forceinline__ void boundary_point5(const double* el, int a, double* out) {
+    int s = a >> 2, k = a & 3;
+    const double* p = el + 3 * s;
+    const double* q = el + 3 * ((s + 1) & 3);
+    for (int d = 0; d < 3; ++d) out[d] = p[d] + (k * (q[d] - p[d])) / 4;
+}
+
+// Boole weight vector of boundary point a (0..15): the point is position
+// a%4 of segment a/4 and, when a%4 == 0, also position 4 of segment a/4 - 1.
+// Segment weight per dim: (2h/45) * c_k with h = x1 - x0, zero when
+// |x4 - x0| <= 1e-3 (integration.py:96, :109).
+__device__ void boole_weight(const double* el, int a, double* w) {
+    int s = a >> 2, k = a & 3;
+    for (int d = 0; d < 3; ++d) w[d] = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int seg, pos;
+        if (pass == 0) {
+            seg = s;
+            pos = k;
+        } else {
+            if (k != 0) break;
+            seg = (s + 3) & 3;
+            pos = 4;
+        }
+        double x0[3], x1[3], x4[3];
+        boundary_point5(el, 4 * seg, x0);
+        boundary_point5(el, 4 * seg + 1, x1);
+        boundary_point5(el, (4 * seg + 4) & 15, x4);
+        for (int d = 0; d < 3; ++d) {
+            if (fabs(x4[d] - x0[d]) > 1e-3) {
+                double h = x1[d] - x0[d];
+                w[d] += 2 * h / 45 * boole_coef(pos);
+            }
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// phi(x) = ln(1 + x) - x, accurate to a few ulp of its value in FP32.
+__device__ __forceinline__ float phi_f(float x) {
+    if (fabsf(x) < 0.2f) {
+        // -x^2/2 + x^3/3 - x^4/4 + ... (16 terms of the Taylor series)
+        float p = -1.0f / 17.0f;
+#pragma unroll
+        for (int k = 16; k >= 2; --k) p = fmaf(p, x, ((k & 1) ? 1.0f : -1.0f) / (float)k);
+        return p * x * x;
+    }
+    return log1pf(x) - x;
+}
+
+// integration.py:38-114 `stokes_integration` for one pair, one warp.
+// Lane l < 16 owns sample point a = l of patch i, lane l >= 16 owns point
+// b = l - 16 of patch j.  Returns the same value on all lanes.
+__device__ double stokes_pair(const double* pi, const double* pj, double area_i, bool fp32, bool* needs_fp64) {
+    int lane = threadIdx.x & 31;
+    bool is_i = lane < 16;
+    int a = lane & 15;
+    const double* el = is_i ? pi : pj;
+    double P[3], w[3];
+    boundary_point5(el, a, P);
+    boole_weight(el, a, w);
+    if (!fp32) {
+        // direct logarithms: lane handles (a = lane & 15, b in half*8 .. +8)
+        double s = 0.0;
+        int half = lane >> 4;
+        double Pa[3], ua[3];
+        for (int d = 0; d < 3; ++d) {
+            Pa[d] = __shfl_sync(0xffffffffu, P[d], a);
+            ua[d] = __shfl_sync(0xffffffffu, w[d], a);
+        }
+        for (int bb = 0; bb < 8; ++bb) {
+            int b = half * 8 + bb;
+            double Qb[3], vb[3];
+            for (int d = 0; d < 3; ++d) {
+                Qb[d] = __shfl_sync(0xffffffffu, P[d], 16 + b);
+                vb[d] = __shfl_sync(0xffffffffu, w[d], 16 + b);
+            }
+            double dd[3] = {Pa[0] - Qb[0], Pa[1] - Qb[1], Pa[2] - Qb[2]};
+            double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+            s += (ua[0] * vb[0] + ua[1] * vb[1] + ua[2] * vb[2]) * log(r);
+        }
+        s = warp_sum(s);
+        *needs_fp64 = false;
+        return fabs(s / (2 * SP_PI * area_i));
+    }
+    // centres (vertex means, geometry.py:412-413)
+    double ci[3], cj[3];
+    for (int d = 0; d < 3; ++d) {
+        ci[d] = (((pi[d] + pi[3 + d]) + pi[6 + d]) + pi[9 + d]) / 4;
+        cj[d] = (((pj[d] + pj[3 + d]) + pj[6 + d]) + pj[9 + d]) / 4;
+    }
+    double D[3] = {ci[0] - cj[0], ci[1] - cj[1], ci[2] - cj[2]};
+    double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    double loc[3];
+    for (int d = 0; d < 3; ++d) loc[d] = P[d] - (is_i ? ci[d] : cj[d]);
+    // FP64 moments: m_w = sum w, m_dw = sum (D.loc) w, m_qw = sum |loc|^2 w,
+    // m_lw[d][e] = sum w[d] loc[e]  (separately over i-lanes and j-lanes)
+    double Dl = D[0] * loc[0] + D[1] * loc[1] + D[2] * loc[2];
+    double l2 = loc[0] * loc[0] + loc[1] * loc[1] + loc[2] * loc[2];
+    double mom[18];
+    for (int d = 0; d < 3; ++d) {
+        mom[d] = w[d];
+        mom[3 + d] = Dl * w[d];
+        mom[6 + d] = l2 * w[d];
+        for (int e = 0; e < 3; ++e) mom[9 + 3 * d + e] = w[d] * loc[e];
+    }
+    // reduce within each half-warp
+    for (int k = 0; k < 18; ++k) {
+        double v = mom[k];
+        for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        mom[k] = v;
+    }
+    double Mi[18], Mj[18];
+    for (int k = 0; k < 18; ++k) {
+        Mi[k] = __shfl_sync(0xffffffffu, mom[k], 0);
+        Mj[k] = __shfl_sync(0xffffffffu, mom[k], 16);
+    }
+    double UV = Mi[0] * Mj[0] + Mi[1] * Mj[1] + Mi[2] * Mj[2];
+    double lin = (Mi[3] * Mj[0] + Mi[4] * Mj[1] + Mi[5] * Mj[2]) - (Mi[0] * Mj[3] + Mi[1] * Mj[4] + Mi[2] * Mj[5]);
+    lin /= D2;
+    double pq = 0.0;
+    for (int k = 0; k < 9; ++k) pq += Mi[9 + k] * Mj[9 + k];
+    double quad = 0.5 * ((Mi[6] * Mj[0] + Mi[7] * Mj[1] + Mi[8] * Mj[2]) +
+                         (Mi[0] * Mj[6] + Mi[1] * Mj[7] + Mi[2] * Mj[8]) - 2.0 * pq) / D2;
+    double base = 0.5 * log(D2) * UV + lin + quad;
+    // FP32 phi sum over the 256 sample pairs
+    float Df[3] = {(float)D[0], (float)D[1], (float)D[2]};
+    float invD2 = (float)(1.0 / D2);
+    float locf[3] = {(float)loc[0], (float)loc[1], (float)loc[2]};
+    float wf[3] = {(float)w[0], (float)w[1], (float)w[2]};
+    int half = lane >> 4;
+    float pa[3], ua[3];
+    for (int d = 0; d < 3; ++d) {
+        pa[d] = __shfl_sync(0xffffffffu, locf[d], a);
+        ua[d] = __shfl_sync(0xffffffffu, wf[d], a);
+    }
+    float acc = 0.0f;
+    float min_ratio = 1e30f;
+    for (int bb = 0; bb < 8; ++bb) {
+        int b = half * 8 + bb;
+        float qb[3], vb[3];
+        for (int d = 0; d < 3; ++d) {
+            qb[d] = __shfl_sync(0xffffffffu, locf[d], 16 + b);
+            vb[d] = __shfl_sync(0xffffffffu, wf[d], 16 + b);
+        }
+        float e[3] = {pa[0] - qb[0], pa[1] - qb[1], pa[2] - qb[2]};
+        float de = Df[0] * e[0] + Df[1] * e[1] + Df[2] * e[2];
+        float ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+        float delta = (2.0f * de + ee) * invD2;
+        min_ratio = fminf(min_ratio, 1.0f + delta);
+        float W = ua[0] * vb[0] + ua[1] * vb[1] + ua[2] * vb[2];
+        acc = fmaf(W, phi_f(delta), acc);
+    }
+    acc = warp_sum(acc);
+    for (int off = 16; off > 0; off >>= 1) min_ratio = fminf(min_ratio, __shfl_xor_sync(0xffffffffu, min_ratio, off));
+    *needs_fp64 = (min_ratio < 0.09f);  // some r_ab < 0.3 |D|
+    double outer = base + 0.5 * (double)acc;
+    return fabs(outer / (2 * SP_PI * area_i));
+}
+
+__device__ __forceinline__ double dsign(double v) { return (v > 0) ? 1.0 : ((v < 0) ? -1.0 : 0.0); }
+
+// 3x3 inverse with partial pivoting (np.linalg.inv in integration.py:380).
+__device__ bool inv3(const double* a, double* out) {
+    double m[3][6];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) m[r][c] = a[r * 3 + c];
+        for (int c = 0; c < 3; ++c) m[r][3 + c] = (r == c) ? 1.0 : 0.0;
+    }
+    for (int col = 0; col < 3; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 3; ++r)
+            if (fabs(m[r][col]) > fabs(m[piv][col])) piv = r;
+        if (m[piv][col] == 0.0) return false;
+        if (piv != col)
+            for (int c = 0; c < 6; ++c) {
+                double t = m[piv][c];
+                m[piv][c] = m[col][c];
+                m[col][c] = t;
+            }
+        double p = m[col][col];
+        for (int c = 0; c < 6; ++c) m[col][c] /= p;
+        for (int r = 0; r < 3; ++r) {
+            if (r == col) continue;
+            double f = m[r][col];
+            for (int c = 0; c < 6; ++c) m[r][c] -= f * m[col][c];
+        }
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[r * 3 + c] = m[r][3 + c];
+    return true;
+}
+
+// integration.py:416-460 `_area_under_curve` (3 samples, order 2).
+__device__ double area_under_curve(const double ps[3][2]) {
+    double f[2] = {ps[2][0] - ps[0][0], ps[2][1] - ps[0][1]};
+    double nf = sqrt(f[0] * f[0] + f[1] * f[1]);
+    double rm[4] = {f[0] / nf, f[1] / nf, -f[1] / nf, f[0] / nf};
+    double x[3] = {0, 0, 0}, y[3] = {0, 0, 0};
+    for (int k = 1; k < 3; ++k) {
+        double c[2] = {ps[k][0] - ps[0][0], ps[k][1] - ps[0][1]};
+        x[k] = rm[0] * c[0] + rm[1] * c[1];
+        y[k] = rm[2] * c[0] + rm[3] * c[1];
+    }
+    double b[3] = {0, 0, 0};
+    if (!(fabs(x[2] - x[0]) < 1e-6)) {
+        double xm[9];
+        for (int i = 0; i < 3; ++i) {
+            xm[i * 3 + 2] = 1.0;
+            xm[i * 3 + 1] = x[i];
+            xm[i * 3 + 0] = x[i] * x[i];
+        }
+        double iv[9];
+        if (inv3(xm, iv))
+            for (int r = 0; r < 3; ++r) b[r] = iv[r * 3] * y[0] + iv[r * 3 + 1] * y[1] + iv[r * 3 + 2] * y[2];
+    }
+    double out = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        int p = 3 - i;
+        double x2p = (p == 3) ? x[2] * x[2] * x[2] : ((p == 2) ? x[2] * x[2] : x[2]);
+        double x0p = (p == 3) ? x[0] * x[0] * x[0] : ((p == 2) ? x[0] * x[0] : x[0]);
+        out += b[i] * x2p / p;
+        out -= b[i] * x0p / p;
+    }
+    return out;
+}
+
+// integration.py:116-230 `nusselt_analog` (quadrilateral receiver).
+__device__ double nusselt_analog(const double* origin, const double* rot, const double* pp, double hand) {
+    double sph[8][3], pln[8][2];
+    for (int ii = 0; ii < 8; ++ii) {
+        int s = ii >> 1, k = ii & 1;
+        const double* p = pp + 3 * s;
+        const double* q = pp + 3 * ((s + 1) & 3);
+        double bp[3], d[3];
+        for (int dd = 0; dd < 3; ++dd) {
+            bp[dd] = p[dd] + (k * (q[dd] - p[dd])) / 2;
+            d[dd] = bp[dd] - origin[dd];
+        }
+        double nd = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int dd = 0; dd < 3; ++dd) sph[ii][dd] = d[dd] / nd;
+        pln[ii][0] = rot[0] * sph[ii][0] + rot[1] * sph[ii][1] + rot[2] * sph[ii][2];
+        pln[ii][1] = rot[3] * sph[ii][0] + rot[4] * sph[ii][1] + rot[5] * sph[ii][2];
+    }
+    // _polygon_area of the 4 projected corners (z = 0)
+    double big = 0.0;
+    for (int t = 0; t < 2; ++t) {
+        double a0 = pln[2 * (t + 1)][0] - pln[0][0], a1 = pln[2 * (t + 1)][1] - pln[0][1];
+        double b0 = pln[2 * (t + 2)][0] - pln[0][0], b1 = pln[2 * (t + 2)][1] - pln[0][1];
+        big += 0.5 * fabs(a0 * b1 - a1 * b0);
+    }
+    double curved = 0.0;
+    for (int jj = 0; jj < 4; ++jj) {
+        int s0 = 2 * jj, s1 = 2 * jj + 1, s2 = (2 * jj + 2) & 7;
+        double crz = pln[s2][0] * pln[s0][1] - pln[s2][1] * pln[s0][0];
+        if (fabs(crz) > 1e-6) {
+            if (pln[s2][0] * pln[s0][0] + pln[s2][1] * pln[s0][1] >= 1e-6) {
+                double seg[3][2] = {{pln[s0][0], pln[s0][1]}, {pln[s1][0], pln[s1][1]}, {pln[s2][0], pln[s2][1]}};
+                curved += area_under_curve(seg);
+            } else {
+                double mp[3], marc[3], a[3], b[3];
+                for (int k = 0; k < 3; ++k) mp[k] = sph[s0][k] + (sph[s2][k] - sph[s0][k]) / 2;
+                double nm = sqrt(mp[0] * mp[0] + mp[1] * mp[1] + mp[2] * mp[2]);
+                for (int k = 0; k < 3; ++k) marc[k] = mp[k] / nm;
+                for (int k = 0; k < 3; ++k) a[k] = sph[s0][k] + (marc[k] - sph[s0][k]) / 2;
+                for (int k = 0; k < 3; ++k) b[k] = marc[k] + (sph[s2][k] - marc[k]) / 2;
+                double na = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+                double nb = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+                for (int k = 0; k < 3; ++k) {
+                    a[k] /= na;
+                    b[k] /= nb;
+                }
+                double mp2[2] = {rot[0] * mp[0] + rot[1] * mp[1] + rot[2] * mp[2],
+                                 rot[3] * mp[0] + rot[4] * mp[1] + rot[5] * mp[2]};
+                double marc2[2] = {rot[0] * marc[0] + rot[1] * marc[1] + rot[2] * marc[2],
+                                   rot[3] * marc[0] + rot[4] * marc[1] + rot[5] * marc[2]};
+                double a2[2] = {rot[0] * a[0] + rot[1] * a[1] + rot[2] * a[2],
+                                rot[3] * a[0] + rot[4] * a[1] + rot[5] * a[2]};
+                double b2[2] = {rot[0] * b[0] + rot[1] * b[1] + rot[2] * b[2],
+                                rot[3] * b[0] + rot[4] * b[1] + rot[5] * b[2]};
+                double d1[2] = {pln[s2][0] - pln[s0][0], pln[s2][1] - pln[s0][1]};
+                double d2[2] = {mp2[0] - marc2[0], mp2[1] - marc2[1]};
+                double lin = sqrt(d1[0] * d1[0] + d1[1] * d1[1]) * sqrt(d2[0] * d2[0] + d2[1] * d2[1]) / 2;
+                double left_seg[3][2] = {{pln[s0][0], pln[s0][1]}, {a2[0], a2[1]}, {marc2[0], marc2[1]}};
+                double right_seg[3][2] = {{marc2[0], marc2[1]}, {b2[0], b2[1]}, {pln[s2][0], pln[s2][1]}};
+                double left = area_under_curve(left_seg);
+                double right = area_under_curve(right_seg);
+                curved += (lin * dsign(left) + left + right);
+            }
+        }
+    }
+    return big + hand * curved;
+}
+
+// integration.py:232-289 `nusselt_integration`, 64 regular-grid samples
+// (integration.py:533-605), one warp per pair.
+__device__ double nusselt_pair(const double* pi, const double* pj, const double* ni, const double* nj) {
+    int lane = threadIdx.x & 31;
+    double u[3] = {pi[3] - pi[0], pi[4] - pi[1], pi[5] - pi[2]};
+    double v[3] = {pi[9] - pi[0], pi[10] - pi[1], pi[11] - pi[2]};
+    double nu = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    double nvv = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    long npx = (long)rint(nu / nvv * sqrt(64.0));
+    long npz = (long)rint(nvv / nu * sqrt(64.0));
+    if (npz == 0) npz = 1;
+    if (npx == 0) npx = 1;
+    double e1[3] = {pj[3] - pj[0], pj[4] - pj[1], pj[5] - pj[2]};
+    double e2[3] = {pj[6] - pj[3], pj[7] - pj[4], pj[8] - pj[5]};
+    double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    double hand = dsign(cr[0] * nj[0] + cr[1] * nj[1] + cr[2] * nj[2]);
+    double rot[9];
+    rotation_matrix_ff(ni, rot);
+    long total = npx * npz;
+    double s = 0.0;
+    for (long idx = lane; idx < total; idx += 32) {
+        long ix = idx / npz, iz = idx % npz;
+        double stopx = 1 - 1.0 / npx, stopz = 1 - 1.0 / npz;
+        double tx = (npx > 1) ? ((ix == npx - 1) ? stopx : ix * (stopx / (npx - 1))) : 0.0;
+        double tz = (npz > 1) ? ((iz == npz - 1) ? stopz : iz * (stopz / (npz - 1))) : 0.0;
+        tx += 1.0 / (npx * 2);
+        tz += 1.0 / (npz * 2);
+        double o[3];
+        for (int d = 0; d < 3; ++d) o[d] = tx * u[d] + tz * v[d] + pi[d];
+        s += nusselt_analog(o, rot, pj, hand);
+    }
+    s = warp_sum(s);
+    return s * (1 / (SP_PI * total));
+}
+
+__device__ __forceinline__ bool coincident(const double* p0, const double* p1) {
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            double d[3] = {p0[3 * i] - p1[3 * j], p0[3 * i + 1] - p1[3 * j + 1], p0[3 * i + 2] - p1[3 * j + 2]};
+            if (sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < 1e-6) return true;
+        }
+    return false;
+}
+
+// method codes written per pair
+enum { kStokes32 = 0, kStokes64 = 1, kNusselt = 2 };
+
+// universal.py:12-96: one warp per visible pair (i < j, i = source).
+__global__ void __launch_bounds__(256) k_form_factors(long long n_pairs, const int32_t* __restrict__ pairs,
+                                                      const double* __restrict__ pts, const double* __restrict__ normals,
+                                                      const double* __restrict__ areas, int fp32, double* __restrict__ ff,
+                                                      uint8_t* __restrict__ method) {
+    long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= n_pairs) return;
+    int lane = threadIdx.x & 31;
+    int i = pairs[2 * q], j = pairs[2 * q + 1];
+    double pi[12], pj[12];
+    for (int k = 0; k < 12; ++k) {
+        pi[k] = pts[(size_t)i * 12 + k];
+        pj[k] = pts[(size_t)j * 12 + k];
+    }
+    double result;
+    int m;
+    if (coincident(pj, pi)) {
+        double ni[3] = {normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]};
+        double nj[3] = {normals[3 * j], normals[3 * j + 1], normals[3 * j + 2]};
+        result = nusselt_pair(pi, pj, ni, nj);
+        m = kNusselt;
+    } else {
+        bool redo = false;
+        result = stokes_pair(pi, pj, areas[i], fp32 != 0, &redo);
+        m = fp32 ? kStokes32 : kStokes64;
+        if (redo) {
+            result = stokes_pair(pi, pj, areas[i], false, &redo);
+            m = kStokes64;
+        }
+    }
+    if (lane == 0) {
+        ff[q] = result;
+        if (method) method[q] = (uint8_t)m;
+    }
+}
+
+// geometry.py:688-715 `_sphere_tangent_vector`.
+__device__ void sphere_tangent(const double* v0, const double* v1, double* out) {
+    if (fabs(v0[0] * v1[0] + v0[1] * v1[1] + v0[2] * v1[2]) > 1e-10) {
+        double d[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+        double f = (d[0] * v0[0] + d[1] * v0[1] + d[2] * v0[2]) / (v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+        for (int k = 0; k < 3; ++k) out[k] = d[k] - f * v0[k];
+        double n = sqrt(out[0] * out[0] + out[1] * out[1] + out[2] * out[2]);
+        for (int k = 0; k < 3; ++k) out[k] /= n;
+    } else {
+        double n = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+        for (int k = 0; k < 3; ++k) out[k] = v1[k] / n;
+    }
+}
+
+}  // namespace
+
+// integration.py:295-344 `pt_solution` (mode 0 = source, 1 = receiver).
+static __device__ double sp_pt_solution(const double* point, const double* patch, int nv, int mode) {
+    double area = 4.0;
+    if (mode == 1) {
+        area = 0.0;
+        for (int t = 0; t < nv - 2; ++t) {
+            const double* p1 = patch + 3 * (t + 1);
+            const double* p2 = patch + 3 * (t + 2);
+            double a[3] = {p1[0] - patch[0], p1[1] - patch[1], p1[2] - patch[2]};
+            double b[3] = {p2[0] - patch[0], p2[1] - patch[1], p2[2] - patch[2]};
+            double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+            area += 0.5 * sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        }
+    }
+    double ons[8][3];
+    for (int i = 0; i < nv; ++i) {
+        double d[3] = {patch[3 * i] - point[0], patch[3 * i + 1] - point[1], patch[3 * i + 2] - point[2]};
+        double n = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; ++k) ons[i][k] = d[k] / n;
+    }
+    double s = 0.0;
+    for (int i = 0; i < nv; ++i) {
+        double v0[3], v1[3];
+        sphere_tangent(ons[i], ons[(i - 1 + nv) % nv], v0);
+        sphere_tangent(ons[i], ons[(i + 1) % nv], v1);
+        s += acos(v0[0] * v1[0] + v0[1] * v1[1] + v0[2] * v1[2]);
+    }
+    double factor = s - (nv - 2) * SP_PI;
+    return factor / (SP_PI * area);
+}
+
+namespace {
+
+// universal.py:98-147 `_source2patch_energy_universal` fused with
+// RadiosityFast.py:988-1034 `_add_directional`.
+__global__ void k_source_energy(const double* __restrict__ src, int n, const double* __restrict__ centers,
+                                const double* __restrict__ pts, const uint8_t* __restrict__ vis, int nb,
+                                const double* __restrict__ att, const int32_t* __restrict__ wall_of,
+                                const int32_t* __restrict__ brdf_index, int n_in, const double* __restrict__ dirs_in,
+                                int n_out, const double* __restrict__ brdf, double* __restrict__ e0,
+                                double* __restrict__ d0, double* __restrict__ e0dir) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double s[3] = {src[0], src[1], src[2]};
+    double c[3] = {centers[3 * j], centers[3 * j + 1], centers[3 * j + 2]};
+    double dist = 0.0, g = 0.0;
+    bool v = vis[j] != 0;
+    if (v) {
+        double dv[3] = {xsub(s[0], c[0]), xsub(s[1], c[1]), xsub(s[2], c[2])};
+        dist = xnorm3(dv);
+        g = sp_pt_solution(s, pts + (size_t)j * 12, 4, 0);
+    }
+    d0[j] = dist;
+    int w = wall_of[j];
+    int slot = brdf_index[w];
+    // get_scattering_data_source(pos_h = source, pos_i = c_j): unit(source - c_j)
+    int sidx = sp_nearest_dir(c, s, dirs_in + (size_t)w * n_in * 3, n_in);
+    const double* row = brdf + ((size_t)slot * n_in + sidx) * n_out * nb;
+    for (int b = 0; b < nb; ++b) {
+        double e = v ? exp(-att[b] * dist) * g : 0.0;
+        e0[(size_t)j * nb + b] = e;
+        for (int o = 0; o < n_out; ++o) e0dir[((size_t)j * n_out + o) * nb + b] = e * row[(size_t)o * nb + b];
+    }
+}
+
+// Receiver side of RadiosityFast.py:711-738: per patch the point-to-patch
+// factor (universal.py:149-160), the outgoing direction toward the receiver
+// (get_scattering_data_receiver_index with pos_j = receiver) and the
+// patch-receiver distance (:712, :745).
+__global__ void k_receiver_factors(const double* __restrict__ rcv, int n, const double* __restrict__ centers,
+                                   const double* __restrict__ pts, const uint8_t* __restrict__ vis,
+                                   const int32_t* __restrict__ wall_of, int n_out, const double* __restrict__ dirs_out,
+                                   double* __restrict__ rfac, int32_t* __restrict__ ridx, double* __restrict__ dist) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double r[3] = {rcv[0], rcv[1], rcv[2]};
+    double c[3] = {centers[3 * k], centers[3 * k + 1], centers[3 * k + 2]};
+    rfac[k] = vis[k] ? sp_pt_solution(r, pts + (size_t)k * 12, 4, 1) : 0.0;
+    ridx[k] = sp_nearest_dir(c, r, dirs_out + (size_t)wall_of[k] * n_out * 3, n_out);
+    double dv[3] = {xsub(c[0], r[0]), xsub(c[1], r[1]), xsub(c[2], r[2])};
+    dist[k] = xnorm3(dv);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sp_source_energy(const double* src, int n, const double* centers, const double* pts, const uint8_t* vis, int nb,
+                     const double* att, const int32_t* wall_of, const int32_t* brdf_index, int n_in,
+                     const double* dirs_in, int n_out, const double* brdf, double* e0, double* d0, double* e0dir,
+                     void* stream) {
+    if (n < 0 || nb < 1 || n_in < 1 || n_out < 1) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!src || !centers || !pts || !vis || !att || !wall_of || !brdf_index || !dirs_in || !brdf || !e0 || !d0 || !e0dir)
+        return SP_ERR_ARG;
+    k_source_energy<<<sp_blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(src, n, centers, pts, vis, nb, att, wall_of,
+                                                                         brdf_index, n_in, dirs_in, n_out, brdf, e0, d0,
+                                                                         e0dir);
+    return sp_check_launch();
+}
+
+int sp_receiver_factors(const double* rcv, int n, const double* centers, const double* pts, const uint8_t* vis,
+                        const int32_t* wall_of, int n_out, const double* dirs_out, double* rfac, int32_t* ridx,
+                        double* dist, void* stream) {
+    if (n < 0 || n_out < 1) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!rcv || !centers || !pts || !vis || !wall_of || !dirs_out || !rfac || !ridx || !dist) return SP_ERR_ARG;
+    k_receiver_factors<<<sp_blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(rcv, n, centers, pts, vis, wall_of, n_out,
+                                                                            dirs_out, rfac, ridx, dist);
+    return sp_check_launch();
+}
+
+int sp_form_factors(int precision, long long n_pairs, const int32_t* pairs, const double* pts, const double* normals,
+                    const double* areas, double* ff, uint8_t* method, void* stream) {
+    if (n_pairs < 0 || (precision != SP_F32 && precision != SP_F64)) return SP_ERR_ARG;
+    if (n_pairs == 0) return SP_OK;
+    if (!pairs || !pts || !normals || !areas || !ff) return SP_ERR_ARG;
+    long long threads = n_pairs * 32;
+    k_form_factors<<<sp_blocks(threads, 256), 256, 0, (cudaStream_t)stream>>>(n_pairs, pairs, pts, normals, areas,
+                                                                              precision == SP_F32 ? 1 : 0, ff, method);
+    return sp_check_launch();
+}
+
+}  // extern "C"

@@ -1,0 +1,599 @@
+// Geometry kernels: patch centres/areas, patch<->patch and point<->patch
+// visibility, visible-pair compaction and the destination-major pair list.
+//
+// The visibility predicate is evaluated in FP64 with the reference's exact
+// operation order (no fused multiply-add) so that the boolean result equals
+// the reference's on inputs in generic position.  A conservative FP32
+// segment-vs-box test, over groups of 32 consecutive blockers and then over
+// single blockers, decides which blockers need the exact test at all: a
+// blocker whose (slightly enlarged) bounding box the segment misses can only
+// return "visible" in the reference predicate (see exact_visibility below).
+#include "common.cuh"
+
+namespace {
+
+constexpr int kGroup = 32;       // blockers per culling group
+constexpr int kMaxVerts = 8;     // polygon vertices supported by the predicate
+
+// geometry.py:498-559 `_rotation_matrix(n_in)` with n_out = (0, 0, 1).
+__device__ void rotation_matrix(const double* n_in, double* m) {
+    if (n_in[0] == 0.0 && n_in[1] == 0.0 && n_in[2] == 1.0) {
+        for (int i = 0; i < 9; ++i) m[i] = (i % 4 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    double nn = xnorm3(n_in);
+    double a[3] = {xdiv(n_in[0], nn), xdiv(n_in[1], nn), xdiv(n_in[2], nn)};
+    double b[3] = {0.0, 0.0, 1.0};
+    double c = xdot3(a, b);
+    if (c != -1.0) {
+        double v[3];
+        xcross3(a, b, v);
+        double s = xnorm3(v);
+        double k[9] = {0.0, -v[2], v[1], v[2], 0.0, -v[0], -v[1], v[0], 0.0};
+        double f = xdiv(xsub(1.0, c), xmul(s, s));
+        for (int r = 0; r < 3; ++r)
+            for (int col = 0; col < 3; ++col) {
+                double kk = xadd(xadd(xmul(k[r * 3 + 0], k[0 * 3 + col]), xmul(k[r * 3 + 1], k[1 * 3 + col])),
+                                 xmul(k[r * 3 + 2], k[2 * 3 + col]));
+                double id = (r == col) ? 1.0 : 0.0;
+                m[r * 3 + col] = xadd(xadd(id, k[r * 3 + col]), xmul(kk, f));
+            }
+    } else {
+        const double flip[9] = {-1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, -1.0};
+        for (int i = 0; i < 9; ++i) m[i] = flip[i];
+    }
+}
+
+// geometry.py:614-686 `_point_in_polygon` (winding number, eta = 1e-6).
+__device__ bool point_in_polygon(const double* p3, const double* poly3, int nv, const double* n) {
+    const double eta = 1e-6;
+    double d0[3] = {xsub(p3[0], poly3[0]), xsub(p3[1], poly3[1]), xsub(p3[2], poly3[2])};
+    if (fabs(xdot3(d0, n)) > eta) return false;
+    double rot[9];
+    rotation_matrix(n, rot);
+    double pt[2] = {xdot3(rot, p3), xdot3(rot + 3, p3)};
+    double poly[kMaxVerts][2];
+    for (int i = 0; i < nv; ++i) {
+        poly[i][0] = xdot3(rot, poly3 + 3 * i);
+        poly[i][1] = xdot3(rot + 3, poly3 + 3 * i);
+    }
+    int count = 0;
+    for (int i = 0; i < nv; ++i) {
+        const double* a1 = poly[(i + 1) % nv];
+        const double* a0 = poly[i];
+        double side[2] = {xsub(a1[0], a0[0]), xsub(a1[1], a0[1])};
+        double ns = xnorm2(side);
+        double nl[2] = {xdiv(-side[1], ns), xdiv(side[0], ns)};
+        double point[2] = {xadd(pt[0], 1.0), xadd(pt[1], 0.0)};
+        double v[2] = {xsub(point[0], pt[0]), xsub(point[1], pt[1])};
+        double dp = xdot2(v, nl);
+        if (!(fabs(dp) > 1e-6)) continue;
+        double w[2] = {xsub(point[0], a1[0]), xsub(point[1], a1[1])};
+        double fac = -xdiv(xdot2(nl, w), dp);
+        double b[2] = {xadd(xadd(w[0], a1[0]), xmul(fac, v[0])), xadd(xadd(w[1], a1[1]), xmul(fac, v[1]))};
+        if (b[0] > pt[0]) {
+            double ba0[2] = {xsub(b[0], a0[0]), xsub(b[1], a0[1])};
+            double ba1[2] = {xsub(b[0], a1[0]), xsub(b[1], a1[1])};
+            double a10[2] = {xsub(a1[0], a0[0]), xsub(a1[1], a0[1])};
+            if (fabs(xsub(xadd(xnorm2(ba0), xnorm2(ba1)), xnorm2(a10))) <= eta) {
+                double bp[2] = {xsub(b[0], pt[0]), xsub(b[1], pt[1])};
+                double s = xdot2(bp, nl);
+                if (s > 0)
+                    count += 1;
+                else if (s < 0)
+                    count -= 1;
+            }
+        }
+    }
+    return count != 0;
+}
+
+// geometry.py:841-909 `_basic_visibility` (with _project_to_plane :561-612).
+__device__ bool exact_visibility(const double* vp, const double* ep, const double* sp, int nv, const double* n) {
+    const double eta = 1e-6;
+    bool vis_in = point_in_polygon(vp, sp, nv, n);
+    bool eval_in = point_in_polygon(ep, sp, nv, n);
+    if (!vis_in && !eval_in) {
+        double v[3] = {xsub(ep[0], vp[0]), xsub(ep[1], vp[1]), xsub(ep[2], vp[2])};
+        double dp = xdot3(v, n);
+        if (fabs(dp) > 1e-6) {
+            double w[3] = {xsub(ep[0], sp[0]), xsub(ep[1], sp[1]), xsub(ep[2], sp[2])};
+            double fac = -xdiv(xdot3(n, w), dp);
+            double pt[3];
+            for (int d = 0; d < 3; ++d) pt[d] = xadd(xadd(w[d], sp[d]), xmul(fac, v[d]));
+            if (point_in_polygon(pt, sp, nv, n)) {
+                double a[3] = {xsub(pt[0], vp[0]), xsub(pt[1], vp[1]), xsub(pt[2], vp[2])};
+                double b[3] = {xsub(pt[0], ep[0]), xsub(pt[1], ep[1]), xsub(pt[2], ep[2])};
+                if (xdot3(a, b) < 0) return false;
+            }
+        }
+        return true;
+    }
+    // geometry.py:895-906: each elif includes its half-space test, so a
+    // failed test falls through to the coplanar case
+    if (vis_in && !eval_in) {
+        double d[3] = {xsub(ep[0], vp[0]), xsub(ep[1], vp[1]), xsub(ep[2], vp[2])};
+        if (xdot3(n, d) < 0) return false;
+    } else if (!vis_in && eval_in) {
+        double d[3] = {xsub(vp[0], ep[0]), xsub(vp[1], ep[1]), xsub(vp[2], ep[2])};
+        if (xdot3(n, d) < 0) return false;
+    }
+    double a[3] = {xsub(vp[0], sp[0]), xsub(vp[1], sp[1]), xsub(vp[2], sp[2])};
+    double b[3] = {xsub(ep[0], sp[0]), xsub(ep[1], sp[1]), xsub(ep[2], sp[2])};
+    return !(fabs(xdot3(a, n)) < eta && fabs(xdot3(b, n)) < eta);
+}
+
+// Conservative segment/box overlap in FP32.  Boxes are already enlarged by a
+// margin that covers the predicate's 1e-6 tolerances and the FP32 rounding
+// of the segment end points, so a miss here proves the exact predicate
+// returns "visible" for every blocker inside the box.
+__device__ __forceinline__ bool seg_hits_box(const float* a, const float* d, const float* lo, const float* hi) {
+    float t0 = 0.0f, t1 = 1.0f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (d[k] == 0.0f) {
+            if (a[k] < lo[k] || a[k] > hi[k]) return false;
+        } else {
+            float inv = 1.0f / d[k];
+            float ta = (lo[k] - a[k]) * inv, tb = (hi[k] - a[k]) * inv;
+            float tn = fminf(ta, tb), tx = fmaxf(ta, tb);
+            t0 = fmaxf(t0, tn);
+            t1 = fminf(t1, tx);
+        }
+    }
+    return t0 <= t1 + 1e-5f;
+}
+
+__global__ void k_patch_geometry(int n, int nv, const double* __restrict__ pts, double* __restrict__ centers,
+                                 double* __restrict__ areas) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* p = pts + (size_t)i * nv * 3;
+    // geometry.py:412-413 `_calculate_center`: sequential sum then divide.
+    for (int d = 0; d < 3; ++d) {
+        double s = p[d];
+        for (int k = 1; k < nv; ++k) s = xadd(s, p[3 * k + d]);
+        centers[3 * i + d] = xdiv(s, (double)nv);
+    }
+    // geometry.py:420-448 `_polygon_area` (fan from vertex 0).
+    double area = 0.0;
+    for (int t = 0; t < nv - 2; ++t) {
+        const double* p1 = p + 3 * (t + 1);
+        const double* p2 = p + 3 * (t + 2);
+        double a[3] = {xsub(p1[0], p[0]), xsub(p1[1], p[1]), xsub(p1[2], p[2])};
+        double b[3] = {xsub(p2[0], p[0]), xsub(p2[1], p[1]), xsub(p2[2], p[2])};
+        double c[3];
+        xcross3(a, b, c);
+        area = xadd(area, xmul(0.5, xnorm3(c)));
+    }
+    areas[i] = area;
+}
+
+// Enlarged FP32 bounding boxes of every blocker and of every group of
+// kGroup consecutive blockers.  box layout: lo[3], hi[3].
+__global__ void k_blocker_boxes(int n, int nv, const double* __restrict__ pts, float margin,
+                                float* __restrict__ box, float* __restrict__ gbox) {
+    int g = blockIdx.x;
+    int lane = threadIdx.x;  // blockDim == kGroup
+    int s = g * kGroup + lane;
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    if (s < n) {
+        for (int k = 0; k < nv; ++k)
+            for (int d = 0; d < 3; ++d) {
+                double v = pts[((size_t)s * nv + k) * 3 + d];
+                lo[d] = fminf(lo[d], __double2float_rd(v));
+                hi[d] = fmaxf(hi[d], __double2float_ru(v));
+            }
+        for (int d = 0; d < 3; ++d) {
+            float m = margin + 4e-6f * fmaxf(fabsf(lo[d]), fabsf(hi[d]));
+            lo[d] -= m;
+            hi[d] += m;
+            box[6 * s + d] = lo[d];
+            box[6 * s + 3 + d] = hi[d];
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], off));
+            hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], off));
+        }
+    }
+    if (lane == 0)
+        for (int d = 0; d < 3; ++d) {
+            gbox[6 * g + d] = lo[d];
+            gbox[6 * g + 3 + d] = hi[d];
+        }
+}
+
+// geometry.py:750-797 `_check_patch2patch_visibility`.  One thread per pair
+// (i < j) of a 16 x 16 pair tile; blockers are all patches.
+__global__ void __launch_bounds__(256) k_patch_visibility(int n, int nv, const double* __restrict__ centers,
+                                                          const double* __restrict__ normals,
+                                                          const double* __restrict__ pts,
+                                                          const float* __restrict__ box,
+                                                          const float* __restrict__ gbox, int n_groups,
+                                                          uint8_t* __restrict__ vis) {
+    extern __shared__ float s_gbox[];
+    int tile_i = blockIdx.y, tile_j = blockIdx.x;
+    if (tile_j < tile_i) return;  // whole tile below the diagonal
+    int i = tile_i * 16 + (threadIdx.x >> 4);
+    int j = tile_j * 16 + (threadIdx.x & 15);
+    bool active = (i < n) && (j < n) && (i < j);
+    double ci[3] = {0, 0, 0}, cj[3] = {0, 0, 0};
+    float a[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+    if (active) {
+        for (int k = 0; k < 3; ++k) {
+            ci[k] = centers[3 * i + k];
+            cj[k] = centers[3 * j + k];
+            a[k] = (float)ci[k];
+            d[k] = (float)cj[k] - a[k];
+        }
+    }
+    bool visible = true;
+    for (int g0 = 0; g0 < n_groups; g0 += 1024) {
+        int cnt = min(1024, n_groups - g0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt * 6; t += blockDim.x) s_gbox[t] = gbox[6 * g0 + t];
+        __syncthreads();
+        if (!active || !visible) continue;
+        for (int g = 0; g < cnt && visible; ++g) {
+            if (!seg_hits_box(a, d, s_gbox + 6 * g, s_gbox + 6 * g + 3)) continue;
+            int s_end = min(n, (g0 + g + 1) * kGroup);
+            for (int s = (g0 + g) * kGroup; s < s_end; ++s) {
+                const float* bx = box + 6 * s;
+                float lo[3] = {bx[0], bx[1], bx[2]}, hi[3] = {bx[3], bx[4], bx[5]};
+                if (!seg_hits_box(a, d, lo, hi)) continue;
+                double nn[3] = {normals[3 * s], normals[3 * s + 1], normals[3 * s + 2]};
+                double sp[kMaxVerts * 3];
+                for (int k = 0; k < nv * 3; ++k) sp[k] = pts[(size_t)s * nv * 3 + k];
+                if (!exact_visibility(ci, cj, sp, nv, nn)) {
+                    visible = false;
+                    break;
+                }
+            }
+        }
+    }
+    if (i < n && j < n) vis[(size_t)i * n + j] = (active && visible) ? 1 : 0;
+}
+
+// geometry.py:799-839 `_check_point2patch_visibility`: point -> each patch
+// centre, blockers are the given surfaces (walls), tested in index order.
+__global__ void k_point_visibility(const double* __restrict__ point, int n, const double* __restrict__ centers,
+                                   int n_surf, int nv, const double* __restrict__ surf_pts,
+                                   const double* __restrict__ surf_normals, const float* __restrict__ sbox,
+                                   uint8_t* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double vp[3] = {point[0], point[1], point[2]};
+    double ep[3] = {centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]};
+    float a[3], d[3];
+    for (int k = 0; k < 3; ++k) {
+        a[k] = (float)vp[k];
+        d[k] = (float)ep[k] - a[k];
+    }
+    bool visible = true;
+    for (int s = 0; s < n_surf && visible; ++s) {
+        const float* bx = sbox + 6 * s;
+        float lo[3] = {bx[0], bx[1], bx[2]}, hi[3] = {bx[3], bx[4], bx[5]};
+        if (!seg_hits_box(a, d, lo, hi)) continue;
+        double nn[3] = {surf_normals[3 * s], surf_normals[3 * s + 1], surf_normals[3 * s + 2]};
+        double sp[kMaxVerts * 3];
+        for (int k = 0; k < nv * 3; ++k) sp[k] = surf_pts[(size_t)s * nv * 3 + k];
+        visible = exact_visibility(vp, ep, sp, nv, nn);
+    }
+    out[i] = visible ? 1 : 0;
+}
+
+// Row counts of a 0/1 matrix restricted to columns > row (upper) or all
+// columns (full).  One block per row.
+__global__ void k_row_counts(int n, const uint8_t* __restrict__ m, int upper, int32_t* __restrict__ counts) {
+    int r = blockIdx.x;
+    const uint8_t* row = m + (size_t)r * n;
+    int c0 = upper ? r + 1 : 0;
+    int cnt = 0;
+    for (int c = c0 + threadIdx.x; c < n; c += blockDim.x) cnt += row[c] ? 1 : 0;
+    for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+    __shared__ int s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        counts[r] = t;
+    }
+}
+
+// Exclusive scan of n counts into offsets[0..n] (single block, 1024 threads).
+__global__ void k_exclusive_scan(int n, const int32_t* __restrict__ counts, int64_t* __restrict__ offsets) {
+    __shared__ int64_t s_part[1024];
+    int tid = threadIdx.x;
+    int per = (n + 1023) / 1024;
+    int b = tid * per, e = min(n, b + per);
+    int64_t loc = 0;
+    for (int k = b; k < e; ++k) loc += counts[k];
+    s_part[tid] = loc;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        int64_t v = (tid >= off) ? s_part[tid - off] : 0;
+        __syncthreads();
+        s_part[tid] += v;
+        __syncthreads();
+    }
+    int64_t run = s_part[tid] - loc;
+    for (int k = b; k < e; ++k) {
+        offsets[k] = run;
+        run += counts[k];
+    }
+    if (tid == 1023) offsets[n] = s_part[1023];
+}
+
+// Ordered fill: entry (r, c) of a 0/1 matrix goes to slot offsets[r] + rank.
+// upper: pairs (r, c) with c > r written as int32 pairs + optional index map.
+// full:  column index written to cols[] and the row to rows[].
+__global__ void k_fill_rows(int n, const uint8_t* __restrict__ m, int upper, const int64_t* __restrict__ offsets,
+                            int32_t* __restrict__ pairs, int32_t* __restrict__ index_map,
+                            int32_t* __restrict__ cols, int32_t* __restrict__ rows) {
+    int r = blockIdx.x;
+    const uint8_t* row = m + (size_t)r * n;
+    int c0 = upper ? r + 1 : 0;
+    __shared__ int s_warp[32];
+    __shared__ int64_t s_base;
+    if (threadIdx.x == 0) s_base = offsets[r];
+    __syncthreads();
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int cb = c0; cb < n; cb += blockDim.x) {
+        int c = cb + threadIdx.x;
+        bool on = (c < n) && row[c];
+        unsigned bal = __ballot_sync(0xffffffffu, on);
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < nw; ++w) {
+            if (w < warp) before += s_warp[w];
+            total += s_warp[w];
+        }
+        if (on) {
+            int64_t slot = s_base + before + __popc(bal & ((1u << lane) - 1u));
+            if (upper) {
+                pairs[2 * slot] = r;
+                pairs[2 * slot + 1] = c;
+                if (index_map) index_map[(size_t)r * n + c] = (int32_t)slot;
+            } else {
+                cols[slot] = c;
+                rows[slot] = r;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_base += total;
+        __syncthreads();
+    }
+}
+
+// Symmetric visibility: S[i, j] = V[i, j] | V[j, i] (32 x 32 tiles).
+__global__ void k_symmetrize(int n, const uint8_t* __restrict__ v, uint8_t* __restrict__ s) {
+    __shared__ uint8_t tile[32][33];
+    int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+    for (int k = ty; k < 32; k += 8) {
+        int r = bx + k, c = by + tx;  // read the transposed block V[bx.., by..]
+        tile[k][tx] = (r < n && c < n) ? v[(size_t)r * n + c] : 0;
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        int r = by + k, c = bx + tx;
+        if (r < n && c < n) s[(size_t)r * n + c] = (v[(size_t)r * n + c] | tile[tx][k]) ? 1 : 0;
+    }
+}
+
+// Per directed pair (src i -> dst j): outgoing direction index of i toward j
+// (RadiosityFast.py:402-414), incoming index used by the ff_tilde BRDF row
+// (:1264-1268), centre distance (:538-543), the normalised-vector length
+// used for air attenuation (:1252-1262) and F'_ij (:1255-1256).
+__global__ void k_pair_setup(long long n_dir, int n, const int32_t* __restrict__ src, const int32_t* __restrict__ dst,
+                             const double* __restrict__ centers, const double* __restrict__ areas,
+                             const int32_t* __restrict__ pair_index, const double* __restrict__ ff,
+                             const int32_t* __restrict__ wall_of, int n_in, const double* __restrict__ dirs_in,
+                             int n_out, const double* __restrict__ dirs_out, int32_t* __restrict__ out_dir,
+                             int32_t* __restrict__ in_dir, double* __restrict__ dist, double* __restrict__ unit_len,
+                             double* __restrict__ fprime) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_dir) return;
+    int i = src[e], j = dst[e];
+    double ci[3] = {centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]};
+    double cj[3] = {centers[3 * j], centers[3 * j + 1], centers[3 * j + 2]};
+    int w = wall_of[i];
+    if (out_dir) out_dir[e] = (n_out > 0 && dirs_out) ? sp_nearest_dir(ci, cj, dirs_out + (size_t)w * n_out * 3, n_out) : 0;
+    if (in_dir) in_dir[e] = (n_in > 0 && dirs_in) ? sp_nearest_dir(cj, ci, dirs_in + (size_t)w * n_in * 3, n_in) : 0;
+    double dv[3] = {xsub(ci[0], cj[0]), xsub(ci[1], cj[1]), xsub(ci[2], cj[2])};
+    double dd = xnorm3(dv);
+    dist[e] = dd;
+    double u[3] = {xdiv(dv[0], dd), xdiv(dv[1], dd), xdiv(dv[2], dd)};
+    unit_len[e] = xnorm3(u);
+    double f;
+    if (i < j) {
+        f = ff[pair_index[(size_t)i * n + j]];
+    } else {
+        f = xdiv(xmul(ff[pair_index[(size_t)j * n + i]], areas[j]), areas[i]);
+    }
+    fprime[e] = f;
+}
+
+// Dense (N, N) outgoing-direction map with sentinel n_out where not visible
+// (RadiosityFast.py:402-414): out[i, j] = p2o(i -> j).
+__global__ void k_fill_i64(long long count, int64_t value, int64_t* __restrict__ out) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < count) out[e] = value;
+}
+__global__ void k_scatter_outdir(long long n_dir, int n, const int32_t* __restrict__ src, const int32_t* __restrict__ dst,
+                                 const int32_t* __restrict__ out_dir, int64_t* __restrict__ out) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_dir) return;
+    out[(size_t)src[e] * n + dst[e]] = out_dir[e];
+}
+
+__global__ void k_scatter_ff(long long n_pairs, int n, const int32_t* __restrict__ pairs, const double* __restrict__ ff,
+                             double* __restrict__ out) {
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    out[(size_t)pairs[2 * q] * n + pairs[2 * q + 1]] = ff[q];
+}
+
+// RadiosityFast.py:1234-1272 `_form_factors_with_directivity_dim`, dense
+// output (n, n, nd, nb): ((F' * exp(-att_b |u|)) * BRDF[slot_i, s_ij, o, b]).
+__global__ void k_ff_tilde(long long n_dir, int n, int nd, int nb, int n_in, const int32_t* __restrict__ src,
+                           const int32_t* __restrict__ dst, const int32_t* __restrict__ in_dir,
+                           const double* __restrict__ fprime, const double* __restrict__ unit_len,
+                           const double* __restrict__ att, const int32_t* __restrict__ wall_of,
+                           const int32_t* __restrict__ brdf_index, const double* __restrict__ brdf,
+                           double* __restrict__ out) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_dir) return;
+    int i = src[e], j = dst[e];
+    double* o_ = out + ((size_t)i * n + j) * nd * nb;
+    const double* row = brdf ? brdf + ((size_t)brdf_index[wall_of[i]] * n_in + in_dir[e]) * nd * nb : nullptr;
+    for (int o = 0; o < nd; ++o)
+        for (int b = 0; b < nb; ++b) {
+            double v = fprime[e];
+            if (att) v = v * exp(-att[b] * unit_len[e]);
+            if (row) v = v * row[(size_t)o * nb + b];
+            o_[(size_t)o * nb + b] = v;
+        }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sp_dense_form_factors(long long n_pairs, int n, const int32_t* pairs, const double* ff, double* out,
+                          void* stream) {
+    if (n_pairs < 0 || n < 0 || (n > 0 && !out) || (n_pairs > 0 && (!pairs || !ff))) return SP_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0) cudaMemsetAsync(out, 0, (size_t)n * n * sizeof(double), st);
+    if (n_pairs > 0) k_scatter_ff<<<sp_blocks(n_pairs, 256), 256, 0, st>>>(n_pairs, n, pairs, ff, out);
+    return sp_check_launch();
+}
+
+int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, const int32_t* src, const int32_t* dst,
+                          const int32_t* in_dir, const double* fprime, const double* unit_len, const double* att,
+                          const int32_t* wall_of, const int32_t* brdf_index, const double* brdf, double* out,
+                          void* stream) {
+    if (n_dir < 0 || n < 0 || nd < 1 || nb < 1 || (n > 0 && !out)) return SP_ERR_ARG;
+    if (brdf && (n_in < 1 || !in_dir || !wall_of || !brdf_index)) return SP_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0) cudaMemsetAsync(out, 0, (size_t)n * n * nd * nb * sizeof(double), st);
+    if (n_dir > 0)
+        k_ff_tilde<<<sp_blocks(n_dir, 128), 128, 0, st>>>(n_dir, n, nd, nb, n_in, src, dst, in_dir, fprime, unit_len,
+                                                          att, wall_of, brdf_index, brdf, out);
+    return sp_check_launch();
+}
+
+int sp_patch_geometry(int n, int nv, const double* pts, double* centers, double* areas, void* stream) {
+    if (n < 0 || nv < 3 || nv > kMaxVerts || (n > 0 && (!pts || !centers || !areas))) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    k_patch_geometry<<<sp_blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(n, nv, pts, centers, areas);
+    return sp_check_launch();
+}
+
+size_t sp_patch_visibility_workspace(int n) {
+    size_t groups = ((size_t)n + kGroup - 1) / kGroup;
+    return (size_t)n * 6 * sizeof(float) + groups * 6 * sizeof(float) + 256;
+}
+
+int sp_patch_visibility(int n, int nv, const double* centers, const double* normals, const double* pts,
+                        uint8_t* vis, void* ws, size_t ws_bytes, void* stream) {
+    if (n < 0 || nv < 3 || nv > kMaxVerts) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!centers || !normals || !pts || !vis || !ws) return SP_ERR_ARG;
+    if (ws_bytes < sp_patch_visibility_workspace(n)) return SP_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    int n_groups = (n + kGroup - 1) / kGroup;
+    float* box = (float*)ws;
+    float* gbox = box + (size_t)n * 6;
+    k_blocker_boxes<<<n_groups, kGroup, 0, st>>>(n, nv, pts, 1e-3f, box, gbox);
+    cudaMemsetAsync(vis, 0, (size_t)n * n, st);
+    int tiles = (n + 15) / 16;
+    dim3 grid(tiles, tiles);
+    k_patch_visibility<<<grid, 256, 1024 * 6 * sizeof(float), st>>>(n, nv, centers, normals, pts, box, gbox,
+                                                                     n_groups, vis);
+    return sp_check_launch();
+}
+
+size_t sp_point_visibility_workspace(int n_surf) {
+    size_t groups = ((size_t)n_surf + kGroup - 1) / kGroup;
+    return (size_t)n_surf * 6 * sizeof(float) + groups * 6 * sizeof(float) + 256;
+}
+
+int sp_point_visibility(const double* point, int n, const double* centers, int n_surf, int nv,
+                        const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws,
+                        size_t ws_bytes, void* stream) {
+    if (n < 0 || n_surf < 0 || nv < 3 || nv > kMaxVerts) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!point || !centers || !out || (n_surf > 0 && (!surf_pts || !surf_normals || !ws))) return SP_ERR_ARG;
+    if (n_surf > 0 && ws_bytes < sp_point_visibility_workspace(n_surf)) return SP_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    float* sbox = (float*)ws;
+    if (n_surf > 0) {
+        int n_groups = (n_surf + kGroup - 1) / kGroup;
+        k_blocker_boxes<<<n_groups, kGroup, 0, st>>>(n_surf, nv, surf_pts, 1e-3f, sbox, sbox + (size_t)n_surf * 6);
+    }
+    k_point_visibility<<<sp_blocks(n, 128), 128, 0, st>>>(point, n, centers, n_surf, nv, surf_pts, surf_normals,
+                                                          sbox, out);
+    return sp_check_launch();
+}
+
+int sp_visible_pairs(int n, const uint8_t* vis, int32_t* row_counts, int64_t* row_offset, int32_t* pairs,
+                     int32_t* pair_index, void* stream) {
+    if (n < 0 || (n > 0 && (!vis || !row_counts || !row_offset || !pairs))) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_row_counts<<<n, 256, 0, st>>>(n, vis, 1, row_counts);
+    k_exclusive_scan<<<1, 1024, 0, st>>>(n, row_counts, row_offset);
+    k_fill_rows<<<n, 256, 0, st>>>(n, vis, 1, row_offset, pairs, pair_index, nullptr, nullptr);
+    return sp_check_launch();
+}
+
+int sp_count_directed(int n, const uint8_t* vis, uint8_t* sym, int32_t* row_counts, int64_t* row_offset,
+                      void* stream) {
+    if (n < 0 || (n > 0 && (!vis || !sym || !row_counts || !row_offset))) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 g((n + 31) / 32, (n + 31) / 32), b(32, 8);
+    k_symmetrize<<<g, b, 0, st>>>(n, vis, sym);
+    k_row_counts<<<n, 256, 0, st>>>(n, sym, 0, row_counts);
+    k_exclusive_scan<<<1, 1024, 0, st>>>(n, row_counts, row_offset);
+    return sp_check_launch();
+}
+
+int sp_directed_pairs(int n, const uint8_t* sym, const int64_t* row_offset, int32_t* src, int32_t* dst,
+                      void* stream) {
+    if (n < 0 || (n > 0 && (!sym || !row_offset || !src || !dst))) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    k_fill_rows<<<n, 256, 0, (cudaStream_t)stream>>>(n, sym, 0, row_offset, nullptr, nullptr, src, dst);
+    return sp_check_launch();
+}
+
+int sp_pair_setup(long long n_dir, int n, const int32_t* src, const int32_t* dst, const double* centers,
+                  const double* areas, const int32_t* pair_index, const double* ff, const int32_t* wall_of,
+                  int n_in, const double* dirs_in, int n_out, const double* dirs_out, int32_t* out_dir,
+                  int32_t* in_dir, double* dist, double* unit_len, double* fprime, void* stream) {
+    if (n_dir < 0 || n < 0) return SP_ERR_ARG;
+    if (n_dir == 0) return SP_OK;
+    if (!src || !dst || !centers || !areas || !pair_index || !ff || !wall_of || !dist || !unit_len || !fprime)
+        return SP_ERR_ARG;
+    k_pair_setup<<<sp_blocks(n_dir, 128), 128, 0, (cudaStream_t)stream>>>(
+        n_dir, n, src, dst, centers, areas, pair_index, ff, wall_of, n_in, dirs_in, n_out, dirs_out, out_dir, in_dir,
+        dist, unit_len, fprime);
+    return sp_check_launch();
+}
+
+int sp_outgoing_index_map(long long n_dir, int n, const int32_t* src, const int32_t* dst, const int32_t* out_dir,
+                          int64_t sentinel, int64_t* out, void* stream) {
+    if (n_dir < 0 || n < 0 || (n > 0 && !out)) return SP_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    long long nn = (long long)n * n;
+    if (nn > 0) k_fill_i64<<<sp_blocks(nn, 256), 256, 0, st>>>(nn, sentinel, out);
+    if (n_dir > 0) k_scatter_outdir<<<sp_blocks(n_dir, 256), 256, 0, st>>>(n_dir, n, src, dst, out_dir, out);
+    return sp_check_launch();
+}
+
+}  // extern "C"

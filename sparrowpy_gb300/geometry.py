@@ -1,0 +1,189 @@
+"""Host-side scene description: polygons, wall patching, direction frames.
+
+These are the inputs of the GPU path: the reference builds them in Python as
+well (sparrowpy/geometry.py, sparrowpy/testing/stub_utils.py,
+sparrowpy/classes/RadiosityFast.py:971-986).  They run once per scene, not
+per solve.
+"""
+import numpy as np
+
+from .coords import Coordinates, _cart
+
+
+def _norm(v):
+    v = np.asarray(v, dtype=float)
+    return v / np.sqrt(np.dot(v, v))
+
+
+class Polygon:
+    """Planar polygon: points (n_points, 3), up vector and normal.
+
+    Mirrors sparrowpy/geometry.py:15-62 (checks: >= 3 points, coplanar
+    points, normal perpendicular to the plane).
+    """
+
+    def __init__(self, points, up_vector, normal):
+        self.pts = np.array(points, dtype=float)
+        normal = np.array(normal, dtype=float)
+        assert self.pts.shape[1] >= 3, 'You need at least 3 points to build a Polygon'
+        if self.pts.shape[0] > 3:
+            x_0 = self.pts[0]
+            for i in range(1, self.pts.shape[0] - 2):
+                det = np.linalg.det([x_0 - self.pts[i], x_0 - self.pts[i + 1], x_0 - self.pts[i + 2]])
+                assert abs(det) < 1e-10, 'Points must be in a plane to create a Polygon'
+        self.up_vector = _norm(up_vector)
+        calc_normal = _norm(np.cross(self.pts[0] - self.pts[1], self.pts[0] - self.pts[2]))
+        assert all(np.abs(np.cross(normal, calc_normal)) < 1e-10), \
+            'The normal vector is not perpendicular to the polygon'
+        self._normal = normal
+
+    @property
+    def normal(self):
+        return self._normal
+
+    @property
+    def n_points(self):
+        return self.pts.shape[0]
+
+    @property
+    def center(self):
+        return np.sum(self.pts, axis=0) / self.pts.shape[0]
+
+    @property
+    def area(self):
+        return float(calculate_area(self.pts[None])[0])
+
+    def to_dict(self):
+        return {'up_vector': self.up_vector.tolist(), 'pts': self.pts.tolist(), 'normal': self._normal.tolist()}
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(d['pts'], d['up_vector'], d['normal'])
+
+
+def shoebox_room_stub(length_x, length_y, length_z):
+    """Six inward-facing walls of a shoebox (sparrowpy/testing/stub_utils.py:5-48)."""
+    lx, ly, lz = length_x, length_y, length_z
+    return [
+        Polygon([[0, 0, 0], [lx, 0, 0], [lx, 0, lz], [0, 0, lz]], [1, 0, 0], [0, 1, 0]),
+        Polygon([[0, ly, 0], [lx, ly, 0], [lx, ly, lz], [0, ly, lz]], [1, 0, 0], [0, -1, 0]),
+        Polygon([[0, 0, 0], [lx, 0, 0], [lx, ly, 0], [0, ly, 0]], [1, 0, 0], [0, 0, 1]),
+        Polygon([[0, 0, lz], [lx, 0, lz], [lx, ly, lz], [0, ly, lz]], [1, 0, 0], [0, 0, -1]),
+        Polygon([[0, 0, 0], [0, 0, lz], [0, ly, lz], [0, ly, 0]], [0, 0, 1], [1, 0, 0]),
+        Polygon([[lx, 0, 0], [lx, 0, lz], [lx, ly, lz], [lx, ly, 0]], [0, 0, 1], [-1, 0, 0]),
+    ]
+
+
+def _patch_axes(polygon_points, max_size):
+    size = polygon_points.max(axis=0) - polygon_points.min(axis=0)
+    patch_nums = np.array([int(n) for n in size / max_size])
+    x_idx = y_idx = None
+    if patch_nums[2] == 0:
+        x_idx, y_idx = 0, 1
+    if patch_nums[1] == 0:
+        x_idx, y_idx = 0, 2
+    if patch_nums[0] == 0:
+        x_idx, y_idx = 1, 2
+    if x_idx is None:
+        raise ValueError("only axis-aligned rectangular walls can be patched")
+    return size, patch_nums, x_idx, y_idx
+
+
+def total_number_of_patches(polygon_points, max_size):
+    """sparrowpy/geometry.py:341-371 `_total_number_of_patches`."""
+    _, patch_nums, x_idx, y_idx = _patch_axes(np.asarray(polygon_points, float), max_size)
+    return int(patch_nums[x_idx] * patch_nums[y_idx])
+
+
+def create_patches(polygon_points, max_size):
+    """sparrowpy/geometry.py:373-410 `_create_patches` (axis-aligned walls)."""
+    polygon_points = np.asarray(polygon_points, dtype=float)
+    size, patch_nums, x_idx, y_idx = _patch_axes(polygon_points, max_size)
+    with np.errstate(divide='ignore', invalid='ignore'):
+        real_size = size / patch_nums
+    x_min = np.min(polygon_points.T[x_idx])
+    y_min = np.min(polygon_points.T[y_idx])
+    n = int(patch_nums[x_idx] * patch_nums[y_idx])
+    out = np.empty((n, 4, 3))
+    i = 0
+    for i_x in range(patch_nums[x_idx]):
+        for i_y in range(patch_nums[y_idx]):
+            points = polygon_points.copy()
+            points[0, x_idx] = x_min + i_x * real_size[x_idx]
+            points[0, y_idx] = y_min + i_y * real_size[y_idx]
+            points[1, x_idx] = x_min + (i_x + 1) * real_size[x_idx]
+            points[1, y_idx] = y_min + i_y * real_size[y_idx]
+            points[3, x_idx] = x_min + i_x * real_size[x_idx]
+            points[3, y_idx] = y_min + (i_y + 1) * real_size[y_idx]
+            points[2, x_idx] = x_min + (i_x + 1) * real_size[x_idx]
+            points[2, y_idx] = y_min + (i_y + 1) * real_size[y_idx]
+            out[i] = points
+            i += 1
+    return out
+
+
+def process_patches(walls_points, walls_normal, patch_size):
+    """sparrowpy/geometry.py:290-339 `_process_patches`.
+
+    Returns patches_points (n, 4, 3), patches_normal (n, 3), n_patches and
+    patch_to_wall_ids (n,).
+    """
+    walls_points = np.asarray(walls_points, dtype=float)
+    parts = [create_patches(walls_points[i], patch_size) for i in range(walls_points.shape[0])]
+    patches_points = np.concatenate(parts, axis=0) if parts else np.zeros((0, 4, 3))
+    patch_to_wall_ids = np.concatenate(
+        [np.full(p.shape[0], i, dtype=np.int64) for i, p in enumerate(parts)]) if parts else np.zeros(0, np.int64)
+    patches_normal = np.asarray(walls_normal, dtype=float)[patch_to_wall_ids, :]
+    return patches_points, patches_normal, patches_points.shape[0], patch_to_wall_ids
+
+
+def calculate_center(points):
+    """sparrowpy/geometry.py:412-413 (host copy used by the properties)."""
+    points = np.asarray(points, dtype=float)
+    return np.sum(points, axis=-2) / points.shape[-2]
+
+
+def calculate_size(points):
+    """sparrowpy/geometry.py:415-418."""
+    points = np.asarray(points, dtype=float)
+    vec1 = points[..., 0, :] - points[..., 1, :]
+    vec2 = points[..., 1, :] - points[..., 2, :]
+    return np.abs(vec1 - vec2)
+
+
+def calculate_area(points):
+    """sparrowpy/geometry.py:420-448 (fan triangulation, host copy)."""
+    points = np.asarray(points, dtype=float)
+    area = np.zeros(points.shape[0])
+    for t in range(points.shape[1] - 2):
+        c = np.cross(points[:, t + 1] - points[:, 0], points[:, t + 2] - points[:, 0])
+        area += .5 * np.sqrt(np.sum(c * c, axis=-1))
+    return area
+
+
+def wall_frame(normal, up_vector):
+    """Rotation taking the BRDF frame (normal +z, up +x) to a wall's frame.
+
+    RadiosityFast.py:971-986 builds it from two pyfar orientations
+    (view/up); the result maps local z to the wall normal, local x to the
+    up vector and local y to normal x up.  Columns: (up, n x up, n).
+    """
+    n = _norm(normal)
+    up = _norm(up_vector)
+    return np.stack([up, np.cross(n, up), n], axis=1)
+
+
+def rotate_coords_to_normal(wall_normal, wall_up_vector, sources, receivers):
+    """RadiosityFast.py:971-986 `_rotate_coords_to_normal`.
+
+    Rotates both direction sets into the wall frame and normalises them to
+    radius 1.  Returns Coordinates copies (weights kept).
+    """
+    rot = wall_frame(wall_normal, wall_up_vector)
+    out = []
+    for c in (sources, receivers):
+        xyz = _cart(c).reshape(-1, 3) @ rot.T
+        xyz = xyz / np.sqrt(np.sum(xyz * xyz, axis=-1))[:, None]
+        w = getattr(c, "weights", None)
+        out.append(Coordinates.from_cartesian(xyz, weights=None if w is None else np.asarray(w).reshape(-1)))
+    return out[0], out[1]

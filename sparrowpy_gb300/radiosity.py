@@ -1,0 +1,808 @@
+"""GB300 DirectionalRadiosityFast: the reference API over the CUDA library.
+
+Drop-in for sparrowpy/classes/RadiosityFast.py:15-968.  Method names,
+arguments, attribute names, error types and messages follow the reference;
+the numeric work of every step runs in libsparrow_gb300.so on one CUDA
+device (device memory and the stream come from PyTorch):
+
+=============================  ==============================================
+reference step                 CUDA entry points
+=============================  ==============================================
+bake_geometry  :369-433        sp_patch_geometry, sp_patch_visibility,
+                               sp_visible_pairs, sp_form_factors,
+                               sp_count_directed/sp_directed_pairs,
+                               sp_pair_setup
+init_source_energy :436-522    sp_point_visibility, sp_source_energy
+calculate_energy_exchange      sp_energy_exchange
+  :524-568
+collect_energy_receiver_*      sp_point_visibility, sp_receiver_factors,
+  :570-752                     sp_collect_receiver
+=============================  ==============================================
+
+`form_factors_tilde` (N, N, D, B) is never needed by the solver; the
+attribute is materialised on access (sp_form_factors_tilde).
+
+Extra keyword (not in the reference): ``precision`` = "fp32" (default; FP32
+exchange and Stokes form factors, FP64 for shared-vertex and near pairs) or
+"fp64" (FP64 throughout).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import geometry as geo
+from .coords import Coordinates, FrequencyData, TimeData, _cart, is_coordinates
+
+_PREC = {"fp32": nat.SP_F32, "fp64": nat.SP_F64}
+
+
+def _ptr(t):
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def analyse_brdf(brdf, rel_tol=1e-12):
+    """Factor BRDF tables as scale[slot, b] * (diff[g, s, b] + spec[g, s, b] [o == m[g, s]]).
+
+    brdf: (n_slots, n_in, n_out, n_bins).  Returns None when some row has
+    more than one outgoing direction off the row's common value (the dense
+    exchange is used then), else a dict with slot_group (S,), slot_scale
+    (S, B), n_groups, class_diff / class_spec (G * n_in, B), class_target
+    (G * n_in,) (-1 = no mirror term).
+    """
+    brdf = np.asarray(brdf, dtype=float)
+    S, Din, Dout, B = brdf.shape
+    big = np.max(np.abs(brdf)) if brdf.size else 0.0
+    tol = rel_tol * max(big, 1e-300)
+    if Dout == 1:
+        diff = brdf[:, :, 0, :]
+        spec = np.zeros_like(diff)
+        target = -np.ones((S, Din), dtype=np.int64)
+    else:
+        if Dout >= 3:
+            diff = np.sort(brdf, axis=2)[:, :, Dout // 2, :]
+        else:
+            diff = brdf[:, :, 0, :]
+        dev = brdf - diff[:, :, None, :]
+        out = np.abs(dev) > tol
+        if np.any(out.sum(axis=2) > 1):
+            return None
+        any_out = out.any(axis=3)
+        if np.any(any_out.sum(axis=2) > 1):
+            return None
+        has = any_out.any(axis=2)
+        target = np.where(has, np.argmax(any_out, axis=2), -1)
+        tsafe = np.where(has, target, 0)
+        spec = np.take_along_axis(dev, tsafe[:, :, None, None], axis=2)[:, :, 0, :]
+        spec = np.where(has[:, :, None], spec, 0.0)
+    scale = np.max(np.abs(brdf), axis=(1, 2))
+    scale = np.where(scale > 0, scale, 1.0)
+    nd = diff / scale[:, None, :]
+    ns = spec / scale[:, None, :]
+    key = np.concatenate([np.round(nd.reshape(S, -1), 12), np.round(ns.reshape(S, -1), 12),
+                          target.reshape(S, -1).astype(float)], axis=1)
+    _, first, inverse = np.unique(key, axis=0, return_index=True, return_inverse=True)
+    inverse = inverse.reshape(-1)
+    G = first.size
+    reps = first
+    class_diff = nd[reps].reshape(G * Din, B)
+    class_spec = ns[reps].reshape(G * Din, B)
+    class_target = target[reps].reshape(G * Din)
+    return dict(slot_group=inverse.astype(np.int32), slot_scale=scale.astype(float), n_groups=int(G),
+                class_diff=np.ascontiguousarray(class_diff), class_spec=np.ascontiguousarray(class_spec),
+                class_target=class_target.astype(np.int32))
+
+
+class DirectionalRadiosityFast:
+    """Radiosity object for directional scattering coefficients (GB300)."""
+
+    def __init__(self, walls_points, walls_normal, walls_up_vector, patches_points, n_patches, patch_to_wall_ids,
+                 visibility_matrix=None, visible_patches=None, form_factors=None, form_factors_tilde=None,
+                 frequencies=None, brdf=None, brdf_index=None, brdf_incoming_directions=None,
+                 brdf_outgoing_directions=None, patch_2_brdf_outgoing_index=None, air_attenuation=None,
+                 speed_of_sound=None, etc_time_resolution=None, etc_duration=None, distance_patches_to_source=None,
+                 energy_init_source=None, energy_exchange_etc=None, *, precision="fp32", device=None):
+        if precision not in _PREC:
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.precision = precision
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device()) \
+            if torch.cuda.is_available() else torch.device("cuda")
+        walls_points = np.atleast_3d(np.asarray(walls_points, dtype=float))
+        self._walls_points = walls_points
+        self._walls_normal = np.atleast_2d(np.asarray(walls_normal, dtype=float))
+        self._walls_up_vector = np.atleast_2d(np.asarray(walls_up_vector, dtype=float))
+        self._patches_points = np.atleast_3d(np.asarray(patches_points, dtype=float))
+        self._n_patches = int(n_patches)
+        self._patch_to_wall_ids = np.atleast_1d(np.array(patch_to_wall_ids, dtype=int))
+        self._frequencies = None if frequencies is None else np.array(frequencies)
+        self._brdf = None if brdf is None else [np.array(b) for b in brdf]
+        self._brdf_index = None if brdf_index is None else np.array(brdf_index, dtype=np.int64)
+        self._brdf_incoming_directions = brdf_incoming_directions
+        self._brdf_outgoing_directions = brdf_outgoing_directions
+        self._air_attenuation = None if air_attenuation is None else np.array(air_attenuation, dtype=float)
+        self._speed_of_sound = None if speed_of_sound is None else float(speed_of_sound)
+        self._etc_time_resolution = None if etc_time_resolution is None else float(etc_time_resolution)
+        self._etc_duration = None if etc_duration is None else float(etc_duration)
+        self._source = None
+        # host copies of results (filled lazily from the device, or given)
+        self._host = {}
+        for key, val in (("visibility_matrix", visibility_matrix), ("visible_patches", visible_patches),
+                         ("form_factors", form_factors), ("form_factors_tilde", form_factors_tilde),
+                         ("patch_2_brdf_outgoing_index", patch_2_brdf_outgoing_index),
+                         ("distance_patches_to_source", distance_patches_to_source),
+                         ("energy_init_source", energy_init_source), ("energy_exchange_etc", energy_exchange_etc)):
+            if val is not None:
+                self._host[key] = np.array(val)
+        self._dev = {}      # device tensors of the current geometry / results
+        self._bake = None   # device state of the last bake
+        self.check()
+
+    # ------------------------------------------------------------ validation
+    def check(self):
+        """Check the input data for consistency (RadiosityFast.py:211-337)."""
+        n_walls = self._walls_points.shape[0]
+        if self._walls_points.shape[2] != 3:
+            raise ValueError("Walls need to be of shape (n_walls, n_points, 3)")
+        if self._walls_up_vector.shape != (n_walls, 3):
+            raise ValueError("Up vector of walls need to be of shape (n_walls, 3)")
+        if self._walls_normal.shape != (n_walls, 3):
+            raise ValueError("Normal of walls need to be of shape (n_walls, 3)")
+        if (self._patches_points.shape[0] != self.n_patches) or (self._patches_points.shape[2] != 3):
+            raise ValueError("Patches need to be of shape (n_patches, n_points, 3)")
+        if self._patch_to_wall_ids.shape != (self.n_patches,):
+            raise ValueError("patch_to_wall_ids need to be of shape (n_patches,)")
+        ids = set(self._patch_to_wall_ids.tolist())
+        if any(i not in range(n_walls) for i in ids) or any(i not in ids for i in range(n_walls)):
+            raise ValueError("patch_to_wall_ids does contain other ids than range(n_walls)")
+        n_bins = 1
+        if self._frequencies is not None:
+            if len(self._frequencies.shape) != 1:
+                raise ValueError("Frequencies need to be of shape (n_bins,)")
+            n_bins = self._frequencies.size
+        ff = self._host.get("form_factors")
+        if ff is not None and ff.shape != (self.n_patches, self.n_patches):
+            raise ValueError("form_factors need to be of shape (n_patches, n_patches)")
+        n_out = 1
+        if self._brdf_index is not None and len(self._brdf_index) != n_walls:
+            raise ValueError("brdf_index need to be of shape (n_walls,)")
+        if self._brdf_incoming_directions is not None:
+            if any(not is_coordinates(i) for i in self._brdf_incoming_directions):
+                raise ValueError("brdf_incoming_directions need to be a list of type pf.Coordinates")
+        if self._brdf_outgoing_directions is not None:
+            if any(not is_coordinates(i) for i in self._brdf_outgoing_directions):
+                raise ValueError("brdf_outgoing_directions need to be a list of type pf.Coordinates")
+            n_out = self._brdf_outgoing_directions[0].csize
+        fft = self._host.get("form_factors_tilde")
+        if fft is not None and fft.shape != (self.n_patches, self.n_patches, n_out, n_bins):
+            raise ValueError("form_factors_tilde need to be of shape "
+                             "(n_patches, n_patches, n_outgoing_directions, n_bins)")
+        if self._air_attenuation is not None:
+            if len(self._air_attenuation.shape) != 1 or self._air_attenuation.shape[0] != n_bins:
+                raise ValueError("Air attenuation need to be of shape (n_bins,)")
+        if self._speed_of_sound is not None and self._speed_of_sound <= 0:
+            raise ValueError("Speed of sound must be positive and non-zero")
+        if self._etc_time_resolution is not None and self._etc_time_resolution <= 0:
+            raise ValueError("Time resolution must be positive and non-zero")
+        if self._etc_duration is not None and self._etc_duration <= 0:
+            raise ValueError("Duration must be positive and non-zero")
+        d0 = self._host.get("distance_patches_to_source")
+        if d0 is not None and d0.shape != (self.n_patches,):
+            raise ValueError("distance_patches_to_source need to be of shape (n_patches,)")
+        e0 = self._host.get("energy_init_source")
+        if e0 is not None and e0.shape != (self.n_patches, n_out, n_bins):
+            raise ValueError("energy_init_source need to be of shape (n_patches, n_outgoing_directions, n_bins)")
+        etc = self._host.get("energy_exchange_etc")
+        if etc is not None:
+            n_samples = int(self._etc_duration / self._etc_time_resolution)
+            if etc.shape != (self.n_patches, n_out, n_bins, n_samples):
+                raise ValueError("energy_exchange_etc need to be of shape "
+                                 "(n_patches, n_outgoing_directions, n_bins, n_samples)")
+
+    # -------------------------------------------------------------- creation
+    @classmethod
+    def from_polygon(cls, polygon_list, patch_size, *, precision="fp32", device=None):
+        """Create the object from wall polygons (RadiosityFast.py:340-367)."""
+        walls_points = np.array([p.pts for p in polygon_list])
+        walls_normal = np.array([p.normal for p in polygon_list])
+        walls_up_vector = np.array([p.up_vector for p in polygon_list])
+        patches_points, _, n_patches, patch_to_wall_ids = geo.process_patches(walls_points, walls_normal, patch_size)
+        return cls(walls_points, walls_normal, walls_up_vector, patches_points, n_patches, patch_to_wall_ids,
+                   precision=precision, device=device)
+
+    # ---------------------------------------------------------- device state
+    def _t(self, arr, dtype):
+        return torch.as_tensor(np.ascontiguousarray(arr), dtype=dtype).to(self.device, non_blocking=False)
+
+    def _geometry(self):
+        d = self._dev
+        if "pts" not in d:
+            n = self.n_patches
+            d["pts"] = self._t(self._patches_points, torch.float64)
+            d["normals"] = self._t(self.patches_normal, torch.float64)
+            d["wall_of"] = self._t(self._patch_to_wall_ids, torch.int32)
+            d["walls_pts"] = self._t(self._walls_points, torch.float64)
+            d["walls_normal"] = self._t(self._walls_normal, torch.float64)
+            d["centers"] = torch.empty((n, 3), dtype=torch.float64, device=self.device)
+            d["areas"] = torch.empty((n,), dtype=torch.float64, device=self.device)
+            nat.call("sp_patch_geometry", n, self._patches_points.shape[1], _ptr(d["pts"]), _ptr(d["centers"]),
+                     _ptr(d["areas"]), _stream())
+        return d
+
+    def _brdf_device(self):
+        """Device copies of the current BRDF tables and direction sets."""
+        if self._brdf_incoming_directions is None:
+            return None
+        key = (id(self._brdf), len(self._brdf), tuple(self._brdf_index.tolist()))
+        cached = self._dev.get("brdf_state")
+        if cached is not None and cached["key"] == key:
+            return cached
+        if np.any(self._brdf_index < 0):
+            raise ValueError("every wall needs a BRDF (set_wall_brdf) before this step")
+        din = np.array([_cart(c).reshape(-1, 3) for c in self._brdf_incoming_directions])
+        dout = np.array([_cart(c).reshape(-1, 3) for c in self._brdf_outgoing_directions])
+        slots = []
+        for b in self._brdf:
+            b = np.asarray(b, dtype=float)
+            if b.ndim == 1:  # default BRDF: one value per band (RadiosityFast.py:459-467)
+                b = b.reshape(1, 1, -1)
+            slots.append(b)
+        brdf = np.array(slots, dtype=float)
+        state = dict(key=key, n_in=din.shape[1], n_out=dout.shape[1], n_slots=brdf.shape[0], brdf_host=brdf,
+                     dirs_in=self._t(din, torch.float64), dirs_out=self._t(dout, torch.float64),
+                     brdf=self._t(brdf, torch.float64), brdf_index=self._t(self._brdf_index, torch.int32))
+        self._dev["brdf_state"] = state
+        return state
+
+    # ------------------------------------------------------------------ bake
+    def bake_geometry(self):
+        """Bake the geometry by calculating all the form factors (RadiosityFast.py:369-433)."""
+        if self._patches_points.shape[1] != 4:
+            raise NotImplementedError("the form factor kernels support quadrilateral patches only")
+        d = self._geometry()
+        n = self.n_patches
+        nv = self._patches_points.shape[1]
+        st = _stream()
+        dev = self.device
+        # visibility (geometry.py:750-797)
+        vis = torch.empty((n, n), dtype=torch.uint8, device=dev)
+        wsz = nat.size("sp_patch_visibility_workspace", n)
+        ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=dev)
+        nat.call("sp_patch_visibility", n, nv, _ptr(d["centers"]), _ptr(d["normals"]), _ptr(d["pts"]), _ptr(vis),
+                 _ptr(ws), wsz, st)
+        # visible pair list (RadiosityFast.py:377-387)
+        cap = max(n * (n - 1) // 2, 1)
+        pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+        pair_index = torch.full((n, n), -1, dtype=torch.int32, device=dev)
+        row_counts = torch.empty((max(n, 1),), dtype=torch.int32, device=dev)
+        row_off = torch.empty((n + 1,), dtype=torch.int64, device=dev)
+        nat.call("sp_visible_pairs", n, _ptr(vis), _ptr(row_counts), _ptr(row_off), _ptr(pairs), _ptr(pair_index), st)
+        n_vis = int(row_off[n].item()) if n > 0 else 0
+        pairs = pairs[:n_vis].contiguous()
+        # form factors (universal.py:12-52)
+        ff = torch.zeros((max(n_vis, 1),), dtype=torch.float64, device=dev)
+        method = torch.zeros((max(n_vis, 1),), dtype=torch.uint8, device=dev)
+        nat.call("sp_form_factors", _PREC[self.precision], n_vis, _ptr(pairs), _ptr(d["pts"]), _ptr(d["normals"]),
+                 _ptr(d["areas"]), _ptr(ff), _ptr(method), st)
+        # directed pairs, destination-major (RadiosityFast.py:1124-1131)
+        sym = torch.empty((n, n), dtype=torch.uint8, device=dev)
+        dcounts = torch.empty((max(n, 1),), dtype=torch.int32, device=dev)
+        dst_off = torch.empty((n + 1,), dtype=torch.int64, device=dev)
+        nat.call("sp_count_directed", n, _ptr(vis), _ptr(sym), _ptr(dcounts), _ptr(dst_off), st)
+        n_dir = int(dst_off[n].item()) if n > 0 else 0
+        src = torch.empty((max(n_dir, 1),), dtype=torch.int32, device=dev)
+        dst = torch.empty((max(n_dir, 1),), dtype=torch.int32, device=dev)
+        nat.call("sp_directed_pairs", n, _ptr(sym), _ptr(dst_off), _ptr(src), _ptr(dst), st)
+        del sym
+        # per-pair directions, distances and F' (RadiosityFast.py:402-414, 1234-1272, 538-543)
+        bs = self._brdf_device()
+        out_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
+        in_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
+        dist = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
+        unit_len = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
+        fprime = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
+        nat.call("sp_pair_setup", n_dir, n, _ptr(src), _ptr(dst), _ptr(d["centers"]), _ptr(d["areas"]),
+                 _ptr(pair_index), _ptr(ff), _ptr(d["wall_of"]),
+                 bs["n_in"] if bs else 0, _ptr(bs["dirs_in"]) if bs else _ptr(None),
+                 bs["n_out"] if bs else 0, _ptr(bs["dirs_out"]) if bs else _ptr(None),
+                 _ptr(out_dir), _ptr(in_dir), _ptr(dist), _ptr(unit_len), _ptr(fprime), st)
+        att = None if self._air_attenuation is None else self._t(self._air_attenuation, torch.float64)
+        n_bins = 1 if self._frequencies is None else self.n_bins
+        self._bake = dict(vis=vis, pairs=pairs, pair_index=pair_index, n_vis=n_vis, ff=ff, ff_method=method,
+                          dst_off=dst_off, src=src, dst=dst, n_dir=n_dir, out_dir=out_dir, in_dir=in_dir, dist=dist,
+                          unit_len=unit_len, fprime=fprime, brdf=bs, att=att, n_bins=n_bins,
+                          n_out=bs["n_out"] if bs else 1)
+        for k in ("visibility_matrix", "visible_patches", "form_factors", "form_factors_tilde",
+                  "patch_2_brdf_outgoing_index"):
+            self._host.pop(k, None)
+
+    # ---------------------------------------------------------------- source
+    def init_source_energy(self, source):
+        """Initialize the source energy (RadiosityFast.py:436-522)."""
+        if is_coordinates(source):
+            if tuple(source.cshape) != (1,):
+                raise ValueError('just one source position is allowed.')
+            source_position = np.asarray(source.cartesian, dtype=float).reshape(-1, 3)[0]
+        elif hasattr(source, "position"):
+            source_position = np.asarray(source.position, dtype=float).reshape(3)
+        else:
+            raise ValueError("source must be a Coordinates or a SoundSource")
+        self._source = source
+        if self._brdf_incoming_directions is None:
+            frequencies = np.array([0]) if self._frequencies is None else self._frequencies
+            self.set_wall_brdf(np.arange(self.n_walls), FrequencyData(np.ones_like(frequencies, dtype=float),
+                                                                      frequencies),
+                               Coordinates(0, 0, 1, weights=1), Coordinates(0, 0, 1, weights=1))
+            self._frequencies = frequencies
+        if self._air_attenuation is None:
+            frequencies = np.array([0]) if self._frequencies is None else self._frequencies
+            self.set_air_attenuation(FrequencyData(np.zeros_like(frequencies, dtype=float), frequencies))
+            self._frequencies = frequencies
+        d = self._geometry()
+        bs = self._brdf_device()
+        n, nb = self.n_patches, self.n_bins
+        st = _stream()
+        dev = self.device
+        src = self._t(source_position, torch.float64)
+        svis = self._point_visibility(src)
+        att = self._t(self._air_attenuation, torch.float64)
+        e0 = torch.empty((n, nb), dtype=torch.float64, device=dev)
+        d0 = torch.empty((n,), dtype=torch.float64, device=dev)
+        e0dir = torch.empty((n, bs["n_out"], nb), dtype=torch.float64, device=dev)
+        nat.call("sp_source_energy", _ptr(src), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(svis), nb, _ptr(att),
+                 _ptr(d["wall_of"]), _ptr(bs["brdf_index"]), bs["n_in"], _ptr(bs["dirs_in"]), bs["n_out"],
+                 _ptr(bs["brdf"]), _ptr(e0), _ptr(d0), _ptr(e0dir), st)
+        directivity = getattr(source, "directivity", None)
+        if directivity is not None and hasattr(source, "get_directivity"):
+            centers = self.patches_center
+            fac = np.stack([np.real(source.get_directivity(centers, self._frequencies[b])) for b in range(nb)], axis=-1)
+            e0dir *= self._t(fac, torch.float64)[:, None, :]
+        self._dev["svis"] = svis
+        self._dev["e0dir"] = e0dir
+        self._dev["d0"] = d0
+        for k in ("distance_patches_to_source", "energy_init_source"):
+            self._host.pop(k, None)
+
+    def _point_visibility(self, point_dev):
+        d = self._geometry()
+        n = self.n_patches
+        out = torch.empty((max(n, 1),), dtype=torch.uint8, device=self.device)
+        nw = self.n_walls
+        wsz = nat.size("sp_point_visibility_workspace", nw)
+        ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=self.device)
+        nat.call("sp_point_visibility", _ptr(point_dev), n, _ptr(d["centers"]), nw, self._walls_points.shape[1],
+                 _ptr(d["walls_pts"]), _ptr(d["walls_normal"]), _ptr(out), _ptr(ws), wsz, _stream())
+        return out
+
+    # -------------------------------------------------------------- exchange
+    def _exchange_plan(self):
+        bk = self._bake
+        if bk is None:
+            raise ValueError("bake_geometry() must run before calculate_energy_exchange()")
+        if "plan" in bk:
+            return bk["plan"]
+        bs = bk["brdf"]
+        n_bins = bk["n_bins"]
+        if bs is None:
+            brdf = np.ones((1, 1, 1, n_bins))
+            plan = dict(brdf=self._t(brdf, torch.float64), brdf_index=self._t(np.zeros(self.n_walls), torch.int32),
+                        n_slots=1, n_in=1, n_out=1, host=brdf)
+        else:
+            plan = dict(brdf=bs["brdf"], brdf_index=bs["brdf_index"], n_slots=bs["n_slots"], n_in=bs["n_in"],
+                        n_out=bs["n_out"], host=bs["brdf_host"])
+        st = analyse_brdf(plan["host"])
+        if st is not None and st["n_groups"] * plan["n_in"] <= 8192:
+            plan["structured"] = dict(
+                slot_group=self._t(st["slot_group"], torch.int32), slot_scale=self._t(st["slot_scale"], torch.float64),
+                n_groups=st["n_groups"], class_diff=self._t(st["class_diff"], torch.float64),
+                class_spec=self._t(st["class_spec"], torch.float64),
+                class_target=self._t(st["class_target"], torch.int32))
+        bk["plan"] = plan
+        return plan
+
+    def calculate_energy_exchange(self, speed_of_sound, etc_time_resolution, etc_duration, max_reflection_order=-1,
+                                  recalculate=False, *, algorithm="auto"):
+        """Calculate the energy exchange between patches (RadiosityFast.py:524-568)."""
+        n_samples = int(etc_duration / etc_time_resolution)
+        if self._dev.get("etc") is None and self._host.get("energy_exchange_etc") is None or recalculate:
+            if "e0dir" not in self._dev:
+                if self._host.get("energy_init_source") is None:
+                    raise ValueError("init_source_energy() must run before calculate_energy_exchange()")
+                self._dev["e0dir"] = self._t(self._host["energy_init_source"], torch.float64)
+                self._dev["d0"] = self._t(self._host["distance_patches_to_source"], torch.float64)
+            self._run_exchange(float(speed_of_sound), float(etc_time_resolution), n_samples,
+                               int(max_reflection_order), algorithm)
+            self._host.pop("energy_exchange_etc", None)
+        self._etc_time_resolution = float(etc_time_resolution)
+        self._speed_of_sound = float(speed_of_sound)
+        self._etc_duration = float(etc_duration)
+
+    def _exchange_args(self, c, dt, n_samples, max_order, algorithm, etc):
+        bk = self._bake
+        plan = self._exchange_plan()
+        d = self._geometry()
+        e0dir, d0 = self._dev["e0dir"], self._dev["d0"]
+        n, nd, nb = e0dir.shape
+        if nd != plan["n_out"] or nb != bk["n_bins"]:
+            raise ValueError("the BRDF directions/bands changed after bake_geometry(); bake again")
+        use_struct = "structured" in plan and algorithm in ("auto", "structured")
+        if algorithm == "structured" and "structured" not in plan:
+            raise ValueError("BRDF tables are not of the diffuse-plus-mirror form")
+        a = nat.ExchangeArgs()
+        a.precision = _PREC[self.precision]
+        a.algorithm = nat.SP_EXCHANGE_STRUCTURED if use_struct else nat.SP_EXCHANGE_DENSE
+        a.n_patches, a.n_dirs, a.n_bins, a.n_samples, a.max_order = n, nd, nb, n_samples, max_order
+        a.energy_0_dir = e0dir.data_ptr()
+        a.distance_0 = d0.data_ptr()
+        a.n_dir_pairs = bk["n_dir"]
+        a.dst_offset = bk["dst_off"].data_ptr()
+        a.pair_src = bk["src"].data_ptr()
+        a.pair_out_dir = bk["out_dir"].data_ptr()
+        a.pair_in_dir = bk["in_dir"].data_ptr()
+        a.pair_distance = bk["dist"].data_ptr()
+        a.pair_fprime = bk["fprime"].data_ptr()
+        a.pair_unit_len = bk["unit_len"].data_ptr()
+        a.air_attenuation = bk["att"].data_ptr() if bk["att"] is not None else None
+        a.wall_of = d["wall_of"].data_ptr()
+        a.brdf_index = plan["brdf_index"].data_ptr()
+        a.n_slots, a.n_in_dirs = plan["n_slots"], plan["n_in"]
+        a.brdf = plan["brdf"].data_ptr()
+        a.speed_of_sound, a.time_resolution = c, dt
+        a.etc_total = etc.data_ptr()
+        if use_struct:
+            s = plan["structured"]
+            a.slot_group = s["slot_group"].data_ptr()
+            a.slot_scale = s["slot_scale"].data_ptr()
+            a.n_groups = s["n_groups"]
+            a.class_diff = s["class_diff"].data_ptr()
+            a.class_spec = s["class_spec"].data_ptr()
+            a.class_target = s["class_target"].data_ptr()
+        return a
+
+    def _run_exchange(self, c, dt, n_samples, max_order, algorithm="auto"):
+        e0dir = self._dev["e0dir"]
+        n, nd, nb = e0dir.shape
+        dtype = torch.float32 if self.precision == "fp32" else torch.float64
+        etc = torch.empty((n, nd, nb, n_samples), dtype=dtype, device=self.device)
+        a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
+        wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
+                       a.n_dir_pairs, a.n_slots, a.n_in_dirs)
+        ws = self._workspace(wsz)
+        rc = nat.lib().sp_energy_exchange(ctypes.byref(a), _ptr(ws), wsz, _stream())
+        if rc == nat.SP_ERR_RANGE:
+            raise IndexError("a source delay exceeds the histogram length (index out of bounds)")
+        if rc != nat.SP_OK:
+            raise nat.NativeError("sp_energy_exchange", rc)
+        self._dev["etc"] = etc
+
+    def _workspace(self, nbytes):
+        ws = self._dev.get("ws")
+        if ws is None or ws.numel() < nbytes:
+            self._dev.pop("ws", None)
+            ws = torch.empty((max(nbytes, 1),), dtype=torch.uint8, device=self.device)
+            self._dev["ws"] = ws
+        return ws
+
+    def _etc_device(self):
+        etc = self._dev.get("etc")
+        if etc is None:
+            host = self._host.get("energy_exchange_etc")
+            if host is None:
+                raise ValueError("calculate_energy_exchange() must run first")
+            dtype = torch.float32 if self.precision == "fp32" else torch.float64
+            etc = self._t(host, dtype)
+            self._dev["etc"] = etc
+        return etc
+
+    # ------------------------------------------------------------- receivers
+    def collect_energy_receiver_mono(self, receivers, direct_sound=False):
+        """Collect the energy at the receivers (RadiosityFast.py:570-602)."""
+        if not isinstance(direct_sound, bool):
+            raise ValueError("direct_sound must be of type boolean")
+        etc = self._collect(receivers, patchwise=False)
+        if direct_sound:
+            ds, n_delay = self.calculate_direct_sound(receivers)
+            i_r = np.arange(len(n_delay))
+            etc.time[i_r, :, n_delay] += ds
+        return etc
+
+    def calculate_direct_sound(self, receivers):
+        """Direct sound at the receivers (RadiosityFast.py:605-657)."""
+        if not is_coordinates(receivers):
+            raise ValueError("Receiver positions must be of type pf.Coordinates")
+        if is_coordinates(self._source):
+            src = np.asarray(self._source.cartesian, float).reshape(-1, 3)[0]
+        else:
+            src = np.asarray(self._source.position, float).reshape(3)
+        rc = np.asarray(receivers.cartesian, float).reshape(-1, 3)
+        r = np.sqrt(np.sum((rc - src) ** 2, axis=-1))
+        direct = np.ones((rc.shape[0], self.n_bins), dtype=float)
+        direct *= (1 / (4 * np.pi * r ** 2))[:, np.newaxis]
+        if self._air_attenuation is not None:
+            for i in range(self.n_bins):
+                direct[:, i] *= np.exp(-self._air_attenuation[i] * r)
+        if not is_coordinates(self._source) and getattr(self._source, "directivity", None) is not None:
+            for i in range(self.n_bins):
+                direct[:, i] *= np.real(self._source.get_directivity(np.squeeze(rc), self._frequencies[i]))
+        n_delay = np.array(r / self.speed_of_sound / self._etc_time_resolution, dtype=int)
+        return direct, n_delay
+
+    def collect_energy_receiver_patchwise(self, receivers):
+        """Per-patch energy at the receivers (RadiosityFast.py:660-684)."""
+        return self._collect(receivers, patchwise=True)
+
+    def _collect(self, receivers, patchwise):
+        if not is_coordinates(receivers):
+            raise ValueError("Receiver positions must be of type pf.Coordinates")
+        if patchwise and receivers.cdim != 1:
+            raise ValueError("Receiver positions must be of shape (n_receivers, 3)")
+        etc = self._etc_device()
+        d = self._geometry()
+        bs = self._brdf_device()
+        n, nd, nb, nt = etc.shape
+        if bs is None or bs["n_out"] != nd:
+            raise ValueError("the outgoing BRDF directions do not match the energy histograms")
+        rc = np.atleast_2d(np.asarray(receivers.cartesian, dtype=float).reshape(-1, 3))
+        n_r = rc.shape[0]
+        dev = self.device
+        st = _stream()
+        prec = nat.SP_F32 if etc.dtype == torch.float32 else nat.SP_F64
+        att = self._t(self._air_attenuation if self._air_attenuation is not None else np.zeros(nb), torch.float64)
+        if patchwise:
+            out = torch.empty((n_r, n, nb, nt), dtype=torch.float64, device=dev)
+        else:
+            out = torch.empty((n_r, nb, nt), dtype=torch.float64, device=dev)
+        rfac = torch.empty((n,), dtype=torch.float64, device=dev)
+        ridx = torch.empty((n,), dtype=torch.int32, device=dev)
+        dist = torch.empty((n,), dtype=torch.float64, device=dev)
+        wsz = nat.size("sp_collect_workspace", n, nb)
+        ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=dev)
+        rdev = self._t(rc, torch.float64)
+        for r in range(n_r):
+            rp = rdev[r]
+            rvis = self._point_visibility(rp)
+            nat.call("sp_receiver_factors", _ptr(rp), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(rvis),
+                     _ptr(d["wall_of"]), bs["n_out"], _ptr(bs["dirs_out"]), _ptr(rfac), _ptr(ridx), _ptr(dist), st)
+            nat.call("sp_collect_receiver", prec, n, nd, nb, nt, _ptr(etc), _ptr(ridx), _ptr(rfac), _ptr(dist),
+                     float(self.speed_of_sound), float(self._etc_time_resolution), _ptr(att),
+                     _ptr(out[r]) if patchwise else _ptr(None), _ptr(None) if patchwise else _ptr(out[r]),
+                     _ptr(ws), wsz, st)
+        data = out.cpu().numpy()
+        times = np.arange(nt) * self._etc_time_resolution
+        return TimeData(data, times)
+
+    # ------------------------------------------------------------- materials
+    def set_air_attenuation(self, air_attenuation):
+        """Set air attenuation factor in Np/m (RadiosityFast.py:754-764)."""
+        self._check_set_frequency(air_attenuation.frequencies)
+        self._air_attenuation = np.atleast_1d(np.asarray(air_attenuation.freq, dtype=float).squeeze())
+
+    def set_wall_brdf(self, wall_indexes, brdf, incoming_directions, outgoing_directions):
+        """Set the wall BRDF (RadiosityFast.py:766-816); stored times pi."""
+        assert (np.asarray(incoming_directions.z) >= 0).all(), "Sources must be in the positive half space"
+        assert (np.asarray(outgoing_directions.z) >= 0).all(), "Receivers must be in the positive half space"
+        self._check_set_frequency(brdf.frequencies)
+        if self._brdf_incoming_directions is None:
+            self._brdf_incoming_directions = np.empty((self.n_walls), dtype=object)
+            self._brdf_outgoing_directions = np.empty((self.n_walls), dtype=object)
+            self._brdf_index = np.full((self.n_walls), -1, dtype=np.int64)
+            self._brdf = []
+        for i in np.atleast_1d(wall_indexes):
+            inc, out = geo.rotate_coords_to_normal(self.walls_normal[i], self.walls_up_vector[i],
+                                                   incoming_directions, outgoing_directions)
+            self._brdf_incoming_directions[i] = inc
+            self._brdf_outgoing_directions[i] = out
+        self._brdf.append(np.asarray(brdf.freq, dtype=float) * np.pi)
+        self._brdf_index[np.atleast_1d(wall_indexes)] = len(self._brdf) - 1
+        self._dev.pop("brdf_state", None)
+
+    def _check_set_frequency(self, frequencies):
+        frequencies = np.atleast_1d(np.asarray(frequencies))
+        if self._frequencies is None:
+            self._frequencies = frequencies
+        else:
+            assert self._frequencies.size == frequencies.size, "Number of frequency bins do not match"
+            assert (self._frequencies == frequencies).all(), "Frequencies do not match"
+
+    # ------------------------------------------------------------ state I/O
+    def to_dict(self) -> dict:
+        """Convert the object to a dictionary (RadiosityFast.py:841-873)."""
+        out = {
+            'walls_points': self._walls_points, 'walls_normal': self._walls_normal,
+            'walls_up_vector': self._walls_up_vector, 'patches_points': self._patches_points,
+            'n_patches': self._n_patches, 'patch_to_wall_ids': self._patch_to_wall_ids,
+            'visibility_matrix': self._visibility_matrix, 'visible_patches': self._visible_patches,
+            'form_factors': self._form_factors, 'form_factors_tilde': self._form_factors_tilde,
+            'frequencies': self._frequencies, 'brdf': self._brdf, 'brdf_index': self._brdf_index,
+            'brdf_incoming_directions': self._brdf_incoming_directions,
+            'brdf_outgoing_directions': self._brdf_outgoing_directions,
+            'patch_2_brdf_outgoing_index': self._patch_2_brdf_outgoing_index,
+            'air_attenuation': self._air_attenuation, 'speed_of_sound': self._speed_of_sound,
+            'etc_time_resolution': self._etc_time_resolution, 'etc_duration': self._etc_duration,
+            'distance_patches_to_source': self._distance_patches_to_source,
+            'energy_init_source': self._energy_init_source, 'energy_exchange_etc': self._energy_exchange_etc,
+        }
+        for key, value in out.items():
+            if value is None:
+                out[key] = 'None'
+            elif isinstance(value, np.ndarray) and value.dtype != object:
+                out[key] = value.tolist()
+        return out
+
+    @classmethod
+    def from_dict(cls, input_dict: dict, **kwargs):
+        """Create an object from a dictionary (RadiosityFast.py:882-886)."""
+        d = {k: (None if isinstance(v, str) and v == 'None' else v) for k, v in input_dict.items()}
+        return cls(**d, **kwargs)
+
+    def __eq__(self, other):
+        if not isinstance(other, DirectionalRadiosityFast):
+            return False
+        a, b = self.to_dict(), other.to_dict()
+        if a.keys() != b.keys():
+            return False
+        for k in a:
+            va, vb = a[k], b[k]
+            if isinstance(va, (list, tuple, np.ndarray)) or isinstance(vb, (list, tuple, np.ndarray)):
+                try:
+                    if not np.array_equal(np.asarray(va, dtype=object if k.startswith('brdf_') else None),
+                                          np.asarray(vb, dtype=object if k.startswith('brdf_') else None)):
+                        return False
+                except ValueError:
+                    return False
+            elif va != vb:
+                return False
+        return True
+
+    # ------------------------------------------------- reference attributes
+    def _host_get(self, key, make):
+        if key not in self._host:
+            val = make()
+            if val is None:
+                return None
+            self._host[key] = val
+        return self._host[key]
+
+    @property
+    def _visibility_matrix(self):
+        return self._host_get("visibility_matrix",
+                              lambda: None if self._bake is None else self._bake["vis"].cpu().numpy().astype(bool))
+
+    @property
+    def _visible_patches(self):
+        return self._host_get("visible_patches",
+                              lambda: None if self._bake is None else self._bake["pairs"].cpu().numpy().astype(np.int32))
+
+    @property
+    def _form_factors(self):
+        def make():
+            if self._bake is None:
+                return None
+            n = self.n_patches
+            out = torch.empty((n, n), dtype=torch.float64, device=self.device)
+            nat.call("sp_dense_form_factors", self._bake["n_vis"], n, _ptr(self._bake["pairs"]),
+                     _ptr(self._bake["ff"]), _ptr(out), _stream())
+            return out.cpu().numpy()
+        return self._host_get("form_factors", make)
+
+    @property
+    def _form_factors_tilde(self):
+        def make():
+            bk = self._bake
+            if bk is None:
+                return None
+            n = self.n_patches
+            bs = bk["brdf"]
+            nd = bk["n_out"]
+            nb = bk["n_bins"]
+            out = torch.empty((n, n, nd, nb), dtype=torch.float64, device=self.device)
+            d = self._geometry()
+            nat.call("sp_form_factors_tilde", bk["n_dir"], n, nd, nb, bs["n_in"] if bs else 1, _ptr(bk["src"]),
+                     _ptr(bk["dst"]), _ptr(bk["in_dir"]), _ptr(bk["fprime"]), _ptr(bk["unit_len"]), _ptr(bk["att"]),
+                     _ptr(d["wall_of"]), _ptr(bs["brdf_index"]) if bs else _ptr(None),
+                     _ptr(bs["brdf"]) if bs else _ptr(None), _ptr(out), _stream())
+            return out.cpu().numpy()
+        return self._host_get("form_factors_tilde", make)
+
+    @property
+    def _patch_2_brdf_outgoing_index(self):
+        def make():
+            bk = self._bake
+            if bk is None:
+                return None
+            n = self.n_patches
+            if bk["brdf"] is None:
+                return np.zeros((n, n), dtype=np.int64)
+            out = torch.empty((n, n), dtype=torch.int64, device=self.device)
+            nat.call("sp_outgoing_index_map", bk["n_dir"], n, _ptr(bk["src"]), _ptr(bk["dst"]), _ptr(bk["out_dir"]),
+                     int(bk["n_out"]), _ptr(out), _stream())
+            return out.cpu().numpy()
+        return self._host_get("patch_2_brdf_outgoing_index", make)
+
+    @property
+    def _energy_init_source(self):
+        return self._host_get("energy_init_source",
+                              lambda: self._dev["e0dir"].cpu().numpy() if "e0dir" in self._dev else None)
+
+    @property
+    def _distance_patches_to_source(self):
+        return self._host_get("distance_patches_to_source",
+                              lambda: self._dev["d0"].cpu().numpy() if "d0" in self._dev else None)
+
+    @property
+    def _source_visibility(self):
+        return self._dev["svis"].cpu().numpy().astype(bool) if "svis" in self._dev else None
+
+    @property
+    def _energy_exchange_etc(self):
+        return self._host_get("energy_exchange_etc",
+                              lambda: self._dev["etc"].cpu().numpy().astype(np.float64) if "etc" in self._dev else None)
+
+    # ------------------------------------------------------------ properties
+    @property
+    def n_bins(self):
+        return None if self._frequencies is None else self._frequencies.shape[0]
+
+    @property
+    def n_walls(self):
+        return self._walls_points.shape[0]
+
+    @property
+    def n_patches(self):
+        return self._n_patches
+
+    @property
+    def form_factors(self):
+        return self._form_factors
+
+    @property
+    def visibility_matrix(self):
+        return self._visibility_matrix
+
+    @property
+    def walls_area(self):
+        return geo.calculate_area(self._walls_points)
+
+    @property
+    def walls_points(self):
+        return self._walls_points
+
+    @property
+    def walls_normal(self):
+        return self._walls_normal
+
+    @property
+    def walls_center(self):
+        return geo.calculate_center(self._walls_points)
+
+    @property
+    def walls_up_vector(self):
+        return self._walls_up_vector
+
+    @property
+    def patches_area(self):
+        return geo.calculate_area(self._patches_points)
+
+    @property
+    def patches_center(self):
+        return geo.calculate_center(self._patches_points)
+
+    @property
+    def patches_size(self):
+        return geo.calculate_size(self._patches_points)
+
+    @property
+    def patches_points(self):
+        return self._patches_points
+
+    @property
+    def patches_normal(self):
+        return self._walls_normal[self._patch_to_wall_ids]
+
+    @property
+    def speed_of_sound(self):
+        return self._speed_of_sound
