@@ -172,13 +172,17 @@ typedef struct sp_exchange_args {
     const double* class_diff;   /* (n_groups * n_in, B) */
     const double* class_spec;   /* (n_groups * n_in, B) */
     const int32_t* class_target;/* (n_groups * n_in) mirror direction, -1 if none */
+    const int32_t* receiver_order; /* (N) receivers in tile order (8 per tile), NULL = 0..N-1 */
+    const int32_t* pair_dst;       /* (P) destination of each directed pair (structured algorithm) */
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070
  * `_energy_exchange_init_energy` (max_order < 1).  Synchronises `stream` once
- * (to report SP_ERR_RANGE for a source delay outside the histogram). */
+ * (to report SP_ERR_RANGE for a source delay outside the histogram).
+ * n_classes = n_groups * n_in_dirs for SP_EXCHANGE_STRUCTURED (<= 256). */
 size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins,
-                                    int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs);
+                                    int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs,
+                                    int n_classes);
 int sp_energy_exchange(const sp_exchange_args* args, void* ws, size_t ws_bytes, void* stream);
 
 /* --------------------------------------------------------------- collection */

@@ -52,6 +52,7 @@ class ExchangeArgs(ctypes.Structure):
         ("etc_total", P),
         ("slot_group", P), ("slot_scale", P), ("n_groups", I),
         ("class_diff", P), ("class_spec", P), ("class_target", P),
+        ("receiver_order", P), ("pair_dst", P),
     ]
 
 
@@ -73,7 +74,7 @@ _SIGS = {
     "sp_form_factors_tilde": (I, [LL, I, I, I, I, P, P, P, P, P, P, P, P, P, P, P]),
     "sp_source_energy": (I, [P, I, P, P, P, I, P, P, P, I, P, I, P, P, P, P, P]),
     "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
-    "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I]),
+    "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I, I]),
     "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
     "sp_collect_workspace": (SZ, [I, I]),
     "sp_collect_receiver": (I, [I, I, I, I, I, P, P, P, P, D, D, P, P, P, P, SZ, P]),

@@ -266,9 +266,10 @@ int run_collect(int n, int nd, int nb, int nt, const void* etot, const int32_t* 
 extern "C" {
 
 size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins,
-                                    int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs) {
+                                    int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs,
+                                    int n_classes) {
     if (algorithm == SP_EXCHANGE_STRUCTURED)
-        return sp_structured_workspace(precision, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_slots, n_in_dirs);
+        return sp_structured_workspace(precision, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_classes);
     if (precision == SP_F64)
         return exchange_dense_workspace<double>(n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_slots, n_in_dirs);
     return exchange_dense_workspace<float>(n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_slots, n_in_dirs);

@@ -1,68 +1,89 @@
-// Structured energy exchange (RadiosityFast.py:1073-1145) for BRDF tables
-// whose rows are  diff + spec * [o == m]  up to a per-slot, per-band scale:
-//   BRDF[slot, s, o, b] = scale[slot, b] * (diff[g, s, b] + spec[g, s, b] * [o == m[g, s]])
-// with g = material group of the slot.  This is the form produced by
-// brdf.py:100-120 (`create_from_scattering`: s(1-a)/pi everywhere plus the
-// mirror term on one outgoing direction), stored times pi.
+// Tiled structured energy exchange (RadiosityFast.py:1073-1145) for BRDF
+// tables whose rows are  diff + spec * [o == m]  up to a per-slot scale:
+//   BRDF[slot, s, o, b] = scale[slot, b] * (diff[c, b] + spec[c, b] * [o == m_c]),
+// c = (material group of the slot, s) is the pair's class.  This is the form
+// brdf.py:100-120 (`create_from_scattering`) produces, stored times pi.
 //
-// For a receiver j, pairs of equal class c = (g, s) share their BRDF row, so
-//   E_k[j, o, b, t] = sum_c (diff_c + spec_c [o == m_c]) * G_c[t],
-//   G_c[t] = sum_{pairs of class c} w_p * E_{k-1}[src_p, p2o_p, b, t - n_p],
-//   w_p = F'_p * exp(-att_b |u_p|) * scale[slot(src_p), b].
-// A class run costs one multiply-add per pair and bin; each run total is then
-// spread once as diff_c (all directions) and spec_c (direction m_c).
+// For receiver j and order k:
+//   G_k[j, c, b, t] = sum_{pairs p -> j of class c} w_pb * E_{k-1}[src_p, p2o_p, b, t - n_p]
+//   E_k[j, o, b, t] = sum_c (diff[c, b] + spec[c, b] [o == m_c]) * G_k[j, c, b, t]
+//   E_total += E_k
+// with w_pb = F'_p * exp(-att_b |u_p|) * scale[slot(src_p), b].
+//
+// Plan (once per exchange call): receivers are cut into tiles of 8 (a given
+// receiver order, normally spatial); a segment is (tile, class).  The
+// segment's pairs are merged by source patch and cut into source groups:
+// one source row (src * D + p2o), up to 8 member receivers, delays within
+// n_base .. n_base + 13.  Everything is built in parallel and
+// deterministically (row-wise class sort, merge by binary search, scans).
+//
+// Scatter (per order, FP32): one CTA per (segment, 2048-bin window, band),
+// 128 threads, each owning 16 consecutive bins of all 8 receivers in
+// registers.  Each group's source window (2064 values) is staged in shared
+// memory by a bulk asynchronous copy (cp.async.bulk + mbarrier, 4 stages);
+// every thread reads its 32-value slice with 8 LDS.128 in a rotated order
+// (conflict-free banks) and applies it to every member with a compile-time
+// shift, so one staged value feeds up to 8 multiply-adds.  FP64 uses the
+// same plan with direct vector loads.  Mix: streams G into E_k and E_total.
 #include "common.cuh"
 #include "exchange_common.cuh"
 
 namespace {
 
-template <typename T>
-struct Cfg;
-template <>
-struct Cfg<float> {
-    static constexpr int R = 2;  // bins per thread
-};
-template <>
-struct Cfg<double> {
-    static constexpr int R = 1;
-};
-constexpr int kThreads = 256;
+constexpr int kTile = 8;          // receivers per tile
+constexpr int kMaxSpan = 13;      // max delay spread inside a source group
+constexpr unsigned kAbsent = 0xFu;
+constexpr int kMaxClasses = 256;
 
-__global__ void k_delays_s(long long n_dir, const double* __restrict__ dist, double c, double dt,
+struct Group {
+    int32_t srcrow;   // src * D + p2o
+    int32_t n_base;   // smallest delay of the members
+    uint32_t offs;    // 8 x 4 bits: delay - n_base, 0xF = no member
+    int32_t pad;
+};
+
+// ------------------------------------------------------------------ plan
+__global__ void k_delays_t(long long n_dir, const double* __restrict__ dist, double c, double dt,
                            int32_t* __restrict__ delay) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_dir) return;
     delay[e] = (int32_t)(long long)xdiv(xdiv(dist[e], c), dt);
 }
 
-__global__ void k_pair_class(long long n_dir, const int32_t* __restrict__ src, const int32_t* __restrict__ in_dir,
-                             const int32_t* __restrict__ wall_of, const int32_t* __restrict__ brdf_index,
-                             const int32_t* __restrict__ slot_group, int n_in, int32_t* __restrict__ cls) {
+__global__ void k_pair_class_t(long long n_dir, const int32_t* __restrict__ src, const int32_t* __restrict__ in_dir,
+                               const int32_t* __restrict__ wall_of, const int32_t* __restrict__ brdf_index,
+                               const int32_t* __restrict__ slot_group, int n_in, int32_t* __restrict__ cls) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_dir) return;
     int slot = brdf_index[wall_of[src[e]]];
     cls[e] = slot_group[slot] * n_in + in_dir[e];
 }
 
-// Stable counting sort of each destination row by class, one warp per row.
-// perm[k] = original entry placed at position k.
-__global__ void k_row_sort_by_class(int n, const int64_t* __restrict__ off, const int32_t* __restrict__ cls,
-                                    int n_class, int64_t* __restrict__ perm) {
+// Stable counting sort of each destination row by class (one warp per row);
+// writes the class boundaries rco[j * (C + 1) + c] and the row of each position.
+__global__ void k_row_sort_by_class_t(int n, const int64_t* __restrict__ off, const int32_t* __restrict__ cls,
+                                      int n_class, int64_t* __restrict__ perm, int64_t* __restrict__ rco,
+                                      int32_t* __restrict__ row_of) {
     extern __shared__ int s_hist[];
     int j = blockIdx.x;
     int lane = threadIdx.x;
     long long b = off[j], e = off[j + 1];
     for (int c = lane; c < n_class; c += 32) s_hist[c] = 0;
     __syncwarp();
-    for (long long k = b + lane; k < e; k += 32) atomicAdd(&s_hist[cls[k]], 1);
+    for (long long k = b + lane; k < e; k += 32) {
+        atomicAdd(&s_hist[cls[k]], 1);
+        row_of[k] = j;
+    }
     __syncwarp();
     if (lane == 0) {
         int run = 0;
         for (int c = 0; c < n_class; ++c) {
             int h = s_hist[c];
             s_hist[c] = run;
+            rco[(size_t)j * (n_class + 1) + c] = b + run;
             run += h;
         }
+        rco[(size_t)j * (n_class + 1) + n_class] = b + run;
     }
     __syncwarp();
     for (long long k0 = b; k0 < e; k0 += 32) {
@@ -82,33 +103,548 @@ __global__ void k_row_sort_by_class(int n, const int64_t* __restrict__ off, cons
     }
 }
 
+__global__ void k_default_tiles(int n, int n_tiles, const int32_t* __restrict__ order, int32_t* __restrict__ tile_recv,
+                                int32_t* __restrict__ tile_of, int32_t* __restrict__ slot_of) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_tiles * kTile) return;
+    int j = (k < n) ? (order ? order[k] : k) : -1;
+    tile_recv[k] = j;
+    if (j >= 0) {
+        tile_of[j] = k / kTile;
+        slot_of[j] = k % kTile;
+    }
+}
+
+__global__ void k_seg_size(long long n_seg, int n_class, const int32_t* __restrict__ tile_recv,
+                           const int64_t* __restrict__ rco, int64_t* __restrict__ seg_size) {
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_seg) return;
+    int tile = (int)(s / n_class), c = (int)(s % n_class);
+    long long tot = 0;
+    for (int w = 0; w < kTile; ++w) {
+        int j = tile_recv[tile * kTile + w];
+        if (j >= 0) tot += rco[(size_t)j * (n_class + 1) + c + 1] - rco[(size_t)j * (n_class + 1) + c];
+    }
+    seg_size[s] = tot;
+}
+
+// Multi-block exclusive scan of int64 values: block sums, scan of the sums,
+// add-back.  out[n] = total.
+constexpr int kScanBlock = 1024;
+__global__ void k_scan_blocks(long long n, const int64_t* __restrict__ in, int64_t* __restrict__ out,
+                              int64_t* __restrict__ block_sums) {
+    __shared__ int64_t s[kScanBlock];
+    long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    int64_t v = (i < n) ? in[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        int64_t x = (threadIdx.x >= (unsigned)off) ? s[threadIdx.x - off] : 0;
+        __syncthreads();
+        s[threadIdx.x] += x;
+        __syncthreads();
+    }
+    if (i < n) out[i] = s[threadIdx.x] - v;
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[kScanBlock - 1];
+}
+__global__ void k_scan_sums(long long nblocks, int64_t* __restrict__ sums, int64_t* __restrict__ total) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t run = 0;
+    for (long long k = 0; k < nblocks; ++k) {
+        int64_t v = sums[k];
+        sums[k] = run;
+        run += v;
+    }
+    *total = run;
+}
+__global__ void k_scan_add(long long n, int64_t* __restrict__ out, const int64_t* __restrict__ sums) {
+    long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+}
+
+// Position of one entry inside its segment's (src, slot)-ordered merge.
+__device__ __forceinline__ long long count_before(const int64_t* __restrict__ perm, const int32_t* __restrict__ src,
+                                                  long long lo, long long hi, int key, bool inclusive) {
+    // number of list elements (sorted by src) with src < key (or <= key)
+    while (lo < hi) {
+        long long mid = (lo + hi) >> 1;
+        int v = src[perm[mid]];
+        if (v < key || (inclusive && v == key))
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_merge_positions(long long n_dir, int n_class, const int64_t* __restrict__ perm,
+                                  const int32_t* __restrict__ row_of, const int32_t* __restrict__ cls,
+                                  const int32_t* __restrict__ src, const int64_t* __restrict__ rco,
+                                  const int32_t* __restrict__ tile_of, const int32_t* __restrict__ slot_of,
+                                  const int32_t* __restrict__ tile_recv, const int64_t* __restrict__ seg_base,
+                                  int64_t* __restrict__ merged) {
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_dir) return;
+    long long e = perm[q];
+    int j = row_of[q];
+    int c = cls[e];
+    int key = src[e];
+    int tile = tile_of[j], w = slot_of[j];
+    long long pos = q - rco[(size_t)j * (n_class + 1) + c];
+    for (int w2 = 0; w2 < kTile; ++w2) {
+        if (w2 == w) continue;
+        int j2 = tile_recv[tile * kTile + w2];
+        if (j2 < 0) continue;
+        long long lo = rco[(size_t)j2 * (n_class + 1) + c], hi = rco[(size_t)j2 * (n_class + 1) + c + 1];
+        pos += count_before(perm, src, lo, hi, key, w2 < w) - lo;
+    }
+    merged[seg_base[(long long)tile * n_class + c] + pos] = e;
+}
+
+// Cells: runs of equal (segment, src) in merged order (<= 8 entries, one per
+// receiver).  For each cell start: sort members by (p2o, delay), cut into
+// groups; write == 0 counts, write == 1 emits.
 template <typename T>
-__global__ void k_gather_pairs(long long n_dir, int nb, const int64_t* __restrict__ perm, const int32_t* __restrict__ src,
-                               const int32_t* __restrict__ out_dir, const int32_t* __restrict__ delay,
-                               const int32_t* __restrict__ cls, const double* __restrict__ fprime,
-                               const double* __restrict__ unit_len, const double* __restrict__ att,
-                               const int32_t* __restrict__ wall_of, const int32_t* __restrict__ brdf_index,
-                               const double* __restrict__ slot_scale, int32_t* __restrict__ s_src,
-                               int32_t* __restrict__ s_odir, int32_t* __restrict__ s_delay,
-                               int32_t* __restrict__ s_cls, T* __restrict__ s_w) {
-    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n_dir) return;
-    long long e = perm[k];
-    int i = src[e];
-    s_src[k] = i;
-    s_odir[k] = out_dir[e];
-    s_delay[k] = delay[e];
-    s_cls[k] = cls[e];
-    int slot = brdf_index[wall_of[i]];
-    for (int b = 0; b < nb; ++b) {
-        double f = fprime[e];
-        if (att) f = f * exp(-att[b] * unit_len[e]);
-        s_w[k * nb + b] = (T)(f * slot_scale[(size_t)slot * nb + b]);
+__global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* __restrict__ merged,
+                        const int32_t* __restrict__ src, const int32_t* __restrict__ dst, const int32_t* __restrict__ out_dir,
+                        const int32_t* __restrict__ delay, const int32_t* __restrict__ cls,
+                        const int32_t* __restrict__ tile_of, const int32_t* __restrict__ slot_of,
+                        const double* __restrict__ fprime, const double* __restrict__ unit_len,
+                        const double* __restrict__ att, const int32_t* __restrict__ wall_of,
+                        const int32_t* __restrict__ brdf_index, const double* __restrict__ slot_scale, int write,
+                        int64_t* __restrict__ cell_count, const int64_t* __restrict__ cell_base,
+                        long long cap, Group* __restrict__ groups, T* __restrict__ coef) {
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_dir) return;
+    long long e = merged[q];
+    int s_src = src[e];
+    int s_tile = tile_of[dst[e]];
+    int s_cls = cls[e];
+    if (q > 0) {
+        long long ep = merged[q - 1];
+        if (src[ep] == s_src && tile_of[dst[ep]] == s_tile && cls[ep] == s_cls) {
+            if (!write) cell_count[q] = 0;
+            return;
+        }
+    }
+    int mo[kTile], md[kTile], mw[kTile];
+    long long me[kTile];
+    int m = 0;
+    for (long long k = q; k < n_dir && m < kTile; ++k) {
+        long long ek = merged[k];
+        if (src[ek] != s_src || tile_of[dst[ek]] != s_tile || cls[ek] != s_cls) break;
+        int dl = delay[ek];
+        if (dl >= nt) continue;  // contributes nothing inside the histogram
+        mo[m] = out_dir[ek];
+        md[m] = dl;
+        mw[m] = slot_of[dst[ek]];
+        me[m] = ek;
+        ++m;
+    }
+    for (int a = 1; a < m; ++a) {
+        int to = mo[a], td = md[a], tw = mw[a];
+        long long te = me[a];
+        int r = a - 1;
+        while (r >= 0 && (mo[r] > to || (mo[r] == to && md[r] > td))) {
+            mo[r + 1] = mo[r];
+            md[r + 1] = md[r];
+            mw[r + 1] = mw[r];
+            me[r + 1] = me[r];
+            --r;
+        }
+        mo[r + 1] = to;
+        md[r + 1] = td;
+        mw[r + 1] = tw;
+        me[r + 1] = te;
+    }
+    long long g_out = write ? cell_base[q] : 0;
+    long long n_groups = 0;
+    int slot = brdf_index[wall_of[s_src]];
+    int a = 0;
+    while (a < m) {
+        int r = a;
+        while (r + 1 < m && mo[r + 1] == mo[a] && md[r + 1] - md[a] <= kMaxSpan) ++r;
+        if (write) {
+            Group g;
+            g.srcrow = s_src * nd + mo[a];
+            g.n_base = md[a];
+            unsigned offs = 0xFFFFFFFFu;
+            for (int b = 0; b < nb; ++b)
+                for (int w = 0; w < kTile; ++w) coef[((size_t)b * cap + g_out) * kTile + w] = T(0);
+            for (int x = a; x <= r; ++x) {
+                int w = mw[x];
+                offs &= ~(0xFu << (4 * w));
+                offs |= (unsigned)(md[x] - md[a]) << (4 * w);
+                long long ex = me[x];
+                for (int b = 0; b < nb; ++b) {
+                    double f = fprime[ex];
+                    if (att) f = f * exp(-att[b] * unit_len[ex]);
+                    coef[((size_t)b * cap + g_out) * kTile + w] = (T)(f * slot_scale[(size_t)slot * nb + b]);
+                }
+            }
+            g.offs = offs;
+            g.pad = 0;
+            groups[g_out] = g;
+            ++g_out;
+        }
+        ++n_groups;
+        a = r + 1;
+    }
+    if (!write) cell_count[q] = n_groups;
+}
+
+// seg_off[s] = group index of the first cell of segment s.
+__global__ void k_seg_offsets(long long n_seg, long long n_dir, const int64_t* __restrict__ seg_base,
+                              const int64_t* __restrict__ cell_base, int64_t* __restrict__ seg_off) {
+    long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > n_seg) return;
+    long long q = seg_base[s];
+    seg_off[s] = (q < n_dir) ? cell_base[q] : cell_base[n_dir];
+}
+
+// --------------------------------------------------------- PTX helpers
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after kWaitLimit polls (each poll may suspend
+// briefly) or as soon as another CTA has reported a failure.
+constexpr unsigned kWaitLimit = 1u << 16;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, const volatile int* err) {
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && *err) return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// --------------------------------------------------------- FP32 scatter
+constexpr int kThreads = 128;
+constexpr int kR = 16;                       // bins per thread
+constexpr int kTW = kThreads * kR;           // 2048 bins per window
+constexpr int kStageF = kTW + 16;            // 2064 floats staged per group
+constexpr int kStages = 6;
+constexpr int kChunk = 256;                  // group headers held in shared memory
+
+// Member in slot W with delay offset d: acc[W][r] += cf * staged[tid + 128 r + kMaxSpan - d + mu].
+// Each read of a warp touches 32 consecutive floats: conflict-free at any offset.
+template <int W>
+__device__ __forceinline__ void slot_f32(float (&acc)[kTile][kR], const float* st, unsigned offs, int f, const float* cf) {
+    unsigned d = (offs >> (4 * W)) & 0xFu;
+    if (d == kAbsent) return;
+    const float cfw = cf[W];
+    const float* sp = st + (f - (int)d);
+#pragma unroll
+    for (int r = 0; r < kR; ++r) acc[W][r] = fmaf(cfw, sp[kThreads * r], acc[W][r]);
+}
+
+__device__ __forceinline__ void group_f32(float (&acc)[kTile][kR], const float* st, unsigned offs, int f,
+                                          const float* cf) {
+    slot_f32<0>(acc, st, offs, f, cf);
+    slot_f32<1>(acc, st, offs, f, cf);
+    slot_f32<2>(acc, st, offs, f, cf);
+    slot_f32<3>(acc, st, offs, f, cf);
+    slot_f32<4>(acc, st, offs, f, cf);
+    slot_f32<5>(acc, st, offs, f, cf);
+    slot_f32<6>(acc, st, offs, f, cf);
+    slot_f32<7>(acc, st, offs, f, cf);
+}
+
+// Histogram rows of eprev/ecur are padded: row r starts at r * rs and bin 0
+// sits at offset `lead` (>= nt + 16 zeros before it), so a window that
+// reaches before bin 0 reads zeros and needs no masking.
+__global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb, int nt, long long rs, int lead,
+                                                             long long cap, const int32_t* __restrict__ tile_recv,
+                                                             const int64_t* __restrict__ seg_off,
+                                                             const Group* __restrict__ groups,
+                                                             const float* __restrict__ coef,
+                                                             const float* __restrict__ eprev,
+                                                             float* __restrict__ gout, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    float* stage = reinterpret_cast<float*>(s_raw);                              // [kStages][kStageF]
+    Group* s_grp = reinterpret_cast<Group*>(stage + kStages * kStageF);          // [kChunk]
+    float* s_cf = reinterpret_cast<float*>(s_grp + kChunk);                      // [kChunk][8]
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_cf + kChunk * kTile);         // [kStages]
+    uint64_t* empty = full + kStages;                                            // [kStages]
+    __shared__ int s_abort;
+
+    const long long seg = blockIdx.x;
+    const int b = blockIdx.z;
+    const int t0 = blockIdx.y * kTW;
+    const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
+    if (g_beg == g_end || *(volatile int*)err) return;
+    const int tid = threadIdx.x;
+    const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kThreads);
+        }
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    float acc[kTile][kR];
+#pragma unroll
+    for (int w = 0; w < kTile; ++w)
+#pragma unroll
+        for (int r = 0; r < kR; ++r) acc[w][r] = 0.0f;
+
+    const unsigned stage_bytes = kStageF * sizeof(float);
+    long long gbase = 0;  // groups of the CTA handled before the current chunk
+    for (long long cb = g_beg; cb < g_end; cb += kChunk) {
+        const int cnt = (int)min((long long)kChunk, g_end - cb);
+        __syncthreads();
+        for (int q = tid; q < cnt; q += kThreads) s_grp[q] = groups[cb + q];
+        for (int q = tid; q < cnt * kTile; q += kThreads) s_cf[q] = coef[((size_t)b * cap + cb) * kTile + q];
+        __syncthreads();
+        if (s_abort) break;
+        int next = 0;  // thread 0: groups of this chunk issued so far
+        int q = 0;
+        for (; q < cnt; ++q) {
+            if (tid == 0) {
+                // Issue ahead every group whose stage has been released by all
+                // threads; block only when group q itself is not issued yet.
+                while (next < cnt && next < q + kStages) {
+                    const long long gi = gbase + next;
+                    const int st = (int)(gi % kStages);
+                    if (gi >= kStages) {
+                        const unsigned par = (unsigned)((gi / kStages - 1) & 1);
+                        bool ready = (next <= q) ? mbar_wait(&empty[st], par, err) : mbar_test(&empty[st], par);
+                        if (!ready) {
+                            if (next <= q) {
+                                atomicExch(err, 1);
+                                s_abort = 1;
+                            }
+                            break;
+                        }
+                    }
+                    const Group gn = s_grp[next];
+                    const long long rown = ((long long)gn.srcrow * nb + b) * rs + lead;
+                    const long long an = (rown + t0 - gn.n_base - kMaxSpan) & ~3LL;
+                    mbar_expect_tx(&full[st], stage_bytes);
+                    bulk_copy_g2s(stage + st * kStageF, eprev + an, stage_bytes, &full[st]);
+                    ++next;
+                }
+            }
+            const long long gi = gbase + q;
+            const int st = (int)(gi % kStages);
+            if (!mbar_wait(&full[st], (unsigned)((gi / kStages) & 1), err)) {
+                atomicExch(err, 1);
+                s_abort = 1;
+            }
+            if (s_abort) break;
+            const Group g = s_grp[q];
+            const long long row = ((long long)g.srcrow * nb + b) * rs + lead;
+            const long long s_cta = (long long)t0 - g.n_base - kMaxSpan;  // source index of staged element mu
+            const long long a0 = (row + s_cta) & ~3LL;
+            const int mu = (int)(row + s_cta - a0);
+            // staged element f holds source index (a0 - row) + f (the zero lead of
+            // the padded row covers negative indices); bin t0 + tid + 128 r of a
+            // member with delay n_base + d reads f = tid + 128 r + kMaxSpan - d + mu
+            group_f32(acc, stage + st * kStageF, g.offs, tid + kMaxSpan + mu, s_cf + q * kTile);
+            mbar_arrive(&empty[st]);
+        }
+        // drain (only after an abort): wait for the copies still in flight
+        if (tid == 0 && s_abort) {
+            for (int k = q; k < next; ++k) {
+                const long long gi = gbase + k;
+                mbar_wait(&full[gi % kStages], (unsigned)((gi / kStages) & 1), err);
+            }
+        }
+        __syncthreads();
+        gbase += cnt;
+    }
+    if (s_abort) return;
+#pragma unroll
+    for (int w = 0; w < kTile; ++w) {
+        int j = tile_recv[tile * kTile + w];
+        if (j < 0) continue;
+        float* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + tid;
+#pragma unroll
+        for (int r = 0; r < kR; ++r)
+            if (t0 + tid + kThreads * r < nt) out[kThreads * r] = acc[w][r];
+    }
+}
+
+// --------------------------------------------------------- FP64 scatter
+constexpr int kR64 = 4;
+constexpr int kWin64 = 18;  // kR64 + kMaxSpan + 1
+
+template <int W>
+__device__ __forceinline__ void apply_f64(double (&acc)[kTile][kR64], const double (&win)[kWin64], int off, double cf) {
+    switch (off) {
+#define SP_CASE(K)                                                                                  \
+    case K:                                                                                         \
+        _Pragma("unroll") for (int r = 0; r < kR64; ++r) acc[W][r] =                                \
+            fma(cf, win[(r + K < kWin64) ? r + K : 0], acc[W][r]);                                  \
+        break;
+        SP_CASE(0) SP_CASE(1) SP_CASE(2) SP_CASE(3) SP_CASE(4) SP_CASE(5) SP_CASE(6) SP_CASE(7)
+        SP_CASE(8) SP_CASE(9) SP_CASE(10) SP_CASE(11) SP_CASE(12) SP_CASE(13) SP_CASE(14)
+#undef SP_CASE
+        default:
+            break;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void slot_f64(double (&acc)[kTile][kR64], const double (&win)[kWin64], unsigned offs,
+                                         int mu, const double* cf) {
+    unsigned d = (offs >> (4 * W)) & 0xFu;
+    if (d != kAbsent) apply_f64<W>(acc, win, mu + kMaxSpan - (int)d, cf[W]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, int nt, long long rs, int lead,
+                                                          long long cap,
+                                                          const int32_t* __restrict__ tile_recv,
+                                                          const int64_t* __restrict__ seg_off,
+                                                          const Group* __restrict__ groups,
+                                                          const double* __restrict__ coef,
+                                                          const double* __restrict__ eprev,
+                                                          double* __restrict__ gout) {
+    const long long seg = blockIdx.x;
+    const int b = blockIdx.z;
+    const int t0 = blockIdx.y * (kThreads * kR64) + threadIdx.x * kR64;
+    const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
+    if (g_beg == g_end) return;
+    const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+    double acc[kTile][kR64];
+#pragma unroll
+    for (int w = 0; w < kTile; ++w)
+#pragma unroll
+        for (int r = 0; r < kR64; ++r) acc[w][r] = 0.0;
+    if (t0 < nt) {
+        for (long long g = g_beg; g < g_end; ++g) {
+            const Group gr = groups[g];
+            const double* cf = coef + ((size_t)b * cap + g) * kTile;
+            // padded rows: the zero lead covers source indices below 0
+            const long long row = ((long long)gr.srcrow * nb + b) * rs + lead;
+            const long long abs0 = row + (long long)t0 - gr.n_base - kMaxSpan;
+            const long long al = abs0 & ~1LL;
+            const int mu = (int)(abs0 - al);
+            double win[kWin64];
+            const double2* p = reinterpret_cast<const double2*>(eprev + al);
+#pragma unroll
+            for (int k = 0; k < kWin64 / 2; ++k) {
+                double2 v = __ldg(p + k);
+                win[2 * k] = v.x;
+                win[2 * k + 1] = v.y;
+            }
+            slot_f64<0>(acc, win, gr.offs, mu, cf);
+            slot_f64<1>(acc, win, gr.offs, mu, cf);
+            slot_f64<2>(acc, win, gr.offs, mu, cf);
+            slot_f64<3>(acc, win, gr.offs, mu, cf);
+            slot_f64<4>(acc, win, gr.offs, mu, cf);
+            slot_f64<5>(acc, win, gr.offs, mu, cf);
+            slot_f64<6>(acc, win, gr.offs, mu, cf);
+            slot_f64<7>(acc, win, gr.offs, mu, cf);
+        }
+    }
+#pragma unroll
+    for (int w = 0; w < kTile; ++w) {
+        int j = tile_recv[tile * kTile + w];
+        if (j < 0) continue;
+        double* out = gout + (((size_t)j * n_class + c) * nb + b) * nt;
+#pragma unroll
+        for (int r = 0; r < kR64; ++r)
+            if (t0 + r < nt) out[t0 + r] = acc[w][r];
+    }
+}
+
+// --------------------------------------------------------------- mix
+// E_k[j, o, b, t] = sum_c (diff_c + spec_c [o == m_c]) G[j, c, b, t];  E_total += E_k.
+template <typename T>
+__global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt, long long rs, int lead,
+                                             const int32_t* __restrict__ tile_of,
+                                             const int64_t* __restrict__ seg_off, const T* __restrict__ cdiff,
+                                             const T* __restrict__ cspec, const int32_t* __restrict__ ctarget,
+                                             const T* __restrict__ g, T* __restrict__ ecur, T* __restrict__ etot) {
+    extern __shared__ int s_int[];
+    int* s_cls = s_int;                    // [n_class] present classes of the tile
+    int* s_inv_off = s_int + n_class;      // [nd + 1] per direction: present classes with m_c == o
+    int* s_inv = s_inv_off + nd + 1;       // [n_class]
+    __shared__ int s_np;
+    const int j = blockIdx.z, b = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tile = tile_of[j];
+    if (threadIdx.x == 0) {
+        int np = 0;
+        for (int c = 0; c < n_class; ++c) {
+            long long s = (long long)tile * n_class + c;
+            if (seg_off[s + 1] > seg_off[s]) s_cls[np++] = c;
+        }
+        s_np = np;
+        int k = 0;
+        for (int o = 0; o < nd; ++o) {
+            s_inv_off[o] = k;
+            for (int q = 0; q < np; ++q)
+                if (ctarget[s_cls[q]] == o) s_inv[k++] = s_cls[q];
+        }
+        s_inv_off[nd] = k;
+    }
+    __syncthreads();
+    if (t >= nt) return;
+    const int np = s_np;
+    const size_t cstride = (size_t)nb * nt;
+    const T* gj = g + ((size_t)j * n_class * nb + b) * nt + t;
+    T diffuse = T(0);
+    for (int q = 0; q < np; ++q) {
+        int c = s_cls[q];
+        diffuse = fma(cdiff[(size_t)c * nb + b], gj[c * cstride], diffuse);
+    }
+    const size_t row = (size_t)nd * nb * nt;
+    T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead + t;  // padded rows, stride rs
+    T* et = etot + (size_t)j * row + (size_t)b * nt + t;
+    for (int o = 0; o < nd; ++o) {
+        T v = diffuse;
+        for (int q = s_inv_off[o]; q < s_inv_off[o + 1]; ++q) {
+            int c = s_inv[q];
+            v = fma(cspec[(size_t)c * nb + b], gj[c * cstride], v);
+        }
+        ek[(size_t)o * nb * rs] = v;
+        et[o * cstride] += v;
     }
 }
 
 template <typename T>
-__global__ void k_init_energy_s(int n, int nd, int nb, int nt, const double* __restrict__ e0dir,
+__global__ void k_init_energy_t(int n, int nd, int nb, int nt, long long rs, int lead, const double* __restrict__ e0dir,
                                 const double* __restrict__ d0, double c, double dt, T* __restrict__ etot,
                                 T* __restrict__ eprev, int* __restrict__ err) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -120,203 +656,202 @@ __global__ void k_init_energy_s(int n, int nd, int nb, int nt, const double* __r
         atomicExch(err, 1);
         return;
     }
-    size_t off = (size_t)e * nt + dly;
     T v = (T)e0dir[e];
-    etot[off] = v;
-    eprev[off] = v;
+    etot[(size_t)e * nt + dly] = v;
+    eprev[(size_t)e * rs + lead + dly] = v;
 }
 
 template <typename T>
-__global__ void k_convert_s(long long count, const double* __restrict__ in, T* __restrict__ out) {
+__global__ void k_convert_t(long long count, const double* __restrict__ in, T* __restrict__ out) {
     long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e < count) out[e] = (T)in[e];
 }
 
-// One order of the structured exchange.  grid (receiver, time chunk, band).
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_exchange_structured(
-    int nd, int nb, int nt, const int64_t* __restrict__ off, const int32_t* __restrict__ s_src,
-    const int32_t* __restrict__ s_odir, const int32_t* __restrict__ s_delay, const int32_t* __restrict__ s_cls,
-    const T* __restrict__ s_w, const T* __restrict__ cdiff, const T* __restrict__ cspec,
-    const int32_t* __restrict__ ctarget, const T* __restrict__ eprev, T* __restrict__ ecur, T* __restrict__ etot) {
-    constexpr int R = Cfg<T>::R;
-    constexpr int CH = kThreads * R;
-    extern __shared__ unsigned char s_raw[];
-    T* spec = reinterpret_cast<T*>(s_raw);  // [nd][CH]
-    const int j = blockIdx.x, b = blockIdx.z;
-    const int t0 = blockIdx.y * CH;
-    for (int o = 0; o < nd; ++o)
-#pragma unroll
-        for (int r = 0; r < R; ++r) spec[o * CH + r * kThreads + threadIdx.x] = T(0);
-    T diffuse[R], run[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) diffuse[r] = run[r] = T(0);
-    const size_t row = (size_t)nd * nb * nt;
-    int cur = -1;
-    const long long e_beg = off[j], e_end = off[j + 1];
-    for (long long e = e_beg; e < e_end; ++e) {
-        int c = s_cls[e];
-        if (c != cur) {
-            if (cur >= 0) {
-                T u = cdiff[(size_t)cur * nb + b], v = cspec[(size_t)cur * nb + b];
-                int m = ctarget[cur];
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    diffuse[r] += u * run[r];
-                    if (m >= 0) spec[m * CH + r * kThreads + threadIdx.x] += v * run[r];
-                    run[r] = T(0);
-                }
-            }
-            cur = c;
-        }
-        const int nsh = s_delay[e];
-        const T w = s_w[e * nb + b];
-        const T* in = eprev + (size_t)s_src[e] * row + ((size_t)s_odir[e] * nb + b) * nt;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            int t = t0 + r * kThreads + threadIdx.x;
-            int ts = t - nsh;
-            if (t < nt && ts >= 0) run[r] += w * in[ts];
-        }
-    }
-    if (cur >= 0) {
-        T u = cdiff[(size_t)cur * nb + b], v = cspec[(size_t)cur * nb + b];
-        int m = ctarget[cur];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            diffuse[r] += u * run[r];
-            if (m >= 0) spec[m * CH + r * kThreads + threadIdx.x] += v * run[r];
-        }
-    }
-    for (int o = 0; o < nd; ++o) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            int t = t0 + r * kThreads + threadIdx.x;
-            if (t < nt) {
-                size_t idx = (size_t)j * row + ((size_t)o * nb + b) * nt + t;
-                T val = diffuse[r] + spec[o * CH + r * kThreads + threadIdx.x];
-                ecur[idx] = val;
-                etot[idx] += val;
-            }
-        }
-    }
-}
-
-template <typename T>
-struct Layout {
-    T* eprev;
-    T* ecur;
+// ------------------------------------------------------------ layout
+struct Plan {
+    size_t bytes;
+    int lead;          // zero elements before bin 0 of every padded histogram row
+    size_t rs;         // padded row stride (elements)
+    size_t rows;       // N * D * B
+    void* eprev;
+    void* ecur;
+    void* g;
     int32_t* delay;
     int32_t* cls;
     int64_t* perm;
-    int32_t* s_src;
-    int32_t* s_odir;
-    int32_t* s_delay;
-    int32_t* s_cls;
-    T* s_w;
-    T* cdiff;
-    T* cspec;
+    int32_t* row_of;
+    int64_t* merged;
+    int64_t* rco;
+    int32_t* tile_recv;
+    int32_t* tile_of;
+    int32_t* slot_of;
+    int64_t* seg_size;
+    int64_t* seg_base;
+    int64_t* seg_off;
+    int64_t* cell_count;
+    int64_t* cell_base;
+    int64_t* scan_tmp;
+    Group* groups;
+    void* coef;
+    void* cdiff;
+    void* cspec;
     int* err;
-    size_t bytes;
 };
 
-template <typename T>
-Layout<T> layout(void* base, int n, int nd, int nb, int nt, long long p, int n_class) {
-    Layout<T> L;
+Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p, int n_class) {
+    Plan L;
     char* q = (char*)base;
-    size_t e = (size_t)n * nd * nb * nt;
     auto take = [&](size_t bytes) {
         char* r = q;
         q += sp_align(bytes);
-        return r;
+        return (void*)r;
     };
-    L.eprev = (T*)take(e * sizeof(T));
-    L.ecur = (T*)take(e * sizeof(T));
+    int n_tiles = (n + kTile - 1) / kTile;
+    // padded histogram rows: `lead` zeros, then nt bins; stride rs (multiple
+    // of 4 elements so rows stay 16-byte aligned); a tail after the last row
+    // keeps the staged windows of the last rows inside the allocation
+    L.lead = (int)((((size_t)nt + 20) + 3) & ~(size_t)3);
+    L.rs = (((size_t)nt + L.lead) + 3) & ~(size_t)3;
+    L.rows = (size_t)n * nd * nb;
+    size_t tail = (size_t)kStageF + 64;
+    L.eprev = take((L.rows * L.rs + tail) * esz);
+    L.ecur = take((L.rows * L.rs + tail) * esz);
+    L.g = take((size_t)n * n_class * nb * nt * esz);
     L.delay = (int32_t*)take((size_t)p * 4);
     L.cls = (int32_t*)take((size_t)p * 4);
     L.perm = (int64_t*)take((size_t)p * 8);
-    L.s_src = (int32_t*)take((size_t)p * 4);
-    L.s_odir = (int32_t*)take((size_t)p * 4);
-    L.s_delay = (int32_t*)take((size_t)p * 4);
-    L.s_cls = (int32_t*)take((size_t)p * 4);
-    L.s_w = (T*)take((size_t)p * nb * sizeof(T));
-    L.cdiff = (T*)take((size_t)n_class * nb * sizeof(T));
-    L.cspec = (T*)take((size_t)n_class * nb * sizeof(T));
+    L.row_of = (int32_t*)take((size_t)p * 4);
+    L.merged = (int64_t*)take((size_t)p * 8);
+    L.rco = (int64_t*)take((size_t)n * (n_class + 1) * 8);
+    L.tile_recv = (int32_t*)take((size_t)n_tiles * kTile * 4);
+    L.tile_of = (int32_t*)take((size_t)n * 4);
+    L.slot_of = (int32_t*)take((size_t)n * 4);
+    long long n_seg = (long long)n_tiles * n_class;
+    L.seg_size = (int64_t*)take(((size_t)n_seg + 1) * 8);
+    L.seg_base = (int64_t*)take(((size_t)n_seg + 1) * 8);
+    L.seg_off = (int64_t*)take(((size_t)n_seg + 1) * 8);
+    L.cell_count = (int64_t*)take(((size_t)p + 1) * 8);
+    L.cell_base = (int64_t*)take(((size_t)p + 1) * 8);
+    long long big = p > n_seg ? p : n_seg;
+    L.scan_tmp = (int64_t*)take(((size_t)(big / kScanBlock) + 2) * 8);
+    L.groups = (Group*)take((size_t)(p + 1) * sizeof(Group));
+    L.coef = take((size_t)(p + 1) * nb * kTile * esz);
+    L.cdiff = take((size_t)n_class * nb * esz);
+    L.cspec = take((size_t)n_class * nb * esz);
     L.err = (int*)take(16);
     L.bytes = (size_t)(q - (char*)base);
     return L;
 }
 
-constexpr int kMaxClasses = 8192;
+void scan64(long long n, const int64_t* in, int64_t* out, int64_t* tmp, cudaStream_t st) {
+    // out[0..n] exclusive scan, out[n] = total
+    long long nblocks = (n + kScanBlock - 1) / kScanBlock;
+    if (nblocks < 1) nblocks = 1;
+    k_scan_blocks<<<(unsigned)nblocks, kScanBlock, 0, st>>>(n, in, out, tmp);
+    k_scan_sums<<<1, 32, 0, st>>>(nblocks, tmp, out + n);
+    k_scan_add<<<(unsigned)nblocks, kScanBlock, 0, st>>>(n, out, tmp);
+}
 
 template <typename T>
-int run_structured(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t st) {
+int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t st) {
     const int n = a->n_patches, nd = a->n_dirs, nb = a->n_bins, nt = a->n_samples;
     const long long p = a->n_dir_pairs;
     if (!a->slot_group || !a->slot_scale || !a->class_diff || !a->class_spec || !a->class_target || a->n_groups < 1)
         return SP_ERR_ARG;
     const int n_class = a->n_groups * a->n_in_dirs;
     if (n_class > kMaxClasses) return SP_ERR_UNSUPPORTED;
-    Layout<T> L = layout<T>(nullptr, n, nd, nb, nt, p, kMaxClasses);
+    Plan L = plan_layout(nullptr, sizeof(T), n, nd, nb, nt, p, n_class);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = layout<T>(ws, n, nd, nb, nt, p, kMaxClasses);
+    L = plan_layout(ws, sizeof(T), n, nd, nb, nt, p, n_class);
+    const int n_tiles = (n + kTile - 1) / kTile;
+    const long long n_seg = (long long)n_tiles * n_class;
     const size_t e = (size_t)n * nd * nb * nt;
     T* etot = (T*)a->etc_total;
+    T* eprev = (T*)L.eprev;
+    T* ecur = (T*)L.ecur;
+    const long long rs = (long long)L.rs;
+    const int lead = L.lead;
     cudaMemsetAsync(L.err, 0, sizeof(int), st);
     cudaMemsetAsync(etot, 0, e * sizeof(T), st);
-    cudaMemsetAsync(L.eprev, 0, e * sizeof(T), st);
+    // eprev: all zero before the initial energies are placed; ecur: only the
+    // leads need zeros (every bin is written each order)
+    cudaMemsetAsync(eprev, 0, (L.rows * L.rs + kStageF + 64) * sizeof(T), st);
+    cudaMemset2DAsync(ecur, L.rs * sizeof(T), 0, (size_t)lead * sizeof(T), L.rows, st);
     long long ne = (long long)n * nd * nb;
-    k_init_energy_s<T><<<sp_blocks(ne, 256), 256, 0, st>>>(n, nd, nb, nt, a->energy_0_dir, a->distance_0,
-                                                           a->speed_of_sound, a->time_resolution, etot, L.eprev, L.err);
+    k_init_energy_t<T><<<sp_blocks(ne, 256), 256, 0, st>>>(n, nd, nb, nt, rs, lead, a->energy_0_dir, a->distance_0,
+                                                           a->speed_of_sound, a->time_resolution, etot, eprev, L.err);
     int herr = 0;
     cudaMemcpyAsync(&herr, L.err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
     if (herr) return SP_ERR_RANGE;
     if (a->max_order < 1 || p == 0) return sp_check_launch();
 
-    k_delays_s<<<sp_blocks(p, 256), 256, 0, st>>>(p, a->pair_distance, a->speed_of_sound, a->time_resolution, L.delay);
-    k_pair_class<<<sp_blocks(p, 256), 256, 0, st>>>(p, a->pair_src, a->pair_in_dir, a->wall_of, a->brdf_index,
-                                                    a->slot_group, a->n_in_dirs, L.cls);
-    k_row_sort_by_class<<<n, 32, n_class * sizeof(int), st>>>(n, a->dst_offset, L.cls, n_class, L.perm);
-    k_gather_pairs<T><<<sp_blocks(p, 256), 256, 0, st>>>(p, nb, L.perm, a->pair_src, a->pair_out_dir, L.delay, L.cls,
-                                                         a->pair_fprime, a->pair_unit_len, a->air_attenuation,
-                                                         a->wall_of, a->brdf_index, a->slot_scale, L.s_src, L.s_odir,
-                                                         L.s_delay, L.s_cls, L.s_w);
+    // ---- plan
+    k_delays_t<<<sp_blocks(p, 256), 256, 0, st>>>(p, a->pair_distance, a->speed_of_sound, a->time_resolution, L.delay);
+    k_pair_class_t<<<sp_blocks(p, 256), 256, 0, st>>>(p, a->pair_src, a->pair_in_dir, a->wall_of, a->brdf_index,
+                                                      a->slot_group, a->n_in_dirs, L.cls);
+    k_row_sort_by_class_t<<<n, 32, n_class * sizeof(int), st>>>(n, a->dst_offset, L.cls, n_class, L.perm, L.rco,
+                                                                L.row_of);
+    k_default_tiles<<<sp_blocks((long long)n_tiles * kTile, 256), 256, 0, st>>>(n, n_tiles, a->receiver_order,
+                                                                               L.tile_recv, L.tile_of, L.slot_of);
+    k_seg_size<<<sp_blocks(n_seg, 256), 256, 0, st>>>(n_seg, n_class, L.tile_recv, L.rco, L.seg_size);
+    scan64(n_seg, L.seg_size, L.seg_base, L.scan_tmp, st);
+    k_merge_positions<<<sp_blocks(p, 256), 256, 0, st>>>(p, n_class, L.perm, L.row_of, L.cls, a->pair_src, L.rco,
+                                                         L.tile_of, L.slot_of, L.tile_recv, L.seg_base, L.merged);
+    k_cells<T><<<sp_blocks(p, 128), 128, 0, st>>>(p, nd, nb, nt, L.merged, a->pair_src, a->pair_dst, a->pair_out_dir,
+                                                  L.delay, L.cls, L.tile_of, L.slot_of, a->pair_fprime,
+                                                  a->pair_unit_len, a->air_attenuation, a->wall_of, a->brdf_index,
+                                                  a->slot_scale, 0, L.cell_count, nullptr, p, nullptr, nullptr);
+    scan64(p, L.cell_count, L.cell_base, L.scan_tmp, st);
+    k_cells<T><<<sp_blocks(p, 128), 128, 0, st>>>(p, nd, nb, nt, L.merged, a->pair_src, a->pair_dst, a->pair_out_dir,
+                                                  L.delay, L.cls, L.tile_of, L.slot_of, a->pair_fprime,
+                                                  a->pair_unit_len, a->air_attenuation, a->wall_of, a->brdf_index,
+                                                  a->slot_scale, 1, nullptr, L.cell_base, p, L.groups, (T*)L.coef);
+    k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, st>>>(n_seg, p, L.seg_base, L.cell_base, L.seg_off);
     long long nc = (long long)n_class * nb;
-    k_convert_s<T><<<sp_blocks(nc, 256), 256, 0, st>>>(nc, a->class_diff, L.cdiff);
-    k_convert_s<T><<<sp_blocks(nc, 256), 256, 0, st>>>(nc, a->class_spec, L.cspec);
+    k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, st>>>(nc, a->class_diff, (T*)L.cdiff);
+    k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, st>>>(nc, a->class_spec, (T*)L.cspec);
 
-    constexpr int CH = kThreads * Cfg<T>::R;
-    size_t smem = (size_t)nd * CH * sizeof(T);
-    if (smem > 227 * 1024) return SP_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_exchange_structured<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid(n, (nt + CH - 1) / CH, nb);
-    T* eprev = L.eprev;
-    T* ecur = L.ecur;
+    // ---- orders
+    dim3 mgrid((nt + 255) / 256, nb, n);
+    size_t msmem = (size_t)(2 * n_class + nd + 1) * sizeof(int);
     for (int k = 0; k < a->max_order; ++k) {
-        k_exchange_structured<T><<<grid, kThreads, smem, st>>>(nd, nb, nt, a->dst_offset, L.s_src, L.s_odir, L.s_delay,
-                                                               L.s_cls, L.s_w, L.cdiff, L.cspec, a->class_target, eprev,
-                                                               ecur, etot);
+        if constexpr (sizeof(T) == 4) {
+            size_t smem = (size_t)kStages * kStageF * 4 + kChunk * sizeof(Group) + kChunk * kTile * 4 +
+                          2 * kStages * 8 + 128;
+            if (k == 0) cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            dim3 sgrid((unsigned)n_seg, (nt + kTW - 1) / kTW, nb);
+            k_scatter_f32<<<sgrid, kThreads, smem, st>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off,
+                                                         L.groups, (const float*)L.coef, (const float*)eprev,
+                                                         (float*)L.g, L.err);
+        } else {
+            dim3 sgrid((unsigned)n_seg, (nt + kThreads * kR64 - 1) / (kThreads * kR64), nb);
+            k_scatter_f64<<<sgrid, kThreads, 0, st>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off, L.groups,
+                                                      (const double*)L.coef, (const double*)eprev, (double*)L.g);
+        }
+        k_mix<T><<<mgrid, 256, msmem, st>>>(n_class, nd, nb, nt, rs, lead, L.tile_of, L.seg_off, (const T*)L.cdiff,
+                                           (const T*)L.cspec, a->class_target, (const T*)L.g, ecur, etot);
         T* tmp = eprev;
         eprev = ecur;
         ecur = tmp;
     }
-    return sp_check_launch();
+    int rc = sp_check_launch();
+    if (rc != SP_OK) return rc;
+    cudaMemcpyAsync(&herr, L.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+    return herr ? SP_ERR_TIMEOUT : SP_OK;
 }
 
 }  // namespace
 
 size_t sp_structured_workspace(int precision, int n_patches, int n_dirs, int n_bins, int n_samples,
-                               long long n_dir_pairs, int n_slots, int n_in_dirs) {
-    (void)n_slots;
-    (void)n_in_dirs;
-    if (precision == SP_F64)
-        return layout<double>(nullptr, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, kMaxClasses).bytes;
-    return layout<float>(nullptr, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, kMaxClasses).bytes;
+                               long long n_dir_pairs, int n_class) {
+    int esz = precision == SP_F64 ? 8 : 4;
+    return plan_layout(nullptr, esz, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_class).bytes;
 }
 
 int sp_run_structured(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t st) {
-    if (a->precision == SP_F64) return run_structured<double>(a, ws, ws_bytes, st);
-    return run_structured<float>(a, ws, ws_bytes, st);
+    if (!a->pair_dst) return SP_ERR_ARG;
+    if (a->precision == SP_F64) return run_tiled<double>(a, ws, ws_bytes, st);
+    return run_tiled<float>(a, ws, ws_bytes, st);
 }

@@ -98,6 +98,28 @@ def analyse_brdf(brdf, rel_tol=1e-12):
                 class_target=class_target.astype(np.int32))
 
 
+def receiver_tile_order(centers, normals, bits=10):
+    """Receiver order for the tiled exchange: grouped by normal, then Morton order.
+
+    Consecutive groups of 8 receivers in this order form one tile; compact
+    tiles of coplanar patches see a source in nearly the same direction and
+    delay, which is what lets the exchange kernel reuse a loaded source
+    window across the tile.
+    """
+    centers = np.asarray(centers, dtype=float)
+    if centers.shape[0] == 0:
+        return np.zeros(0, dtype=np.int32)
+    lo = centers.min(axis=0)
+    span = np.maximum(centers.max(axis=0) - lo, 1e-12)
+    q = np.clip(((centers - lo) / span * ((1 << bits) - 1)).astype(np.int64), 0, (1 << bits) - 1)
+    code = np.zeros(centers.shape[0], dtype=np.int64)
+    for bit in range(bits):
+        for axis in range(3):
+            code |= ((q[:, axis] >> bit) & 1) << (3 * bit + axis)
+    _, nid = np.unique(np.round(np.asarray(normals, float), 6), axis=0, return_inverse=True)
+    return np.lexsort((code, nid.reshape(-1))).astype(np.int32)
+
+
 class DirectionalRadiosityFast:
     """Radiosity object for directional scattering coefficients (GB300)."""
 
@@ -395,7 +417,9 @@ class DirectionalRadiosityFast:
             plan = dict(brdf=bs["brdf"], brdf_index=bs["brdf_index"], n_slots=bs["n_slots"], n_in=bs["n_in"],
                         n_out=bs["n_out"], host=bs["brdf_host"])
         st = analyse_brdf(plan["host"])
-        if st is not None and st["n_groups"] * plan["n_in"] <= 8192:
+        if st is not None and st["n_groups"] * plan["n_in"] <= 256:
+            plan["receiver_order"] = self._t(receiver_tile_order(self.patches_center, self.patches_normal),
+                                             torch.int32)
             plan["structured"] = dict(
                 slot_group=self._t(st["slot_group"], torch.int32), slot_scale=self._t(st["slot_scale"], torch.float64),
                 n_groups=st["n_groups"], class_diff=self._t(st["class_diff"], torch.float64),
@@ -461,6 +485,8 @@ class DirectionalRadiosityFast:
             a.class_diff = s["class_diff"].data_ptr()
             a.class_spec = s["class_spec"].data_ptr()
             a.class_target = s["class_target"].data_ptr()
+            a.receiver_order = plan["receiver_order"].data_ptr()
+            a.pair_dst = bk["dst"].data_ptr()
         return a
 
     def _run_exchange(self, c, dt, n_samples, max_order, algorithm="auto"):
@@ -470,7 +496,7 @@ class DirectionalRadiosityFast:
         etc = torch.empty((n, nd, nb, n_samples), dtype=dtype, device=self.device)
         a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
         wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
-                       a.n_dir_pairs, a.n_slots, a.n_in_dirs)
+                       a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups * a.n_in_dirs)
         ws = self._workspace(wsz)
         rc = nat.lib().sp_energy_exchange(ctypes.byref(a), _ptr(ws), wsz, _stream())
         if rc == nat.SP_ERR_RANGE:

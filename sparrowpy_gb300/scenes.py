@@ -148,7 +148,9 @@ def rotated_room(patch_size=0.5, n_dirs=8, n_bins=2, seed=3, precision="fp32", d
     positive BRDF table without that structure when ``dense_box``.
     """
     room = shoebox_room_stub(3.0, 2.0, 2.0)
-    box = _box_faces(1.2, 1.8, 0.7, 1.3, 0.0, 0.6, skip_y0=False)
+    # box corners off the patch grid: no centre-to-centre segment passes
+    # exactly through a box edge (generic position)
+    box = _box_faces(1.2113, 1.8187, 0.7071, 1.3091, 0.0, 0.6133, skip_y0=False)
     box = [f for f in box if f.normal[2] != -1]  # no face on the floor
     walls = room + box
     wp = np.array([w.pts for w in walls])
@@ -158,7 +160,13 @@ def rotated_room(patch_size=0.5, n_dirs=8, n_bins=2, seed=3, precision="fp32", d
     rot = lambda a: a @ ROT.T
     r = DirectionalRadiosityFast(rot(wp) + SHIFT, rot(wn), rot(wu), rot(pp) + SHIFT, n, p2w, precision=precision)
     freqs = OCTAVES[3:3 + n_bins]
-    dirs = hemisphere_directions(n_dirs)
+    # seeded jitter of the direction set: a ring of equal colatitudes is
+    # equidistant to a vector along the wall normal (an exact argmin tie)
+    rng_d = np.random.default_rng(seed + 100)
+    base = hemisphere_directions(n_dirs)
+    col = np.clip(base.colatitude + rng_d.uniform(-0.08, 0.08, base.csize), 0.05, np.pi / 2 - 0.05)
+    az = base.azimuth + rng_d.uniform(-0.08, 0.08, base.csize)
+    dirs = Coordinates.from_spherical_colatitude(az, col, 1.0, weights=base.weights)
     brdf = create_from_scattering(dirs, dirs, FrequencyData(np.full(n_bins, 0.3), freqs),
                                   FrequencyData(np.linspace(0.1, 0.2, n_bins), freqs))
     r.set_wall_brdf(np.arange(6), brdf, dirs, dirs)

@@ -50,9 +50,11 @@ def test_workspace_queries_without_gpu():
     from sparrowpy_gb300 import _native as nat
     if not os.path.exists(nat.LIB_PATH):
         pytest.skip("library not built")
-    a = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_DENSE, 10, 4, 2, 100, 50, 1, 4)
-    b = nat.size("sp_energy_exchange_workspace", nat.SP_F64, nat.SP_EXCHANGE_DENSE, 10, 4, 2, 100, 50, 1, 4)
+    a = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_DENSE, 10, 4, 2, 100, 50, 1, 4, 0)
+    b = nat.size("sp_energy_exchange_workspace", nat.SP_F64, nat.SP_EXCHANGE_DENSE, 10, 4, 2, 100, 50, 1, 4, 0)
     assert b > a > 2 * 10 * 4 * 2 * 100 * 4
+    s = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_STRUCTURED, 10, 4, 2, 100, 50, 1, 4, 4)
+    assert s > 3 * 10 * 4 * 2 * 100 * 4
     assert nat.size("sp_patch_visibility_workspace", 100) >= 100 * 24
 
 
