@@ -46,6 +46,10 @@ enum { SP_EXCHANGE_DENSE = 0, SP_EXCHANGE_STRUCTURED = 1 };
 /* Library version string (static storage). */
 const char* sp_version(void);
 
+/* Number of CUDA kernels this library has launched in the process so far
+ * (host counter; no GPU work). */
+long long sp_kernel_launches(void);
+
 /* ---------------------------------------------------------------- geometry */
 
 /* Patch centres (vertex mean) and areas (fan triangulation).
@@ -174,6 +178,8 @@ typedef struct sp_exchange_args {
     const int32_t* class_target;/* (n_groups * n_in) mirror direction, -1 if none */
     const int32_t* receiver_order; /* (N) receivers in tile order (8 per tile), NULL = 0..N-1 */
     const int32_t* pair_dst;       /* (P) destination of each directed pair (structured algorithm) */
+    int64_t* plan_stats;           /* HOST array of 4 or NULL: source groups, segments, pairs kept, tiles */
+    float* order_ms;               /* HOST float or NULL: CUDA-event time of the order loop (all orders) */
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070

@@ -647,6 +647,65 @@ int orc_exchange(int n, int nd, int nb, int nt, int max_order, const double* e0d
     return 0;
 }
 
+// Timing samples for the CPU baseline (same loops as above, on a subset).
+// Rows i0 <= i < i1 (step stride) of geometry.py:750-797; returns the
+// visible count.  With full != 0 a row covers every j != i (the pair
+// evaluated as (min, max), i.e. one row of the symmetric matrix), else j > i.
+long long orc_patch_visibility_rows(int n, int nv, const double* centers, const double* normals,
+                                    const double* points, int i0, int i1, int stride, int full, uint8_t* vis_rows) {
+    long long total = 0;
+    int rows = 0;
+    for (int i = i0; i < i1; i += stride) ++rows;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (int r = 0; r < rows; ++r) {
+        int i = i0 + r * stride;
+        for (int j = full ? 0 : i + 1; j < n; ++j) {
+            if (j == i) continue;
+            int a = i < j ? i : j, b = i < j ? j : i;
+            bool v = true;
+            for (int s = 0; s < n && v; ++s)
+                v = basic_visibility(centers + 3 * a, centers + 3 * b, points + (size_t)s * nv * 3, nv,
+                                     normals + 3 * s);
+            if (vis_rows) vis_rows[(size_t)r * n + j] = v ? 1 : 0;
+            total += v ? 1 : 0;
+        }
+    }
+    return total;
+}
+
+// One order of RadiosityFast.py:1121-1143 for destination rows
+// rows[0..n_rows) only, with the destination-major pair list (dst_off, src,
+// ...).  Source rows are read from `prev` at row (src % prev_rows) (the cost
+// does not depend on the values).  Returns the sum of the produced values.
+double orc_exchange_rows_sample(int nd, int nb, int nt, const double* prev, int prev_rows, const int64_t* dst_off,
+                                const int32_t* src, const int32_t* p2o, const int32_t* delay, const double* fprime,
+                                const double* att_fac, const int32_t* slot, const int32_t* s_in, const double* brdf,
+                                int n_in, int n_rows, const int32_t* rows) {
+    const size_t row = (size_t)nd * nb * nt;
+    double total = 0.0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+    for (int q = 0; q < n_rows; ++q) {
+        int j = rows[q];
+        std::vector<double> out(row, 0.0);
+        for (int64_t e = dst_off[j]; e < dst_off[j + 1]; ++e) {
+            int i = src[e] % prev_rows;
+            int nsh = delay[e];
+            const double* brow = brdf + (((size_t)slot[e] * n_in + s_in[e]) * nd) * nb;
+            for (int o = 0; o < nd; ++o)
+                for (int b = 0; b < nb; ++b) {
+                    double f = (fprime[e] * att_fac[(size_t)e * nb + b]) * brow[(size_t)o * nb + b];
+                    const double* in = prev + (size_t)i * row + ((size_t)p2o[e] * nb + b) * nt;
+                    double* o_ = out.data() + ((size_t)o * nb + b) * nt;
+                    for (int t = nsh; t < nt; ++t) o_[t] += f * in[t - nsh];
+                }
+        }
+        double s = 0.0;
+        for (size_t k = 0; k < row; ++k) s += out[k];
+        total += s;
+    }
+    return total;
+}
+
 // RadiosityFast.py:686-752 `_collect_energy_patches` + :1148-1185
 // `_collect_receiver_energy` for one receiver: out is (N, B, T).
 int orc_collect(int n, int nd, int nb, int nt, const double* etot, const int32_t* ridx, const double* rfac,

@@ -275,3 +275,31 @@ def solve(scene, src_pos, receivers, c, dt, duration, max_order):
     etot = exchange(scene, bk, e0dir, d0, c, dt, nt, max_order)
     mono = collect(scene, bk, etot, receivers, c, dt)
     return dict(bake=bk, e0dir=e0dir, d0=d0, svis=svis, etot=etot, mono=mono)
+
+
+# ------------------------------------------------- CPU-baseline timing samples
+def visibility_rows_sample(ctr, normals, points, i0, i1, stride, full=False):
+    """Rows i0, i0 + stride, ... < i1 of the visibility matrix (geometry.py:750-797 loop).
+
+    Returns (visible count, rows (R, N) uint8).  ``full`` evaluates every
+    j != i of a row (the symmetric matrix's row), else only j > i.
+    """
+    lib().orc_patch_visibility_rows.restype = ctypes.c_longlong
+    ctr, normals, points = _c(ctr, float), _c(normals, float), _c(points, float)
+    n = ctr.shape[0]
+    rows = np.zeros((len(range(int(i0), int(i1), int(stride))), n), dtype=np.uint8)
+    cnt = int(lib().orc_patch_visibility_rows(n, points.shape[1], _p(ctr), _p(normals), _p(points), int(i0), int(i1),
+                                              int(stride), int(bool(full)), _p(rows)))
+    return cnt, rows
+
+
+def exchange_rows_sample(nd, nb, nt, prev, dst_off, src, p2o, delay, fprime, att_fac, slot, s_in, brdf, rows):
+    """One exchange order for the given destination rows (RadiosityFast.py:1121-1143 loop)."""
+    lib().orc_exchange_rows_sample.restype = ctypes.c_double
+    args = [_c(prev, float), _c(dst_off, np.int64), _c(src, np.int32), _c(p2o, np.int32), _c(delay, np.int32),
+            _c(fprime, float), _c(att_fac, float), _c(slot, np.int32), _c(s_in, np.int32), _c(brdf, float),
+            _c(rows, np.int32)]
+    prev_rows = args[0].shape[0]
+    return float(lib().orc_exchange_rows_sample(nd, nb, nt, _p(args[0]), prev_rows, _p(args[1]), _p(args[2]),
+                                                _p(args[3]), _p(args[4]), _p(args[5]), _p(args[6]), _p(args[7]),
+                                                _p(args[8]), _p(args[9]), brdf.shape[1], len(rows), _p(args[10])))

@@ -52,13 +52,15 @@ class ExchangeArgs(ctypes.Structure):
         ("etc_total", P),
         ("slot_group", P), ("slot_scale", P), ("n_groups", I),
         ("class_diff", P), ("class_spec", P), ("class_target", P),
-        ("receiver_order", P), ("pair_dst", P),
+        ("receiver_order", P), ("pair_dst", P), ("plan_stats", ctypes.POINTER(ctypes.c_int64)),
+        ("order_ms", ctypes.POINTER(ctypes.c_float)),
     ]
 
 
 # name: (restype, argtypes)
 _SIGS = {
     "sp_version": (ctypes.c_char_p, []),
+    "sp_kernel_launches": (LL, []),
     "sp_patch_geometry": (I, [I, I, P, P, P, P]),
     "sp_patch_visibility_workspace": (SZ, [I]),
     "sp_patch_visibility": (I, [I, I, P, P, P, P, P, SZ, P]),

@@ -51,6 +51,14 @@ __device__ __forceinline__ int sp_nearest_dir(const double* from, const double* 
     return best;
 }
 
+// Every kernel launch of the library passes its stream through sp_counted(),
+// which counts launches (read with sp_kernel_launches()).
+void sp_note_launch();
+inline cudaStream_t sp_counted(cudaStream_t st) {
+    sp_note_launch();
+    return st;
+}
+
 inline int sp_check_launch() {
     cudaError_t e = cudaGetLastError();
     return (e == cudaSuccess) ? SP_OK : SP_ERR_CUDA;

@@ -154,7 +154,7 @@ int run_exchange_dense(const sp_exchange_args* a, void* ws, size_t ws_bytes, cud
     cudaMemsetAsync(eprev, 0, e * sizeof(T), st);
     long long ne = (long long)n * nd * nb;
     if (ne > 0)
-        k_init_energy<T><<<sp_blocks(ne, 256), 256, 0, st>>>(n, nd, nb, nt, a->energy_0_dir, a->distance_0,
+        k_init_energy<T><<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(n, nd, nb, nt, a->energy_0_dir, a->distance_0,
                                                              a->speed_of_sound, a->time_resolution, etot, eprev, err);
     int hrr = 0;
     cudaMemcpyAsync(&hrr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -162,26 +162,33 @@ int run_exchange_dense(const sp_exchange_args* a, void* ws, size_t ws_bytes, cud
     if (hrr) return SP_ERR_RANGE;
     if (a->max_order < 1 || n_dir == 0) return sp_check_launch();
 
-    k_pair_delays<<<sp_blocks(n_dir, 256), 256, 0, st>>>(n_dir, a->pair_distance, a->speed_of_sound,
+    k_pair_delays<<<sp_blocks(n_dir, 256), 256, 0, sp_counted(st)>>>(n_dir, a->pair_distance, a->speed_of_sound,
                                                           a->time_resolution, delay);
-    k_pair_base<T><<<sp_blocks(n_dir, 256), 256, 0, st>>>(n_dir, nb, a->pair_fprime, a->pair_unit_len,
+    k_pair_base<T><<<sp_blocks(n_dir, 256), 256, 0, sp_counted(st)>>>(n_dir, nb, a->pair_fprime, a->pair_unit_len,
                                                           a->air_attenuation, base);
     long long nbr = (long long)a->n_slots * a->n_in_dirs * nd * nb;
-    k_convert<T><<<sp_blocks(nbr, 256), 256, 0, st>>>(nbr, a->brdf, brdf);
-    k_slot_of_patch<<<sp_blocks(n, 128), 128, 0, st>>>(n, a->wall_of, a->brdf_index, slot);
+    k_convert<T><<<sp_blocks(nbr, 256), 256, 0, sp_counted(st)>>>(nbr, a->brdf, brdf);
+    k_slot_of_patch<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(n, a->wall_of, a->brdf_index, slot);
 
     size_t smem = (size_t)nd * kChunk * sizeof(T);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_exchange_dense<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((nt + kChunk - 1) / kChunk, nb, n);
+    SpEventTimer timer(a->order_ms != nullptr, st);
     for (int k = 0; k < a->max_order; ++k) {
-        k_exchange_dense<T><<<grid, kChunk, smem, st>>>(n, nd, nb, nt, a->dst_offset, a->pair_src, a->pair_out_dir,
+        k_exchange_dense<T><<<grid, kChunk, smem, sp_counted(st)>>>(n, nd, nb, nt, a->dst_offset, a->pair_src, a->pair_out_dir,
                                                         a->pair_in_dir, delay, base, slot, a->n_in_dirs, brdf, eprev,
                                                         ecur, etot);
         T* tmp = eprev;
         eprev = ecur;
         ecur = tmp;
     }
-    return sp_check_launch();
+    timer.stop(st);
+    int rc = sp_check_launch();
+    if (rc == SP_OK && a->order_ms) {
+        if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+        *a->order_ms = timer.elapsed_ms();
+    }
+    return rc;
 }
 
 // RadiosityFast.py:686-752 + :1148-1185 for one receiver: per patch k the
@@ -249,14 +256,14 @@ int run_collect(int n, int nd, int nb, int nt, const void* etot, const int32_t* 
     if (ws_bytes < need) return SP_ERR_WORKSPACE;
     double* coef = (double*)ws;
     int32_t* shift = (int32_t*)((char*)ws + sp_align((size_t)n * nb * 2 * sizeof(double)));
-    k_collect_coef<<<sp_blocks(n, 128), 128, 0, st>>>(n, nb, nt, rfac, dist, c, dt, att, coef, shift);
+    k_collect_coef<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(n, nb, nt, rfac, dist, c, dt, att, coef, shift);
     if (patchwise) {
         dim3 g((nt + 255) / 256, nb, n);
-        k_collect_patchwise<T><<<g, 256, 0, st>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift, patchwise);
+        k_collect_patchwise<T><<<g, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift, patchwise);
     }
     if (mono) {
         dim3 g((nt + 127) / 128, nb);
-        k_collect_mono<T><<<g, 128, 0, st>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift, mono);
+        k_collect_mono<T><<<g, 128, 0, sp_counted(st)>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift, mono);
     }
     return sp_check_launch();
 }

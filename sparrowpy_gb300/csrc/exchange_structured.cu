@@ -10,37 +10,39 @@
 //   E_total += E_k
 // with w_pb = F'_p * exp(-att_b |u_p|) * scale[slot(src_p), b].
 //
-// Plan (once per exchange call): receivers are cut into tiles of 8 (a given
+// Plan (once per exchange call): receivers are cut into tiles of 16 (a given
 // receiver order, normally spatial); a segment is (tile, class).  The
 // segment's pairs are merged by source patch and cut into source groups:
-// one source row (src * D + p2o), up to 8 member receivers, delays within
-// n_base .. n_base + 13.  Everything is built in parallel and
+// one source row (src * D + p2o), up to 16 member receivers, delays within
+// n_base .. n_base + 45.  Everything is built in parallel and
 // deterministically (row-wise class sort, merge by binary search, scans).
 //
-// Scatter (per order, FP32): one CTA per (segment, 2048-bin window, band),
-// 128 threads, each owning 16 consecutive bins of all 8 receivers in
-// registers.  Each group's source window (2064 values) is staged in shared
-// memory by a bulk asynchronous copy (cp.async.bulk + mbarrier, 4 stages);
-// every thread reads its 32-value slice with 8 LDS.128 in a rotated order
-// (conflict-free banks) and applies it to every member with a compile-time
-// shift, so one staged value feeds up to 8 multiply-adds.  FP64 uses the
-// same plan with direct vector loads.  Mix: streams G into E_k and E_total.
+// Scatter (per order, FP32): one CTA per (segment, 1024-bin window, band),
+// 128 threads; thread tid owns bins t0 + tid + 128 r (r < 8) of all 16
+// receivers in registers.  Each group's source window (1072 values) is
+// staged in shared memory by a bulk asynchronous copy (cp.async.bulk +
+// mbarrier, 12 stages, refilled by the last warp to finish a stage); every
+// member reads the staged window at its own delay offset, each warp read
+// covering 32 consecutive floats, so one staged window feeds every member
+// of the group.  FP64 uses the same plan with direct loads.  Mix: streams G
+// into E_k and E_total.
 #include "common.cuh"
 #include "exchange_common.cuh"
 
 namespace {
 
-constexpr int kTile = 8;          // receivers per tile
-constexpr int kMaxSpan = 13;      // max delay spread inside a source group
-constexpr unsigned kAbsent = 0xFu;
+constexpr int kTile = 16;         // receivers per tile
+constexpr int kMaxSpan = 45;      // max delay spread inside a source group
 constexpr int kMaxClasses = 256;
 
 struct Group {
-    int32_t srcrow;   // src * D + p2o
-    int32_t n_base;   // smallest delay of the members
-    uint32_t offs;    // 8 x 4 bits: delay - n_base, 0xF = no member
+    int32_t srcrow;      // src * D + p2o
+    int32_t n_base;      // smallest delay of the members
+    uint32_t mask;       // bit w set: receiver slot w of the tile is a member
     int32_t pad;
+    uint8_t off[kTile];  // per slot: delay - n_base (0 .. kMaxSpan)
 };
+static_assert(sizeof(Group) == 32, "Group is copied in 16-byte units");
 
 // ------------------------------------------------------------------ plan
 __global__ void k_delays_t(long long n_dir, const double* __restrict__ dist, double c, double dt,
@@ -268,13 +270,15 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
             Group g;
             g.srcrow = s_src * nd + mo[a];
             g.n_base = md[a];
-            unsigned offs = 0xFFFFFFFFu;
+            g.mask = 0;
+            g.pad = 0;
+            for (int k = 0; k < kTile; ++k) g.off[k] = 0;
             for (int b = 0; b < nb; ++b)
-                for (int w = 0; w < kTile; ++w) coef[((size_t)b * cap + g_out) * kTile + w] = T(0);
+                for (int k = 0; k < kTile; ++k) coef[((size_t)b * cap + g_out) * kTile + k] = T(0);
             for (int x = a; x <= r; ++x) {
-                int w = mw[x];
-                offs &= ~(0xFu << (4 * w));
-                offs |= (unsigned)(md[x] - md[a]) << (4 * w);
+                const int w = mw[x];
+                g.mask |= 1u << w;
+                g.off[w] = (uint8_t)(md[x] - md[a]);
                 long long ex = me[x];
                 for (int b = 0; b < nb; ++b) {
                     double f = fprime[ex];
@@ -282,8 +286,6 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
                     coef[((size_t)b * cap + g_out) * kTile + w] = (T)(f * slot_scale[(size_t)slot * nb + b]);
                 }
             }
-            g.offs = offs;
-            g.pad = 0;
             groups[g_out] = g;
             ++g_out;
         }
@@ -311,25 +313,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
 }
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     unsigned ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
         : "r"(smem_addr(bar)), "r"(parity)
@@ -356,39 +344,58 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
 
 // --------------------------------------------------------- FP32 scatter
 constexpr int kThreads = 128;
-constexpr int kR = 16;                       // bins per thread
-constexpr int kTW = kThreads * kR;           // 2048 bins per window
-constexpr int kStageF = kTW + 16;            // 2064 floats staged per group
-constexpr int kStages = 6;
-constexpr int kChunk = 256;                  // group headers held in shared memory
+constexpr int kWarps = kThreads / 32;
+constexpr int kR = 8;                        // bins per thread (strided by 128)
+constexpr int kTW = kThreads * kR;           // 1024 bins per window
+constexpr int kStageF = kTW + kMaxSpan + 3;  // staged floats per group (multiple of 4)
+static_assert(kStageF % 4 == 0, "staged window must be a whole number of 16-byte chunks");
+constexpr int kStages = 12;
+constexpr int kChunk = 128;                  // group headers held in shared memory
 
-// Member in slot W with delay offset d: acc[W][r] += cf * staged[tid + 128 r + kMaxSpan - d + mu].
-// Each read of a warp touches 32 consecutive floats: conflict-free at any offset.
+// Every member slot of the group: acc[W][r] += cf[W] * staged[f - off[W] + 128 r].
 template <int W>
-__device__ __forceinline__ void slot_f32(float (&acc)[kTile][kR], const float* st, unsigned offs, int f, const float* cf) {
-    unsigned d = (offs >> (4 * W)) & 0xFu;
-    if (d == kAbsent) return;
-    const float cfw = cf[W];
-    const float* sp = st + (f - (int)d);
+__device__ __forceinline__ void slot_f32(float (&acc)[kTile][kR], const Group& g, const float* sp, const float* cf) {
+    if (g.mask & (1u << W)) {
+        const float cfw = cf[W];
+        const float* p = sp - g.off[W];
 #pragma unroll
-    for (int r = 0; r < kR; ++r) acc[W][r] = fmaf(cfw, sp[kThreads * r], acc[W][r]);
+        for (int r = 0; r < kR; ++r) acc[W][r] = fmaf(cfw, p[kThreads * r], acc[W][r]);
+    }
+}
+__device__ __forceinline__ void group_f32(float (&acc)[kTile][kR], const Group& g, const float* sp, const float* cf) {
+    slot_f32<0>(acc, g, sp, cf);
+    slot_f32<1>(acc, g, sp, cf);
+    slot_f32<2>(acc, g, sp, cf);
+    slot_f32<3>(acc, g, sp, cf);
+    slot_f32<4>(acc, g, sp, cf);
+    slot_f32<5>(acc, g, sp, cf);
+    slot_f32<6>(acc, g, sp, cf);
+    slot_f32<7>(acc, g, sp, cf);
+    slot_f32<8>(acc, g, sp, cf);
+    slot_f32<9>(acc, g, sp, cf);
+    slot_f32<10>(acc, g, sp, cf);
+    slot_f32<11>(acc, g, sp, cf);
+    slot_f32<12>(acc, g, sp, cf);
+    slot_f32<13>(acc, g, sp, cf);
+    slot_f32<14>(acc, g, sp, cf);
+    slot_f32<15>(acc, g, sp, cf);
 }
 
-__device__ __forceinline__ void group_f32(float (&acc)[kTile][kR], const float* st, unsigned offs, int f,
-                                          const float* cf) {
-    slot_f32<0>(acc, st, offs, f, cf);
-    slot_f32<1>(acc, st, offs, f, cf);
-    slot_f32<2>(acc, st, offs, f, cf);
-    slot_f32<3>(acc, st, offs, f, cf);
-    slot_f32<4>(acc, st, offs, f, cf);
-    slot_f32<5>(acc, st, offs, f, cf);
-    slot_f32<6>(acc, st, offs, f, cf);
-    slot_f32<7>(acc, st, offs, f, cf);
+// Issue the bulk copy of group `g`'s source window into stage `st`.
+__device__ __forceinline__ void issue_window(const Group& g, int b, int nb, int t0, long long rs, int lead,
+                                             const float* eprev, float* stage, uint64_t* bar) {
+    const long long row = ((long long)g.srcrow * nb + b) * rs + lead;
+    const long long a0 = (row + t0 - g.n_base - kMaxSpan) & ~3LL;
+    mbar_expect_tx(bar, kStageF * sizeof(float));
+    bulk_copy_g2s(stage, eprev + a0, kStageF * sizeof(float), bar);
 }
 
-// Histogram rows of eprev/ecur are padded: row r starts at r * rs and bin 0
-// sits at offset `lead` (>= nt + 16 zeros before it), so a window that
-// reaches before bin 0 reads zeros and needs no masking.
+// One order, one band, one 1024-bin window: G[j, c, b, window] for the 16
+// receivers of a segment.  Histogram rows of eprev are padded: row r starts
+// at r * rs and bin 0 sits at offset `lead` (>= nt + 16 zeros before it), so
+// a staged window reaching before bin 0 reads zeros and needs no masking.
+// Thread tid owns bins t0 + tid + 128 r (r < 8): every shared-memory read
+// of a warp covers 32 consecutive floats (no bank conflict at any offset).
 __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb, int nt, long long rs, int lead,
                                                              long long cap, const int32_t* __restrict__ tile_recv,
                                                              const int64_t* __restrict__ seg_off,
@@ -399,9 +406,9 @@ __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb
     extern __shared__ __align__(128) unsigned char s_raw[];
     float* stage = reinterpret_cast<float*>(s_raw);                              // [kStages][kStageF]
     Group* s_grp = reinterpret_cast<Group*>(stage + kStages * kStageF);          // [kChunk]
-    float* s_cf = reinterpret_cast<float*>(s_grp + kChunk);                      // [kChunk][8]
+    float* s_cf = reinterpret_cast<float*>(s_grp + kChunk);                      // [kChunk][kTile]
     uint64_t* full = reinterpret_cast<uint64_t*>(s_cf + kChunk * kTile);         // [kStages]
-    uint64_t* empty = full + kStages;                                            // [kStages]
+    __shared__ unsigned s_done[kStages];  // warps that finished each stage, monotone
     __shared__ int s_abort;
 
     const long long seg = blockIdx.x;
@@ -410,11 +417,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
     if (g_beg == g_end || *(volatile int*)err) return;
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], kThreads);
+            s_done[s] = 0;
         }
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -427,8 +435,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb
 #pragma unroll
         for (int r = 0; r < kR; ++r) acc[w][r] = 0.0f;
 
-    const unsigned stage_bytes = kStageF * sizeof(float);
-    long long gbase = 0;  // groups of the CTA handled before the current chunk
+    long long gbase = 0;  // groups of this CTA handled before the current chunk
     for (long long cb = g_beg; cb < g_end; cb += kChunk) {
         const int cnt = (int)min((long long)kChunk, g_end - cb);
         __syncthreads();
@@ -436,34 +443,14 @@ __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb
         for (int q = tid; q < cnt * kTile; q += kThreads) s_cf[q] = coef[((size_t)b * cap + cb) * kTile + q];
         __syncthreads();
         if (s_abort) break;
-        int next = 0;  // thread 0: groups of this chunk issued so far
-        int q = 0;
-        for (; q < cnt; ++q) {
-            if (tid == 0) {
-                // Issue ahead every group whose stage has been released by all
-                // threads; block only when group q itself is not issued yet.
-                while (next < cnt && next < q + kStages) {
-                    const long long gi = gbase + next;
-                    const int st = (int)(gi % kStages);
-                    if (gi >= kStages) {
-                        const unsigned par = (unsigned)((gi / kStages - 1) & 1);
-                        bool ready = (next <= q) ? mbar_wait(&empty[st], par, err) : mbar_test(&empty[st], par);
-                        if (!ready) {
-                            if (next <= q) {
-                                atomicExch(err, 1);
-                                s_abort = 1;
-                            }
-                            break;
-                        }
-                    }
-                    const Group gn = s_grp[next];
-                    const long long rown = ((long long)gn.srcrow * nb + b) * rs + lead;
-                    const long long an = (rown + t0 - gn.n_base - kMaxSpan) & ~3LL;
-                    mbar_expect_tx(&full[st], stage_bytes);
-                    bulk_copy_g2s(stage + st * kStageF, eprev + an, stage_bytes, &full[st]);
-                    ++next;
-                }
+        // prologue: every stage is free at a chunk start
+        if (tid == 0) {
+            for (int q = 0; q < min(cnt, kStages); ++q) {
+                const int st = (int)((gbase + q) % kStages);
+                issue_window(s_grp[q], b, nb, t0, rs, lead, eprev, stage + st * kStageF, &full[st]);
             }
+        }
+        for (int q = 0; q < cnt; ++q) {
             const long long gi = gbase + q;
             const int st = (int)(gi % kStages);
             if (!mbar_wait(&full[st], (unsigned)((gi / kStages) & 1), err)) {
@@ -471,25 +458,36 @@ __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb
                 s_abort = 1;
             }
             if (s_abort) break;
-            const Group g = s_grp[q];
+            const Group& g = s_grp[q];  // read in place (no local copy)
             const long long row = ((long long)g.srcrow * nb + b) * rs + lead;
-            const long long s_cta = (long long)t0 - g.n_base - kMaxSpan;  // source index of staged element mu
-            const long long a0 = (row + s_cta) & ~3LL;
-            const int mu = (int)(row + s_cta - a0);
-            // staged element f holds source index (a0 - row) + f (the zero lead of
-            // the padded row covers negative indices); bin t0 + tid + 128 r of a
-            // member with delay n_base + d reads f = tid + 128 r + kMaxSpan - d + mu
-            group_f32(acc, stage + st * kStageF, g.offs, tid + kMaxSpan + mu, s_cf + q * kTile);
-            mbar_arrive(&empty[st]);
-        }
-        // drain (only after an abort): wait for the copies still in flight
-        if (tid == 0 && s_abort) {
-            for (int k = q; k < next; ++k) {
-                const long long gi = gbase + k;
-                mbar_wait(&full[gi % kStages], (unsigned)((gi / kStages) & 1), err);
+            const long long s0 = row + t0 - g.n_base - kMaxSpan;
+            const int mu = (int)(s0 - (s0 & ~3LL));
+            // member with delay n_base + d: bin t0 + tid + 128 r reads staged f = tid + 128 r + kMaxSpan - d + mu
+            const float* stp = stage + st * kStageF + tid + kMaxSpan + mu;
+            const float* cf = s_cf + q * kTile;
+            group_f32(acc, g, stp, cf);
+            // the last warp to finish this stage refills it with group q + kStages
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                unsigned prev = atomicAdd(&s_done[st], 1u);
+                const unsigned use = (unsigned)(gi / kStages);
+                if (prev == use * kWarps + (kWarps - 1) && q + kStages < cnt) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue_window(s_grp[q + kStages], b, nb, t0, rs, lead, eprev, stage + st * kStageF, &full[st]);
+                }
             }
         }
         __syncthreads();
+        if (s_abort) {
+            // drain: wait (bounded) for any window still in flight in each stage
+            if (tid == 0)
+                for (int k = 0; k < min(cnt, kStages); ++k) {
+                    const long long gi = gbase + cnt - 1 - k;
+                    if (gi >= gbase) mbar_wait(&full[gi % kStages], (unsigned)((gi / kStages) & 1), err);
+                }
+            break;
+        }
         gbase += cnt;
     }
     if (s_abort) return;
@@ -506,34 +504,39 @@ __global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb
 
 // --------------------------------------------------------- FP64 scatter
 constexpr int kR64 = 4;
-constexpr int kWin64 = 18;  // kR64 + kMaxSpan + 1
+constexpr int kTW64 = kThreads * kR64;
 
 template <int W>
-__device__ __forceinline__ void apply_f64(double (&acc)[kTile][kR64], const double (&win)[kWin64], int off, double cf) {
-    switch (off) {
-#define SP_CASE(K)                                                                                  \
-    case K:                                                                                         \
-        _Pragma("unroll") for (int r = 0; r < kR64; ++r) acc[W][r] =                                \
-            fma(cf, win[(r + K < kWin64) ? r + K : 0], acc[W][r]);                                  \
-        break;
-        SP_CASE(0) SP_CASE(1) SP_CASE(2) SP_CASE(3) SP_CASE(4) SP_CASE(5) SP_CASE(6) SP_CASE(7)
-        SP_CASE(8) SP_CASE(9) SP_CASE(10) SP_CASE(11) SP_CASE(12) SP_CASE(13) SP_CASE(14)
-#undef SP_CASE
-        default:
-            break;
+__device__ __forceinline__ void slot_f64(double (&acc)[kTile][kR64], const Group& g, const double* sp, const double* cf) {
+    if (g.mask & (1u << W)) {
+        const double cfw = cf[W];
+        const double* p = sp - g.off[W];
+#pragma unroll
+        for (int r = 0; r < kR64; ++r) acc[W][r] = fma(cfw, __ldg(p + kThreads * r), acc[W][r]);
     }
 }
-
-template <int W>
-__device__ __forceinline__ void slot_f64(double (&acc)[kTile][kR64], const double (&win)[kWin64], unsigned offs,
-                                         int mu, const double* cf) {
-    unsigned d = (offs >> (4 * W)) & 0xFu;
-    if (d != kAbsent) apply_f64<W>(acc, win, mu + kMaxSpan - (int)d, cf[W]);
+__device__ __forceinline__ void group_f64(double (&acc)[kTile][kR64], const Group& g, const double* sp, const double* cf) {
+    slot_f64<0>(acc, g, sp, cf);
+    slot_f64<1>(acc, g, sp, cf);
+    slot_f64<2>(acc, g, sp, cf);
+    slot_f64<3>(acc, g, sp, cf);
+    slot_f64<4>(acc, g, sp, cf);
+    slot_f64<5>(acc, g, sp, cf);
+    slot_f64<6>(acc, g, sp, cf);
+    slot_f64<7>(acc, g, sp, cf);
+    slot_f64<8>(acc, g, sp, cf);
+    slot_f64<9>(acc, g, sp, cf);
+    slot_f64<10>(acc, g, sp, cf);
+    slot_f64<11>(acc, g, sp, cf);
+    slot_f64<12>(acc, g, sp, cf);
+    slot_f64<13>(acc, g, sp, cf);
+    slot_f64<14>(acc, g, sp, cf);
+    slot_f64<15>(acc, g, sp, cf);
 }
 
+// FP64: same plan, direct (L1-cached) loads, thread owns bins t0 + tid + 128 r.
 __global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, int nt, long long rs, int lead,
-                                                          long long cap,
-                                                          const int32_t* __restrict__ tile_recv,
+                                                          long long cap, const int32_t* __restrict__ tile_recv,
                                                           const int64_t* __restrict__ seg_off,
                                                           const Group* __restrict__ groups,
                                                           const double* __restrict__ coef,
@@ -541,50 +544,31 @@ __global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, i
                                                           double* __restrict__ gout) {
     const long long seg = blockIdx.x;
     const int b = blockIdx.z;
-    const int t0 = blockIdx.y * (kThreads * kR64) + threadIdx.x * kR64;
+    const int t0 = blockIdx.y * kTW64;
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
     if (g_beg == g_end) return;
+    const int tid = threadIdx.x;
     const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
     double acc[kTile][kR64];
 #pragma unroll
     for (int w = 0; w < kTile; ++w)
 #pragma unroll
         for (int r = 0; r < kR64; ++r) acc[w][r] = 0.0;
-    if (t0 < nt) {
-        for (long long g = g_beg; g < g_end; ++g) {
-            const Group gr = groups[g];
-            const double* cf = coef + ((size_t)b * cap + g) * kTile;
-            // padded rows: the zero lead covers source indices below 0
-            const long long row = ((long long)gr.srcrow * nb + b) * rs + lead;
-            const long long abs0 = row + (long long)t0 - gr.n_base - kMaxSpan;
-            const long long al = abs0 & ~1LL;
-            const int mu = (int)(abs0 - al);
-            double win[kWin64];
-            const double2* p = reinterpret_cast<const double2*>(eprev + al);
-#pragma unroll
-            for (int k = 0; k < kWin64 / 2; ++k) {
-                double2 v = __ldg(p + k);
-                win[2 * k] = v.x;
-                win[2 * k + 1] = v.y;
-            }
-            slot_f64<0>(acc, win, gr.offs, mu, cf);
-            slot_f64<1>(acc, win, gr.offs, mu, cf);
-            slot_f64<2>(acc, win, gr.offs, mu, cf);
-            slot_f64<3>(acc, win, gr.offs, mu, cf);
-            slot_f64<4>(acc, win, gr.offs, mu, cf);
-            slot_f64<5>(acc, win, gr.offs, mu, cf);
-            slot_f64<6>(acc, win, gr.offs, mu, cf);
-            slot_f64<7>(acc, win, gr.offs, mu, cf);
-        }
+    for (long long gidx = g_beg; gidx < g_end; ++gidx) {
+        const Group& g = groups[gidx];  // read in place (no local copy)
+        const double* cf = coef + ((size_t)b * cap + gidx) * kTile;
+        // padded rows: the zero lead covers source indices below 0
+        const double* sp = eprev + ((long long)g.srcrow * nb + b) * rs + lead + t0 + tid - g.n_base;
+        group_f64(acc, g, sp, cf);
     }
 #pragma unroll
     for (int w = 0; w < kTile; ++w) {
         int j = tile_recv[tile * kTile + w];
         if (j < 0) continue;
-        double* out = gout + (((size_t)j * n_class + c) * nb + b) * nt;
+        double* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + tid;
 #pragma unroll
         for (int r = 0; r < kR64; ++r)
-            if (t0 + r < nt) out[t0 + r] = acc[w][r];
+            if (t0 + tid + kThreads * r < nt) out[kThreads * r] = acc[w][r];
     }
 }
 
@@ -747,9 +731,9 @@ void scan64(long long n, const int64_t* in, int64_t* out, int64_t* tmp, cudaStre
     // out[0..n] exclusive scan, out[n] = total
     long long nblocks = (n + kScanBlock - 1) / kScanBlock;
     if (nblocks < 1) nblocks = 1;
-    k_scan_blocks<<<(unsigned)nblocks, kScanBlock, 0, st>>>(n, in, out, tmp);
-    k_scan_sums<<<1, 32, 0, st>>>(nblocks, tmp, out + n);
-    k_scan_add<<<(unsigned)nblocks, kScanBlock, 0, st>>>(n, out, tmp);
+    k_scan_blocks<<<(unsigned)nblocks, kScanBlock, 0, sp_counted(st)>>>(n, in, out, tmp);
+    k_scan_sums<<<1, 32, 0, sp_counted(st)>>>(nblocks, tmp, out + n);
+    k_scan_add<<<(unsigned)nblocks, kScanBlock, 0, sp_counted(st)>>>(n, out, tmp);
 }
 
 template <typename T>
@@ -778,7 +762,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     cudaMemsetAsync(eprev, 0, (L.rows * L.rs + kStageF + 64) * sizeof(T), st);
     cudaMemset2DAsync(ecur, L.rs * sizeof(T), 0, (size_t)lead * sizeof(T), L.rows, st);
     long long ne = (long long)n * nd * nb;
-    k_init_energy_t<T><<<sp_blocks(ne, 256), 256, 0, st>>>(n, nd, nb, nt, rs, lead, a->energy_0_dir, a->distance_0,
+    k_init_energy_t<T><<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(n, nd, nb, nt, rs, lead, a->energy_0_dir, a->distance_0,
                                                            a->speed_of_sound, a->time_resolution, etot, eprev, L.err);
     int herr = 0;
     cudaMemcpyAsync(&herr, L.err, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -787,58 +771,70 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     if (a->max_order < 1 || p == 0) return sp_check_launch();
 
     // ---- plan
-    k_delays_t<<<sp_blocks(p, 256), 256, 0, st>>>(p, a->pair_distance, a->speed_of_sound, a->time_resolution, L.delay);
-    k_pair_class_t<<<sp_blocks(p, 256), 256, 0, st>>>(p, a->pair_src, a->pair_in_dir, a->wall_of, a->brdf_index,
+    k_delays_t<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, a->pair_distance, a->speed_of_sound, a->time_resolution, L.delay);
+    k_pair_class_t<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, a->pair_src, a->pair_in_dir, a->wall_of, a->brdf_index,
                                                       a->slot_group, a->n_in_dirs, L.cls);
-    k_row_sort_by_class_t<<<n, 32, n_class * sizeof(int), st>>>(n, a->dst_offset, L.cls, n_class, L.perm, L.rco,
+    k_row_sort_by_class_t<<<n, 32, n_class * sizeof(int), sp_counted(st)>>>(n, a->dst_offset, L.cls, n_class, L.perm, L.rco,
                                                                 L.row_of);
-    k_default_tiles<<<sp_blocks((long long)n_tiles * kTile, 256), 256, 0, st>>>(n, n_tiles, a->receiver_order,
+    k_default_tiles<<<sp_blocks((long long)n_tiles * kTile, 256), 256, 0, sp_counted(st)>>>(n, n_tiles, a->receiver_order,
                                                                                L.tile_recv, L.tile_of, L.slot_of);
-    k_seg_size<<<sp_blocks(n_seg, 256), 256, 0, st>>>(n_seg, n_class, L.tile_recv, L.rco, L.seg_size);
+    k_seg_size<<<sp_blocks(n_seg, 256), 256, 0, sp_counted(st)>>>(n_seg, n_class, L.tile_recv, L.rco, L.seg_size);
     scan64(n_seg, L.seg_size, L.seg_base, L.scan_tmp, st);
-    k_merge_positions<<<sp_blocks(p, 256), 256, 0, st>>>(p, n_class, L.perm, L.row_of, L.cls, a->pair_src, L.rco,
+    k_merge_positions<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, n_class, L.perm, L.row_of, L.cls, a->pair_src, L.rco,
                                                          L.tile_of, L.slot_of, L.tile_recv, L.seg_base, L.merged);
-    k_cells<T><<<sp_blocks(p, 128), 128, 0, st>>>(p, nd, nb, nt, L.merged, a->pair_src, a->pair_dst, a->pair_out_dir,
+    k_cells<T><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(p, nd, nb, nt, L.merged, a->pair_src, a->pair_dst, a->pair_out_dir,
                                                   L.delay, L.cls, L.tile_of, L.slot_of, a->pair_fprime,
                                                   a->pair_unit_len, a->air_attenuation, a->wall_of, a->brdf_index,
                                                   a->slot_scale, 0, L.cell_count, nullptr, p, nullptr, nullptr);
     scan64(p, L.cell_count, L.cell_base, L.scan_tmp, st);
-    k_cells<T><<<sp_blocks(p, 128), 128, 0, st>>>(p, nd, nb, nt, L.merged, a->pair_src, a->pair_dst, a->pair_out_dir,
+    k_cells<T><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(p, nd, nb, nt, L.merged, a->pair_src, a->pair_dst, a->pair_out_dir,
                                                   L.delay, L.cls, L.tile_of, L.slot_of, a->pair_fprime,
                                                   a->pair_unit_len, a->air_attenuation, a->wall_of, a->brdf_index,
                                                   a->slot_scale, 1, nullptr, L.cell_base, p, L.groups, (T*)L.coef);
-    k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, st>>>(n_seg, p, L.seg_base, L.cell_base, L.seg_off);
+    k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, sp_counted(st)>>>(n_seg, p, L.seg_base, L.cell_base, L.seg_off);
     long long nc = (long long)n_class * nb;
-    k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, st>>>(nc, a->class_diff, (T*)L.cdiff);
-    k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, st>>>(nc, a->class_spec, (T*)L.cspec);
+    k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_diff, (T*)L.cdiff);
+    k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_spec, (T*)L.cspec);
+    if (a->plan_stats) {
+        int64_t ng = 0;
+        cudaMemcpyAsync(&ng, L.seg_off + n_seg, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+        a->plan_stats[0] = ng;
+        a->plan_stats[1] = n_seg;
+        a->plan_stats[2] = p;
+        a->plan_stats[3] = n_tiles;
+    }
 
     // ---- orders
     dim3 mgrid((nt + 255) / 256, nb, n);
     size_t msmem = (size_t)(2 * n_class + nd + 1) * sizeof(int);
+    SpEventTimer timer(a->order_ms != nullptr, st);
     for (int k = 0; k < a->max_order; ++k) {
         if constexpr (sizeof(T) == 4) {
             size_t smem = (size_t)kStages * kStageF * 4 + kChunk * sizeof(Group) + kChunk * kTile * 4 +
-                          2 * kStages * 8 + 128;
+                          kStages * 8 + 128;
             if (k == 0) cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             dim3 sgrid((unsigned)n_seg, (nt + kTW - 1) / kTW, nb);
-            k_scatter_f32<<<sgrid, kThreads, smem, st>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off,
+            k_scatter_f32<<<sgrid, kThreads, smem, sp_counted(st)>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off,
                                                          L.groups, (const float*)L.coef, (const float*)eprev,
                                                          (float*)L.g, L.err);
         } else {
-            dim3 sgrid((unsigned)n_seg, (nt + kThreads * kR64 - 1) / (kThreads * kR64), nb);
-            k_scatter_f64<<<sgrid, kThreads, 0, st>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off, L.groups,
+            dim3 sgrid((unsigned)n_seg, (nt + kTW64 - 1) / kTW64, nb);
+            k_scatter_f64<<<sgrid, kThreads, 0, sp_counted(st)>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off, L.groups,
                                                       (const double*)L.coef, (const double*)eprev, (double*)L.g);
         }
-        k_mix<T><<<mgrid, 256, msmem, st>>>(n_class, nd, nb, nt, rs, lead, L.tile_of, L.seg_off, (const T*)L.cdiff,
+        k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.tile_of, L.seg_off, (const T*)L.cdiff,
                                            (const T*)L.cspec, a->class_target, (const T*)L.g, ecur, etot);
         T* tmp = eprev;
         eprev = ecur;
         ecur = tmp;
     }
+    timer.stop(st);
     int rc = sp_check_launch();
     if (rc != SP_OK) return rc;
     cudaMemcpyAsync(&herr, L.err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+    if (a->order_ms) *a->order_ms = timer.elapsed_ms();
     return herr ? SP_ERR_TIMEOUT : SP_OK;
 }
 

@@ -542,7 +542,7 @@ int sp_source_energy(const double* src, int n, const double* centers, const doub
     if (n == 0) return SP_OK;
     if (!src || !centers || !pts || !vis || !att || !wall_of || !brdf_index || !dirs_in || !brdf || !e0 || !d0 || !e0dir)
         return SP_ERR_ARG;
-    k_source_energy<<<sp_blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(src, n, centers, pts, vis, nb, att, wall_of,
+    k_source_energy<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(src, n, centers, pts, vis, nb, att, wall_of,
                                                                          brdf_index, n_in, dirs_in, n_out, brdf, e0, d0,
                                                                          e0dir);
     return sp_check_launch();
@@ -554,7 +554,7 @@ int sp_receiver_factors(const double* rcv, int n, const double* centers, const d
     if (n < 0 || n_out < 1) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
     if (!rcv || !centers || !pts || !vis || !wall_of || !dirs_out || !rfac || !ridx || !dist) return SP_ERR_ARG;
-    k_receiver_factors<<<sp_blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(rcv, n, centers, pts, vis, wall_of, n_out,
+    k_receiver_factors<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(rcv, n, centers, pts, vis, wall_of, n_out,
                                                                             dirs_out, rfac, ridx, dist);
     return sp_check_launch();
 }
@@ -565,7 +565,7 @@ int sp_form_factors(int precision, long long n_pairs, const int32_t* pairs, cons
     if (n_pairs == 0) return SP_OK;
     if (!pairs || !pts || !normals || !areas || !ff) return SP_ERR_ARG;
     long long threads = n_pairs * 32;
-    k_form_factors<<<sp_blocks(threads, 256), 256, 0, (cudaStream_t)stream>>>(n_pairs, pairs, pts, normals, areas,
+    k_form_factors<<<sp_blocks(threads, 256), 256, 0, sp_counted((cudaStream_t)stream)>>>(n_pairs, pairs, pts, normals, areas,
                                                                               precision == SP_F32 ? 1 : 0, ff, method);
     return sp_check_launch();
 }

@@ -469,7 +469,7 @@ int sp_dense_form_factors(long long n_pairs, int n, const int32_t* pairs, const 
     if (n_pairs < 0 || n < 0 || (n > 0 && !out) || (n_pairs > 0 && (!pairs || !ff))) return SP_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (n > 0) cudaMemsetAsync(out, 0, (size_t)n * n * sizeof(double), st);
-    if (n_pairs > 0) k_scatter_ff<<<sp_blocks(n_pairs, 256), 256, 0, st>>>(n_pairs, n, pairs, ff, out);
+    if (n_pairs > 0) k_scatter_ff<<<sp_blocks(n_pairs, 256), 256, 0, sp_counted(st)>>>(n_pairs, n, pairs, ff, out);
     return sp_check_launch();
 }
 
@@ -482,7 +482,7 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
     cudaStream_t st = (cudaStream_t)stream;
     if (n > 0) cudaMemsetAsync(out, 0, (size_t)n * n * nd * nb * sizeof(double), st);
     if (n_dir > 0)
-        k_ff_tilde<<<sp_blocks(n_dir, 128), 128, 0, st>>>(n_dir, n, nd, nb, n_in, src, dst, in_dir, fprime, unit_len,
+        k_ff_tilde<<<sp_blocks(n_dir, 128), 128, 0, sp_counted(st)>>>(n_dir, n, nd, nb, n_in, src, dst, in_dir, fprime, unit_len,
                                                           att, wall_of, brdf_index, brdf, out);
     return sp_check_launch();
 }
@@ -490,7 +490,7 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
 int sp_patch_geometry(int n, int nv, const double* pts, double* centers, double* areas, void* stream) {
     if (n < 0 || nv < 3 || nv > kMaxVerts || (n > 0 && (!pts || !centers || !areas))) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
-    k_patch_geometry<<<sp_blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(n, nv, pts, centers, areas);
+    k_patch_geometry<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(n, nv, pts, centers, areas);
     return sp_check_launch();
 }
 
@@ -509,11 +509,11 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
     int n_groups = (n + kGroup - 1) / kGroup;
     float* box = (float*)ws;
     float* gbox = box + (size_t)n * 6;
-    k_blocker_boxes<<<n_groups, kGroup, 0, st>>>(n, nv, pts, 1e-3f, box, gbox);
+    k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n, nv, pts, 1e-3f, box, gbox);
     cudaMemsetAsync(vis, 0, (size_t)n * n, st);
     int tiles = (n + 15) / 16;
     dim3 grid(tiles, tiles);
-    k_patch_visibility<<<grid, 256, 1024 * 6 * sizeof(float), st>>>(n, nv, centers, normals, pts, box, gbox,
+    k_patch_visibility<<<grid, 256, 1024 * 6 * sizeof(float), sp_counted(st)>>>(n, nv, centers, normals, pts, box, gbox,
                                                                      n_groups, vis);
     return sp_check_launch();
 }
@@ -534,9 +534,9 @@ int sp_point_visibility(const double* point, int n, const double* centers, int n
     float* sbox = (float*)ws;
     if (n_surf > 0) {
         int n_groups = (n_surf + kGroup - 1) / kGroup;
-        k_blocker_boxes<<<n_groups, kGroup, 0, st>>>(n_surf, nv, surf_pts, 1e-3f, sbox, sbox + (size_t)n_surf * 6);
+        k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n_surf, nv, surf_pts, 1e-3f, sbox, sbox + (size_t)n_surf * 6);
     }
-    k_point_visibility<<<sp_blocks(n, 128), 128, 0, st>>>(point, n, centers, n_surf, nv, surf_pts, surf_normals,
+    k_point_visibility<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(point, n, centers, n_surf, nv, surf_pts, surf_normals,
                                                           sbox, out);
     return sp_check_launch();
 }
@@ -546,9 +546,9 @@ int sp_visible_pairs(int n, const uint8_t* vis, int32_t* row_counts, int64_t* ro
     if (n < 0 || (n > 0 && (!vis || !row_counts || !row_offset || !pairs))) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    k_row_counts<<<n, 256, 0, st>>>(n, vis, 1, row_counts);
-    k_exclusive_scan<<<1, 1024, 0, st>>>(n, row_counts, row_offset);
-    k_fill_rows<<<n, 256, 0, st>>>(n, vis, 1, row_offset, pairs, pair_index, nullptr, nullptr);
+    k_row_counts<<<n, 256, 0, sp_counted(st)>>>(n, vis, 1, row_counts);
+    k_exclusive_scan<<<1, 1024, 0, sp_counted(st)>>>(n, row_counts, row_offset);
+    k_fill_rows<<<n, 256, 0, sp_counted(st)>>>(n, vis, 1, row_offset, pairs, pair_index, nullptr, nullptr);
     return sp_check_launch();
 }
 
@@ -558,9 +558,9 @@ int sp_count_directed(int n, const uint8_t* vis, uint8_t* sym, int32_t* row_coun
     if (n == 0) return SP_OK;
     cudaStream_t st = (cudaStream_t)stream;
     dim3 g((n + 31) / 32, (n + 31) / 32), b(32, 8);
-    k_symmetrize<<<g, b, 0, st>>>(n, vis, sym);
-    k_row_counts<<<n, 256, 0, st>>>(n, sym, 0, row_counts);
-    k_exclusive_scan<<<1, 1024, 0, st>>>(n, row_counts, row_offset);
+    k_symmetrize<<<g, b, 0, sp_counted(st)>>>(n, vis, sym);
+    k_row_counts<<<n, 256, 0, sp_counted(st)>>>(n, sym, 0, row_counts);
+    k_exclusive_scan<<<1, 1024, 0, sp_counted(st)>>>(n, row_counts, row_offset);
     return sp_check_launch();
 }
 
@@ -568,7 +568,7 @@ int sp_directed_pairs(int n, const uint8_t* sym, const int64_t* row_offset, int3
                       void* stream) {
     if (n < 0 || (n > 0 && (!sym || !row_offset || !src || !dst))) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
-    k_fill_rows<<<n, 256, 0, (cudaStream_t)stream>>>(n, sym, 0, row_offset, nullptr, nullptr, src, dst);
+    k_fill_rows<<<n, 256, 0, sp_counted((cudaStream_t)stream)>>>(n, sym, 0, row_offset, nullptr, nullptr, src, dst);
     return sp_check_launch();
 }
 
@@ -580,7 +580,7 @@ int sp_pair_setup(long long n_dir, int n, const int32_t* src, const int32_t* dst
     if (n_dir == 0) return SP_OK;
     if (!src || !dst || !centers || !areas || !pair_index || !ff || !wall_of || !dist || !unit_len || !fprime)
         return SP_ERR_ARG;
-    k_pair_setup<<<sp_blocks(n_dir, 128), 128, 0, (cudaStream_t)stream>>>(
+    k_pair_setup<<<sp_blocks(n_dir, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
         n_dir, n, src, dst, centers, areas, pair_index, ff, wall_of, n_in, dirs_in, n_out, dirs_out, out_dir, in_dir,
         dist, unit_len, fprime);
     return sp_check_launch();
@@ -591,8 +591,8 @@ int sp_outgoing_index_map(long long n_dir, int n, const int32_t* src, const int3
     if (n_dir < 0 || n < 0 || (n > 0 && !out)) return SP_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     long long nn = (long long)n * n;
-    if (nn > 0) k_fill_i64<<<sp_blocks(nn, 256), 256, 0, st>>>(nn, sentinel, out);
-    if (n_dir > 0) k_scatter_outdir<<<sp_blocks(n_dir, 256), 256, 0, st>>>(n_dir, n, src, dst, out_dir, out);
+    if (nn > 0) k_fill_i64<<<sp_blocks(nn, 256), 256, 0, sp_counted(st)>>>(nn, sentinel, out);
+    if (n_dir > 0) k_scatter_outdir<<<sp_blocks(n_dir, 256), 256, 0, sp_counted(st)>>>(n_dir, n, src, dst, out_dir, out);
     return sp_check_launch();
 }
 

@@ -162,6 +162,7 @@ class DirectionalRadiosityFast:
                 self._host[key] = np.array(val)
         self._dev = {}      # device tensors of the current geometry / results
         self._bake = None   # device state of the last bake
+        self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
         self.check()
 
     # ------------------------------------------------------------ validation
@@ -236,9 +237,24 @@ class DirectionalRadiosityFast:
         return cls(walls_points, walls_normal, walls_up_vector, patches_points, n_patches, patch_to_wall_ids,
                    precision=precision, device=device)
 
+    def clone(self):
+        """A new object with copies of this object's host-side inputs (no device state)."""
+        r = DirectionalRadiosityFast(self._walls_points, self._walls_normal, self._walls_up_vector,
+                                     self._patches_points, self._n_patches, self._patch_to_wall_ids,
+                                     frequencies=self._frequencies, air_attenuation=self._air_attenuation,
+                                     precision=self.precision, device=self.device)
+        if self._brdf is not None:
+            r._brdf = [np.array(b) for b in self._brdf]
+            r._brdf_index = self._brdf_index.copy()
+            r._brdf_incoming_directions = self._brdf_incoming_directions.copy()
+            r._brdf_outgoing_directions = self._brdf_outgoing_directions.copy()
+        return r
+
     # ---------------------------------------------------------- device state
     def _t(self, arr, dtype):
-        return torch.as_tensor(np.ascontiguousarray(arr), dtype=dtype).to(self.device, non_blocking=False)
+        t = torch.as_tensor(np.ascontiguousarray(arr), dtype=dtype)
+        self.host_bytes_uploaded += t.numel() * t.element_size()
+        return t.to(self.device, non_blocking=False)
 
     def _geometry(self):
         d = self._dev
@@ -495,6 +511,10 @@ class DirectionalRadiosityFast:
         dtype = torch.float32 if self.precision == "fp32" else torch.float64
         etc = torch.empty((n, nd, nb, n_samples), dtype=dtype, device=self.device)
         a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
+        stats = (ctypes.c_int64 * 4)()
+        a.plan_stats = stats
+        order_ms = ctypes.c_float(-1.0)
+        a.order_ms = ctypes.pointer(order_ms)
         wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
                        a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups * a.n_in_dirs)
         ws = self._workspace(wsz)
@@ -504,6 +524,9 @@ class DirectionalRadiosityFast:
         if rc != nat.SP_OK:
             raise nat.NativeError("sp_energy_exchange", rc)
         self._dev["etc"] = etc
+        self.exchange_stats = dict(algorithm="structured" if a.algorithm == nat.SP_EXCHANGE_STRUCTURED else "dense",
+                                   source_groups=int(stats[0]), segments=int(stats[1]), pairs=int(stats[2]),
+                                   tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order))
 
     def _workspace(self, nbytes):
         ws = self._dev.get("ws")

@@ -197,6 +197,13 @@ def config(name, precision="fp32"):
         r = street_canyon(seed=3, precision=precision)
         src, rcv = street_canyon_setup(seed=3)
         return dict(radiosity=r, source=src, receivers=rcv, c=343.0, dt=1e-3, duration=2.0, max_order=50)
+    if name == "canyon_small":
+        # the street canyon at 30 m length, 10 occluders and 2 bands (same
+        # directions, patch size and histogram length): a profiling case
+        # whose histograms stay near 1 GB each
+        r = street_canyon(n_boxes=10, n_bins=2, seed=3, length=30.0, precision=precision)
+        src, rcv = street_canyon_setup(seed=3, length=30.0)
+        return dict(radiosity=r, source=src, receivers=rcv, c=343.0, dt=1e-3, duration=2.0, max_order=50)
     raise ValueError(name)
 
 
