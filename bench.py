@@ -32,6 +32,9 @@ import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+# the FP32 and FP64 solves each hold tens of GB of histograms and workspace;
+# growable segments let the second reuse what the first released
+os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "expandable_segments:True")
 
 import numpy as np  # noqa: E402
 
@@ -321,6 +324,7 @@ def run_gpu(args):
         h2d = int(r2.host_bytes_uploaded)
         d2h = int(mono.nbytes)
         del r2, mono
+        torch.cuda.empty_cache()
     e2e_ms = float(np.mean(e2e_times)) if e2e_times else None
     if world > 1 and e2e_ms is not None:
         t = torch.tensor([e2e_ms], device="cuda")
@@ -340,6 +344,8 @@ def run_gpu(args):
 
     fp64 = None
     if not args.no_fp64 and args.precision == "fp32" and rank == 0:
+        r._dev.pop("ws", None)  # the FP64 solve needs the room of the FP32 workspace
+        torch.cuda.empty_cache()
         c64 = scenes.config(args.config, precision="fp64")
         c64["max_order"] = cfg["max_order"]
         r64 = c64["radiosity"]
