@@ -64,6 +64,30 @@ size_t sp_patch_visibility_workspace(int n);
 int sp_patch_visibility(int n, int nv, const double* centers, const double* normals, const double* pts,
                         uint8_t* vis, void* ws, size_t ws_bytes, void* stream);
 
+/* Allocation-free sp_patch_visibility (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory when visibility is
+ * recomputed, e.g. an engine that reserves its whole device budget up front
+ * and re-bakes after geometry edits, or a binding without a device allocator
+ * of its own, so it has no workspace to pass.  Same arguments, results and
+ * kernels as sp_patch_visibility, without ws/ws_bytes: the blocker-box
+ * scratch is a fixed 405,504-byte array inside this library's device image
+ * (reserved when the module loads).  This call allocates nothing.
+ *
+ * Limit: n <= 16384 patches; larger n returns SP_ERR_WORKSPACE before any
+ *   device work (use sp_patch_visibility there).
+ * Set-up: the first call on each device, made with that device current,
+ *   looks up the array's address (cudaGetSymbolAddress) and keeps it; make
+ *   that first call before any stream capture.  A failed lookup returns
+ *   SP_ERR_CUDA.
+ * Zeroing: nothing has to start at zero (every box read is written earlier
+ *   in the same call; vis is cleared on the stream as in sp_patch_visibility).
+ * Concurrency: all calls on a device share the one scratch array, so calls
+ *   that overlap in time (different streams or host threads) race and give
+ *   wrong results; order them on one stream or serialise them. */
+int sp_patch_visibility_static(int n, int nv, const double* centers, const double* normals, const double* pts,
+                               uint8_t* vis, void* stream);
+
 /* Point-to-patch visibility; blockers are n_surf surfaces (walls).
  * Replaces geometry.py:799-839 `_check_point2patch_visibility`.
  * point (3) -> out (n) 0/1. */

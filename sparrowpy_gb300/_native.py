@@ -64,6 +64,7 @@ _SIGS = {
     "sp_patch_geometry": (I, [I, I, P, P, P, P]),
     "sp_patch_visibility_workspace": (SZ, [I]),
     "sp_patch_visibility": (I, [I, I, P, P, P, P, P, SZ, P]),
+    "sp_patch_visibility_static": (I, [I, I, P, P, P, P, P]),
     "sp_point_visibility_workspace": (SZ, [I]),
     "sp_point_visibility": (I, [P, I, P, I, I, P, P, P, P, SZ, P]),
     "sp_visible_pairs": (I, [I, P, P, P, P, P, P]),

@@ -8,6 +8,8 @@
 // single blockers, decides which blockers need the exact test at all: a
 // blocker whose (slightly enlarged) bounding box the segment misses can only
 // return "visible" in the reference predicate (see exact_visibility below).
+#include <atomic>
+
 #include "common.cuh"
 
 namespace {
@@ -597,3 +599,46 @@ int sp_outgoing_index_map(long long n_dir, int n, const int32_t* src, const int3
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ allocation-free variant
+// sp_patch_visibility_static: the same kernels as sp_patch_visibility with
+// the blocker-box scratch in a fixed array of this library's device image
+// instead of a caller-provided workspace.
+namespace {
+constexpr int kStaticVisMaxPatches = 16384;
+constexpr size_t kStaticVisScratchFloats =
+    (size_t)kStaticVisMaxPatches * 6 + (((size_t)kStaticVisMaxPatches + kGroup - 1) / kGroup) * 6;
+// 405,504 bytes, reserved when the module loads.  Every box the kernels read
+// is written earlier in the same call, so nothing here has to start at zero.
+static __device__ __align__(256) float g_static_vis_scratch[kStaticVisScratchFloats];
+constexpr int kStaticMaxDevices = 64;
+std::atomic<float*> g_static_vis_ptr[kStaticMaxDevices];  // per device, looked up once
+}  // namespace
+
+extern "C" int sp_patch_visibility_static(int n, int nv, const double* centers, const double* normals,
+                                          const double* pts, uint8_t* vis, void* stream) {
+    if (n > kStaticVisMaxPatches) return SP_ERR_WORKSPACE;
+    if (n < 0 || nv < 3 || nv > kMaxVerts) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!centers || !normals || !pts || !vis) return SP_ERR_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kStaticMaxDevices) return SP_ERR_CUDA;
+    float* box = g_static_vis_ptr[dev].load(std::memory_order_acquire);
+    if (!box) {
+        // first call on this device (with it current): find the array's address
+        void* addr = nullptr;
+        if (cudaGetSymbolAddress(&addr, g_static_vis_scratch) != cudaSuccess || !addr) return SP_ERR_CUDA;
+        box = static_cast<float*>(addr);
+        g_static_vis_ptr[dev].store(box, std::memory_order_release);
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int n_groups = (n + kGroup - 1) / kGroup;
+    float* gbox = box + (size_t)n * 6;
+    k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n, nv, pts, 1e-3f, box, gbox);
+    cudaMemsetAsync(vis, 0, (size_t)n * n, st);
+    int tiles = (n + 15) / 16;
+    dim3 grid(tiles, tiles);
+    k_patch_visibility<<<grid, 256, 1024 * 6 * sizeof(float), sp_counted(st)>>>(n, nv, centers, normals, pts, box,
+                                                                                 gbox, n_groups, vis);
+    return sp_check_launch();
+}
