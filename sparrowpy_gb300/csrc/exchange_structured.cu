@@ -27,6 +27,9 @@
 // of the group.  FP64 uses the same plan with direct loads.  Mix: streams G
 // into E_k and E_total.
 #include "common.cuh"
+#include <algorithm>
+#include <vector>
+
 #include "exchange_common.cuh"
 
 namespace {
@@ -342,163 +345,205 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
         : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // --------------------------------------------------------- FP32 scatter
-constexpr int kThreads = 128;
-constexpr int kWarps = kThreads / 32;
-constexpr int kR = 8;                        // bins per thread (strided by 128)
-constexpr int kTW = kThreads * kR;           // 1024 bins per window
-constexpr int kStageF = kTW + kMaxSpan + 3;  // staged floats per group (multiple of 4)
+// Warp-specialised pipeline.  One producer warp streams the groups of a
+// segment through kStages shared-memory stages of kGps groups each, with
+// bulk copies (per group the source window; per stage the kGps 32-byte group
+// records and their 16 coefficients of this band).  kConsumers consumer
+// warps, warp w owning receiver slots 2w and 2w + 1 of the tile, accumulate
+// those slots' 1024-bin windows in registers (lane l owns bins t0 + l + 32 r).
+// Stage hand-off: `full` (producer arrival + transaction bytes) and `empty`
+// (one arrival per consumer warp); every wait is bounded.
+constexpr int kThreads = 128;                        // FP64 scatter block
+constexpr int kSlotsPerWarp = 2;
+constexpr int kConsumers = kTile / kSlotsPerWarp;    // 8 consumer warps
+constexpr int kWsThreads = (kConsumers + 1) * 32;    // + one producer warp
+constexpr int kBins = 32;                            // bins per lane, strided by 32
+constexpr int kTW = 32 * kBins;                      // 1024 bins per window
+constexpr int kStageF = kTW + kMaxSpan + 3;          // staged floats per group (multiple of 4)
 static_assert(kStageF % 4 == 0, "staged window must be a whole number of 16-byte chunks");
-constexpr int kStages = 12;
-constexpr int kChunk = 128;                  // group headers held in shared memory
+constexpr int kGps = 4;                              // groups per stage
+constexpr int kWinBytes = kStageF * 4;
+constexpr int kHdrOff = kGps * kWinBytes;            // kGps group records
+constexpr int kCoefOff = kHdrOff + kGps * (int)sizeof(Group);  // kGps x 16 coefficients
+constexpr int kStageBytes = kCoefOff + kGps * kTile * 4;
+static_assert(kWinBytes % 16 == 0 && kHdrOff % 16 == 0 && kCoefOff % 16 == 0 && kStageBytes % 16 == 0,
+              "stage parts must stay 16-byte aligned");
+constexpr int kStages = 6;
+constexpr int kBarBytes = 128;                       // full[kStages], empty[kStages]
+static_assert(2 * kStages * 8 <= kBarBytes, "barrier area too small");
+constexpr size_t kScatterSmem = (size_t)kBarBytes + (size_t)kStages * kStageBytes;
 
-// Every member slot of the group: acc[W][r] += cf[W] * staged[f - off[W] + 128 r].
-template <int W>
-__device__ __forceinline__ void slot_f32(float (&acc)[kTile][kR], const Group& g, const float* sp, const float* cf) {
-    if (g.mask & (1u << W)) {
-        const float cfw = cf[W];
-        const float* p = sp - g.off[W];
+// acc[r] += cf * staged[lane + 32 r + base - off] for one member slot, with
+// base = kMaxSpan + mu (mu: floats the staged start was rounded down by).
+__device__ __forceinline__ void slot_window(float (&acc)[kBins], const float* win, float cf, int off, int base,
+                                            int lane) {
+    const float* p = win + lane + base - off;
 #pragma unroll
-        for (int r = 0; r < kR; ++r) acc[W][r] = fmaf(cfw, p[kThreads * r], acc[W][r]);
-    }
-}
-__device__ __forceinline__ void group_f32(float (&acc)[kTile][kR], const Group& g, const float* sp, const float* cf) {
-    slot_f32<0>(acc, g, sp, cf);
-    slot_f32<1>(acc, g, sp, cf);
-    slot_f32<2>(acc, g, sp, cf);
-    slot_f32<3>(acc, g, sp, cf);
-    slot_f32<4>(acc, g, sp, cf);
-    slot_f32<5>(acc, g, sp, cf);
-    slot_f32<6>(acc, g, sp, cf);
-    slot_f32<7>(acc, g, sp, cf);
-    slot_f32<8>(acc, g, sp, cf);
-    slot_f32<9>(acc, g, sp, cf);
-    slot_f32<10>(acc, g, sp, cf);
-    slot_f32<11>(acc, g, sp, cf);
-    slot_f32<12>(acc, g, sp, cf);
-    slot_f32<13>(acc, g, sp, cf);
-    slot_f32<14>(acc, g, sp, cf);
-    slot_f32<15>(acc, g, sp, cf);
-}
-
-// Issue the bulk copy of group `g`'s source window into stage `st`.
-__device__ __forceinline__ void issue_window(const Group& g, int b, int nb, int t0, long long rs, int lead,
-                                             const float* eprev, float* stage, uint64_t* bar) {
-    const long long row = ((long long)g.srcrow * nb + b) * rs + lead;
-    const long long a0 = (row + t0 - g.n_base - kMaxSpan) & ~3LL;
-    mbar_expect_tx(bar, kStageF * sizeof(float));
-    bulk_copy_g2s(stage, eprev + a0, kStageF * sizeof(float), bar);
+    for (int r = 0; r < kBins; ++r) acc[r] = fmaf(cf, p[32 * r], acc[r]);
 }
 
 // One order, one band, one 1024-bin window: G[j, c, b, window] for the 16
 // receivers of a segment.  Histogram rows of eprev are padded: row r starts
-// at r * rs and bin 0 sits at offset `lead` (>= nt + 16 zeros before it), so
-// a staged window reaching before bin 0 reads zeros and needs no masking.
-// Thread tid owns bins t0 + tid + 128 r (r < 8): every shared-memory read
-// of a warp covers 32 consecutive floats (no bank conflict at any offset).
-__global__ void __launch_bounds__(kThreads, 3) k_scatter_f32(int n_class, int nb, int nt, long long rs, int lead,
-                                                             long long cap, const int32_t* __restrict__ tile_recv,
-                                                             const int64_t* __restrict__ seg_off,
-                                                             const Group* __restrict__ groups,
-                                                             const float* __restrict__ coef,
-                                                             const float* __restrict__ eprev,
-                                                             float* __restrict__ gout, int* __restrict__ err) {
+// at r * rs with bin 0 at offset `lead` (>= nt + kMaxSpan + 4 zeros before
+// it), so a staged window reaching before bin 0 reads zeros and needs no
+// masking, and no window starts before the buffer.  Every shared-memory read
+// of a consumer warp covers 32 consecutive floats (no bank conflict at any
+// offset).
+__global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int nb, int nt, long long rs, int lead,
+                                                               long long cap, const int32_t* __restrict__ tile_recv,
+                                                               const int32_t* __restrict__ seg_order,
+                                                               const int64_t* __restrict__ seg_off,
+                                                               const Group* __restrict__ groups,
+                                                               const float* __restrict__ coef,
+                                                               const float* __restrict__ eprev,
+                                                               float* __restrict__ gout, int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char s_raw[];
-    float* stage = reinterpret_cast<float*>(s_raw);                              // [kStages][kStageF]
-    Group* s_grp = reinterpret_cast<Group*>(stage + kStages * kStageF);          // [kChunk]
-    float* s_cf = reinterpret_cast<float*>(s_grp + kChunk);                      // [kChunk][kTile]
-    uint64_t* full = reinterpret_cast<uint64_t*>(s_cf + kChunk * kTile);         // [kStages]
-    __shared__ unsigned s_done[kStages];  // warps that finished each stage, monotone
-    __shared__ int s_abort;
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_raw);
+    uint64_t* empty = full + kStages;
+    unsigned char* stages = s_raw + kBarBytes;
+    __shared__ volatile int s_abort;
+    __shared__ volatile int s_issued;  // stages issued
 
-    const long long seg = blockIdx.x;
+    const long long seg = seg_order[blockIdx.x];
     const int b = blockIdx.z;
     const int t0 = blockIdx.y * kTW;
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
-    if (g_beg == g_end || *(volatile int*)err) return;
-    const int tid = threadIdx.x;
-    const int lane = tid & 31;
-    const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
-    if (tid == 0) {
+    const int n_grp = (int)(g_end - g_beg);  // groups of one segment (< 2^31)
+    if (n_grp == 0) return;                   // the same for every thread of the block
+    const int n_stage = (n_grp + kGps - 1) / kGps;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&full[s], 1);
-            s_done[s] = 0;
+            mbar_init(&empty[s], kConsumers);
         }
-        s_abort = 0;
+        s_abort = *(volatile int*)err ? 1 : 0;  // one reading of the flag for the whole block
+        s_issued = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-
-    float acc[kTile][kR];
-#pragma unroll
-    for (int w = 0; w < kTile; ++w)
-#pragma unroll
-        for (int r = 0; r < kR; ++r) acc[w][r] = 0.0f;
-
-    long long gbase = 0;  // groups of this CTA handled before the current chunk
-    for (long long cb = g_beg; cb < g_end; cb += kChunk) {
-        const int cnt = (int)min((long long)kChunk, g_end - cb);
-        __syncthreads();
-        for (int q = tid; q < cnt; q += kThreads) s_grp[q] = groups[cb + q];
-        for (int q = tid; q < cnt * kTile; q += kThreads) s_cf[q] = coef[((size_t)b * cap + cb) * kTile + q];
-        __syncthreads();
-        if (s_abort) break;
-        // prologue: every stage is free at a chunk start
-        if (tid == 0) {
-            for (int q = 0; q < min(cnt, kStages); ++q) {
-                const int st = (int)((gbase + q) % kStages);
-                issue_window(s_grp[q], b, nb, t0, rs, lead, eprev, stage + st * kStageF, &full[st]);
-            }
-        }
-        for (int q = 0; q < cnt; ++q) {
-            const long long gi = gbase + q;
-            const int st = (int)(gi % kStages);
-            if (!mbar_wait(&full[st], (unsigned)((gi / kStages) & 1), err)) {
-                atomicExch(err, 1);
-                s_abort = 1;
-            }
-            if (s_abort) break;
-            const Group& g = s_grp[q];  // read in place (no local copy)
-            const long long row = ((long long)g.srcrow * nb + b) * rs + lead;
-            const long long s0 = row + t0 - g.n_base - kMaxSpan;
-            const int mu = (int)(s0 - (s0 & ~3LL));
-            // member with delay n_base + d: bin t0 + tid + 128 r reads staged f = tid + 128 r + kMaxSpan - d + mu
-            const float* stp = stage + st * kStageF + tid + kMaxSpan + mu;
-            const float* cf = s_cf + q * kTile;
-            group_f32(acc, g, stp, cf);
-            // the last warp to finish this stage refills it with group q + kStages
-            __syncwarp();
-            if (lane == 0) {
-                __threadfence_block();
-                unsigned prev = atomicAdd(&s_done[st], 1u);
-                const unsigned use = (unsigned)(gi / kStages);
-                if (prev == use * kWarps + (kWarps - 1) && q + kStages < cnt) {
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    issue_window(s_grp[q + kStages], b, nb, t0, rs, lead, eprev, stage + st * kStageF, &full[st]);
-                }
-            }
-        }
-        __syncthreads();
-        if (s_abort) {
-            // drain: wait (bounded) for any window still in flight in each stage
-            if (tid == 0)
-                for (int k = 0; k < min(cnt, kStages); ++k) {
-                    const long long gi = gbase + cnt - 1 - k;
-                    if (gi >= gbase) mbar_wait(&full[gi % kStages], (unsigned)((gi / kStages) & 1), err);
-                }
-            break;
-        }
-        gbase += cnt;
-    }
     if (s_abort) return;
+
+    float acc0[kBins], acc1[kBins];
 #pragma unroll
-    for (int w = 0; w < kTile; ++w) {
-        int j = tile_recv[tile * kTile + w];
-        if (j < 0) continue;
-        float* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + tid;
+    for (int r = 0; r < kBins; ++r) {
+        acc0[r] = 0.0f;
+        acc1[r] = 0.0f;
+    }
+
+    if (warp == kConsumers) {
+        // producer: lane q computes the window address of group base + q and,
+        // once lane 0 has claimed the stage, issues that group's copy itself
+        bool stop = false;
+        for (int base = 0; base < n_grp && !stop; base += 32) {
+            long long a0 = 0;
+            if (base + lane < n_grp) {
+                const int2 h = __ldg(reinterpret_cast<const int2*>(groups + g_beg + base + lane));
+                const long long row = ((long long)h.x * nb + b) * rs + lead;
+                a0 = (row + t0 - h.y - kMaxSpan) & ~3LL;  // 16-byte aligned start of the window
+            }
+            const int cnt = min(32, n_grp - base);
+            for (int k0 = 0; k0 < cnt; k0 += kGps) {
+                const int si = (base + k0) / kGps;  // stage index (base is a multiple of kGps)
+                const int st = si % kStages;
+                const int ng = min(kGps, cnt - k0);
+                int halt = 0;
+                if (lane == 0) {
+                    if (s_abort) {
+                        halt = 1;
+                    } else if (si >= kStages && !mbar_wait(&empty[st], (unsigned)((si / kStages - 1) & 1), err)) {
+                        atomicExch(err, 1);
+                        s_abort = 1;
+                        halt = 1;
+                    } else {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        mbar_expect_tx(&full[st], (unsigned)(ng * (kWinBytes + (int)sizeof(Group) + kTile * 4)));
+                    }
+                }
+                halt = __shfl_sync(0xffffffffu, halt, 0);
+                if (halt) {
+                    stop = true;
+                    break;
+                }
+                unsigned char* sp = stages + (size_t)st * kStageBytes;
+                const int q = lane - k0;  // this lane's group within the stage
+                if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * kWinBytes, eprev + a0, kWinBytes, &full[st]);
+                if (lane == 0) {
+                    const long long g0 = g_beg + base + k0;
+                    bulk_copy_g2s(sp + kHdrOff, groups + g0, (unsigned)(ng * sizeof(Group)), &full[st]);
+                    bulk_copy_g2s(sp + kCoefOff, coef + ((size_t)b * cap + g0) * kTile, (unsigned)(ng * kTile * 4),
+                                  &full[st]);
+                    s_issued = si + 1;
+                }
+            }
+        }
+    } else {
+        // consumer: receiver slots 2 warp and 2 warp + 1 of the tile
+        const int sh = kSlotsPerWarp * warp;
+        for (int si = 0; si < n_stage; ++si) {
+            const int st = si % kStages;
+            const bool ok = mbar_wait(&full[st], (unsigned)((si / kStages) & 1), err);
+            if (!__all_sync(0xffffffffu, ok)) {  // the whole warp leaves together
+                if (lane == 0) {
+                    atomicExch(err, 1);
+                    s_abort = 1;
+                }
+                break;
+            }
+            const unsigned char* sp = stages + (size_t)st * kStageBytes;
+            const int ng = min(kGps, n_grp - si * kGps);
+            // the stage's records first (independent loads), then the windows
+            unsigned bits[kGps];
+            int base_off[kGps];  // kMaxSpan + mu, per group
+            float2 cf[kGps];
+            unsigned offs[kGps];  // off of slot sh (low byte) and sh + 1 (second byte)
 #pragma unroll
-        for (int r = 0; r < kR; ++r)
-            if (t0 + tid + kThreads * r < nt) out[kThreads * r] = acc[w][r];
+            for (int q = 0; q < kGps; ++q) {
+                const Group* g = reinterpret_cast<const Group*>(sp + kHdrOff) + q;
+                // record at a 16-byte boundary: srcrow, n_base, mask, pad
+                const int4 hdr = q < ng ? *reinterpret_cast<const int4*>(g) : make_int4(0, 0, 0, 0);
+                bits[q] = ((unsigned)hdr.z >> sh) & 3u;
+                base_off[q] = kMaxSpan + ((-hdr.y - kMaxSpan) & 3);  // staged start was rounded down by mu floats
+                cf[q] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(sp + kCoefOff) + q * kTile + sh);
+                offs[q] = *reinterpret_cast<const uint16_t*>(&g->off[sh]);
+            }
+#pragma unroll
+            for (int q = 0; q < kGps; ++q) {
+                const float* win = reinterpret_cast<const float*>(sp + q * kWinBytes);
+                if (bits[q] & 1u) slot_window(acc0, win, cf[q].x, (int)(offs[q] & 0xffu), base_off[q], lane);
+                if (bits[q] & 2u) slot_window(acc1, win, cf[q].y, (int)(offs[q] >> 8), base_off[q], lane);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+        }
+    }
+    __syncthreads();
+    if (s_abort) {
+        // drain: wait (bounded) until every issued copy has landed
+        if (threadIdx.x == 0) {
+            const int issued = s_issued;
+            for (int si = issued - 1; si >= 0 && si >= issued - kStages; --si)
+                mbar_wait(&full[si % kStages], (unsigned)((si / kStages) & 1), err);
+        }
+        return;
+    }
+    if (warp < kConsumers) {
+        const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+#pragma unroll
+        for (int h = 0; h < kSlotsPerWarp; ++h) {
+            const int j = tile_recv[tile * kTile + kSlotsPerWarp * warp + h];
+            if (j < 0) continue;
+            float* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + lane;
+#pragma unroll
+            for (int r = 0; r < kBins; ++r)
+                if (t0 + lane + 32 * r < nt) out[32 * r] = h == 0 ? acc0[r] : acc1[r];
+        }
     }
 }
 
@@ -537,12 +582,13 @@ __device__ __forceinline__ void group_f64(double (&acc)[kTile][kR64], const Grou
 // FP64: same plan, direct (L1-cached) loads, thread owns bins t0 + tid + 128 r.
 __global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, int nt, long long rs, int lead,
                                                           long long cap, const int32_t* __restrict__ tile_recv,
+                                                          const int32_t* __restrict__ seg_order,
                                                           const int64_t* __restrict__ seg_off,
                                                           const Group* __restrict__ groups,
                                                           const double* __restrict__ coef,
                                                           const double* __restrict__ eprev,
                                                           double* __restrict__ gout) {
-    const long long seg = blockIdx.x;
+    const long long seg = seg_order[blockIdx.x];
     const int b = blockIdx.z;
     const int t0 = blockIdx.y * kTW64;
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
@@ -574,56 +620,145 @@ __global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, i
 
 // --------------------------------------------------------------- mix
 // E_k[j, o, b, t] = sum_c (diff_c + spec_c [o == m_c]) G[j, c, b, t];  E_total += E_k.
+// Per tile: the classes present (segments with groups) and, per outgoing
+// direction o, the present classes whose mirror direction is o.  Layout of a
+// row of kTab(n_class, nd) ints: [np, cls[n_class], inv_off[nd + 1], inv[n_class]].
+__host__ __device__ inline int tile_tab_stride(int n_class, int nd) { return 2 + 2 * n_class + nd; }
+
+__global__ void k_tile_table(int n_tiles, int n_class, int nd, const int64_t* __restrict__ seg_off,
+                             const int32_t* __restrict__ ctarget, int32_t* __restrict__ tab) {
+    const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tile >= n_tiles) return;
+    int32_t* row = tab + (size_t)tile * tile_tab_stride(n_class, nd);
+    int32_t* cls = row + 1;
+    int32_t* inv_off = cls + n_class;
+    int32_t* inv = inv_off + nd + 1;
+    int np = 0;
+    for (int c = 0; c < n_class; ++c) {
+        const long long sg = (long long)tile * n_class + c;
+        if (seg_off[sg + 1] > seg_off[sg]) cls[np++] = c;
+    }
+    row[0] = np;
+    int k = 0;
+    for (int o = 0; o < nd; ++o) {
+        inv_off[o] = k;
+        for (int q = 0; q < np; ++q)
+            if (ctarget[cls[q]] == o) inv[k++] = cls[q];
+    }
+    inv_off[nd] = k;
+}
+
+// E_k[j, o, b, t] = sum_c diff[c, b] G[j, c, b, t] + sum_{c: m_c = o} spec[c, b] G[j, c, b, t]
+// (the slot scale is folded into the scatter coefficients), written to the
+// padded row of ecur, and E_total += E_k.  One block per (band, receiver),
+// all bins; only the classes present in the receiver's tile are read.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt, long long rs, int lead,
-                                             const int32_t* __restrict__ tile_of,
-                                             const int64_t* __restrict__ seg_off, const T* __restrict__ cdiff,
-                                             const T* __restrict__ cspec, const int32_t* __restrict__ ctarget,
+                                             const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
+                                             const T* __restrict__ cdiff, const T* __restrict__ cspec,
                                              const T* __restrict__ g, T* __restrict__ ecur, T* __restrict__ etot) {
-    extern __shared__ int s_int[];
-    int* s_cls = s_int;                    // [n_class] present classes of the tile
-    int* s_inv_off = s_int + n_class;      // [nd + 1] per direction: present classes with m_c == o
-    int* s_inv = s_inv_off + nd + 1;       // [n_class]
-    __shared__ int s_np;
-    const int j = blockIdx.z, b = blockIdx.y;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    extern __shared__ __align__(16) unsigned char s_mix[];
+    const int stride = tile_tab_stride(n_class, nd);
+    T* s_cd = reinterpret_cast<T*>(s_mix);  // [n_class] diffuse weight of band b
+    T* s_cs = s_cd + n_class;               // [n_class] specular weight of band b
+    int* s_tab = reinterpret_cast<int*>(s_cs + n_class);
+    const int b = blockIdx.x, j = blockIdx.y;
     const int tile = tile_of[j];
-    if (threadIdx.x == 0) {
-        int np = 0;
-        for (int c = 0; c < n_class; ++c) {
-            long long s = (long long)tile * n_class + c;
-            if (seg_off[s + 1] > seg_off[s]) s_cls[np++] = c;
-        }
-        s_np = np;
-        int k = 0;
-        for (int o = 0; o < nd; ++o) {
-            s_inv_off[o] = k;
-            for (int q = 0; q < np; ++q)
-                if (ctarget[s_cls[q]] == o) s_inv[k++] = s_cls[q];
-        }
-        s_inv_off[nd] = k;
+    for (int k = threadIdx.x; k < stride; k += blockDim.x) s_tab[k] = tab[(size_t)tile * stride + k];
+    for (int c = threadIdx.x; c < n_class; c += blockDim.x) {
+        s_cd[c] = cdiff[(size_t)c * nb + b];
+        s_cs[c] = cspec[(size_t)c * nb + b];
     }
     __syncthreads();
-    if (t >= nt) return;
-    const int np = s_np;
+    const int np = s_tab[0];
+    const int* cls = s_tab + 1;
+    const int* inv_off = cls + n_class;
+    const int* inv = inv_off + nd + 1;
     const size_t cstride = (size_t)nb * nt;
-    const T* gj = g + ((size_t)j * n_class * nb + b) * nt + t;
-    T diffuse = T(0);
-    for (int q = 0; q < np; ++q) {
-        int c = s_cls[q];
-        diffuse = fma(cdiff[(size_t)c * nb + b], gj[c * cstride], diffuse);
-    }
-    const size_t row = (size_t)nd * nb * nt;
-    T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead + t;  // padded rows, stride rs
-    T* et = etot + (size_t)j * row + (size_t)b * nt + t;
-    for (int o = 0; o < nd; ++o) {
-        T v = diffuse;
-        for (int q = s_inv_off[o]; q < s_inv_off[o + 1]; ++q) {
-            int c = s_inv[q];
-            v = fma(cspec[(size_t)c * nb + b], gj[c * cstride], v);
+    const T* gj = g + ((size_t)j * n_class * nb + b) * nt;
+    T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;  // padded rows, stride rs
+    T* et = etot + ((size_t)j * nd * nb + b) * nt;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        T diffuse = T(0);
+        for (int q = 0; q < np; ++q) {
+            const int c = cls[q];
+            diffuse = fma(s_cd[c], gj[c * cstride + t], diffuse);
         }
-        ek[(size_t)o * nb * rs] = v;
-        et[o * cstride] += v;
+        for (int o = 0; o < nd; ++o) {
+            T v = diffuse;
+            for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
+                const int c = inv[q];
+                v = fma(s_cs[c], gj[c * cstride + t], v);
+            }
+            ek[(size_t)o * nb * rs + t] = v;
+            et[o * cstride + t] += v;
+        }
+    }
+}
+
+// k_mix for FP32 with nt % 4 == 0: four bins per thread (16-byte accesses),
+// and the E_total values of up to 8 directions loaded before any is stored.
+__device__ __forceinline__ float4 fma4(float a, float4 x, float4 y) {
+    return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+__device__ __forceinline__ float4 add4(float4 x, float4 y) {
+    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+}
+
+__global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
+                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
+                                              const float* __restrict__ cdiff, const float* __restrict__ cspec,
+                                              const float* __restrict__ g, float* __restrict__ ecur,
+                                              float* __restrict__ etot) {
+    extern __shared__ __align__(16) unsigned char s_mix[];
+    const int stride = tile_tab_stride(n_class, nd);
+    float* s_cd = reinterpret_cast<float*>(s_mix);
+    float* s_cs = s_cd + n_class;
+    int* s_tab = reinterpret_cast<int*>(s_cs + n_class);
+    const int b = blockIdx.x, j = blockIdx.y;
+    const int tile = tile_of[j];
+    for (int k = threadIdx.x; k < stride; k += blockDim.x) s_tab[k] = tab[(size_t)tile * stride + k];
+    for (int c = threadIdx.x; c < n_class; c += blockDim.x) {
+        s_cd[c] = cdiff[(size_t)c * nb + b];
+        s_cs[c] = cspec[(size_t)c * nb + b];
+    }
+    __syncthreads();
+    const int np = s_tab[0];
+    const int* cls = s_tab + 1;
+    const int* inv_off = cls + n_class;
+    const int* inv = inv_off + nd + 1;
+    const int nt4 = nt >> 2;
+    const size_t cs4 = (size_t)nb * nt4;  // class (G) and direction (E_total) stride, in float4
+    const size_t ers4 = (size_t)nb * (size_t)(rs >> 2);  // direction stride of the padded ecur rows
+    const float4* gj = reinterpret_cast<const float4*>(g + ((size_t)j * n_class * nb + b) * nt);
+    float4* ek = reinterpret_cast<float4*>(ecur + ((size_t)j * nd * nb + b) * rs + lead);
+    float4* et = reinterpret_cast<float4*>(etot + ((size_t)j * nd * nb + b) * nt);
+    for (int t = threadIdx.x; t < nt4; t += blockDim.x) {
+        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int q = 0; q < np; ++q) {
+            const int c = cls[q];
+            d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);
+        }
+        for (int o0 = 0; o0 < nd; o0 += 8) {
+            const int no = min(8, nd - o0);
+            float4 e[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < no) e[k] = et[(o0 + k) * cs4 + t];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (k < no) {
+                    const int o = o0 + k;
+                    float4 v = d;
+                    for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
+                        const int c = inv[q];
+                        v = fma4(s_cs[c], __ldg(gj + c * cs4 + t), v);
+                    }
+                    ek[o * ers4 + t] = v;
+                    et[o * cs4 + t] = add4(e[k], v);
+                }
+            }
+        }
     }
 }
 
@@ -672,6 +807,8 @@ struct Plan {
     int64_t* seg_size;
     int64_t* seg_base;
     int64_t* seg_off;
+    int32_t* tile_tab;
+    int32_t* seg_order;
     int64_t* cell_count;
     int64_t* cell_base;
     int64_t* scan_tmp;
@@ -694,7 +831,7 @@ Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p
     // padded histogram rows: `lead` zeros, then nt bins; stride rs (multiple
     // of 4 elements so rows stay 16-byte aligned); a tail after the last row
     // keeps the staged windows of the last rows inside the allocation
-    L.lead = (int)((((size_t)nt + 20) + 3) & ~(size_t)3);
+    L.lead = (int)((((size_t)nt + kMaxSpan + 4) + 3) & ~(size_t)3);
     L.rs = (((size_t)nt + L.lead) + 3) & ~(size_t)3;
     L.rows = (size_t)n * nd * nb;
     size_t tail = (size_t)kStageF + 64;
@@ -714,6 +851,8 @@ Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p
     L.seg_size = (int64_t*)take(((size_t)n_seg + 1) * 8);
     L.seg_base = (int64_t*)take(((size_t)n_seg + 1) * 8);
     L.seg_off = (int64_t*)take(((size_t)n_seg + 1) * 8);
+    L.tile_tab = (int32_t*)take((size_t)n_tiles * tile_tab_stride(n_class, nd) * 4);
+    L.seg_order = (int32_t*)take((size_t)n_seg * 4);
     L.cell_count = (int64_t*)take(((size_t)p + 1) * 8);
     L.cell_base = (int64_t*)take(((size_t)p + 1) * 8);
     long long big = p > n_seg ? p : n_seg;
@@ -795,36 +934,61 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     long long nc = (long long)n_class * nb;
     k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_diff, (T*)L.cdiff);
     k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_spec, (T*)L.cspec);
-    if (a->plan_stats) {
-        int64_t ng = 0;
-        cudaMemcpyAsync(&ng, L.seg_off + n_seg, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    k_tile_table<<<sp_blocks(n_tiles, 128), 128, 0, sp_counted(st)>>>(n_tiles, n_class, nd, L.seg_off, a->class_target,
+                                                                         L.tile_tab);
+    // scatter blocks visit the non-empty segments longest first, so the
+    // longest blocks do not end up in the tail of the grid
+    std::vector<int64_t> h_off((size_t)n_seg + 1);
+    cudaMemcpyAsync(h_off.data(), L.seg_off, h_off.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+    std::vector<int32_t> order;
+    order.reserve((size_t)n_seg);
+    for (long long sg = 0; sg < n_seg; ++sg)
+        if (h_off[sg + 1] > h_off[sg]) order.push_back((int32_t)sg);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return h_off[x + 1] - h_off[x] > h_off[y + 1] - h_off[y];
+    });
+    const unsigned n_active = (unsigned)order.size();
+    if (n_active > 0) {
+        cudaMemcpyAsync(L.seg_order, order.data(), order.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
-        a->plan_stats[0] = ng;
+    }
+    if (a->plan_stats) {
+        a->plan_stats[0] = h_off[n_seg];
         a->plan_stats[1] = n_seg;
         a->plan_stats[2] = p;
         a->plan_stats[3] = n_tiles;
     }
 
     // ---- orders
-    dim3 mgrid((nt + 255) / 256, nb, n);
-    size_t msmem = (size_t)(2 * n_class + nd + 1) * sizeof(int);
+    dim3 mgrid(nb, n);
+    size_t msmem = (size_t)2 * n_class * sizeof(T) + (size_t)tile_tab_stride(n_class, nd) * sizeof(int);
     SpEventTimer timer(a->order_ms != nullptr, st);
     for (int k = 0; k < a->max_order; ++k) {
         if constexpr (sizeof(T) == 4) {
-            size_t smem = (size_t)kStages * kStageF * 4 + kChunk * sizeof(Group) + kChunk * kTile * 4 +
-                          kStages * 8 + 128;
-            if (k == 0) cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            dim3 sgrid((unsigned)n_seg, (nt + kTW - 1) / kTW, nb);
-            k_scatter_f32<<<sgrid, kThreads, smem, sp_counted(st)>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off,
-                                                         L.groups, (const float*)L.coef, (const float*)eprev,
-                                                         (float*)L.g, L.err);
+            if (k == 0)
+                cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
+            dim3 sgrid(n_active, (nt + kTW - 1) / kTW, nb);
+            if (n_active > 0)
+                k_scatter_f32<<<sgrid, kWsThreads, kScatterSmem, sp_counted(st)>>>(
+                    n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_order, L.seg_off, L.groups, (const float*)L.coef,
+                    (const float*)eprev, (float*)L.g, L.err);
         } else {
-            dim3 sgrid((unsigned)n_seg, (nt + kTW64 - 1) / kTW64, nb);
-            k_scatter_f64<<<sgrid, kThreads, 0, sp_counted(st)>>>(n_class, nb, nt, rs, lead, p, L.tile_recv, L.seg_off, L.groups,
-                                                      (const double*)L.coef, (const double*)eprev, (double*)L.g);
+            dim3 sgrid(n_active, (nt + kTW64 - 1) / kTW64, nb);
+            if (n_active > 0)
+                k_scatter_f64<<<sgrid, kThreads, 0, sp_counted(st)>>>(n_class, nb, nt, rs, lead, p, L.tile_recv,
+                                                                      L.seg_order, L.seg_off, L.groups,
+                                                                      (const double*)L.coef, (const double*)eprev,
+                                                                      (double*)L.g);
         }
-        k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.tile_of, L.seg_off, (const T*)L.cdiff,
-                                           (const T*)L.cspec, a->class_target, (const T*)L.g, ecur, etot);
+        if (sizeof(T) == 4 && nt % 4 == 0)
+            k_mix4<<<mgrid, 128, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.tile_of, L.tile_tab,
+                                                          (const float*)L.cdiff, (const float*)L.cspec,
+                                                          (const float*)L.g, (float*)ecur, (float*)etot);
+        else
+            k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.tile_of, L.tile_tab,
+                                                            (const T*)L.cdiff, (const T*)L.cspec, (const T*)L.g, ecur,
+                                                            etot);
         T* tmp = eprev;
         eprev = ecur;
         ecur = tmp;
