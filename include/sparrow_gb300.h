@@ -221,6 +221,21 @@ int sp_energy_exchange(const sp_exchange_args* args, void* ws, size_t ws_bytes, 
  * Replaces RadiosityFast.py:686-752 `_collect_energy_patches` with
  * :1148-1185 `_collect_receiver_energy` (circular roll by ceil(d/c/dt)) and
  * the patch sum of :592.  etot in `precision`. */
+/* Structure of the BRDF tables brdf (n_slots, n_in, n_out, nb) for the
+ * structured exchange (no counterpart in the reference, which applies the
+ * full tables).  Per row (slot, incoming direction): diff (n_slots, n_in, nb)
+ * = median over the outgoing directions, target (n_slots, n_in) = the one
+ * outgoing direction deviating from diff by more than rel_tol * max|brdf|
+ * (-1: none), spec (n_slots, n_in, nb) = that direction's value - diff;
+ * scale (n_slots, nb) = max |brdf| per slot and band.  *n_irregular (device
+ * int) = rows with more than one deviating direction (the tables are then
+ * not of the diffuse-plus-mirror form).  Scratch: ws of
+ * sp_brdf_structure_workspace() bytes. */
+size_t sp_brdf_structure_workspace(void);
+int sp_brdf_structure(int n_slots, int n_in, int n_out, int nb, const double* brdf, double rel_tol, double* diff,
+                      double* spec, int32_t* target, double* scale, int* n_irregular, void* ws, size_t ws_bytes,
+                      void* stream);
+
 size_t sp_collect_workspace(int n_patches, int n_bins);
 int sp_collect_receiver(int precision, int n, int nd, int nb, int nt, const void* etot, const int32_t* ridx,
                         const double* rfac, const double* dist, double c, double dt, const double* att,

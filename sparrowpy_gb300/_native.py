@@ -79,6 +79,8 @@ _SIGS = {
     "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
     "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I, I]),
     "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
+    "sp_brdf_structure_workspace": (SZ, []),
+    "sp_brdf_structure": (I, [I, I, I, I, P, D, P, P, P, P, P, P, SZ, P]),
     "sp_collect_workspace": (SZ, [I, I]),
     "sp_collect_receiver": (I, [I, I, I, I, I, P, P, P, P, D, D, P, P, P, P, SZ, P]),
 }

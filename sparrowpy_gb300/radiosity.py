@@ -46,14 +46,15 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def analyse_brdf(brdf, rel_tol=1e-12):
-    """Factor BRDF tables as scale[slot, b] * (diff[g, s, b] + spec[g, s, b] [o == m[g, s]]).
+def brdf_rows_host(brdf, rel_tol=1e-12):
+    """Host restatement of sp_brdf_structure (the per-row step of analyse_brdf).
 
-    brdf: (n_slots, n_in, n_out, n_bins).  Returns None when some row has
-    more than one outgoing direction off the row's common value (the dense
-    exchange is used then), else a dict with slot_group (S,), slot_scale
-    (S, B), n_groups, class_diff / class_spec (G * n_in, B), class_target
-    (G * n_in,) (-1 = no mirror term).
+    brdf: (n_slots, n_in, n_out, n_bins).  Returns (diff, spec, target,
+    scale, irregular): per row (slot, incoming direction) the median over the
+    outgoing directions (diff, per band), the one outgoing direction deviating
+    from it by more than rel_tol * max|brdf| (target, -1 if none) with its
+    excess (spec), per slot and band max |brdf| (scale), and whether any row
+    has more than one deviating direction.
     """
     brdf = np.asarray(brdf, dtype=float)
     S, Din, Dout, B = brdf.shape
@@ -63,24 +64,33 @@ def analyse_brdf(brdf, rel_tol=1e-12):
         diff = brdf[:, :, 0, :]
         spec = np.zeros_like(diff)
         target = -np.ones((S, Din), dtype=np.int64)
+        irregular = False
     else:
         if Dout >= 3:
             diff = np.sort(brdf, axis=2)[:, :, Dout // 2, :]
         else:
             diff = brdf[:, :, 0, :]
         dev = brdf - diff[:, :, None, :]
-        out = np.abs(dev) > tol
-        if np.any(out.sum(axis=2) > 1):
-            return None
-        any_out = out.any(axis=3)
-        if np.any(any_out.sum(axis=2) > 1):
-            return None
+        any_out = (np.abs(dev) > tol).any(axis=3)
+        irregular = bool(np.any(any_out.sum(axis=2) > 1))
         has = any_out.any(axis=2)
         target = np.where(has, np.argmax(any_out, axis=2), -1)
         tsafe = np.where(has, target, 0)
         spec = np.take_along_axis(dev, tsafe[:, :, None, None], axis=2)[:, :, 0, :]
         spec = np.where(has[:, :, None], spec, 0.0)
-    scale = np.max(np.abs(brdf), axis=(1, 2))
+    scale = np.max(np.abs(brdf), axis=(1, 2)) if brdf.size else np.zeros((S, B))
+    return diff, spec, target, scale, irregular
+
+
+def group_brdf_rows(diff, spec, target, scale):
+    """Group slots whose normalised rows agree: BRDF = scale[slot, b] * (diff + spec [o == m]).
+
+    Returns slot_group (S,), slot_scale (S, B), n_groups, class_diff /
+    class_spec (G * n_in, B), class_target (G * n_in,) (-1 = no mirror term).
+    """
+    diff, spec, target = np.asarray(diff, float), np.asarray(spec, float), np.asarray(target)
+    S, Din, B = diff.shape
+    scale = np.asarray(scale, float)
     scale = np.where(scale > 0, scale, 1.0)
     nd = diff / scale[:, None, :]
     ns = spec / scale[:, None, :]
@@ -98,10 +108,25 @@ def analyse_brdf(brdf, rel_tol=1e-12):
                 class_target=class_target.astype(np.int32))
 
 
+def analyse_brdf(brdf, rel_tol=1e-12):
+    """Factor BRDF tables as scale[slot, b] * (diff[g, s, b] + spec[g, s, b] [o == m[g, s]]) on the host.
+
+    brdf: (n_slots, n_in, n_out, n_bins).  Returns None when some row has
+    more than one outgoing direction off the row's common value (the dense
+    exchange is used then), else the dict of group_brdf_rows.  The solver
+    runs the row step on the GPU (sp_brdf_structure); this host version is
+    its reference.
+    """
+    diff, spec, target, scale, irregular = brdf_rows_host(brdf, rel_tol)
+    if irregular:
+        return None
+    return group_brdf_rows(diff, spec, target, scale)
+
+
 def receiver_tile_order(centers, normals, bits=10):
     """Receiver order for the tiled exchange: grouped by normal, then Morton order.
 
-    Consecutive groups of 8 receivers in this order form one tile; compact
+    Consecutive groups of 16 receivers in this order form one tile; compact
     tiles of coplanar patches see a source in nearly the same direction and
     delay, which is what lets the exchange kernel reuse a loaded source
     window across the tile.
@@ -289,12 +314,39 @@ class DirectionalRadiosityFast:
             if b.ndim == 1:  # default BRDF: one value per band (RadiosityFast.py:459-467)
                 b = b.reshape(1, 1, -1)
             slots.append(b)
-        brdf = np.array(slots, dtype=float)
+        brdf = np.stack(slots)
         state = dict(key=key, n_in=din.shape[1], n_out=dout.shape[1], n_slots=brdf.shape[0], brdf_host=brdf,
                      dirs_in=self._t(din, torch.float64), dirs_out=self._t(dout, torch.float64),
                      brdf=self._t(brdf, torch.float64), brdf_index=self._t(self._brdf_index, torch.int32))
         self._dev["brdf_state"] = state
         return state
+
+    def _brdf_structure(self, bs):
+        """Diffuse-plus-mirror structure of the current BRDF tables (None if absent), kept with them.
+
+        The row step runs on the device (sp_brdf_structure); grouping the
+        slots works on the small per-row results on the host.
+        """
+        if "structure" in bs:
+            return bs["structure"]
+        S, Din, Dout = bs["n_slots"], bs["n_in"], bs["n_out"]
+        B = bs["brdf"].shape[-1]
+        dev = self.device
+        diff = torch.empty((S, Din, B), dtype=torch.float64, device=dev)
+        spec = torch.empty((S, Din, B), dtype=torch.float64, device=dev)
+        target = torch.empty((S, Din), dtype=torch.int32, device=dev)
+        scale = torch.empty((S, B), dtype=torch.float64, device=dev)
+        n_irr = torch.empty((1,), dtype=torch.int32, device=dev)
+        wsz = nat.size("sp_brdf_structure_workspace")
+        ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
+        nat.call("sp_brdf_structure", S, Din, Dout, B, _ptr(bs["brdf"]), 1e-12, _ptr(diff), _ptr(spec),
+                 _ptr(target), _ptr(scale), _ptr(n_irr), _ptr(ws), wsz, _stream())
+        if int(n_irr.item()) > 0:
+            st = None
+        else:
+            st = group_brdf_rows(diff.cpu().numpy(), spec.cpu().numpy(), target.cpu().numpy(), scale.cpu().numpy())
+        bs["structure"] = st
+        return st
 
     # ------------------------------------------------------------------ bake
     def bake_geometry(self):
@@ -432,10 +484,12 @@ class DirectionalRadiosityFast:
         else:
             plan = dict(brdf=bs["brdf"], brdf_index=bs["brdf_index"], n_slots=bs["n_slots"], n_in=bs["n_in"],
                         n_out=bs["n_out"], host=bs["brdf_host"])
-        st = analyse_brdf(plan["host"])
+        st = analyse_brdf(plan["host"]) if bs is None else self._brdf_structure(bs)
         if st is not None and st["n_groups"] * plan["n_in"] <= 256:
-            plan["receiver_order"] = self._t(receiver_tile_order(self.patches_center, self.patches_normal),
-                                             torch.int32)
+            if "receiver_order" not in self._dev:
+                self._dev["receiver_order"] = self._t(
+                    receiver_tile_order(self.patches_center, self.patches_normal), torch.int32)
+            plan["receiver_order"] = self._dev["receiver_order"]
             plan["structured"] = dict(
                 slot_group=self._t(st["slot_group"], torch.int32), slot_scale=self._t(st["slot_scale"], torch.float64),
                 n_groups=st["n_groups"], class_diff=self._t(st["class_diff"], torch.float64),

@@ -118,3 +118,33 @@ def test_oracle_agreement_seeded_per_patch_room():
         tol = 1e-10 if precision == "fp64" else 1e-4
         assert rel_l2(mono, ref["mono"]) < tol
         assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
+
+
+def test_brdf_structure_matches_host():
+    """sp_brdf_structure (device) against brdf_rows_host: same medians, deviations and scales, bit for bit."""
+    import torch
+    from sparrowpy_gb300 import _native as nat
+    from sparrowpy_gb300 import scenes
+    from sparrowpy_gb300.radiosity import _ptr, _stream, brdf_rows_host
+    cases = [scenes.rotated_room(dense_box=False)[0], scenes.rotated_room(dense_box=True)[0],
+             scenes.shoebox(0.5, n_dirs=8, n_bins=3, scattering=0.3, per_patch=True, seed=4, dims=(2.0, 1.5, 1.0))]
+    for r in cases:
+        bs = r._brdf_device()
+        S, Din, Dout = bs["n_slots"], bs["n_in"], bs["n_out"]
+        B = bs["brdf"].shape[-1]
+        out = dict(diff=torch.empty((S, Din, B), dtype=torch.float64, device="cuda"),
+                   spec=torch.empty((S, Din, B), dtype=torch.float64, device="cuda"),
+                   target=torch.empty((S, Din), dtype=torch.int32, device="cuda"),
+                   scale=torch.empty((S, B), dtype=torch.float64, device="cuda"))
+        n_irr = torch.empty((1,), dtype=torch.int32, device="cuda")
+        wsz = nat.size("sp_brdf_structure_workspace")
+        ws = torch.empty((wsz,), dtype=torch.uint8, device="cuda")
+        nat.call("sp_brdf_structure", S, Din, Dout, B, _ptr(bs["brdf"]), 1e-12, _ptr(out["diff"]), _ptr(out["spec"]),
+                 _ptr(out["target"]), _ptr(out["scale"]), _ptr(n_irr), _ptr(ws), wsz, _stream())
+        diff, spec, target, scale, irregular = brdf_rows_host(bs["brdf_host"])
+        assert (int(n_irr.item()) > 0) == irregular
+        np.testing.assert_array_equal(out["diff"].cpu().numpy(), diff)
+        np.testing.assert_array_equal(out["scale"].cpu().numpy(), scale)
+        if not irregular:
+            np.testing.assert_array_equal(out["target"].cpu().numpy(), target)
+            np.testing.assert_array_equal(out["spec"].cpu().numpy(), spec)
