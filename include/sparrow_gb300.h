@@ -41,7 +41,7 @@ typedef enum {
 } sp_status;
 
 enum { SP_F32 = 0, SP_F64 = 1 };
-enum { SP_EXCHANGE_DENSE = 0, SP_EXCHANGE_STRUCTURED = 1 };
+enum { SP_EXCHANGE_DENSE = 0, SP_EXCHANGE_STRUCTURED = 1, SP_EXCHANGE_MATERIAL = 2 };
 
 /* Library version string (static storage). */
 const char* sp_version(void);
@@ -200,27 +200,81 @@ typedef struct sp_exchange_args {
     const double* class_diff;   /* (n_groups * n_in, B) */
     const double* class_spec;   /* (n_groups * n_in, B) */
     const int32_t* class_target;/* (n_groups * n_in) mirror direction, -1 if none */
-    const int32_t* receiver_order; /* (N) receivers in tile order (8 per tile), NULL = 0..N-1 */
+    const int32_t* receiver_order; /* (N) receivers in tile order (16 per tile), NULL = 0..N-1 */
     const int32_t* pair_dst;       /* (P) destination of each directed pair (structured algorithm) */
     int64_t* plan_stats;           /* HOST array of 4 or NULL: source groups, segments, pairs kept, tiles */
     float* order_ms;               /* HOST float or NULL: CUDA-event time of the order loop (all orders) */
+    /* structured algorithm, optional (checkpoints for the adjoint; NULL/0 = off): */
+    const void* state_in;   /* (N, D, B, T) E_{state_order}: start there instead of at the source energy */
+    int state_order;        /* order of state_in (0 without it); orders state_order + 1 .. max_order run */
+    void* states_out;       /* (n, N, D, B, T): E_k for k = state_order + i * states_every, i = 0, 1, ... */
+    int states_every;
+    int skip_total;         /* 1: etc_total is neither cleared nor written */
+    /* SP_EXCHANGE_MATERIAL only: per-slot create_from_scattering materials
+       BRDF_s[c, o, b] = (1 - alpha[s, b]) (scat[s, b] + (1 - scat[s, b]) gain[c] [o == mirror[c]])
+       (brdf, slot_group, slot_scale and class_* are not used; FP32 only) */
+    const double* mat_alpha;        /* (n_slots, B) */
+    const double* mat_scattering;   /* (n_slots, B) */
+    const int32_t* mat_mirror;      /* (n_in) mirror outgoing direction, -1: none */
+    const double* mat_gain;         /* (n_in) */
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070
  * `_energy_exchange_init_energy` (max_order < 1).  Synchronises `stream` once
  * (to report SP_ERR_RANGE for a source delay outside the histogram).
- * n_classes = n_groups * n_in_dirs for SP_EXCHANGE_STRUCTURED (<= 256). */
+ * n_classes = n_groups * n_in_dirs for SP_EXCHANGE_STRUCTURED (<= 256),
+ * 1 + n_in_dirs for SP_EXCHANGE_MATERIAL. */
 size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins,
                                     int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs,
                                     int n_classes);
 int sp_energy_exchange(const sp_exchange_args* args, void* ws, size_t ws_bytes, void* stream);
 
-/* --------------------------------------------------------------- collection */
+/* ------------------------------------------------------------------ adjoint */
 
-/* One receiver: patchwise (n, nb, nt) and/or mono (nb, nt) FP64 histograms.
- * Replaces RadiosityFast.py:686-752 `_collect_energy_patches` with
- * :1148-1185 `_collect_receiver_energy` (circular roll by ceil(d/c/dt)) and
- * the patch sum of :592.  etot in `precision`. */
+/* Reverse-mode gradient of the FP32 structured exchange (no counterpart in
+ * the reference, which is not differentiable).  Materials: every slot s uses
+ * the create_from_scattering table stored x pi (sparrowpy/brdf.py:8-130,
+ * RadiosityFast.py:815): BRDF_s[c, o, b] = (1 - alpha[s, b]) (scattering[s, b]
+ * + (1 - scattering[s, b]) mirror_gain[c] [o == mirror_of_in[c]]).  Given
+ * dL/d(receiver mono histograms), accumulates dL/dalpha and dL/dscattering
+ * of the exchange orders and returns dL/dE0dir for the source term.
+ *
+ * Use: sp_adjoint_begin once (transposed plan, mu_K = dL/dE_total), then
+ * sp_adjoint_order for k = K, K-1, ..., 1 with e_prev = E_{k-1} (FP32,
+ * (N, D, B, T), e.g. from sp_energy_exchange states_out), then
+ * sp_adjoint_finish.  The workspace carries the state between the calls;
+ * `state` is a HOST struct owned by the caller (zeroed before begin). */
+typedef struct sp_adjoint_state {
+    int ready;            /* set by sp_adjoint_begin */
+    int cur;              /* which internal buffer holds mu_k */
+    unsigned n_active;    /* non-empty segments of the transposed plan */
+    long long n_groups;   /* source groups of the transposed plan */
+} sp_adjoint_state;
+
+typedef struct sp_adjoint_args {
+    const sp_exchange_args* fwd;  /* the forward exchange (FP32, structured inputs: pairs, pair_dst,
+                                     receiver_order, c, dt, T, distance_0) */
+    const int32_t* mirror_of_in;  /* (n_in) mirror outgoing direction of each incoming direction, -1: none */
+    const double* mirror_gain;    /* (n_in) K_c */
+    const double* alpha;          /* (n_slots, B) */
+    const double* scattering;     /* (n_slots, B) */
+    int n_receivers;
+    const int32_t* recv_dir;      /* (R, N) outgoing index of each patch toward each receiver */
+    const double* recv_factor;    /* (R, N) patch-to-receiver factors (0 where not visible) */
+    const double* recv_dist;      /* (R, N) patch-to-receiver distances */
+    const double* grad_mono;      /* (R, B, T) dL/d(mono histograms) */
+    double* grad_alpha;           /* (n_slots, B), accumulated (+=) */
+    double* grad_scattering;      /* (n_slots, B), accumulated (+=) */
+    sp_adjoint_state* state;      /* HOST */
+} sp_adjoint_args;
+
+size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs);
+int sp_adjoint_begin(const sp_adjoint_args* args, void* ws, size_t ws_bytes, void* stream);
+int sp_adjoint_order(const sp_adjoint_args* args, const void* e_prev, void* ws, size_t ws_bytes, void* stream);
+int sp_adjoint_finish(const sp_adjoint_args* args, double* grad_e0dir, void* ws, size_t ws_bytes, void* stream);
+
+/* ------------------------------------------------------ BRDF structure / collection */
+
 /* Structure of the BRDF tables brdf (n_slots, n_in, n_out, nb) for the
  * structured exchange (no counterpart in the reference, which applies the
  * full tables).  Per row (slot, incoming direction): diff (n_slots, n_in, nb)
@@ -236,6 +290,10 @@ int sp_brdf_structure(int n_slots, int n_in, int n_out, int nb, const double* br
                       double* spec, int32_t* target, double* scale, int* n_irregular, void* ws, size_t ws_bytes,
                       void* stream);
 
+/* One receiver: patchwise (n, nb, nt) and/or mono (nb, nt) FP64 histograms.
+ * Replaces RadiosityFast.py:686-752 `_collect_energy_patches` with
+ * :1148-1185 `_collect_receiver_energy` (circular roll by ceil(d/c/dt)) and
+ * the patch sum of :592.  etot in `precision`. */
 size_t sp_collect_workspace(int n_patches, int n_bins);
 int sp_collect_receiver(int precision, int n, int nd, int nb, int nt, const void* etot, const int32_t* ridx,
                         const double* rfac, const double* dist, double c, double dt, const double* att,

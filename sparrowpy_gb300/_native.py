@@ -20,6 +20,7 @@ SP_F32 = 0
 SP_F64 = 1
 SP_EXCHANGE_DENSE = 0
 SP_EXCHANGE_STRUCTURED = 1
+SP_EXCHANGE_MATERIAL = 2
 
 _ERRORS = {
     SP_ERR_ARG: "invalid argument",
@@ -54,6 +55,23 @@ class ExchangeArgs(ctypes.Structure):
         ("class_diff", P), ("class_spec", P), ("class_target", P),
         ("receiver_order", P), ("pair_dst", P), ("plan_stats", ctypes.POINTER(ctypes.c_int64)),
         ("order_ms", ctypes.POINTER(ctypes.c_float)),
+        ("state_in", P), ("state_order", I), ("states_out", P), ("states_every", I), ("skip_total", I),
+        ("mat_alpha", P), ("mat_scattering", P), ("mat_mirror", P), ("mat_gain", P),
+    ]
+
+
+class AdjointState(ctypes.Structure):
+    """Mirror of `sp_adjoint_state` (host memory)."""
+    _fields_ = [("ready", I), ("cur", I), ("n_active", ctypes.c_uint), ("n_groups", LL)]
+
+
+class AdjointArgs(ctypes.Structure):
+    """Mirror of `sp_adjoint_args`."""
+    _fields_ = [
+        ("fwd", ctypes.POINTER(ExchangeArgs)), ("mirror_of_in", P), ("mirror_gain", P),
+        ("alpha", P), ("scattering", P), ("n_receivers", I), ("recv_dir", P), ("recv_factor", P),
+        ("recv_dist", P), ("grad_mono", P), ("grad_alpha", P), ("grad_scattering", P),
+        ("state", ctypes.POINTER(AdjointState)),
     ]
 
 
@@ -79,6 +97,10 @@ _SIGS = {
     "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
     "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I, I]),
     "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
+    "sp_adjoint_workspace": (SZ, [I, I, I, I, LL]),
+    "sp_adjoint_begin": (I, [ctypes.POINTER(AdjointArgs), P, SZ, P]),
+    "sp_adjoint_order": (I, [ctypes.POINTER(AdjointArgs), P, P, SZ, P]),
+    "sp_adjoint_finish": (I, [ctypes.POINTER(AdjointArgs), P, P, SZ, P]),
     "sp_brdf_structure_workspace": (SZ, []),
     "sp_brdf_structure": (I, [I, I, I, I, P, D, P, P, P, P, P, P, SZ, P]),
     "sp_collect_workspace": (SZ, [I, I]),

@@ -34,6 +34,6 @@ struct SpEventTimer {
     }
 };
 
-size_t sp_structured_workspace(int precision, int n_patches, int n_dirs, int n_bins, int n_samples,
+size_t sp_structured_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins, int n_samples,
                                long long n_dir_pairs, int n_class);
 int sp_run_structured(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t st);

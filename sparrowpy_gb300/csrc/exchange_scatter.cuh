@@ -1,0 +1,319 @@
+// Tiled scatter kernels of the exchange: G[d, c, b, t] += coef * src_row[t - delay]
+// over the source groups of a plan (exchange_plan.cuh).
+#pragma once
+#include "exchange_plan.cuh"
+
+namespace {
+
+// --------------------------------------------------------- PTX helpers
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after kWaitLimit polls (each poll may suspend
+// briefly) or as soon as another CTA has reported a failure.
+constexpr unsigned kWaitLimit = 1u << 16;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, const volatile int* err) {
+    for (unsigned it = 0; it < kWaitLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && *err) return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// --------------------------------------------------------- FP32 scatter
+// Warp-specialised pipeline.  One producer warp streams the groups of a
+// segment through kStages shared-memory stages of kGps groups each, with
+// bulk copies (per group the source window; per stage the kGps 32-byte group
+// records and their 16 coefficients of this band).  kConsumers consumer
+// warps, warp w owning receiver slots 2w and 2w + 1 of the tile, accumulate
+// those slots' 1024-bin windows in registers (lane l owns bins t0 + l + 32 r).
+// Stage hand-off: `full` (producer arrival + transaction bytes) and `empty`
+// (one arrival per consumer warp); every wait is bounded.
+constexpr int kThreads = 128;                        // FP64 scatter block
+constexpr int kSlotsPerWarp = 2;
+constexpr int kConsumers = kTile / kSlotsPerWarp;    // 8 consumer warps
+constexpr int kWsThreads = (kConsumers + 1) * 32;    // + one producer warp
+constexpr int kBins = 32;                            // bins per lane, strided by 32
+constexpr int kTW = 32 * kBins;                      // 1024 bins per window
+constexpr int kStageF = kTW + kMaxSpan + 3;          // staged floats per group (multiple of 4)
+static_assert(kStageF % 4 == 0, "staged window must be a whole number of 16-byte chunks");
+constexpr int kGps = 4;                              // groups per stage
+constexpr int kWinBytes = kStageF * 4;
+constexpr int kHdrOff = kGps * kWinBytes;            // kGps group records
+constexpr int kCoefOff = kHdrOff + kGps * (int)sizeof(Group);  // kGps x 16 coefficients
+constexpr int kStageBytes = kCoefOff + kGps * kTile * 4;
+static_assert(kWinBytes % 16 == 0 && kHdrOff % 16 == 0 && kCoefOff % 16 == 0 && kStageBytes % 16 == 0,
+              "stage parts must stay 16-byte aligned");
+constexpr int kStages = 6;
+constexpr int kBarBytes = 128;                       // full[kStages], empty[kStages]
+static_assert(2 * kStages * 8 <= kBarBytes, "barrier area too small");
+constexpr size_t kScatterSmem = (size_t)kBarBytes + (size_t)kStages * kStageBytes;
+
+// acc[r] += cf * staged[lane + 32 r + base - off] for one member slot, with
+// base = kMaxSpan + mu (mu: floats the staged start was rounded down by).
+__device__ __forceinline__ void slot_window(float (&acc)[kBins], const float* win, float cf, int off, int base,
+                                            int lane) {
+    const float* p = win + lane + base - off;
+#pragma unroll
+    for (int r = 0; r < kBins; ++r) acc[r] = fmaf(cf, p[32 * r], acc[r]);
+}
+
+// One order, one band, one 1024-bin window: G[j, c, b, window] for the 16
+// receivers of a segment.  Histogram rows of eprev are padded: row r starts
+// at r * rs with bin 0 at offset `lead` (>= nt + kMaxSpan + 4 zeros before
+// it), so a staged window reaching before bin 0 reads zeros and needs no
+// masking, and no window starts before the buffer.  Every shared-memory read
+// of a consumer warp covers 32 consecutive floats (no bank conflict at any
+// offset).
+__global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int nb, int nt, long long rs, int lead,
+                                                               long long cap, const int32_t* __restrict__ tile_recv,
+                                                               const int32_t* __restrict__ seg_order,
+                                                               const int64_t* __restrict__ seg_off,
+                                                               const Group* __restrict__ groups,
+                                                               const float* __restrict__ coef,
+                                                               const float* __restrict__ eprev,
+                                                               float* __restrict__ gout, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char s_raw[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_raw);
+    uint64_t* empty = full + kStages;
+    unsigned char* stages = s_raw + kBarBytes;
+    __shared__ volatile int s_abort;
+    __shared__ volatile int s_issued;  // stages issued
+
+    const long long seg = seg_order[blockIdx.x];
+    const int b = blockIdx.z;
+    const int t0 = blockIdx.y * kTW;
+    const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
+    const int n_grp = (int)(g_end - g_beg);  // groups of one segment (< 2^31)
+    if (n_grp == 0) return;                   // the same for every thread of the block
+    const int n_stage = (n_grp + kGps - 1) / kGps;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kConsumers);
+        }
+        s_abort = *(volatile int*)err ? 1 : 0;  // one reading of the flag for the whole block
+        s_issued = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (s_abort) return;
+
+    float acc0[kBins], acc1[kBins];
+#pragma unroll
+    for (int r = 0; r < kBins; ++r) {
+        acc0[r] = 0.0f;
+        acc1[r] = 0.0f;
+    }
+
+    if (warp == kConsumers) {
+        // producer: lane q computes the window address of group base + q and,
+        // once lane 0 has claimed the stage, issues that group's copy itself
+        bool stop = false;
+        for (int base = 0; base < n_grp && !stop; base += 32) {
+            long long a0 = 0;
+            if (base + lane < n_grp) {
+                const int2 h = __ldg(reinterpret_cast<const int2*>(groups + g_beg + base + lane));
+                const long long row = ((long long)h.x * nb + b) * rs + lead;
+                a0 = (row + t0 - h.y - kMaxSpan) & ~3LL;  // 16-byte aligned start of the window
+            }
+            const int cnt = min(32, n_grp - base);
+            for (int k0 = 0; k0 < cnt; k0 += kGps) {
+                const int si = (base + k0) / kGps;  // stage index (base is a multiple of kGps)
+                const int st = si % kStages;
+                const int ng = min(kGps, cnt - k0);
+                int halt = 0;
+                if (lane == 0) {
+                    if (s_abort) {
+                        halt = 1;
+                    } else if (si >= kStages && !mbar_wait(&empty[st], (unsigned)((si / kStages - 1) & 1), err)) {
+                        atomicExch(err, 1);
+                        s_abort = 1;
+                        halt = 1;
+                    } else {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        mbar_expect_tx(&full[st], (unsigned)(ng * (kWinBytes + (int)sizeof(Group) + kTile * 4)));
+                    }
+                }
+                halt = __shfl_sync(0xffffffffu, halt, 0);
+                if (halt) {
+                    stop = true;
+                    break;
+                }
+                unsigned char* sp = stages + (size_t)st * kStageBytes;
+                const int q = lane - k0;  // this lane's group within the stage
+                if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * kWinBytes, eprev + a0, kWinBytes, &full[st]);
+                if (lane == 0) {
+                    const long long g0 = g_beg + base + k0;
+                    bulk_copy_g2s(sp + kHdrOff, groups + g0, (unsigned)(ng * sizeof(Group)), &full[st]);
+                    bulk_copy_g2s(sp + kCoefOff, coef + ((size_t)b * cap + g0) * kTile, (unsigned)(ng * kTile * 4),
+                                  &full[st]);
+                    s_issued = si + 1;
+                }
+            }
+        }
+    } else {
+        // consumer: receiver slots 2 warp and 2 warp + 1 of the tile
+        const int sh = kSlotsPerWarp * warp;
+        for (int si = 0; si < n_stage; ++si) {
+            const int st = si % kStages;
+            const bool ok = mbar_wait(&full[st], (unsigned)((si / kStages) & 1), err);
+            if (!__all_sync(0xffffffffu, ok)) {  // the whole warp leaves together
+                if (lane == 0) {
+                    atomicExch(err, 1);
+                    s_abort = 1;
+                }
+                break;
+            }
+            const unsigned char* sp = stages + (size_t)st * kStageBytes;
+            const int ng = min(kGps, n_grp - si * kGps);
+            // the stage's records first (independent loads), then the windows
+            unsigned bits[kGps];
+            int base_off[kGps];  // kMaxSpan + mu, per group
+            float2 cf[kGps];
+            unsigned offs[kGps];  // off of slot sh (low byte) and sh + 1 (second byte)
+#pragma unroll
+            for (int q = 0; q < kGps; ++q) {
+                const Group* g = reinterpret_cast<const Group*>(sp + kHdrOff) + q;
+                // record at a 16-byte boundary: srcrow, n_base, mask, pad
+                const int4 hdr = q < ng ? *reinterpret_cast<const int4*>(g) : make_int4(0, 0, 0, 0);
+                bits[q] = ((unsigned)hdr.z >> sh) & 3u;
+                base_off[q] = kMaxSpan + ((-hdr.y - kMaxSpan) & 3);  // staged start was rounded down by mu floats
+                cf[q] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(sp + kCoefOff) + q * kTile + sh);
+                offs[q] = *reinterpret_cast<const uint16_t*>(&g->off[sh]);
+            }
+#pragma unroll
+            for (int q = 0; q < kGps; ++q) {
+                const float* win = reinterpret_cast<const float*>(sp + q * kWinBytes);
+                if (bits[q] & 1u) slot_window(acc0, win, cf[q].x, (int)(offs[q] & 0xffu), base_off[q], lane);
+                if (bits[q] & 2u) slot_window(acc1, win, cf[q].y, (int)(offs[q] >> 8), base_off[q], lane);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[st]);
+        }
+    }
+    __syncthreads();
+    if (s_abort) {
+        // drain: wait (bounded) until every issued copy has landed
+        if (threadIdx.x == 0) {
+            const int issued = s_issued;
+            for (int si = issued - 1; si >= 0 && si >= issued - kStages; --si)
+                mbar_wait(&full[si % kStages], (unsigned)((si / kStages) & 1), err);
+        }
+        return;
+    }
+    if (warp < kConsumers) {
+        const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+#pragma unroll
+        for (int h = 0; h < kSlotsPerWarp; ++h) {
+            const int j = tile_recv[tile * kTile + kSlotsPerWarp * warp + h];
+            if (j < 0) continue;
+            float* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + lane;
+#pragma unroll
+            for (int r = 0; r < kBins; ++r)
+                if (t0 + lane + 32 * r < nt) out[32 * r] = h == 0 ? acc0[r] : acc1[r];
+        }
+    }
+}
+
+// --------------------------------------------------------- FP64 scatter
+constexpr int kR64 = 4;
+constexpr int kTW64 = kThreads * kR64;
+
+template <int W>
+__device__ __forceinline__ void slot_f64(double (&acc)[kTile][kR64], const Group& g, const double* sp, const double* cf) {
+    if (g.mask & (1u << W)) {
+        const double cfw = cf[W];
+        const double* p = sp - g.off[W];
+#pragma unroll
+        for (int r = 0; r < kR64; ++r) acc[W][r] = fma(cfw, __ldg(p + kThreads * r), acc[W][r]);
+    }
+}
+__device__ __forceinline__ void group_f64(double (&acc)[kTile][kR64], const Group& g, const double* sp, const double* cf) {
+    slot_f64<0>(acc, g, sp, cf);
+    slot_f64<1>(acc, g, sp, cf);
+    slot_f64<2>(acc, g, sp, cf);
+    slot_f64<3>(acc, g, sp, cf);
+    slot_f64<4>(acc, g, sp, cf);
+    slot_f64<5>(acc, g, sp, cf);
+    slot_f64<6>(acc, g, sp, cf);
+    slot_f64<7>(acc, g, sp, cf);
+    slot_f64<8>(acc, g, sp, cf);
+    slot_f64<9>(acc, g, sp, cf);
+    slot_f64<10>(acc, g, sp, cf);
+    slot_f64<11>(acc, g, sp, cf);
+    slot_f64<12>(acc, g, sp, cf);
+    slot_f64<13>(acc, g, sp, cf);
+    slot_f64<14>(acc, g, sp, cf);
+    slot_f64<15>(acc, g, sp, cf);
+}
+
+// FP64: same plan, direct (L1-cached) loads, thread owns bins t0 + tid + 128 r.
+__global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, int nt, long long rs, int lead,
+                                                          long long cap, const int32_t* __restrict__ tile_recv,
+                                                          const int32_t* __restrict__ seg_order,
+                                                          const int64_t* __restrict__ seg_off,
+                                                          const Group* __restrict__ groups,
+                                                          const double* __restrict__ coef,
+                                                          const double* __restrict__ eprev,
+                                                          double* __restrict__ gout) {
+    const long long seg = seg_order[blockIdx.x];
+    const int b = blockIdx.z;
+    const int t0 = blockIdx.y * kTW64;
+    const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
+    if (g_beg == g_end) return;
+    const int tid = threadIdx.x;
+    const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+    double acc[kTile][kR64];
+#pragma unroll
+    for (int w = 0; w < kTile; ++w)
+#pragma unroll
+        for (int r = 0; r < kR64; ++r) acc[w][r] = 0.0;
+    for (long long gidx = g_beg; gidx < g_end; ++gidx) {
+        const Group& g = groups[gidx];  // read in place (no local copy)
+        const double* cf = coef + ((size_t)b * cap + gidx) * kTile;
+        // padded rows: the zero lead covers source indices below 0
+        const double* sp = eprev + ((long long)g.srcrow * nb + b) * rs + lead + t0 + tid - g.n_base;
+        group_f64(acc, g, sp, cf);
+    }
+#pragma unroll
+    for (int w = 0; w < kTile; ++w) {
+        int j = tile_recv[tile * kTile + w];
+        if (j < 0) continue;
+        double* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + tid;
+#pragma unroll
+        for (int r = 0; r < kR64; ++r)
+            if (t0 + tid + kThreads * r < nt) out[kThreads * r] = acc[w][r];
+    }
+}
+
+}  // namespace

@@ -188,6 +188,7 @@ class DirectionalRadiosityFast:
         self._dev = {}      # device tensors of the current geometry / results
         self._bake = None   # device state of the last bake
         self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
+        self._device_brdf_key = None  # set while device-built tables are installed
         self.check()
 
     # ------------------------------------------------------------ validation
@@ -302,7 +303,7 @@ class DirectionalRadiosityFast:
             return None
         key = (id(self._brdf), len(self._brdf), tuple(self._brdf_index.tolist()))
         cached = self._dev.get("brdf_state")
-        if cached is not None and cached["key"] == key:
+        if cached is not None and (cached["key"] == key or cached["key"] == self._device_brdf_key):
             return cached
         if np.any(self._brdf_index < 0):
             raise ValueError("every wall needs a BRDF (set_wall_brdf) before this step")
@@ -319,6 +320,30 @@ class DirectionalRadiosityFast:
                      dirs_in=self._t(din, torch.float64), dirs_out=self._t(dout, torch.float64),
                      brdf=self._t(brdf, torch.float64), brdf_index=self._t(self._brdf_index, torch.int32))
         self._dev["brdf_state"] = state
+        return state
+
+    def _install_device_brdf(self, tables, brdf_index):
+        """Use device-built BRDF tables (S, n_in, n_out, B) float64 with the current direction sets.
+
+        For solvers that build the tables on the GPU (the differentiable
+        exchange); set_wall_brdf replaces them again.  Keeps the baked
+        geometry; the next exchange re-plans for the new tables.
+        """
+        base = self._brdf_device()
+        if base is None:
+            raise ValueError("set the BRDF direction sets (set_wall_brdf) first")
+        if tuple(tables.shape[1:3]) != (base["n_in"], base["n_out"]):
+            raise ValueError("tables must be (n_slots, n_in, n_out, n_bins) for the current direction sets")
+        state = dict(base)
+        state.pop("structure", None)
+        key = ("device", id(tables))
+        state.update(key=key, brdf=tables.contiguous(), n_slots=int(tables.shape[0]), brdf_host=None,
+                     brdf_index=self._t(brdf_index, torch.int32))
+        self._dev["brdf_state"] = state
+        self._device_brdf_key = key
+        if self._bake is not None:
+            self._bake["brdf"] = state
+            self._bake.pop("plan", None)
         return state
 
     def _brdf_structure(self, bs):
@@ -453,6 +478,7 @@ class DirectionalRadiosityFast:
             e0dir *= self._t(fac, torch.float64)[:, None, :]
         self._dev["svis"] = svis
         self._dev["e0dir"] = e0dir
+        self._dev["e0"] = e0
         self._dev["d0"] = d0
         for k in ("distance_patches_to_source", "energy_init_source"):
             self._host.pop(k, None)
@@ -559,12 +585,18 @@ class DirectionalRadiosityFast:
             a.pair_dst = bk["dst"].data_ptr()
         return a
 
-    def _run_exchange(self, c, dt, n_samples, max_order, algorithm="auto"):
+    def _run_exchange(self, c, dt, n_samples, max_order, algorithm="auto", states=None, states_every=0):
+        """Exchange of all orders; optional `states` (n, N, D, B, T) receives E_0, E_m, E_2m, ... (m = states_every)."""
         e0dir = self._dev["e0dir"]
         n, nd, nb = e0dir.shape
         dtype = torch.float32 if self.precision == "fp32" else torch.float64
         etc = torch.empty((n, nd, nb, n_samples), dtype=dtype, device=self.device)
         a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
+        if states is not None:
+            if a.algorithm != nat.SP_EXCHANGE_STRUCTURED:
+                raise ValueError("saving exchange states needs the structured exchange")
+            a.states_out = states.data_ptr()
+            a.states_every = int(states_every)
         stats = (ctypes.c_int64 * 4)()
         a.plan_stats = stats
         order_ms = ctypes.c_float(-1.0)
@@ -581,6 +613,21 @@ class DirectionalRadiosityFast:
         self.exchange_stats = dict(algorithm="structured" if a.algorithm == nat.SP_EXCHANGE_STRUCTURED else "dense",
                                    source_groups=int(stats[0]), segments=int(stats[1]), pairs=int(stats[2]),
                                    tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order))
+
+    def _resume_exchange(self, c, dt, n_samples, state_in, k_from, k_to, states):
+        """Orders k_from + 1 .. k_to from E_{k_from} = state_in; states[i] receives E_{k_from + i} (no E_total)."""
+        dummy = torch.empty((1,), dtype=state_in.dtype, device=self.device)
+        a = self._exchange_args(c, dt, n_samples, int(k_to), "structured", dummy)
+        a.state_in = state_in.data_ptr()
+        a.state_order = int(k_from)
+        a.states_out = states.data_ptr()
+        a.states_every = 1
+        a.skip_total = 1
+        n, nd, nb = self._dev["e0dir"].shape
+        wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
+                       a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups * a.n_in_dirs)
+        ws = self._workspace(wsz)
+        nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())
 
     def _workspace(self, nbytes):
         ws = self._dev.get("ws")
@@ -643,13 +690,18 @@ class DirectionalRadiosityFast:
             raise ValueError("Receiver positions must be of type pf.Coordinates")
         if patchwise and receivers.cdim != 1:
             raise ValueError("Receiver positions must be of shape (n_receivers, 3)")
+        rc = np.atleast_2d(np.asarray(receivers.cartesian, dtype=float).reshape(-1, 3))
+        data = self._collect_device(rc, patchwise).cpu().numpy()
+        times = np.arange(data.shape[-1]) * self._etc_time_resolution
+        return TimeData(data, times)
+
+    def _collect_device(self, rc, patchwise=False):
+        """Receiver histograms on the device, FP64: (R, B, T), or (R, N, B, T) patchwise."""
         etc = self._etc_device()
-        d = self._geometry()
         bs = self._brdf_device()
         n, nd, nb, nt = etc.shape
         if bs is None or bs["n_out"] != nd:
             raise ValueError("the outgoing BRDF directions do not match the energy histograms")
-        rc = np.atleast_2d(np.asarray(receivers.cartesian, dtype=float).reshape(-1, 3))
         n_r = rc.shape[0]
         dev = self.device
         st = _stream()
@@ -659,24 +711,36 @@ class DirectionalRadiosityFast:
             out = torch.empty((n_r, n, nb, nt), dtype=torch.float64, device=dev)
         else:
             out = torch.empty((n_r, nb, nt), dtype=torch.float64, device=dev)
-        rfac = torch.empty((n,), dtype=torch.float64, device=dev)
-        ridx = torch.empty((n,), dtype=torch.int32, device=dev)
-        dist = torch.empty((n,), dtype=torch.float64, device=dev)
+        ridx_all, rfac_all, dist_all = self._receiver_factors(rc)
         wsz = nat.size("sp_collect_workspace", n, nb)
         ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=dev)
+        for r in range(n_r):
+            ridx, rfac, dist = ridx_all[r], rfac_all[r], dist_all[r]
+            nat.call("sp_collect_receiver", prec, n, nd, nb, nt, _ptr(etc), _ptr(ridx), _ptr(rfac), _ptr(dist),
+                     float(self.speed_of_sound), float(self._etc_time_resolution), _ptr(att),
+                     _ptr(out[r]) if patchwise else _ptr(None), _ptr(None) if patchwise else _ptr(out[r]),
+                     _ptr(ws), wsz, st)
+        return out
+
+    def _receiver_factors(self, rc):
+        """Per receiver (rows of rc, (R, 3)) and patch: outgoing index, point factor, distance (R, N) each."""
+        d = self._geometry()
+        bs = self._brdf_device()
+        n = self.n_patches
+        n_r = rc.shape[0]
+        dev = self.device
+        st = _stream()
+        ridx = torch.empty((n_r, n), dtype=torch.int32, device=dev)
+        rfac = torch.empty((n_r, n), dtype=torch.float64, device=dev)
+        dist = torch.empty((n_r, n), dtype=torch.float64, device=dev)
         rdev = self._t(rc, torch.float64)
         for r in range(n_r):
             rp = rdev[r]
             rvis = self._point_visibility(rp)
             nat.call("sp_receiver_factors", _ptr(rp), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(rvis),
-                     _ptr(d["wall_of"]), bs["n_out"], _ptr(bs["dirs_out"]), _ptr(rfac), _ptr(ridx), _ptr(dist), st)
-            nat.call("sp_collect_receiver", prec, n, nd, nb, nt, _ptr(etc), _ptr(ridx), _ptr(rfac), _ptr(dist),
-                     float(self.speed_of_sound), float(self._etc_time_resolution), _ptr(att),
-                     _ptr(out[r]) if patchwise else _ptr(None), _ptr(None) if patchwise else _ptr(out[r]),
-                     _ptr(ws), wsz, st)
-        data = out.cpu().numpy()
-        times = np.arange(nt) * self._etc_time_resolution
-        return TimeData(data, times)
+                     _ptr(d["wall_of"]), bs["n_out"], _ptr(bs["dirs_out"]), _ptr(rfac[r]), _ptr(ridx[r]),
+                     _ptr(dist[r]), st)
+        return ridx, rfac, dist
 
     # ------------------------------------------------------------- materials
     def set_air_attenuation(self, air_attenuation):
@@ -702,6 +766,7 @@ class DirectionalRadiosityFast:
         self._brdf.append(np.asarray(brdf.freq, dtype=float) * np.pi)
         self._brdf_index[np.atleast_1d(wall_indexes)] = len(self._brdf) - 1
         self._dev.pop("brdf_state", None)
+        self._device_brdf_key = None
 
     def _check_set_frequency(self, frequencies):
         frequencies = np.atleast_1d(np.asarray(frequencies))

@@ -129,3 +129,23 @@ def test_to_dict_round_trip():
     assert r2.n_patches == r.n_patches
     np.testing.assert_array_equal(r2.patches_points, r.patches_points)
     np.testing.assert_array_equal(r2._air_attenuation, r._air_attenuation)
+
+
+def test_material_tables_reproduce_create_from_scattering():
+    """The adjoint's material parametrisation is create_from_scattering x pi (brdf.py:8-130, RadiosityFast.py:815)."""
+    import torch
+    from sparrowpy_gb300.adjoint import material_tables, mirror_table
+    from sparrowpy_gb300.brdf import create_from_scattering, hemisphere_directions
+    from sparrowpy_gb300.coords import FrequencyData
+    dirs = hemisphere_directions(16)
+    mirror, gain = mirror_table(dirs)
+    assert (mirror >= 0).all()
+    rng = np.random.default_rng(1)
+    alpha = rng.uniform(0.0, 0.6, (3, 4))
+    scat = rng.uniform(0.0, 1.0, (3, 4))
+    tabs = material_tables(torch.tensor(alpha), torch.tensor(scat), mirror, gain, 16).numpy()
+    freqs = np.array([125.0, 250.0, 500.0, 1000.0])
+    for k in range(3):
+        ref = np.asarray(create_from_scattering(dirs, dirs, FrequencyData(scat[k], freqs),
+                                                FrequencyData(alpha[k], freqs)).freq) * np.pi
+        np.testing.assert_allclose(tabs[k], ref, rtol=1e-13, atol=1e-15)
