@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--max-order", type=int, default=None, help="override the workload's reflection order")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-fwd-bwd", action="store_true", help="skip the gradient (forward + backward) leg")
+    ap.add_argument("--fwd-bwd-only", action="store_true",
+                    help="print only the gradient leg (shoebox, 2016 patches) as one JSON line")
     return ap.parse_args()
 
 
@@ -367,6 +370,15 @@ def run_gpu(args):
         del r64, c64
         torch.cuda.empty_cache()
 
+    fwd_bwd = None
+    if not args.no_fwd_bwd and rank == 0:
+        r._dev.pop("ws", None)
+        torch.cuda.empty_cache()
+        try:
+            fwd_bwd = fwd_bwd_config4()
+        except Exception as exc:  # the gradient leg must not hide the solve result
+            fwd_bwd = {"error": f"{type(exc).__name__}: {exc}"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -390,6 +402,7 @@ def run_gpu(args):
                          "algorithmic_bytes": bytes_order, "ms_per_launch": ms_order},
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
+            "fwd_bwd": fwd_bwd,
             "clocks": clk,
             "gpu_launches": int(launches),
             "exchange": {"algorithm": stats["algorithm"], "directed_pairs": n_pairs,
@@ -399,6 +412,69 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+# ------------------------------------------------------- forward + backward
+def fwd_bwd_config4(steps=2, fd_params=2, seed=4):
+    """Energy-decay-loss gradient w.r.t. per-patch, per-band absorption and scattering.
+
+    Shoebox 5 x 6 x 3 m, 0.25 m patches, one wall per patch (2016 patches), 6
+    bands, 64 directions, 1 ms x 2 s, order 50, 1 source, 1 receiver; the
+    target comes from a second seeded material set.  Times the forward solve
+    (with checkpoints) and forward + backward with CUDA events; checks the
+    largest gradients against central differences of the FP32 forward.
+    """
+    import torch
+    from sparrowpy_gb300.adjoint import DifferentiableExchange, as_source, energy_decay_loss, per_patch_room
+    from sparrowpy_gb300.brdf import hemisphere_directions
+    dirs = hemisphere_directions(64)
+    r = per_patch_room((5.0, 6.0, 3.0), 0.25, dirs, 6)
+    src, rcv = np.array([2.0, 2.0, 1.5]), np.array([[3.0, 4.0, 1.5]])
+    solver = DifferentiableExchange(r, dirs, as_source(src), rcv, 343.0, 1e-3, 2.0, 50)
+    rng = np.random.default_rng(seed)
+    S = solver.n_slots
+    dev = "cuda"
+    t = lambda x, g=False: torch.tensor(x, dtype=torch.float64, device=dev, requires_grad=g)
+    alpha0, scat0 = rng.uniform(0.02, 0.6, (S, 6)), rng.uniform(0.1, 0.9, (S, 6))
+    target = solver.forward_only(t(rng.uniform(0.02, 0.6, (S, 6))), t(rng.uniform(0.1, 0.9, (S, 6))))
+    st = torch.cuda.current_stream()
+    fwd_ms, both_ms = [], []
+    for k in range(steps + 1):  # first pass warms up
+        a_t, s_t = t(alpha0, True), t(scat0, True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        loss = energy_decay_loss(solver(a_t, s_t), target)
+        e1.record(st)
+        loss.backward()
+        e2.record(st)
+        e2.synchronize()
+        if k > 0:
+            fwd_ms.append(e0.elapsed_time(e1))
+            both_ms.append(e0.elapsed_time(e2))
+    ga, gs = a_t.grad.cpu().numpy(), s_t.grad.cpu().numpy()
+    fd = []
+    h = 1e-3
+    flat = np.abs(np.concatenate([ga.ravel(), gs.ravel()]))
+    for q in np.argsort(flat)[::-1][:fd_params]:
+        which, k = (0, q) if q < ga.size else (1, q - ga.size)
+        idx = np.unravel_index(k, ga.shape)
+        vals = []
+        for sign in (1, -1):
+            a, s_ = alpha0.copy(), scat0.copy()
+            (a if which == 0 else s_)[idx] += sign * h
+            vals.append(float(energy_decay_loss(solver.forward_only(t(a), t(s_)), target)))
+        fdv = (vals[0] - vals[1]) / (2 * h)
+        g = float((ga if which == 0 else gs)[idx])
+        fd.append({"param": ["absorption", "scattering"][which], "index": [int(x) for x in idx], "adjoint": g,
+                   "central_difference": fdv, "rel_err": abs(g - fdv) / max(abs(fdv), 1e-300)})
+    out = {"workload": "shoebox 5x6x3 m, 0.25 m patches, one wall per patch: 2016 patches, 6 bands, 64 directions, "
+                       "T=2000, order 50; loss = sum (log EDC - log EDC_target)^2",
+           "params": int(ga.size + gs.size), "fwd_ms": float(np.mean(fwd_ms)), "fwd_bwd_ms": float(np.mean(both_ms)),
+           "fwd_bwd_over_fwd": float(np.mean(both_ms) / np.mean(fwd_ms)), "checkpoint_every": solver.m,
+           "fd_check_h": h, "fd_check": fd}
+    del solver, r, target
+    torch.cuda.empty_cache()
+    return out
 
 
 # ----------------------------------------------------------- reference arm
@@ -430,7 +506,12 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.fwd_bwd_only:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps({"metric": "fwd+bwd ms", "fwd_bwd": fwd_bwd_config4(steps=a.steps, fd_params=0)}),
+              flush=True)
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_gpu(a)
