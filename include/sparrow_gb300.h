@@ -217,6 +217,10 @@ typedef struct sp_exchange_args {
     const double* mat_scattering;   /* (n_slots, B) */
     const int32_t* mat_mirror;      /* (n_in) mirror outgoing direction, -1: none */
     const double* mat_gain;         /* (n_in) */
+    /* structured / material: nonzero = the caller promises identical pairs and
+       materials to every call with the same tag; the plan left in `ws` by the
+       previous call with this tag (and these sizes) is then reused */
+    long long plan_tag;
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070
@@ -258,7 +262,7 @@ typedef struct sp_adjoint_args {
     const double* mirror_gain;    /* (n_in) K_c */
     const double* alpha;          /* (n_slots, B) */
     const double* scattering;     /* (n_slots, B) */
-    int n_receivers;
+    int n_receivers;              /* R <= 64 */
     const int32_t* recv_dir;      /* (R, N) outgoing index of each patch toward each receiver */
     const double* recv_factor;    /* (R, N) patch-to-receiver factors (0 where not visible) */
     const double* recv_dist;      /* (R, N) patch-to-receiver distances */
@@ -268,7 +272,8 @@ typedef struct sp_adjoint_args {
     sp_adjoint_state* state;      /* HOST */
 } sp_adjoint_args;
 
-size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs);
+size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs,
+                            int n_receivers);
 int sp_adjoint_begin(const sp_adjoint_args* args, void* ws, size_t ws_bytes, void* stream);
 int sp_adjoint_order(const sp_adjoint_args* args, const void* e_prev, void* ws, size_t ws_bytes, void* stream);
 int sp_adjoint_finish(const sp_adjoint_args* args, double* grad_e0dir, void* ws, size_t ws_bytes, void* stream);

@@ -57,6 +57,7 @@ class ExchangeArgs(ctypes.Structure):
         ("order_ms", ctypes.POINTER(ctypes.c_float)),
         ("state_in", P), ("state_order", I), ("states_out", P), ("states_every", I), ("skip_total", I),
         ("mat_alpha", P), ("mat_scattering", P), ("mat_mirror", P), ("mat_gain", P),
+        ("plan_tag", LL),
     ]
 
 
@@ -97,7 +98,7 @@ _SIGS = {
     "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
     "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I, I]),
     "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
-    "sp_adjoint_workspace": (SZ, [I, I, I, I, LL]),
+    "sp_adjoint_workspace": (SZ, [I, I, I, I, LL, I]),
     "sp_adjoint_begin": (I, [ctypes.POINTER(AdjointArgs), P, SZ, P]),
     "sp_adjoint_order": (I, [ctypes.POINTER(AdjointArgs), P, P, SZ, P]),
     "sp_adjoint_finish": (I, [ctypes.POINTER(AdjointArgs), P, P, SZ, P]),

@@ -10,11 +10,13 @@ per-band absorption a and scattering s:
 brdf.py:110-118).  `DifferentiableExchange` runs the forward solve (the
 same CUDA path as DirectionalRadiosityFast, FP32 histograms) and, behind a
 torch.autograd.Function, the hand-written adjoint of the exchange
-(libsparrow_gb300: sp_adjoint_*).  Exchange states are checkpointed every
-m = ceil(sqrt(K)) orders on the forward pass and recomputed segment by
-segment on the backward pass.  The reference has no differentiable path.
+(libsparrow_gb300: sp_adjoint_*).  Exchange states are checkpointed every m
+orders on the forward pass (the smallest m whose states fit in device
+memory; sqrt(K) when memory is short) and recomputed segment by segment on
+the backward pass.  The reference has no differentiable path.
 """
 import ctypes
+import itertools
 import math
 
 import numpy as np
@@ -24,6 +26,8 @@ from . import _native as nat
 from .brdf import create_from_scattering
 from .coords import Coordinates, FrequencyData, _cart
 from .radiosity import _ptr, _stream, receiver_tile_order
+
+_PLAN_TAGS = itertools.count(1)  # plan reuse tags: one per backward pass (process-wide, never 0)
 
 
 def mirror_table(directions):
@@ -83,7 +87,8 @@ class DifferentiableExchange:
         self.dt = float(etc_time_resolution)
         self.nt = int(etc_duration / etc_time_resolution)
         self.K = int(max_reflection_order)
-        self.m = int(checkpoint_every) if checkpoint_every else max(1, int(math.ceil(math.sqrt(self.K))))
+        self._m_fixed = int(checkpoint_every) if checkpoint_every else None
+        self.m = self._m_fixed or max(1, int(math.ceil(math.sqrt(self.K))))
         self.slot_of_wall = np.arange(r.n_walls) if slot_of_wall is None else np.asarray(slot_of_wall, dtype=int)
         self.n_slots = int(self.slot_of_wall.max()) + 1
         mirror, gain = mirror_table(directions)
@@ -101,6 +106,29 @@ class DifferentiableExchange:
         self._slot_of_wall_dev = torch.as_tensor(self.slot_of_wall, dtype=torch.int32, device=dev)
         self._ckpt = None
         self._e0dir = None
+        if self._m_fixed is None:
+            self.m = self._choose_spacing()
+
+    def _choose_spacing(self, margin=24 << 30):
+        """Smallest checkpoint spacing whose states fit in the free device memory (at least sqrt(K) otherwise).
+
+        Stored states are (K // m + 1) checkpoints plus m - 1 recomputed ones
+        per segment; fewer recomputed orders for a smaller m.
+        """
+        r = self.r
+        n, nd, nb = r._dev["e0dir"].shape
+        h = n * nd * nb * self.nt * 4
+        p = int(r._bake["n_dir"])
+        fw = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_MATERIAL, n, nd, nb, self.nt, p,
+                      self.n_slots, self.mirror_np.size, 1 + self.mirror_np.size)
+        adj = nat.size("sp_adjoint_workspace", n, nd, nb, self.nt, p, int(self.receivers.shape[0]))
+        free, _ = torch.cuda.mem_get_info(r.device)
+        avail = free + torch.cuda.memory_reserved(r.device) - torch.cuda.memory_allocated(r.device)
+        for m in range(1, self.K + 1):
+            need = (self.K // m + 1) * h + (m if m > 1 else 0) * h + fw + adj + 2 * h + margin
+            if need <= avail:
+                return m
+        return max(1, int(math.ceil(math.sqrt(self.K))))
 
     # ------------------------------------------------------------- forward
     def _args(self, alpha64, scat64, etc):
@@ -145,6 +173,7 @@ class DifferentiableExchange:
 
     def _solve(self, alpha, scattering, keep_states):
         r = self.r
+        self._ckpt = None  # the previous pass's checkpoints go before new ones are allocated
         alpha64 = alpha.detach().to(torch.float64).contiguous()
         scat64 = scattering.detach().to(torch.float64).contiguous()
         self._e0dir = self._source_dir(alpha64, scat64).contiguous()
@@ -175,6 +204,7 @@ class DifferentiableExchange:
         a.states_out = states.data_ptr()
         a.states_every = 1
         a.skip_total = 1
+        a.plan_tag = self._tag  # one plan for every segment of this backward pass
         ws, wsz = self._workspace(a)
         nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())
 
@@ -194,6 +224,7 @@ class DifferentiableExchange:
         nt, K, m = self.nt, self.K, self.m
         alpha64 = alpha.detach().to(torch.float64).contiguous()
         scat64 = scattering.detach().to(torch.float64).contiguous()
+        self._tag = next(_PLAN_TAGS)
         ga = torch.zeros_like(alpha64)
         gs = torch.zeros_like(scat64)
         ridx, rfac, rdist = r._receiver_factors(self.receivers)
@@ -215,7 +246,7 @@ class DifferentiableExchange:
         a.grad_alpha = ga.data_ptr()
         a.grad_scattering = gs.data_ptr()
         a.state = ctypes.pointer(state)
-        wsz = nat.size("sp_adjoint_workspace", n, nd, nb, nt, fwd.n_dir_pairs)
+        wsz = nat.size("sp_adjoint_workspace", n, nd, nb, nt, fwd.n_dir_pairs, int(self.receivers.shape[0]))
         ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
         st = _stream()
         nat.call("sp_adjoint_begin", ctypes.byref(a), _ptr(ws), wsz, st)
@@ -231,6 +262,7 @@ class DifferentiableExchange:
         g_e0 = torch.empty((n, nd, nb), dtype=torch.float64, device=dev)
         nat.call("sp_adjoint_finish", ctypes.byref(a), _ptr(g_e0), _ptr(ws), wsz, st)
         self._source_term(alpha64, scat64, g_e0, ga, gs)
+        self._ckpt = None  # the checkpoints serve one backward pass
         return ga, gs
 
     def _source_term(self, alpha, scat, g_e0, ga, gs):

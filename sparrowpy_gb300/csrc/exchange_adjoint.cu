@@ -113,12 +113,13 @@ struct AdjCoef {
     }
 };
 
-// g (reversed time) from dL/dmono: mono[r, b, t] = sum_k E[k, ridx_rk, b, (t - s_rk) mod T] f_rk a_rkb
-// (k_collect_mono), so g[k, ridx_rk, b, t] += f_rk a_rkb gm[r, b, (t + s_rk) mod T].
-// One block per (band, patch).
-__global__ void k_adjoint_g(int n, int nd, int nb, int nt, int n_rcv, const int32_t* __restrict__ ridx,
-                            const double* __restrict__ rfac, const double* __restrict__ rdist, double c, double dt,
-                            const double* __restrict__ att, const double* __restrict__ gm, float* __restrict__ g_rev) {
+// g = dL/dE_total is nonzero only in the row (k, ridx_rk) of each receiver r:
+// mono[r, b, t] = sum_k E[k, ridx_rk, b, (t - s_rk) mod T] f_rk a_rkb (k_collect_mono),
+// so that row of g, reversed, is g_r[k, b, tau] = f_rk a_rkb gm[r, b, (T - 1 - tau + s_rk) mod T].
+// One block per (band, patch); g_rev is (R, N, B, T).
+__global__ void k_adjoint_g(int n, int nb, int nt, int n_rcv, const double* __restrict__ rfac,
+                            const double* __restrict__ rdist, double c, double dt, const double* __restrict__ att,
+                            const double* __restrict__ gm, float* __restrict__ g_rev) {
     const int b = blockIdx.x, k = blockIdx.y;
     for (int r = 0; r < n_rcv; ++r) {
         const size_t rk = (size_t)r * n + k;
@@ -127,14 +128,13 @@ __global__ void k_adjoint_g(int n, int nd, int nb, int nt, int n_rcv, const int3
         s %= nt;
         if (s < 0) s += nt;
         const double f = rfac[rk] * (att ? exp(-att[b] * rdist[rk]) : 1.0);
-        float* out = g_rev + (((size_t)k * nd + ridx[rk]) * nb + b) * nt;
+        float* out = g_rev + (rk * nb + b) * nt;
         const double* src = gm + ((size_t)r * nb + b) * nt;
         for (int tau = threadIdx.x; tau < nt; tau += blockDim.x) {
             long long t = nt - 1 - tau + s;
             if (t >= nt) t -= nt;
-            out[tau] += (float)(f * src[t]);
+            out[tau] = (float)(f * src[t]);
         }
-        __syncthreads();  // the same row may be hit by several receivers
     }
 }
 
@@ -142,25 +142,53 @@ __global__ void k_adjoint_g(int n, int nd, int nb, int nt, int n_rcv, const int3
 // (rows 0..D-1 of each patch, reversed time) with U = sum over rows in row D;
 // gradient dot products with E_{k-1} (normal time).  lam == nullptr: mu = g
 // (the first step, no gradient).  One block per (band, patch).
+constexpr int kMaxReceivers = 64;  // receivers one adjoint pass can take (dL/dmono rows)
+constexpr int kCombineBins = 16;   // bins per thread in k_adjoint_combine: nt <= 256 * 16
+
+// Rows of dL/dE_total beyond the first two that fall on direction p of patch i
+// (three or more receivers seen along one direction): added to `out` (a mu
+// row, or the U row) at the bins this thread owns.
+__device__ __noinline__ void add_extra_rows(int p, int n_rcv, const int* s_ridx, const float* __restrict__ g_rev,
+                                            int n, int i, int nb, int b, int nt, float* out) {
+    for (int r = 0, h = 0; r < n_rcv; ++r) {
+        if (s_ridx[r] != p || h++ < 2) continue;
+        const float* row = g_rev + (((size_t)r * n + i) * nb + b) * nt;
+        for (int tau = threadIdx.x; tau < nt; tau += 256) out[tau] += row[tau];
+    }
+}
+
 __global__ void __launch_bounds__(256) k_adjoint_combine(
-    int n, int nd, int nb, int nt, long long rs, int lead, const float* __restrict__ g_rev,
-    const float* __restrict__ lam, const uint32_t* __restrict__ present, int words, const int32_t* __restrict__ tile_of,
+    int n, int nd, int nb, int nt, long long rs, int lead, int n_rcv, const int32_t* __restrict__ ridx,
+    const float* __restrict__ g_rev, const float* __restrict__ lam, const uint32_t* __restrict__ present, int words, const int32_t* __restrict__ tile_of,
     const float* __restrict__ e_prev, const int32_t* __restrict__ wall_of, const int32_t* __restrict__ brdf_index,
     const double* __restrict__ alpha, const double* __restrict__ scat, float* __restrict__ mu_out,
     double* __restrict__ grad_a, double* __restrict__ grad_s) {
     const int b = blockIdx.x, i = blockIdx.y;
+    __shared__ int s_ridx[kMaxReceivers];
+    for (int r = threadIdx.x; r < n_rcv; r += blockDim.x) s_ridx[r] = ridx[(size_t)r * n + i];
+    __syncthreads();
     const int slot = brdf_index[wall_of[i]];
     const float a = (float)alpha[(size_t)slot * nb + b];
     const float sc = (float)scat[(size_t)slot * nb + b];
     const float keep = 1.0f - a;
     const uint32_t* pres = lam ? present + (size_t)tile_of[i] * words : nullptr;
-    constexpr int kMaxPerThread = 16;  // nt <= 256 * 16
+    constexpr int kMaxPerThread = kCombineBins;
     float usum[kMaxPerThread];
 #pragma unroll
     for (int q = 0; q < kMaxPerThread; ++q) usum[q] = 0.0f;
     float dot_mix = 0.0f, dot_diff = 0.0f;
     for (int p = 0; p < nd; ++p) {
-        const float* gr = g_rev + (((size_t)i * nd + p) * nb + b) * nt;
+        // rows of dL/dE_total in direction p of this patch (one per receiver seeing it along p)
+        const float* g0 = nullptr;
+        const float* g1 = nullptr;
+        int n_hit = 0;
+        for (int r = 0; r < n_rcv; ++r)
+            if (s_ridx[r] == p) {
+                const float* row = g_rev + (((size_t)r * n + i) * nb + b) * nt;
+                if (n_hit == 0) g0 = row;
+                else if (n_hit == 1) g1 = row;
+                ++n_hit;
+            }
         const bool has_u = pres && ((pres[p >> 5] >> (p & 31)) & 1u);
         const bool has_v = pres && ((pres[(nd + p) >> 5] >> ((nd + p) & 31)) & 1u);
         const float* lu = has_u ? lam + (((size_t)i * 2 * nd + p) * nb + b) * nt : nullptr;
@@ -174,7 +202,9 @@ __global__ void __launch_bounds__(256) k_adjoint_combine(
                 const float u = lu ? lu[tau] : 0.0f;
                 const float v = lv ? lv[tau] : 0.0f;
                 const float mixed = sc * u + (1.0f - sc) * v;
-                const float m = gr[tau] + keep * mixed;
+                float m = keep * mixed;
+                if (g0) m += g0[tau];
+                if (g1) m += g1[tau];
                 mo[tau] = m;
                 usum[q] += m;
                 if (ep) {
@@ -184,12 +214,18 @@ __global__ void __launch_bounds__(256) k_adjoint_combine(
                 }
             }
         }
+        if (n_hit > 2) add_extra_rows(p, n_rcv, s_ridx, g_rev, n, i, nb, b, nt, mo);
     }
     float* mu_u = mu_out + (((size_t)i * (nd + 1) + nd) * nb + b) * rs + lead;
 #pragma unroll
     for (int q = 0; q < kMaxPerThread; ++q) {
         const int tau = threadIdx.x + 256 * q;
         if (tau < nt) mu_u[tau] = usum[q];
+    }
+    for (int p = 0; p < nd; ++p) {  // the extra rows' share of U (rare)
+        int hits = 0;
+        for (int r = 0; r < n_rcv; ++r) hits += s_ridx[r] == p;
+        if (hits > 2) add_extra_rows(p, n_rcv, s_ridx, g_rev, n, i, nb, b, nt, mu_u);
     }
     if (!e_prev) return;
     // block reduction of the two dot products
@@ -251,7 +287,7 @@ struct AdjLayout {
     size_t rows;  // N * (D + 1) * B
     float* mu[2];
     float* lam;   // (N, 2D, B, T)
-    float* g_rev; // (N, D, B, T)
+    float* g_rev; // (R, N, B, T): the receivers' rows of dL/dE_total, reversed
     int32_t* rev;
     int32_t* delay;
     int64_t* t_off;
@@ -261,7 +297,7 @@ struct AdjLayout {
     int* err;
 };
 
-AdjLayout adj_layout(void* base, int n, int nd, int nb, int nt, long long p) {
+AdjLayout adj_layout(void* base, int n, int nd, int nb, int nt, long long p, int n_rcv) {
     AdjLayout L;
     char* q = (char*)base;
     auto take = [&](size_t bytes) {
@@ -277,7 +313,7 @@ AdjLayout adj_layout(void* base, int n, int nd, int nb, int nt, long long p) {
     const size_t tail = (size_t)kStageF + 64;
     for (int k = 0; k < 2; ++k) L.mu[k] = (float*)take((L.rows * L.rs + tail) * 4);
     L.lam = (float*)take((size_t)n * n_class * nb * nt * 4);
-    L.g_rev = (float*)take((size_t)n * nd * nb * nt * 4);
+    L.g_rev = (float*)take((size_t)(n_rcv > 0 ? n_rcv : 1) * n * nb * nt * 4);
     L.rev = (int32_t*)take((size_t)p * 4);
     L.delay = (int32_t*)take((size_t)p * 4);
     L.t_off = (int64_t*)take(((size_t)n + 1) * 8);
@@ -302,15 +338,17 @@ bool adj_args_ok(const sp_adjoint_args* a) {
            f->n_samples <= 256 * 16 && f->n_dir_pairs >= 0 && 2 * f->n_dir_pairs < (1LL << 31) && f->dst_offset &&
            f->pair_src && f->pair_dst && f->pair_out_dir && f->pair_in_dir && f->pair_distance && f->pair_fprime &&
            f->pair_unit_len && f->wall_of && f->brdf_index && a->mirror_of_in && a->mirror_gain && a->alpha &&
-           a->scattering && a->grad_alpha && a->grad_scattering && a->state;
+           a->scattering && a->grad_alpha && a->grad_scattering && a->state && a->n_receivers >= 0 &&
+           a->n_receivers <= kMaxReceivers && (a->n_receivers == 0 || a->recv_dir);
 }
 
 }  // namespace
 
 extern "C" {
 
-size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs) {
-    return adj_layout(nullptr, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs).bytes;
+size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs,
+                            int n_receivers) {
+    return adj_layout(nullptr, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_receivers).bytes;
 }
 
 int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* stream) {
@@ -320,9 +358,9 @@ int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* 
     const sp_exchange_args* f = a->fwd;
     const int n = f->n_patches, nd = f->n_dirs, nb = f->n_bins, nt = f->n_samples;
     const long long p = f->n_dir_pairs;
-    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, p);
+    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, p, a->n_receivers);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = adj_layout(ws, n, nd, nb, nt, p);
+    L = adj_layout(ws, n, nd, nb, nt, p, a->n_receivers);
     cudaStream_t st = (cudaStream_t)stream;
     sp_adjoint_state* S = a->state;
     S->ready = 0;
@@ -357,17 +395,16 @@ int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* 
         S->n_groups = n_groups;
     }
     // g and mu_K = g
-    const size_t e = (size_t)n * nd * nb * nt;
-    cudaMemsetAsync(L.g_rev, 0, e * 4, st);
     if (a->n_receivers > 0) {
         dim3 gg(nb, n);
-        k_adjoint_g<<<gg, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, a->n_receivers, a->recv_dir, a->recv_factor,
-                                                    a->recv_dist, f->speed_of_sound, f->time_resolution,
-                                                    f->air_attenuation, a->grad_mono, L.g_rev);
+        k_adjoint_g<<<gg, 256, 0, sp_counted(st)>>>(n, nb, nt, a->n_receivers, a->recv_factor, a->recv_dist,
+                                                    f->speed_of_sound, f->time_resolution, f->air_attenuation,
+                                                    a->grad_mono, L.g_rev);
     }
     for (int k = 0; k < 2; ++k) cudaMemsetAsync(L.mu[k], 0, (L.rows * L.rs + kStageF + 64) * 4, st);
     dim3 cg(nb, n);
-    k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (long long)L.rs, L.lead, L.g_rev, nullptr,
+    k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers,
+                                                      a->recv_dir, L.g_rev, nullptr,
                                                       nullptr, 0, L.C.tile_of, nullptr, f->wall_of, f->brdf_index,
                                                       a->alpha, a->scattering, L.mu[0], a->grad_alpha,
                                                       a->grad_scattering);
@@ -380,9 +417,9 @@ int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, siz
     const sp_exchange_args* f = a->fwd;
     const int n = f->n_patches, nd = f->n_dirs, nb = f->n_bins, nt = f->n_samples;
     const long long p = f->n_dir_pairs;
-    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, p);
+    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, p, a->n_receivers);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = adj_layout(ws, n, nd, nb, nt, p);
+    L = adj_layout(ws, n, nd, nb, nt, p, a->n_receivers);
     cudaStream_t st = (cudaStream_t)stream;
     sp_adjoint_state* S = a->state;
     const int words = (2 * nd + 31) / 32;
@@ -397,7 +434,8 @@ int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, siz
     }
     dim3 cg(nb, n);
     k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(
-        n, nd, nb, nt, (long long)L.rs, L.lead, L.g_rev, S->n_active > 0 ? L.lam : nullptr, L.present, words,
+        n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, L.g_rev,
+        S->n_active > 0 ? L.lam : nullptr, L.present, words,
         L.C.tile_of, (const float*)e_prev, f->wall_of, f->brdf_index, a->alpha, a->scattering, mu_out,
         a->grad_alpha, a->grad_scattering);
     S->cur = 1 - S->cur;
@@ -413,9 +451,9 @@ int sp_adjoint_finish(const sp_adjoint_args* a, double* grad_e0dir, void* ws, si
     if (!adj_args_ok(a) || !ws || !grad_e0dir || !a->state->ready || !a->fwd->distance_0) return SP_ERR_ARG;
     const sp_exchange_args* f = a->fwd;
     const int n = f->n_patches, nd = f->n_dirs, nb = f->n_bins, nt = f->n_samples;
-    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, f->n_dir_pairs);
+    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, f->n_dir_pairs, a->n_receivers);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = adj_layout(ws, n, nd, nb, nt, f->n_dir_pairs);
+    L = adj_layout(ws, n, nd, nb, nt, f->n_dir_pairs, a->n_receivers);
     cudaStream_t st = (cudaStream_t)stream;
     const long long ne = (long long)n * nd * nb;
     k_adjoint_e0<<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (long long)L.rs, L.lead,
