@@ -147,9 +147,13 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
  * integration.py:38-114 Stokes, :116-289 Nusselt).  Quadrilateral patches.
  * precision SP_F64: FP64 throughout; SP_F32: Stokes in re-centred FP32 with
  * FP64 for vertex-sharing and near-coincident pairs.  ff (n_pairs) FP64;
- * method (optional, n_pairs): 0 Stokes FP32, 1 Stokes FP64, 2 Nusselt FP64. */
-int sp_form_factors(int precision, long long n_pairs, const int32_t* pairs, const double* pts, const double* normals,
-                    const double* areas, double* ff, uint8_t* method, void* stream);
+ * method (n_pairs): 0 Stokes FP32, 1 Stokes FP64, 2 Nusselt FP64.  pts holds
+ * n_patches patches; SP_F32 with method needs ws (sp_form_factors_workspace
+ * bytes) and synchronises `stream` once; SP_F64 or method == NULL uses no ws. */
+size_t sp_form_factors_workspace(int n_patches, long long n_pairs);
+int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
+                    const double* normals, const double* areas, double* ff, uint8_t* method, void* ws,
+                    size_t ws_bytes, void* stream);
 
 /* Source -> patch energy and directional initial energy.
  * Replaces universal.py:98-147 `_source2patch_energy_universal` and

@@ -91,7 +91,8 @@ _SIGS = {
     "sp_directed_pairs": (I, [I, P, P, P, P, P]),
     "sp_pair_setup": (I, [LL, I, P, P, P, P, P, P, P, I, P, I, P, P, P, P, P, P, P]),
     "sp_outgoing_index_map": (I, [LL, I, P, P, P, ctypes.c_int64, P, P]),
-    "sp_form_factors": (I, [I, LL, P, P, P, P, P, P, P]),
+    "sp_form_factors_workspace": (SZ, [I, LL]),
+    "sp_form_factors": (I, [I, I, LL, P, P, P, P, P, P, P, SZ, P]),
     "sp_dense_form_factors": (I, [LL, I, P, P, P, P]),
     "sp_form_factors_tilde": (I, [LL, I, I, I, I, P, P, P, P, P, P, P, P, P, P, P]),
     "sp_source_energy": (I, [P, I, P, P, P, I, P, P, P, I, P, I, P, P, P, P, P]),

@@ -15,6 +15,7 @@
 //     sum for FP32.  Pairs whose sample points come closer than 0.3 |D| are
 //     recomputed in FP64 inside the same warp.
 #include "common.cuh"
+#include "exchange_common.cuh"
 
 namespace {
 
@@ -431,6 +432,180 @@ __global__ void __launch_bounds__(256) k_form_factors(long long n_pairs, const i
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 Stokes in three passes (the FP64 pipe carries only per-patch sums and
+// one short base term per pair):
+//   k_ff_patch_data: per patch, the 16 boundary points relative to the centre
+//     and their Boole weights (FP32 copies for the phi sum) and the FP64 sums
+//     W[d] = sum w[d], Q[d] = sum |loc|^2 w[d], M[d][e] = sum w[d] loc[e];
+//   k_ff_base: one pair per thread: shared-vertex test (Nusselt pairs are
+//     set aside) and base = 1/2 ln|D|^2 W_i.W_j + lin + quad from the sums;
+//   k_ff_phi: one pair per warp: the FP32 sum of (u_a.v_b) phi(delta_ab);
+//     pairs whose sample points come closer than 0.3 |D| are set aside;
+//   k_ff_rework: set-aside pairs, one warp each, in FP64 (Stokes or Nusselt).
+struct PatchStokes {
+    double c[3];   // centre (vertex mean, geometry.py:412-413)
+    double W[3];
+    double Q[3];
+    double M[9];   // M[3 d + e] = sum_a w_a[d] loc_a[e]
+};
+constexpr int kPatchF = 16 * 8;  // per patch: 16 x (loc.xyz, 0, w.xyz, 0) floats
+
+// Two patches per warp: lanes 0-15 patch 2w, lanes 16-31 patch 2w + 1 (the
+// half-warp reduction order of stokes_pair).
+__global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStokes* __restrict__ out,
+                                float* __restrict__ outf) {
+    const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    const int k = 2 * warp + (lane >> 4);
+    const bool on = k < n;
+    const int a = lane & 15;
+    double el[12];
+    for (int q = 0; q < 12; ++q) el[q] = on ? pts[(size_t)k * 12 + q] : 0.0;
+    double P[3], w[3], c[3];
+    boundary_point5(el, a, P);
+    boole_weight(el, a, w);
+    for (int d = 0; d < 3; ++d) c[d] = (((el[d] + el[3 + d]) + el[6 + d]) + el[9 + d]) / 4;
+    double loc[3] = {P[0] - c[0], P[1] - c[1], P[2] - c[2]};
+    double l2 = loc[0] * loc[0] + loc[1] * loc[1] + loc[2] * loc[2];
+    double mom[15];
+    for (int d = 0; d < 3; ++d) {
+        mom[d] = w[d];
+        mom[3 + d] = l2 * w[d];
+        for (int e = 0; e < 3; ++e) mom[6 + 3 * d + e] = w[d] * loc[e];
+    }
+    for (int q = 0; q < 15; ++q) {
+        double v = mom[q];
+        for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        mom[q] = v;
+    }
+    if (!on) return;
+    float* f = outf + (size_t)k * kPatchF + 8 * a;
+    f[0] = (float)loc[0];
+    f[1] = (float)loc[1];
+    f[2] = (float)loc[2];
+    f[3] = 0.0f;
+    f[4] = (float)w[0];
+    f[5] = (float)w[1];
+    f[6] = (float)w[2];
+    f[7] = 0.0f;
+    if (a == 0) {
+        PatchStokes r;
+        for (int d = 0; d < 3; ++d) {
+            r.c[d] = c[d];
+            r.W[d] = mom[d];
+            r.Q[d] = mom[3 + d];
+        }
+        for (int q = 0; q < 9; ++q) r.M[q] = mom[6 + q];
+        out[k] = r;
+    }
+}
+
+// One pair per thread.  method: kNusselt for shared-vertex pairs (handled in
+// k_ff_rework), else kStokes32 with ff = base (completed by k_ff_phi).
+__global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, const double* __restrict__ pts,
+                          const PatchStokes* __restrict__ pd, double* __restrict__ ff, uint8_t* __restrict__ method,
+                          unsigned long long* __restrict__ n_rework, int64_t* __restrict__ rework) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    const int i = pairs[2 * q], j = pairs[2 * q + 1];
+    double pi[12], pj[12];
+    for (int k = 0; k < 12; ++k) {
+        pi[k] = pts[(size_t)i * 12 + k];
+        pj[k] = pts[(size_t)j * 12 + k];
+    }
+    if (coincident(pj, pi)) {
+        method[q] = kNusselt;
+        rework[atomicAdd(n_rework, 1ull)] = q;
+        return;
+    }
+    const PatchStokes& A = pd[i];
+    const PatchStokes& B = pd[j];
+    const double D[3] = {A.c[0] - B.c[0], A.c[1] - B.c[1], A.c[2] - B.c[2]};
+    const double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    double UV = 0.0, lin = 0.0, pq = 0.0, qq = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        const double dmA = D[0] * A.M[3 * d] + D[1] * A.M[3 * d + 1] + D[2] * A.M[3 * d + 2];
+        const double dmB = D[0] * B.M[3 * d] + D[1] * B.M[3 * d + 1] + D[2] * B.M[3 * d + 2];
+        UV += A.W[d] * B.W[d];
+        lin += dmA * B.W[d] - A.W[d] * dmB;
+        qq += A.Q[d] * B.W[d] + A.W[d] * B.Q[d];
+        for (int e = 0; e < 3; ++e) pq += A.M[3 * d + e] * B.M[3 * d + e];
+    }
+    ff[q] = 0.5 * log(D2) * UV + lin / D2 + 0.5 * (qq - 2.0 * pq) / D2;
+    method[q] = kStokes32;
+}
+
+// One pair per warp: ff = |base + 1/2 sum_ab (u_a.v_b) phi(delta_ab)| / (2 pi A_i).
+__global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t* __restrict__ pairs,
+                                                const PatchStokes* __restrict__ pd, const float* __restrict__ pf,
+                                                const double* __restrict__ areas, double* __restrict__ ff,
+                                                uint8_t* __restrict__ method, unsigned long long* __restrict__ n_rework,
+                                                int64_t* __restrict__ rework) {
+    const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= n_pairs) return;
+    if (method[q] != kStokes32) return;  // the same for the whole warp
+    const int lane = threadIdx.x & 31;
+    const int i = pairs[2 * q], j = pairs[2 * q + 1];
+    const double D[3] = {pd[i].c[0] - pd[j].c[0], pd[i].c[1] - pd[j].c[1], pd[i].c[2] - pd[j].c[2]};
+    const double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    const float Df[3] = {(float)D[0], (float)D[1], (float)D[2]};
+    const float invD2 = (float)(1.0 / D2);
+    const int a = lane & 15, half = lane >> 4;
+    const float4* fi = reinterpret_cast<const float4*>(pf + (size_t)i * kPatchF) + 2 * a;
+    const float4 pa = fi[0], ua = fi[1];
+    const float4* fj = reinterpret_cast<const float4*>(pf + (size_t)j * kPatchF);
+    float acc = 0.0f, min_ratio = 1e30f;
+#pragma unroll
+    for (int bb = 0; bb < 8; ++bb) {
+        const int b = half * 8 + bb;
+        const float4 qb = fj[2 * b], vb = fj[2 * b + 1];
+        const float e[3] = {pa.x - qb.x, pa.y - qb.y, pa.z - qb.z};
+        const float de = Df[0] * e[0] + Df[1] * e[1] + Df[2] * e[2];
+        const float ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+        const float delta = (2.0f * de + ee) * invD2;
+        min_ratio = fminf(min_ratio, 1.0f + delta);
+        const float W = ua.x * vb.x + ua.y * vb.y + ua.z * vb.z;
+        acc = fmaf(W, phi_f(delta), acc);
+    }
+    acc = warp_sum(acc);
+    for (int off = 16; off > 0; off >>= 1) min_ratio = fminf(min_ratio, __shfl_xor_sync(0xffffffffu, min_ratio, off));
+    if (lane != 0) return;
+    if (min_ratio < 0.09f) {  // some r_ab < 0.3 |D|: FP64
+        method[q] = kStokes64;
+        rework[atomicAdd(n_rework, 1ull)] = q;
+        return;
+    }
+    ff[q] = fabs((ff[q] + 0.5 * (double)acc) / (2 * SP_PI * areas[i]));
+}
+
+// Set-aside pairs, one warp each: FP64 Stokes or the Nusselt analogue.
+__global__ void __launch_bounds__(256) k_ff_rework(long long count, const int64_t* __restrict__ rework,
+                                                   const int32_t* __restrict__ pairs, const double* __restrict__ pts,
+                                                   const double* __restrict__ normals, const double* __restrict__ areas,
+                                                   double* __restrict__ ff, const uint8_t* __restrict__ method) {
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= count) return;
+    const int lane = threadIdx.x & 31;
+    const long long q = rework[w];
+    const int i = pairs[2 * q], j = pairs[2 * q + 1];
+    double pi[12], pj[12];
+    for (int k = 0; k < 12; ++k) {
+        pi[k] = pts[(size_t)i * 12 + k];
+        pj[k] = pts[(size_t)j * 12 + k];
+    }
+    double result;
+    if (method[q] == kNusselt) {
+        double ni[3] = {normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]};
+        double nj[3] = {normals[3 * j], normals[3 * j + 1], normals[3 * j + 2]};
+        result = nusselt_pair(pi, pj, ni, nj);
+    } else {
+        bool redo = false;
+        result = stokes_pair(pi, pj, areas[i], false, &redo);
+    }
+    if (lane == 0) ff[q] = result;
+}
+
 // geometry.py:688-715 `_sphere_tangent_vector`.
 __device__ void sphere_tangent(const double* v0, const double* v1, double* out) {
     if (fabs(v0[0] * v1[0] + v0[1] * v1[1] + v0[2] * v1[2]) > 1e-10) {
@@ -559,14 +734,47 @@ int sp_receiver_factors(const double* rcv, int n, const double* centers, const d
     return sp_check_launch();
 }
 
-int sp_form_factors(int precision, long long n_pairs, const int32_t* pairs, const double* pts, const double* normals,
-                    const double* areas, double* ff, uint8_t* method, void* stream) {
-    if (n_pairs < 0 || (precision != SP_F32 && precision != SP_F64)) return SP_ERR_ARG;
+size_t sp_form_factors_workspace(int n_patches, long long n_pairs) {
+    return sp_align((size_t)n_patches * sizeof(PatchStokes)) + sp_align((size_t)n_patches * kPatchF * 4) +
+           sp_align(((size_t)n_pairs + 1) * 8) + 256;
+}
+
+int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
+                    const double* normals, const double* areas, double* ff, uint8_t* method, void* ws,
+                    size_t ws_bytes, void* stream) {
+    if (n_pairs < 0 || n_patches < 0 || (precision != SP_F32 && precision != SP_F64)) return SP_ERR_ARG;
     if (n_pairs == 0) return SP_OK;
     if (!pairs || !pts || !normals || !areas || !ff) return SP_ERR_ARG;
-    long long threads = n_pairs * 32;
-    k_form_factors<<<sp_blocks(threads, 256), 256, 0, sp_counted((cudaStream_t)stream)>>>(n_pairs, pairs, pts, normals, areas,
-                                                                              precision == SP_F32 ? 1 : 0, ff, method);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == SP_F64 || !method) {
+        long long threads = n_pairs * 32;
+        k_form_factors<<<sp_blocks(threads, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, pts, normals, areas,
+                                                                           precision == SP_F32 ? 1 : 0, ff, method);
+        return sp_check_launch();
+    }
+    if (!ws || ws_bytes < sp_form_factors_workspace(n_patches, n_pairs)) return SP_ERR_WORKSPACE;
+    char* q = (char*)ws;
+    PatchStokes* pd = (PatchStokes*)q;
+    q += sp_align((size_t)n_patches * sizeof(PatchStokes));
+    float* pf = (float*)q;
+    q += sp_align((size_t)n_patches * kPatchF * 4);
+    int64_t* rework = (int64_t*)q;
+    q += sp_align(((size_t)n_pairs + 1) * 8);
+    unsigned long long* n_rework = (unsigned long long*)q;
+    cudaMemsetAsync(n_rework, 0, sizeof(unsigned long long), st);
+    const long long warps = ((long long)n_patches + 1) / 2;
+    k_ff_patch_data<<<sp_blocks(warps * 32, 256), 256, 0, sp_counted(st)>>>(n_patches, pts, pd, pf);
+    k_ff_base<<<sp_blocks(n_pairs, 128), 128, 0, sp_counted(st)>>>(n_pairs, pairs, pts, pd, ff, method, n_rework,
+                                                                  rework);
+    k_ff_phi<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, pd, pf, areas, ff, method,
+                                                                      n_rework, rework);
+    unsigned long long count = 0;
+    cudaMemcpyAsync(&count, n_rework, sizeof(count), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+    if (count > (unsigned long long)n_pairs) return SP_ERR_CUDA;
+    if (count > 0)
+        k_ff_rework<<<sp_blocks((long long)count * 32, 256), 256, 0, sp_counted(st)>>>(
+            (long long)count, rework, pairs, pts, normals, areas, ff, method);
     return sp_check_launch();
 }
 

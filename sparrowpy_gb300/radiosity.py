@@ -401,8 +401,11 @@ class DirectionalRadiosityFast:
         # form factors (universal.py:12-52)
         ff = torch.zeros((max(n_vis, 1),), dtype=torch.float64, device=dev)
         method = torch.zeros((max(n_vis, 1),), dtype=torch.uint8, device=dev)
-        nat.call("sp_form_factors", _PREC[self.precision], n_vis, _ptr(pairs), _ptr(d["pts"]), _ptr(d["normals"]),
-                 _ptr(d["areas"]), _ptr(ff), _ptr(method), st)
+        fsz = nat.size("sp_form_factors_workspace", n, n_vis)
+        fws = torch.empty((max(fsz, 1),), dtype=torch.uint8, device=dev)
+        nat.call("sp_form_factors", _PREC[self.precision], n, n_vis, _ptr(pairs), _ptr(d["pts"]), _ptr(d["normals"]),
+                 _ptr(d["areas"]), _ptr(ff), _ptr(method), _ptr(fws), fsz, st)
+        del fws
         # directed pairs, destination-major (RadiosityFast.py:1124-1131)
         sym = torch.empty((n, n), dtype=torch.uint8, device=dev)
         dcounts = torch.empty((max(n, 1),), dtype=torch.int32, device=dev)
