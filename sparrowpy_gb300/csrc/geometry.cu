@@ -9,8 +9,10 @@
 // blocker whose (slightly enlarged) bounding box the segment misses can only
 // return "visible" in the reference predicate (see exact_visibility below).
 #include <atomic>
+#include <vector>
 
 #include "common.cuh"
+#include "exchange_common.cuh"
 
 namespace {
 
@@ -258,6 +260,154 @@ __global__ void __launch_bounds__(256) k_patch_visibility(int n, int nv, const d
     if (i < n && j < n) vis[(size_t)i * n + j] = (active && visible) ? 1 : 0;
 }
 
+// Patch visibility in steps that keep the FP64 predicate on full warps:
+// k_vis_self (the pair's own patches as blockers), then k_vis_cull (one
+// 16 x 16 pair tile per block, one pair per thread) writes, after the FP32
+// box culling, the (pair, blocker) candidates to a buffer, each block reserving a slice
+// with one atomic; k_vis_exact evaluates one candidate per thread and clears
+// the pair when the blocker hides it (visibility is the AND over blockers,
+// so the order of evaluation does not change the result).  A block whose
+// slice does not fit records its tile and is culled again in a later round.
+constexpr int kCandBits = 20;  // i, j, s < 2^20
+// Box hits of one segment against blocker groups g0 .. g0 + cnt - 1, the
+// pair's own patches excluded (one compiled copy, so the counting and the
+// writing pass agree); writes at most `limit` candidates when `out` is given.
+__device__ __noinline__ int vis_cull_pair(bool active, const float* a, const float* d, const float* gb, int g0,
+                                          int cnt, int n, const float* __restrict__ box, int64_t code, int64_t* out,
+                                          int limit, int self_i, int self_j) {
+    int hits = 0;
+    if (!active) return 0;
+    for (int g = 0; g < cnt; ++g) {
+        if (!seg_hits_box(a, d, gb + 6 * g, gb + 6 * g + 3)) continue;
+        const int s_end = min(n, (g0 + g + 1) * kGroup);
+        for (int s = (g0 + g) * kGroup; s < s_end; ++s) {
+            const float* bx = box + 6 * s;
+            float lo[3] = {bx[0], bx[1], bx[2]}, hi[3] = {bx[3], bx[4], bx[5]};
+            if (s == self_i || s == self_j || !seg_hits_box(a, d, lo, hi)) continue;
+            if (out) {
+                if (hits >= limit) return hits;
+                out[hits] = code | s;
+            }
+            ++hits;
+        }
+    }
+    return hits;
+}
+
+// The pair's own patches as blockers first (every thread the same two exact
+// tests): they hide every coplanar pair, whose segments would otherwise
+// cross the boxes of all patches between them.  Writes the base value.
+__global__ void __launch_bounds__(256) k_vis_self(int n, int nv, const int32_t* __restrict__ tiles,
+                                                  const double* __restrict__ centers,
+                                                  const double* __restrict__ normals, const double* __restrict__ pts,
+                                                  uint8_t* __restrict__ vis) {
+    const int tile = tiles[blockIdx.x];
+    const int tile_i = tile >> 16, tile_j = tile & 0xffff;
+    const int i = tile_i * 16 + (threadIdx.x >> 4);
+    const int j = tile_j * 16 + (threadIdx.x & 15);
+    if (i >= n || j >= n) return;
+    bool visible = i < j;
+    if (visible) {
+        double ci[3], cj[3];
+        for (int q = 0; q < 3; ++q) {
+            ci[q] = centers[3 * i + q];
+            cj[q] = centers[3 * j + q];
+        }
+        for (int k = 0; k < 2 && visible; ++k) {
+            const int s = k == 0 ? i : j;
+            double nn[3], sp[kMaxVerts * 3];
+            for (int q = 0; q < 3; ++q) nn[q] = normals[3 * s + q];
+            for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)s * nv * 3 + q];
+            visible = exact_visibility(ci, cj, sp, nv, nn);
+        }
+    }
+    vis[(size_t)i * n + j] = visible ? 1 : 0;
+}
+
+__global__ void __launch_bounds__(256) k_vis_cull(int n, const int32_t* __restrict__ tiles,
+                                                  const double* __restrict__ centers, const float* __restrict__ box,
+                                                  const float* __restrict__ gbox, int n_groups,
+                                                  uint8_t* __restrict__ vis, int64_t* __restrict__ cand,
+                                                  long long cap, unsigned long long* __restrict__ counter,
+                                                  int32_t* __restrict__ overflow, int* __restrict__ n_overflow) {
+    extern __shared__ float s_gbox[];
+    __shared__ int s_scan[256];
+    __shared__ long long s_base;
+    const int tile = tiles[blockIdx.x];
+    const int tile_i = tile >> 16, tile_j = tile & 0xffff;
+    const int i = tile_i * 16 + (threadIdx.x >> 4);
+    const int j = tile_j * 16 + (threadIdx.x & 15);
+    // pairs the own-patch pass (k_vis_self) already hid need no candidates
+    const bool active = (i < n) && (j < n) && (i < j) && vis[(size_t)i * n + j] != 0;
+    float a[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+    if (active)
+        for (int k = 0; k < 3; ++k) {
+            a[k] = (float)centers[3 * i + k];
+            d[k] = (float)centers[3 * j + k] - a[k];
+        }
+    const int64_t code = ((int64_t)i << (2 * kCandBits)) | ((int64_t)j << kCandBits);
+    // pass 1: count
+    int hits = 0;
+    for (int g0 = 0; g0 < n_groups; g0 += 1024) {
+        const int cnt = min(1024, n_groups - g0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt * 6; t += blockDim.x) s_gbox[t] = gbox[6 * g0 + t];
+        __syncthreads();
+        hits += vis_cull_pair(active, a, d, s_gbox, g0, cnt, n, box, code, nullptr, 0, i, j);
+    }
+    // block prefix sum and one reservation
+    s_scan[threadIdx.x] = hits;
+    __syncthreads();
+    for (int off = 1; off < 256; off <<= 1) {
+        const int x = threadIdx.x >= (unsigned)off ? s_scan[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 255) {
+        const long long total = s_scan[255];
+        long long base = total > 0 ? (long long)atomicAdd(counter, (unsigned long long)total) : 0;
+        if (base + total > cap) {
+            overflow[atomicAdd(n_overflow, 1)] = tile;
+            base = -1;
+        }
+        s_base = base;
+    }
+    __syncthreads();
+    const long long base = s_base;
+    if (base < 0 || hits == 0) return;  // no further barriers below
+    int64_t* out = cand + base + (s_scan[threadIdx.x] - hits);
+    // pass 2: write (the group boxes are read from global memory here)
+    int left = hits;
+    for (int g0 = 0; g0 < n_groups && left > 0; g0 += 1024) {
+        const int cnt = min(1024, n_groups - g0);
+        const int w = min(left, vis_cull_pair(active, a, d, gbox + 6 * g0, g0, cnt, n, box, code, out, left, i, j));
+        out += w;
+        left -= w;
+    }
+}
+
+__global__ void k_vis_exact(long long count, const int64_t* __restrict__ cand, int n, int nv,
+                            const double* __restrict__ centers, const double* __restrict__ normals,
+                            const double* __restrict__ pts, uint8_t* __restrict__ vis) {
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int64_t c = cand[k];
+    if (c < 0) return;  // slot of a block that did not fit
+    const int mask = (1 << kCandBits) - 1;
+    const int i = (int)(c >> (2 * kCandBits)), j = (int)((c >> kCandBits) & mask), s = (int)(c & mask);
+    uint8_t* v = vis + (size_t)i * n + j;
+    if (*v == 0) return;  // already hidden by another blocker
+    double ci[3], cj[3], nn[3], sp[kMaxVerts * 3];
+    for (int q = 0; q < 3; ++q) {
+        ci[q] = centers[3 * i + q];
+        cj[q] = centers[3 * j + q];
+        nn[q] = normals[3 * s + q];
+    }
+    for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)s * nv * 3 + q];
+    if (!exact_visibility(ci, cj, sp, nv, nn)) *v = 0;
+}
+
 // geometry.py:799-839 `_check_point2patch_visibility`: point -> each patch
 // centre, blockers are the given surfaces (walls), tested in index order.
 __global__ void k_point_visibility(const double* __restrict__ point, int n, const double* __restrict__ centers,
@@ -496,27 +646,79 @@ int sp_patch_geometry(int n, int nv, const double* pts, double* centers, double*
     return sp_check_launch();
 }
 
+// Workspace: blocker boxes, group boxes, the candidate buffer (at least 256 n
+// entries, so one tile always fits an empty buffer), two tile lists, counters.
+inline long long vis_cand_capacity(int n) {
+    const long long pairs = (long long)n * (n - 1) / 2;
+    long long cap = pairs * 4;
+    if (cap < 256LL * n) cap = 256LL * n;
+    if (cap > (128LL << 20)) cap = (128LL << 20) > 256LL * n ? (128LL << 20) : 256LL * n;
+    return cap;
+}
+inline long long vis_tile_count(int n) {
+    const long long t = (n + 15) / 16;
+    return t * (t + 1) / 2;
+}
+
 size_t sp_patch_visibility_workspace(int n) {
+    if (n <= 0) return 256;
     size_t groups = ((size_t)n + kGroup - 1) / kGroup;
-    return (size_t)n * 6 * sizeof(float) + groups * 6 * sizeof(float) + 256;
+    return sp_align((size_t)n * 6 * sizeof(float) + groups * 6 * sizeof(float)) +
+           sp_align((size_t)vis_cand_capacity(n) * 8) + 2 * sp_align((size_t)vis_tile_count(n) * 4) + 256;
 }
 
 int sp_patch_visibility(int n, int nv, const double* centers, const double* normals, const double* pts,
                         uint8_t* vis, void* ws, size_t ws_bytes, void* stream) {
-    if (n < 0 || nv < 3 || nv > kMaxVerts) return SP_ERR_ARG;
+    if (n < 0 || nv < 3 || nv > kMaxVerts || n >= (1 << kCandBits)) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
     if (!centers || !normals || !pts || !vis || !ws) return SP_ERR_ARG;
     if (ws_bytes < sp_patch_visibility_workspace(n)) return SP_ERR_WORKSPACE;
     cudaStream_t st = (cudaStream_t)stream;
-    int n_groups = (n + kGroup - 1) / kGroup;
-    float* box = (float*)ws;
+    const int n_groups = (n + kGroup - 1) / kGroup;
+    const long long cap = vis_cand_capacity(n);
+    const long long n_tiles = vis_tile_count(n);
+    char* q = (char*)ws;
+    float* box = (float*)q;
     float* gbox = box + (size_t)n * 6;
+    q += sp_align((size_t)n * 6 * sizeof(float) + (size_t)n_groups * 6 * sizeof(float));
+    int64_t* cand = (int64_t*)q;
+    q += sp_align((size_t)cap * 8);
+    int32_t* list[2];
+    list[0] = (int32_t*)q;
+    q += sp_align((size_t)n_tiles * 4);
+    list[1] = (int32_t*)q;
+    q += sp_align((size_t)n_tiles * 4);
+    unsigned long long* counter = (unsigned long long*)q;
+    int* n_overflow = (int*)(q + 8);
     k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n, nv, pts, 1e-3f, box, gbox);
-    cudaMemsetAsync(vis, 0, (size_t)n * n, st);
-    int tiles = (n + 15) / 16;
-    dim3 grid(tiles, tiles);
-    k_patch_visibility<<<grid, 256, 1024 * 6 * sizeof(float), sp_counted(st)>>>(n, nv, centers, normals, pts, box, gbox,
-                                                                     n_groups, vis);
+    cudaMemsetAsync(vis, 0, (size_t)n * n, st);  // tiles below the diagonal are never visited
+    // upper-triangle tiles (tile_j >= tile_i)
+    const int nt = (n + 15) / 16;
+    std::vector<int32_t> h_tiles;
+    h_tiles.reserve((size_t)n_tiles);
+    for (int ti = 0; ti < nt; ++ti)
+        for (int tj = ti; tj < nt; ++tj) h_tiles.push_back((ti << 16) | tj);
+    cudaMemcpyAsync(list[0], h_tiles.data(), h_tiles.size() * 4, cudaMemcpyHostToDevice, st);
+    long long todo = (long long)h_tiles.size();
+    k_vis_self<<<(unsigned)todo, 256, 0, sp_counted(st)>>>(n, nv, list[0], centers, normals, pts, vis);
+    int cur = 0;
+    for (int round = 0; todo > 0; ++round) {
+        cudaMemsetAsync(counter, 0, 16, st);
+        cudaMemsetAsync(cand, 0xff, (size_t)cap * 8, st);
+        k_vis_cull<<<(unsigned)todo, 256, 1024 * 6 * sizeof(float), sp_counted(st)>>>(
+            n, list[cur], centers, box, gbox, n_groups, vis, cand, cap, counter, list[1 - cur], n_overflow);
+        unsigned long long h[2] = {0, 0};
+        cudaMemcpyAsync(h, counter, 16, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+        const long long used = (long long)h[0] < cap ? (long long)h[0] : cap;
+        const int overflowed = (int)(h[1] & 0xffffffffull);
+        if (used > 0)
+            k_vis_exact<<<sp_blocks(used, 256), 256, 0, sp_counted(st)>>>(used, cand, n, nv, centers, normals, pts,
+                                                                         vis);
+        if (overflowed >= todo) return SP_ERR_CUDA;  // no progress: cannot happen with cap >= 256 n
+        todo = overflowed;
+        cur = 1 - cur;
+    }
     return sp_check_launch();
 }
 
