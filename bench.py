@@ -42,7 +42,7 @@ METRIC = "ms/solve (bake+exchange) ~5.5k patches FP32 vs FP64 GPU; fwd+bwd ms; H
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 # DRAM bytes moved per algorithmic byte by one exchange order (scatter + mix),
 # from the ncu capture summarised in profiles/exchange_street_canyon_small.md
-TRAFFIC_PER_ALGO_BYTE = 1.27
+TRAFFIC_PER_ALGO_BYTE = 1.31
 
 
 def parse():
@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fwd-bwd", action="store_true", help="skip the gradient (forward + backward) leg")
+    ap.add_argument("--batch-rooms", type=int, default=8, help="seeded shoebox rooms for the batch leg (0: skip)")
     ap.add_argument("--fwd-bwd-only", action="store_true",
                     help="print only the gradient leg (shoebox, 2016 patches) as one JSON line")
     return ap.parse_args()
@@ -352,9 +353,8 @@ def run_gpu(args):
         c64 = scenes.config(args.config, precision="fp64")
         c64["max_order"] = cfg["max_order"]
         r64 = c64["radiosity"]
-        solve(r64, c64, as_coords)  # warm-up
-        t64 = []
-        for _ in range(2):
+        t64 = []  # one timed FP64 solve (about a minute; its first-use allocations are small against that)
+        for _ in range(1):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)
             solve(r64, c64, as_coords)
@@ -372,12 +372,20 @@ def run_gpu(args):
 
     fwd_bwd = None
     if not args.no_fwd_bwd and rank == 0:
-        r._dev.pop("ws", None)
+        r._dev.clear()  # the street canyon's device state; its host inputs stay for the CPU leg
+        r._bake = None
         torch.cuda.empty_cache()
         try:
             fwd_bwd = fwd_bwd_config4()
         except Exception as exc:  # the gradient leg must not hide the solve result
             fwd_bwd = {"error": f"{type(exc).__name__}: {exc}"}
+
+    batch = None
+    if args.batch_rooms > 0 and rank == 0:
+        try:
+            batch = batch_rooms(args.batch_rooms)
+        except Exception as exc:  # the batch leg must not hide the solve result
+            batch = {"error": f"{type(exc).__name__}: {exc}"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -403,6 +411,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
             "fwd_bwd": fwd_bwd,
+            "batch": batch,
             "clocks": clk,
             "gpu_launches": int(launches),
             "exchange": {"algorithm": stats["algorithm"], "directed_pairs": n_pairs,
@@ -475,6 +484,20 @@ def fwd_bwd_config4(steps=2, fd_params=2, seed=4):
     del solver, r, target
     torch.cuda.empty_cache()
     return out
+
+
+# ------------------------------------------------------------------- batch
+def batch_rooms(n_rooms, seed=5):
+    """Seeded shoebox rooms, dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, 1 s, order 30,
+    1 source + 4 receivers each, solved one after another; device time per room."""
+    from sparrowpy_gb300.batch import shoebox_rooms, solve_rooms
+    rooms = shoebox_rooms(n_rooms, seed=seed)
+    _, ms, patches = solve_rooms(rooms)
+    return {"workload": f"{n_rooms} seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, "
+                        "T=1000, order 30, 4 receivers), one after another",
+            "rooms": n_rooms, "patches_min": int(min(patches)), "patches_mean": float(np.mean(patches)),
+            "patches_max": int(max(patches)), "total_ms": float(np.sum(ms)),
+            "rooms_per_s": float(n_rooms / (np.sum(ms) * 1e-3)), "ms_per_room": [float(x) for x in ms]}
 
 
 # ----------------------------------------------------------- reference arm
