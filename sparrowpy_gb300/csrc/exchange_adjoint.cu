@@ -429,7 +429,7 @@ int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, siz
         cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
         dim3 sgrid(S->n_active, (nt + kTW - 1) / kTW, nb);
         k_scatter_f32<<<sgrid, kWsThreads, kScatterSmem, sp_counted(st)>>>(
-            2 * nd, nb, nt, (long long)L.rs, L.lead, 2 * p, L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups,
+            2 * nd, nb, nt, (long long)L.rs, L.lead, 2 * p, L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups, L.C.wpack,
             (const float*)L.C.coef, mu_in, L.lam, L.err);
     }
     dim3 cg(nb, n);

@@ -29,6 +29,14 @@ struct Group {
 };
 static_assert(sizeof(Group) == 32, "Group is copied in 16-byte units");
 
+// What consumer warp w of the FP32 scatter needs of a group, in one word:
+// offsets of slots 2w and 2w + 1 (6 bits each), their membership (2 bits),
+// the window alignment mu (2 bits) and the base delay (16 bits).
+constexpr int kPackWarps = kTile / 2;
+__host__ __device__ inline uint32_t warp_pack(int off0, int off1, unsigned bits, int mu, int n_base) {
+    return (uint32_t)off0 | ((uint32_t)off1 << 6) | (bits << 12) | ((uint32_t)mu << 14) | ((uint32_t)n_base << 16);
+}
+
 // ------------------------------------------------------------------ plan
 __global__ void k_delays_t(long long n_dir, const double* __restrict__ dist, double c, double dt,
                            int32_t* __restrict__ delay) {
@@ -197,7 +205,8 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
                         const int32_t* __restrict__ delay, const int32_t* __restrict__ cls,
                         const int32_t* __restrict__ tile_of, const int32_t* __restrict__ slot_of, Coef pair_coef,
                         int write, int64_t* __restrict__ cell_count, const int64_t* __restrict__ cell_base,
-                        long long cap, Group* __restrict__ groups, T* __restrict__ coef) {
+                        long long cap, Group* __restrict__ groups, T* __restrict__ coef,
+                        uint32_t* __restrict__ wpack) {
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_dir) return;
     long long e = merged[q];
@@ -264,6 +273,10 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
                 for (int b = 0; b < nb; ++b) coef[((size_t)b * cap + g_out) * kTile + w] = (T)pair_coef(ex, b);
             }
             groups[g_out] = g;
+            const int mu = (-g.n_base - kMaxSpan) & 3;
+            for (int w = 0; w < kPackWarps; ++w)
+                wpack[(size_t)g_out * kPackWarps + w] =
+                    warp_pack(g.off[2 * w], g.off[2 * w + 1], (g.mask >> (2 * w)) & 3u, mu, g.n_base);
             ++g_out;
         }
         ++n_groups;
@@ -367,7 +380,8 @@ struct PlanCore {
     int64_t* cell_base;
     int64_t* scan_tmp;
     Group* groups;
-    void* coef;  // [nb][cap][kTile]
+    uint32_t* wpack;  // [cap][kPackWarps]
+    void* coef;       // [nb][cap][kTile]
 };
 
 // Carve PlanCore arrays from q (advanced); esz = coefficient element size.
@@ -392,6 +406,7 @@ PlanCore plan_core_layout(Take& take, int esz, int n, int nb, long long p, int n
     long long big = p > n_seg ? p : n_seg;
     C.scan_tmp = (int64_t*)take(((size_t)(big / kScanBlock) + 2) * 8);
     C.groups = (Group*)take((size_t)(p + 1) * sizeof(Group));
+    C.wpack = (uint32_t*)take((size_t)(p + 1) * kPackWarps * 4);
     C.coef = take((size_t)(p + 1) * nb * kTile * esz);
     return C;
 }
@@ -419,11 +434,11 @@ int build_groups(int n, int nb, int nt, const PairSet& ps, const int32_t* order,
                                                                      C.seg_base, C.merged);
     k_cells<T, Coef><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
         p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of, coef, 0,
-        C.cell_count, nullptr, p, nullptr, nullptr);
+        C.cell_count, nullptr, p, nullptr, nullptr, nullptr);
     scan64(p, C.cell_count, C.cell_base, C.scan_tmp, st);
     k_cells<T, Coef><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
         p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of, coef, 1,
-        nullptr, C.cell_base, p, C.groups, (T*)C.coef);
+        nullptr, C.cell_base, p, C.groups, (T*)C.coef, C.wpack);
     k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, sp_counted(st)>>>(n_seg, p, C.seg_base, C.cell_base,
                                                                          C.seg_off);
     // scatter blocks visit the non-empty segments longest first, so the

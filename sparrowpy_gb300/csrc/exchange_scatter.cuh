@@ -50,8 +50,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // --------------------------------------------------------- FP32 scatter
 // Warp-specialised pipeline.  One producer warp streams the groups of a
 // segment through kStages shared-memory stages of kGps groups each, with
-// bulk copies (per group the source window; per stage the kGps 32-byte group
-// records and their 16 coefficients of this band).  kConsumers consumer
+// bulk copies (per group the source window; per stage the groups' packed
+// per-warp words and their 16 coefficients of this band).  kConsumers consumer
 // warps, warp w owning receiver slots 2w and 2w + 1 of the tile, accumulate
 // those slots' 1024-bin windows in registers (lane l owns bins t0 + l + 32 r).
 // Stage hand-off: `full` (producer arrival + transaction bytes) and `empty`
@@ -66,11 +66,12 @@ constexpr int kStageF = kTW + kMaxSpan + 3;          // staged floats per group 
 static_assert(kStageF % 4 == 0, "staged window must be a whole number of 16-byte chunks");
 constexpr int kGps = 4;                              // groups per stage
 constexpr int kWinBytes = kStageF * 4;
-constexpr int kHdrOff = kGps * kWinBytes;            // kGps group records
-constexpr int kCoefOff = kHdrOff + kGps * (int)sizeof(Group);  // kGps x 16 coefficients
+constexpr int kPackOff = kGps * kWinBytes;           // kGps x kPackWarps packed words
+constexpr int kCoefOff = kPackOff + kGps * kPackWarps * 4;  // kGps x 16 coefficients
 constexpr int kStageBytes = kCoefOff + kGps * kTile * 4;
-static_assert(kWinBytes % 16 == 0 && kHdrOff % 16 == 0 && kCoefOff % 16 == 0 && kStageBytes % 16 == 0,
+static_assert(kWinBytes % 16 == 0 && kPackOff % 16 == 0 && kCoefOff % 16 == 0 && kStageBytes % 16 == 0,
               "stage parts must stay 16-byte aligned");
+static_assert(kPackWarps == kConsumers, "one packed word per consumer warp");
 constexpr int kStages = 6;
 constexpr int kBarBytes = 128;                       // full[kStages], empty[kStages]
 static_assert(2 * kStages * 8 <= kBarBytes, "barrier area too small");
@@ -97,6 +98,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                                                                const int32_t* __restrict__ seg_order,
                                                                const int64_t* __restrict__ seg_off,
                                                                const Group* __restrict__ groups,
+                                                               const uint32_t* __restrict__ wpack,
                                                                const float* __restrict__ coef,
                                                                const float* __restrict__ eprev,
                                                                float* __restrict__ gout, int* __restrict__ err) {
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                         halt = 1;
                     } else {
                         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                        mbar_expect_tx(&full[st], (unsigned)(ng * (kWinBytes + (int)sizeof(Group) + kTile * 4)));
+                        mbar_expect_tx(&full[st], (unsigned)(ng * (kWinBytes + kPackWarps * 4 + kTile * 4)));
                     }
                 }
                 halt = __shfl_sync(0xffffffffu, halt, 0);
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                 if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * kWinBytes, eprev + a0, kWinBytes, &full[st]);
                 if (lane == 0) {
                     const long long g0 = g_beg + base + k0;
-                    bulk_copy_g2s(sp + kHdrOff, groups + g0, (unsigned)(ng * sizeof(Group)), &full[st]);
+                    bulk_copy_g2s(sp + kPackOff, wpack + g0 * kPackWarps, (unsigned)(ng * kPackWarps * 4), &full[st]);
                     bulk_copy_g2s(sp + kCoefOff, coef + ((size_t)b * cap + g0) * kTile, (unsigned)(ng * kTile * 4),
                                   &full[st]);
                     s_issued = si + 1;
@@ -196,26 +198,23 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
             }
             const unsigned char* sp = stages + (size_t)st * kStageBytes;
             const int ng = min(kGps, n_grp - si * kGps);
-            // the stage's records first (independent loads), then the windows
-            unsigned bits[kGps];
-            int base_off[kGps];  // kMaxSpan + mu, per group
+            const uint32_t* packs = reinterpret_cast<const uint32_t*>(sp + kPackOff) + warp;
+            const float* coefs = reinterpret_cast<const float*>(sp + kCoefOff) + sh;
+            // the stage's words first (independent loads), then the windows
+            uint32_t pk[kGps];
             float2 cf[kGps];
-            unsigned offs[kGps];  // off of slot sh (low byte) and sh + 1 (second byte)
 #pragma unroll
             for (int q = 0; q < kGps; ++q) {
-                const Group* g = reinterpret_cast<const Group*>(sp + kHdrOff) + q;
-                // record at a 16-byte boundary: srcrow, n_base, mask, pad
-                const int4 hdr = q < ng ? *reinterpret_cast<const int4*>(g) : make_int4(0, 0, 0, 0);
-                bits[q] = ((unsigned)hdr.z >> sh) & 3u;
-                base_off[q] = kMaxSpan + ((-hdr.y - kMaxSpan) & 3);  // staged start was rounded down by mu floats
-                cf[q] = *reinterpret_cast<const float2*>(reinterpret_cast<const float*>(sp + kCoefOff) + q * kTile + sh);
-                offs[q] = *reinterpret_cast<const uint16_t*>(&g->off[sh]);
+                pk[q] = q < ng ? packs[q * kPackWarps] : 0u;  // 0: no member of this warp
+                cf[q] = *reinterpret_cast<const float2*>(coefs + q * kTile);
             }
 #pragma unroll
             for (int q = 0; q < kGps; ++q) {
+                const unsigned bits = (pk[q] >> 12) & 3u;
+                const int base_off = kMaxSpan + (int)((pk[q] >> 14) & 3u);
                 const float* win = reinterpret_cast<const float*>(sp + q * kWinBytes);
-                if (bits[q] & 1u) slot_window(acc0, win, cf[q].x, (int)(offs[q] & 0xffu), base_off[q], lane);
-                if (bits[q] & 2u) slot_window(acc1, win, cf[q].y, (int)(offs[q] >> 8), base_off[q], lane);
+                if (bits & 1u) slot_window(acc0, win, cf[q].x, (int)(pk[q] & 63u), base_off, lane);
+                if (bits & 2u) slot_window(acc1, win, cf[q].y, (int)((pk[q] >> 6) & 63u), base_off, lane);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[st]);

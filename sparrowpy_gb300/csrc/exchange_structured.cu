@@ -369,6 +369,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     if (n_class > kMaxClasses) return SP_ERR_UNSUPPORTED;
     const int k0 = a->state_in ? a->state_order : 0;
     if (k0 < 0 || (a->states_out && a->states_every < 1)) return SP_ERR_ARG;
+    if (nt > 65535) return SP_ERR_UNSUPPORTED;  // base delays are packed in 16 bits
     Plan L = plan_layout(nullptr, sizeof(T), n, nd, nb, nt, p, n_class, material);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
     L = plan_layout(ws, sizeof(T), n, nd, nb, nt, p, n_class, material);
@@ -473,7 +474,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
             dim3 sgrid(n_active, (nt + kTW - 1) / kTW, nb);
             if (n_active > 0)
                 k_scatter_f32<<<sgrid, kWsThreads, kScatterSmem, sp_counted(st)>>>(
-                    n_class, nb, nt, rs, lead, pp, L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups,
+                    n_class, nb, nt, rs, lead, pp, L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups, L.C.wpack,
                     (const float*)L.C.coef, (const float*)eprev, (float*)L.g, L.err);
         } else {
             dim3 sgrid(n_active, (nt + kTW64 - 1) / kTW64, nb);
