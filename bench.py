@@ -316,19 +316,22 @@ def run_gpu(args):
 
     # end to end through the public API from host arrays: upload of the
     # scene and materials, bake, source, exchange, receiver histograms back
+    # (one untimed step first: a fresh object's first allocations come from
+    # cudaMalloc; later objects reuse the allocator's cache, as a user's
+    # repeated solves do; every timed step still uploads all inputs)
     e2e_times, h2d, d2h = [], 0, 0
-    for _ in range(args.e2e_steps):
+    for k in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         r2 = host_template.clone()
         barrier()
         t0 = time.perf_counter()
         solve(r2, cfg, as_coords)
         mono = r2.collect_energy_receiver_mono(as_coords(cfg["receivers"])).time
         torch.cuda.synchronize()
-        e2e_times.append((time.perf_counter() - t0) * 1e3)
+        if k > 0:
+            e2e_times.append((time.perf_counter() - t0) * 1e3)
         h2d = int(r2.host_bytes_uploaded)
         d2h = int(mono.nbytes)
         del r2, mono
-        torch.cuda.empty_cache()
     e2e_ms = float(np.mean(e2e_times)) if e2e_times else None
     if world > 1 and e2e_ms is not None:
         t = torch.tensor([e2e_ms], device="cuda")
