@@ -36,6 +36,7 @@ from . import geometry as geo
 from .coords import Coordinates, FrequencyData, TimeData, _cart, is_coordinates
 
 _PREC = {"fp32": nat.SP_F32, "fp64": nat.SP_F64}
+STRUCTURED_MAX_SAMPLES = 65535  # time bins the structured exchange kernels address (16-bit base delays)
 
 
 def _ptr(t):
@@ -544,6 +545,29 @@ class DirectionalRadiosityFast:
         self._speed_of_sound = float(speed_of_sound)
         self._etc_duration = float(etc_duration)
 
+    def _init_only_args(self, c, dt, n_samples, etc):
+        """Arguments of an exchange of order < 1: E_total is the source energy at its delays
+        (RadiosityFast.py:550-556, _energy_exchange_init_energy :1037-1070).  It reads no pair
+        data, so it needs no bake_geometry(), as in the reference."""
+        d = self._geometry()
+        bs = self._brdf_device()
+        e0dir, d0 = self._dev["e0dir"], self._dev["d0"]
+        n, nd, nb = e0dir.shape
+        a = nat.ExchangeArgs()
+        a.precision = _PREC[self.precision]
+        a.algorithm = nat.SP_EXCHANGE_DENSE
+        a.n_patches, a.n_dirs, a.n_bins, a.n_samples, a.max_order = n, nd, nb, n_samples, 0
+        a.energy_0_dir = e0dir.data_ptr()
+        a.distance_0 = d0.data_ptr()
+        a.n_dir_pairs = 0
+        a.wall_of = d["wall_of"].data_ptr()
+        a.brdf_index = bs["brdf_index"].data_ptr()
+        a.n_slots, a.n_in_dirs = bs["n_slots"], bs["n_in"]
+        a.brdf = bs["brdf"].data_ptr()
+        a.speed_of_sound, a.time_resolution = c, dt
+        a.etc_total = etc.data_ptr()
+        return a
+
     def _exchange_args(self, c, dt, n_samples, max_order, algorithm, etc):
         bk = self._bake
         plan = self._exchange_plan()
@@ -552,9 +576,13 @@ class DirectionalRadiosityFast:
         n, nd, nb = e0dir.shape
         if nd != plan["n_out"] or nb != bk["n_bins"]:
             raise ValueError("the BRDF directions/bands changed after bake_geometry(); bake again")
-        use_struct = "structured" in plan and algorithm in ("auto", "structured")
+        # the structured kernels pack base delays in 16 bits; longer histograms take the dense kernel
+        fits = n_samples <= STRUCTURED_MAX_SAMPLES
+        use_struct = "structured" in plan and (algorithm == "structured" or (algorithm == "auto" and fits))
         if algorithm == "structured" and "structured" not in plan:
             raise ValueError("BRDF tables are not of the diffuse-plus-mirror form")
+        if algorithm == "structured" and not fits:
+            raise ValueError(f"the structured exchange holds at most {STRUCTURED_MAX_SAMPLES} time bins")
         a = nat.ExchangeArgs()
         a.precision = _PREC[self.precision]
         a.algorithm = nat.SP_EXCHANGE_STRUCTURED if use_struct else nat.SP_EXCHANGE_DENSE
@@ -594,7 +622,10 @@ class DirectionalRadiosityFast:
         n, nd, nb = e0dir.shape
         dtype = torch.float32 if self.precision == "fp32" else torch.float64
         etc = torch.empty((n, nd, nb, n_samples), dtype=dtype, device=self.device)
-        a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
+        if max_order < 1 and states is None:
+            a = self._init_only_args(c, dt, n_samples, etc)
+        else:
+            a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
         if states is not None:
             if a.algorithm != nat.SP_EXCHANGE_STRUCTURED:
                 raise ValueError("saving exchange states needs the structured exchange")
