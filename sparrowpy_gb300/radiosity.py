@@ -47,6 +47,17 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+_SIDE_STREAMS = {}
+
+
+def _side_stream(device):
+    """One side stream per device for host-bound preparation that overlaps the bake kernels."""
+    key = torch.device(device).index
+    if key not in _SIDE_STREAMS:
+        _SIDE_STREAMS[key] = torch.cuda.Stream(device=device)
+    return _SIDE_STREAMS[key]
+
+
 def brdf_rows_host(brdf, rel_tol=1e-12):
     """Host restatement of sp_brdf_structure (the per-row step of analyse_brdf).
 
@@ -83,6 +94,36 @@ def brdf_rows_host(brdf, rel_tol=1e-12):
     return diff, spec, target, scale, irregular
 
 
+_ROW_HASH = np.random.default_rng(0x5EED).integers(1, 2 ** 63, size=4096, dtype=np.uint64) | np.uint64(1)
+
+
+def _unique_rows(key):
+    """First index and inverse of the distinct rows of a float matrix, as np.unique(axis=0) gives them.
+
+    Rows are hashed exactly (their bits times odd 64-bit multipliers, summed
+    modulo 2^64, with -0.0 taken as 0.0), the hashes made unique, and every
+    row checked against its group's first row; the groups are then ranked by
+    the lexicographic order of those rows.  A hash collision or an over-long
+    row falls back to np.unique(axis=0).
+    """
+    S, K = key.shape
+    if S == 0 or K > _ROW_HASH.size or np.isnan(key).any():
+        _, first, inverse = np.unique(key, axis=0, return_index=True, return_inverse=True)
+        return first, inverse.reshape(-1)
+    key = np.ascontiguousarray(key, dtype=np.float64)
+    bits = (key + 0.0).view(np.uint64)
+    h = bits @ _ROW_HASH[:K]  # integer product: exact, wraps modulo 2^64
+    _, first_h, inv_h = np.unique(h, return_index=True, return_inverse=True)
+    inv_h = inv_h.reshape(-1)
+    if not np.array_equal(key, key[first_h[inv_h]]):
+        _, first, inverse = np.unique(key, axis=0, return_index=True, return_inverse=True)
+        return first, inverse.reshape(-1)
+    order = np.lexsort(key[first_h].T[::-1])  # first column most significant
+    rank = np.empty_like(order)
+    rank[order] = np.arange(order.size)
+    return first_h[order], rank[inv_h]
+
+
 def group_brdf_rows(diff, spec, target, scale):
     """Group slots whose normalised rows agree: BRDF = scale[slot, b] * (diff + spec [o == m]).
 
@@ -97,8 +138,7 @@ def group_brdf_rows(diff, spec, target, scale):
     ns = spec / scale[:, None, :]
     key = np.concatenate([np.round(nd.reshape(S, -1), 12), np.round(ns.reshape(S, -1), 12),
                           target.reshape(S, -1).astype(float)], axis=1)
-    _, first, inverse = np.unique(key, axis=0, return_index=True, return_inverse=True)
-    inverse = inverse.reshape(-1)
+    first, inverse = _unique_rows(key)
     G = first.size
     reps = first
     class_diff = nd[reps].reshape(G * Din, B)
@@ -298,14 +338,24 @@ class DirectionalRadiosityFast:
                      _ptr(d["areas"]), _stream())
         return d
 
+    def _brdf_key(self):
+        return (id(self._brdf), len(self._brdf), tuple(self._brdf_index.tolist()))
+
+    def _cached_brdf(self):
+        """The device BRDF state if it still matches the object's tables, else None."""
+        cached = self._dev.get("brdf_state")
+        if cached is not None and (cached["key"] == self._brdf_key() or cached["key"] == self._device_brdf_key):
+            return cached
+        return None
+
     def _brdf_device(self):
         """Device copies of the current BRDF tables and direction sets."""
         if self._brdf_incoming_directions is None:
             return None
-        key = (id(self._brdf), len(self._brdf), tuple(self._brdf_index.tolist()))
-        cached = self._dev.get("brdf_state")
-        if cached is not None and (cached["key"] == key or cached["key"] == self._device_brdf_key):
+        cached = self._cached_brdf()
+        if cached is not None:
             return cached
+        key = self._brdf_key()
         if np.any(self._brdf_index < 0):
             raise ValueError("every wall needs a BRDF (set_wall_brdf) before this step")
         din = np.array([_cart(c).reshape(-1, 3) for c in self._brdf_incoming_directions])
@@ -322,6 +372,30 @@ class DirectionalRadiosityFast:
                      brdf=self._t(brdf, torch.float64), brdf_index=self._t(self._brdf_index, torch.int32))
         self._dev["brdf_state"] = state
         return state
+
+    def _prepare_brdf(self):
+        """Device BRDF tables and their diffuse-plus-mirror structure, made on a side stream.
+
+        Stacking, uploading and grouping new tables is host work; issued right
+        after the visibility kernels it runs while they do, since none of it
+        reads the geometry.  The current stream then waits for the side
+        stream, and the tables are recorded as used on it.
+        """
+        if self._brdf_incoming_directions is None:
+            return None
+        cached = self._cached_brdf()
+        if cached is not None and "structure" in cached:
+            return cached
+        main = torch.cuda.current_stream(self.device)
+        side = _side_stream(self.device)
+        with torch.cuda.stream(side):
+            bs = self._brdf_device()
+            self._brdf_structure(bs)
+        main.wait_stream(side)
+        for v in bs.values():
+            if isinstance(v, torch.Tensor) and v.is_cuda:
+                v.record_stream(main)
+        return bs
 
     def _install_device_brdf(self, tables, brdf_index):
         """Use device-built BRDF tables (S, n_in, n_out, B) float64 with the current direction sets.
@@ -390,6 +464,7 @@ class DirectionalRadiosityFast:
         ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=dev)
         nat.call("sp_patch_visibility", n, nv, _ptr(d["centers"]), _ptr(d["normals"]), _ptr(d["pts"]), _ptr(vis),
                  _ptr(ws), wsz, st)
+        bs = self._prepare_brdf()  # host work while the visibility kernels run
         # visible pair list (RadiosityFast.py:377-387)
         cap = max(n * (n - 1) // 2, 1)
         pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
@@ -418,7 +493,6 @@ class DirectionalRadiosityFast:
         nat.call("sp_directed_pairs", n, _ptr(sym), _ptr(dst_off), _ptr(src), _ptr(dst), st)
         del sym
         # per-pair directions, distances and F' (RadiosityFast.py:402-414, 1234-1272, 538-543)
-        bs = self._brdf_device()
         out_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
         in_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
         dist = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
