@@ -196,14 +196,26 @@ __global__ void k_merge_positions(long long n_dir, int n_class, const int64_t* _
     merged[seg_base[(long long)tile * n_class + c] + pos] = e;
 }
 
+// Per pair and band, the coefficient a source group carries for it (Coef:
+// F', air attenuation, material), one pair per thread so that every lane of
+// a warp runs the FP64 arithmetic together.
+template <typename T, typename Coef>
+__global__ void k_pair_coef(long long n_dir, int nb, Coef pair_coef, T* __restrict__ out) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_dir) return;
+    for (int b = 0; b < nb; ++b) out[e * nb + b] = (T)pair_coef(e, b);
+}
+
 // Cells: runs of equal (segment, src) in merged order (<= kTile entries, one
 // per destination).  For each cell start: sort members by (p2o, delay), cut into
-// groups; write == 0 counts, write == 1 emits.
-template <typename T, typename Coef>
+// groups; write == 0 counts, write == 1 emits with the coefficients of
+// k_pair_coef.
+template <typename T>
 __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* __restrict__ merged,
                         const int32_t* __restrict__ src, const int32_t* __restrict__ dst, const int32_t* __restrict__ out_dir,
                         const int32_t* __restrict__ delay, const int32_t* __restrict__ cls,
-                        const int32_t* __restrict__ tile_of, const int32_t* __restrict__ slot_of, Coef pair_coef,
+                        const int32_t* __restrict__ tile_of, const int32_t* __restrict__ slot_of,
+                        const T* __restrict__ pair_coef,
                         int write, int64_t* __restrict__ cell_count, const int64_t* __restrict__ cell_base,
                         long long cap, Group* __restrict__ groups, T* __restrict__ coef,
                         uint32_t* __restrict__ wpack) {
@@ -270,7 +282,7 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
                 g.mask |= 1u << w;
                 g.off[w] = (uint8_t)(md[x] - md[a]);
                 long long ex = me[x];
-                for (int b = 0; b < nb; ++b) coef[((size_t)b * cap + g_out) * kTile + w] = (T)pair_coef(ex, b);
+                for (int b = 0; b < nb; ++b) coef[((size_t)b * cap + g_out) * kTile + w] = pair_coef[ex * nb + b];
             }
             groups[g_out] = g;
             const int mu = (-g.n_base - kMaxSpan) & 3;
@@ -382,6 +394,7 @@ struct PlanCore {
     Group* groups;
     uint32_t* wpack;  // [cap][kPackWarps]
     void* coef;       // [nb][cap][kTile]
+    void* pcoef;      // [pairs][nb] per-pair coefficients (k_pair_coef)
 };
 
 // Carve PlanCore arrays from q (advanced); esz = coefficient element size.
@@ -408,6 +421,7 @@ PlanCore plan_core_layout(Take& take, int esz, int n, int nb, long long p, int n
     C.groups = (Group*)take((size_t)(p + 1) * sizeof(Group));
     C.wpack = (uint32_t*)take((size_t)(p + 1) * kPackWarps * 4);
     C.coef = take((size_t)(p + 1) * nb * kTile * esz);
+    C.pcoef = take((size_t)(p + 1) * nb * esz);
     return C;
 }
 
@@ -432,13 +446,14 @@ int build_groups(int n, int nb, int nt, const PairSet& ps, const int32_t* order,
     k_merge_positions<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, n_class, C.perm, C.row_of, ps.cls, ps.src,
                                                                      C.rco, C.tile_of, C.slot_of, C.tile_recv,
                                                                      C.seg_base, C.merged);
-    k_cells<T, Coef><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
-        p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of, coef, 0,
-        C.cell_count, nullptr, p, nullptr, nullptr, nullptr);
+    k_pair_coef<T, Coef><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(p, nb, coef, (T*)C.pcoef);
+    k_cells<T><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
+        p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of,
+        (const T*)C.pcoef, 0, C.cell_count, nullptr, p, nullptr, nullptr, nullptr);
     scan64(p, C.cell_count, C.cell_base, C.scan_tmp, st);
-    k_cells<T, Coef><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
-        p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of, coef, 1,
-        nullptr, C.cell_base, p, C.groups, (T*)C.coef, C.wpack);
+    k_cells<T><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
+        p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of,
+        (const T*)C.pcoef, 1, nullptr, C.cell_base, p, C.groups, (T*)C.coef, C.wpack);
     k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, sp_counted(st)>>>(n_seg, p, C.seg_base, C.cell_base,
                                                                          C.seg_off);
     // scatter blocks visit the non-empty segments longest first, so the

@@ -131,6 +131,12 @@ __device__ bool exact_visibility(const double* vp, const double* ep, const doubl
 // margin that covers the predicate's 1e-6 tolerances and the FP32 rounding
 // of the segment end points, so a miss here proves the exact predicate
 // returns "visible" for every blocker inside the box.
+// d holds the segment direction in d[0..2] and its reciprocals in d[3..5]
+// (seg_reciprocals, once per segment).
+__device__ __forceinline__ void seg_reciprocals(float* d) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) d[3 + k] = d[k] != 0.0f ? 1.0f / d[k] : 0.0f;
+}
 __device__ __forceinline__ bool seg_hits_box(const float* a, const float* d, const float* lo, const float* hi) {
     float t0 = 0.0f, t1 = 1.0f;
 #pragma unroll
@@ -138,7 +144,7 @@ __device__ __forceinline__ bool seg_hits_box(const float* a, const float* d, con
         if (d[k] == 0.0f) {
             if (a[k] < lo[k] || a[k] > hi[k]) return false;
         } else {
-            float inv = 1.0f / d[k];
+            const float inv = d[3 + k];
             float ta = (lo[k] - a[k]) * inv, tb = (hi[k] - a[k]) * inv;
             float tn = fminf(ta, tb), tx = fmaxf(ta, tb);
             t0 = fmaxf(t0, tn);
@@ -224,7 +230,7 @@ __global__ void __launch_bounds__(256) k_patch_visibility(int n, int nv, const d
     int j = tile_j * 16 + (threadIdx.x & 15);
     bool active = (i < n) && (j < n) && (i < j);
     double ci[3] = {0, 0, 0}, cj[3] = {0, 0, 0};
-    float a[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+    float a[3] = {0, 0, 0}, d[6] = {0, 0, 0, 0, 0, 0};
     if (active) {
         for (int k = 0; k < 3; ++k) {
             ci[k] = centers[3 * i + k];
@@ -232,6 +238,7 @@ __global__ void __launch_bounds__(256) k_patch_visibility(int n, int nv, const d
             a[k] = (float)ci[k];
             d[k] = (float)cj[k] - a[k];
         }
+        seg_reciprocals(d);
     }
     bool visible = true;
     for (int g0 = 0; g0 < n_groups; g0 += 1024) {
@@ -294,13 +301,57 @@ __device__ __noinline__ int vis_cull_pair(bool active, const float* a, const flo
     return hits;
 }
 
-// The pair's own patches as blockers first (every thread the same two exact
-// tests): they hide every coplanar pair, whose segments would otherwise
-// cross the boxes of all patches between them.  Writes the base value.
+// Per patch: whether its centre lies inside it (the winding test of
+// `_point_in_polygon`) and within eta of its plane, each in the reference
+// predicate's arithmetic.  Both hold for every non-degenerate patch.
+__global__ void k_own_patch(int n, int nv, const double* __restrict__ centers, const double* __restrict__ normals,
+                            const double* __restrict__ pts, uint8_t* __restrict__ own_ok) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double c[3], nn[3], sp[kMaxVerts * 3];
+    for (int q = 0; q < 3; ++q) {
+        c[q] = centers[3 * i + q];
+        nn[q] = normals[3 * i + q];
+    }
+    for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)i * nv * 3 + q];
+    const double a[3] = {xsub(c[0], sp[0]), xsub(c[1], sp[1]), xsub(c[2], sp[2])};
+    own_ok[i] = (point_in_polygon(c, sp, nv, nn) && fabs(xdot3(a, nn)) < 1e-6) ? 1 : 0;
+}
+
+// exact_visibility for a blocker that is the patch of one end point, in
+// closed form.  With own_ok for that patch (its centre inside it and on its
+// plane), `_basic_visibility` (geometry.py:841-909) depends only on h, the
+// distance of the other end point from the blocker's plane as
+// `_point_in_polygon` computes it:
+//   h > eta: that point is outside the blocker (no winding test), so the
+//            segment is hidden iff it leaves the blocker's front side
+//            (the vis_in / eval_in branch with its half-space test);
+//   h < eta: both points are coplanar with the blocker and one is inside it:
+//            hidden, whatever the winding test of the other point gives.
+// Returns 1 visible, 0 hidden, -1 when exact_visibility has to decide
+// (a degenerate patch, or h == eta).
+__device__ __forceinline__ int own_patch_test(const double* vp, const double* ep, bool blocker_of_vp,
+                                              const double* p0, const double* n, bool own_ok) {
+    if (!own_ok) return -1;
+    const double* other = blocker_of_vp ? ep : vp;
+    const double d0[3] = {xsub(other[0], p0[0]), xsub(other[1], p0[1]), xsub(other[2], p0[2])};
+    const double h = fabs(xdot3(d0, n));
+    if (h > 1e-6) {
+        const double* from = blocker_of_vp ? vp : ep;
+        const double d[3] = {xsub(other[0], from[0]), xsub(other[1], from[1]), xsub(other[2], from[2])};
+        return xdot3(n, d) < 0 ? 0 : 1;
+    }
+    return h < 1e-6 ? 0 : -1;
+}
+
+// The pair's own patches as blockers first: they hide every coplanar pair,
+// whose segments would otherwise cross the boxes of all patches between
+// them.  Two closed-form tests per pair (own_patch_test), the full predicate
+// only where they cannot decide.  Writes the base value.
 __global__ void __launch_bounds__(256) k_vis_self(int n, int nv, const int32_t* __restrict__ tiles,
                                                   const double* __restrict__ centers,
                                                   const double* __restrict__ normals, const double* __restrict__ pts,
-                                                  uint8_t* __restrict__ vis) {
+                                                  const uint8_t* __restrict__ own_ok, uint8_t* __restrict__ vis) {
     const int tile = tiles[blockIdx.x];
     const int tile_i = tile >> 16, tile_j = tile & 0xffff;
     const int i = tile_i * 16 + (threadIdx.x >> 4);
@@ -315,10 +366,18 @@ __global__ void __launch_bounds__(256) k_vis_self(int n, int nv, const int32_t* 
         }
         for (int k = 0; k < 2 && visible; ++k) {
             const int s = k == 0 ? i : j;
-            double nn[3], sp[kMaxVerts * 3];
-            for (int q = 0; q < 3; ++q) nn[q] = normals[3 * s + q];
-            for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)s * nv * 3 + q];
-            visible = exact_visibility(ci, cj, sp, nv, nn);
+            double nn[3], p0[3];
+            for (int q = 0; q < 3; ++q) {
+                nn[q] = normals[3 * s + q];
+                p0[q] = pts[(size_t)s * nv * 3 + q];
+            }
+            int r = own_patch_test(ci, cj, k == 0, p0, nn, own_ok[s] != 0);
+            if (r < 0) {
+                double sp[kMaxVerts * 3];
+                for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)s * nv * 3 + q];
+                r = exact_visibility(ci, cj, sp, nv, nn) ? 1 : 0;
+            }
+            visible = r != 0;
         }
     }
     vis[(size_t)i * n + j] = visible ? 1 : 0;
@@ -339,12 +398,14 @@ __global__ void __launch_bounds__(256) k_vis_cull(int n, const int32_t* __restri
     const int j = tile_j * 16 + (threadIdx.x & 15);
     // pairs the own-patch pass (k_vis_self) already hid need no candidates
     const bool active = (i < n) && (j < n) && (i < j) && vis[(size_t)i * n + j] != 0;
-    float a[3] = {0, 0, 0}, d[3] = {0, 0, 0};
-    if (active)
+    float a[3] = {0, 0, 0}, d[6] = {0, 0, 0, 0, 0, 0};
+    if (active) {
         for (int k = 0; k < 3; ++k) {
             a[k] = (float)centers[3 * i + k];
             d[k] = (float)centers[3 * j + k] - a[k];
         }
+        seg_reciprocals(d);
+    }
     const int64_t code = ((int64_t)i << (2 * kCandBits)) | ((int64_t)j << kCandBits);
     // pass 1: count
     int hits = 0;
@@ -418,11 +479,12 @@ __global__ void k_point_visibility(const double* __restrict__ point, int n, cons
     if (i >= n) return;
     double vp[3] = {point[0], point[1], point[2]};
     double ep[3] = {centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]};
-    float a[3], d[3];
+    float a[3], d[6];
     for (int k = 0; k < 3; ++k) {
         a[k] = (float)vp[k];
         d[k] = (float)ep[k] - a[k];
     }
+    seg_reciprocals(d);
     bool visible = true;
     for (int s = 0; s < n_surf && visible; ++s) {
         const float* bx = sbox + 6 * s;
@@ -541,6 +603,52 @@ __global__ void k_symmetrize(int n, const uint8_t* __restrict__ v, uint8_t* __re
 // (RadiosityFast.py:402-414), incoming index used by the ff_tilde BRDF row
 // (:1264-1268), centre distance (:538-543), the normalised-vector length
 // used for air attenuation (:1252-1262) and F'_ij (:1255-1256).
+// FP64 -> FP32 by truncating the mantissa with integer operations (the
+// conversion instruction runs on GB300's narrow FP64 pipe).  |error| <
+// 2^-23 |x|; |x| < 2^-126 gives a signed zero; |x| >= 2^128 gives NaN.
+__device__ __forceinline__ float f64_trunc_f32(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    const unsigned sign = hi & 0x80000000u;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(0x7fc00000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
+// The reference argmin (sp_nearest_dir) decided in FP32 where that is
+// provably the same index.  With unit direction vectors:
+// * each FP32 unit(diff) component is within 5.1e-7 of the FP64 one (inputs
+//   truncated to 2^-23, square sum, square root, reciprocal, product);
+// * each difference a = dir - u is within 7.5e-7;
+// * so each value sum a^2 (sum |a| <= 2 sqrt 3) is within 1.1e-5 of its
+//   FP64 counterpart.
+// When the two smallest FP32 values differ by more than kDirGap = 3e-5 >
+// 2 x 1.1e-5, the smallest one is the unique FP64 minimum.
+// Returns the index, or -1 when the gap is smaller (or not a number) and the
+// FP64 loop has to decide.
+constexpr float kDirGap = 3e-5f;
+__device__ __forceinline__ int nearest_dir_f32(const double* diff, const double* __restrict__ dirs, int nd) {
+    const float x = f64_trunc_f32(diff[0]), y = f64_trunc_f32(diff[1]), z = f64_trunc_f32(diff[2]);
+    const float inv = 1.0f / sqrtf(x * x + y * y + z * z);
+    const float u[3] = {x * inv, y * inv, z * inv};
+    float b1 = __int_as_float(0x7f800000), b2 = b1;
+    int i1 = 0;
+    for (int o = 0; o < nd; ++o) {
+        const float a = f64_trunc_f32(dirs[3 * o]) - u[0];
+        const float b = f64_trunc_f32(dirs[3 * o + 1]) - u[1];
+        const float c = f64_trunc_f32(dirs[3 * o + 2]) - u[2];
+        const float v = a * a + b * b + c * c;
+        if (v < b1) {
+            b2 = b1;
+            b1 = v;
+            i1 = o;
+        } else if (v < b2) {
+            b2 = v;
+        }
+    }
+    return (b2 - b1 > kDirGap) ? i1 : -1;
+}
+
 __global__ void k_pair_setup(long long n_dir, int n, const int32_t* __restrict__ src, const int32_t* __restrict__ dst,
                              const double* __restrict__ centers, const double* __restrict__ areas,
                              const int32_t* __restrict__ pair_index, const double* __restrict__ ff,
@@ -554,9 +662,26 @@ __global__ void k_pair_setup(long long n_dir, int n, const int32_t* __restrict__
     double ci[3] = {centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]};
     double cj[3] = {centers[3 * j], centers[3 * j + 1], centers[3 * j + 2]};
     int w = wall_of[i];
-    if (out_dir) out_dir[e] = (n_out > 0 && dirs_out) ? sp_nearest_dir(ci, cj, dirs_out + (size_t)w * n_out * 3, n_out) : 0;
-    if (in_dir) in_dir[e] = (n_in > 0 && dirs_in) ? sp_nearest_dir(cj, ci, dirs_in + (size_t)w * n_in * 3, n_in) : 0;
     double dv[3] = {xsub(ci[0], cj[0]), xsub(ci[1], cj[1]), xsub(ci[2], cj[2])};
+    if (out_dir) {
+        int o = 0;
+        if (n_out > 0 && dirs_out) {
+            const double* tab = dirs_out + (size_t)w * n_out * 3;
+            const double fwd[3] = {xsub(cj[0], ci[0]), xsub(cj[1], ci[1]), xsub(cj[2], ci[2])};
+            o = nearest_dir_f32(fwd, tab, n_out);
+            if (o < 0) o = sp_nearest_dir(ci, cj, tab, n_out);
+        }
+        out_dir[e] = o;
+    }
+    if (in_dir) {
+        int o = 0;
+        if (n_in > 0 && dirs_in) {
+            const double* tab = dirs_in + (size_t)w * n_in * 3;
+            o = nearest_dir_f32(dv, tab, n_in);
+            if (o < 0) o = sp_nearest_dir(cj, ci, tab, n_in);
+        }
+        in_dir[e] = o;
+    }
     double dd = xnorm3(dv);
     dist[e] = dd;
     double u[3] = {xdiv(dv[0], dd), xdiv(dv[1], dd), xdiv(dv[2], dd)};
@@ -664,7 +789,8 @@ size_t sp_patch_visibility_workspace(int n) {
     if (n <= 0) return 256;
     size_t groups = ((size_t)n + kGroup - 1) / kGroup;
     return sp_align((size_t)n * 6 * sizeof(float) + groups * 6 * sizeof(float)) +
-           sp_align((size_t)vis_cand_capacity(n) * 8) + 2 * sp_align((size_t)vis_tile_count(n) * 4) + 256;
+           sp_align((size_t)vis_cand_capacity(n) * 8) + 2 * sp_align((size_t)vis_tile_count(n) * 4) +
+           sp_align((size_t)n) + 256;
 }
 
 int sp_patch_visibility(int n, int nv, const double* centers, const double* normals, const double* pts,
@@ -688,6 +814,8 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
     q += sp_align((size_t)n_tiles * 4);
     list[1] = (int32_t*)q;
     q += sp_align((size_t)n_tiles * 4);
+    uint8_t* own_ok = (uint8_t*)q;
+    q += sp_align((size_t)n);
     unsigned long long* counter = (unsigned long long*)q;
     int* n_overflow = (int*)(q + 8);
     k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n, nv, pts, 1e-3f, box, gbox);
@@ -700,7 +828,8 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
         for (int tj = ti; tj < nt; ++tj) h_tiles.push_back((ti << 16) | tj);
     cudaMemcpyAsync(list[0], h_tiles.data(), h_tiles.size() * 4, cudaMemcpyHostToDevice, st);
     long long todo = (long long)h_tiles.size();
-    k_vis_self<<<(unsigned)todo, 256, 0, sp_counted(st)>>>(n, nv, list[0], centers, normals, pts, vis);
+    k_own_patch<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(n, nv, centers, normals, pts, own_ok);
+    k_vis_self<<<(unsigned)todo, 256, 0, sp_counted(st)>>>(n, nv, list[0], centers, normals, pts, own_ok, vis);
     int cur = 0;
     for (int round = 0; todo > 0; ++round) {
         cudaMemsetAsync(counter, 0, 16, st);
