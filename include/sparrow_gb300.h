@@ -211,7 +211,8 @@ typedef struct sp_exchange_args {
     /* structured algorithm, optional (checkpoints for the adjoint; NULL/0 = off): */
     const void* state_in;   /* (N, D, B, T) E_{state_order}: start there instead of at the source energy */
     int state_order;        /* order of state_in (0 without it); orders state_order + 1 .. max_order run */
-    void* states_out;       /* (n, N, D, B, T): E_k for k = state_order + i * states_every, i = 0, 1, ... */
+    void* states_out;       /* (n, N, D, B, T): E_k for k = state_order + i * states_every, i = 0, 1, ...
+                               (with state_in, i = 0 is not written: it is state_in) */
     int states_every;
     int skip_total;         /* 1: etc_total is neither cleared nor written */
     /* SP_EXCHANGE_MATERIAL only: per-slot create_from_scattering materials

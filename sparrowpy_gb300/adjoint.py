@@ -195,7 +195,8 @@ class DifferentiableExchange:
         return r._collect_device(self.receivers)
 
     def _resume(self, alpha64, scat64, state_in, k_from, k_to, states):
-        """Orders k_from + 1 .. k_to from E_{k_from}; states[i] = E_{k_from + i}."""
+        """Orders k_from + 1 .. k_to from E_{k_from}; states[i] = E_{k_from + i} for i >= 1 (states[0] is not
+        written: it would repeat state_in)."""
         dummy = torch.empty((1,), dtype=torch.float32, device=self.r.device)
         a = self._args(alpha64, scat64, dummy)
         a.max_order = int(k_to)

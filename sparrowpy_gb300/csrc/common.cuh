@@ -30,6 +30,18 @@ __device__ __forceinline__ void xcross3(const double* a, const double* b, double
     c[2] = xsub(xmul(a[0], b[1]), xmul(a[1], b[0]));
 }
 
+// FP64 -> FP32 by truncating the mantissa with integer operations (the
+// conversion instruction runs on GB300's narrow FP64 pipe).  |error| <
+// 2^-23 |x|; |x| < 2^-126 gives a signed zero; |x| >= 2^128 gives NaN.
+__device__ __forceinline__ float f64_trunc_f32(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    const unsigned sign = hi & 0x80000000u;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(0x7fc00000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
 // RadiosityFast.py:1277-1312 `get_scattering_data_receiver_index` (one row)
 // and :1359-1390 `get_scattering_data_source`: argmin over a wall's direction
 // table of |dir - unit(to - from)|^2, first index on ties.

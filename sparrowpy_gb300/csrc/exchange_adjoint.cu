@@ -111,6 +111,12 @@ struct AdjCoef {
         if (att) f = f * exp(-att[b] * unit_len[e]);
         return cls[t] >= nd ? f * gain[in_dir[e]] : f;
     }
+    __device__ float f32(long long t, int b) const {
+        const long long e = fwd[t];
+        float f = f64_trunc_f32(fprime[e]);
+        if (att) f = f * expf(-f64_trunc_f32(att[b]) * f64_trunc_f32(unit_len[e]));
+        return cls[t] >= nd ? f * f64_trunc_f32(gain[in_dir[e]]) : f;
+    }
 };
 
 // g = dL/dE_total is nonzero only in the row (k, ridx_rk) of each receiver r:
@@ -229,6 +235,126 @@ __global__ void __launch_bounds__(256) k_adjoint_combine(
     }
     if (!e_prev) return;
     // block reduction of the two dot products
+    __shared__ float s_red[2][8];
+    for (int off = 16; off > 0; off >>= 1) {
+        dot_mix += __shfl_xor_sync(0xffffffffu, dot_mix, off);
+        dot_diff += __shfl_xor_sync(0xffffffffu, dot_diff, off);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_red[0][w] = dot_mix;
+        s_red[1][w] = dot_diff;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double dm = 0.0, dd = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            dm += s_red[0][k];
+            dd += s_red[1][k];
+        }
+        atomicAdd(&grad_a[(size_t)slot * nb + b], -dm);
+        atomicAdd(&grad_s[(size_t)slot * nb + b], (double)keep * dd);
+    }
+}
+
+// k_adjoint_combine for nt % 4 == 0: four bins per thread (16-byte accesses;
+// the reversed-time E_{k-1} row is read as float4 and taken back to front).
+__device__ __forceinline__ float4 c4_add(float4 x, float4 y) {
+    return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+}
+__device__ __noinline__ void add_extra_rows4(int p, int n_rcv, const int* s_ridx, const float* __restrict__ g_rev,
+                                             int n, int i, int nb, int b, int nt, float4* out) {
+    const int nt4 = nt >> 2;
+    for (int r = 0, h = 0; r < n_rcv; ++r) {
+        if (s_ridx[r] != p || h++ < 2) continue;
+        const float4* row = reinterpret_cast<const float4*>(g_rev + (((size_t)r * n + i) * nb + b) * nt);
+        for (int t = threadIdx.x; t < nt4; t += 256) out[t] = c4_add(out[t], row[t]);
+    }
+}
+
+constexpr int kCombine4 = kCombineBins / 4;  // float4 per thread
+
+__global__ void __launch_bounds__(256) k_adjoint_combine4(
+    int n, int nd, int nb, int nt, long long rs, int lead, int n_rcv, const int32_t* __restrict__ ridx,
+    const float* __restrict__ g_rev, const float* __restrict__ lam, const uint32_t* __restrict__ present, int words,
+    const int32_t* __restrict__ tile_of, const float* __restrict__ e_prev, const int32_t* __restrict__ wall_of,
+    const int32_t* __restrict__ brdf_index, const double* __restrict__ alpha, const double* __restrict__ scat,
+    float* __restrict__ mu_out, double* __restrict__ grad_a, double* __restrict__ grad_s) {
+    const int b = blockIdx.x, i = blockIdx.y;
+    __shared__ int s_ridx[kMaxReceivers];
+    for (int r = threadIdx.x; r < n_rcv; r += blockDim.x) s_ridx[r] = ridx[(size_t)r * n + i];
+    __syncthreads();
+    const int slot = brdf_index[wall_of[i]];
+    const float a = (float)alpha[(size_t)slot * nb + b];
+    const float sc = (float)scat[(size_t)slot * nb + b];
+    const float keep = 1.0f - a;
+    const uint32_t* pres = lam ? present + (size_t)tile_of[i] * words : nullptr;
+    const int nt4 = nt >> 2;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 usum[kCombine4];
+#pragma unroll
+    for (int q = 0; q < kCombine4; ++q) usum[q] = zero;
+    float dot_mix = 0.0f, dot_diff = 0.0f;
+    for (int p = 0; p < nd; ++p) {
+        const float4* g0 = nullptr;
+        const float4* g1 = nullptr;
+        int n_hit = 0;
+        for (int r = 0; r < n_rcv; ++r)
+            if (s_ridx[r] == p) {
+                const float4* row = reinterpret_cast<const float4*>(g_rev + (((size_t)r * n + i) * nb + b) * nt);
+                if (n_hit == 0) g0 = row;
+                else if (n_hit == 1) g1 = row;
+                ++n_hit;
+            }
+        const bool has_u = pres && ((pres[p >> 5] >> (p & 31)) & 1u);
+        const bool has_v = pres && ((pres[(nd + p) >> 5] >> ((nd + p) & 31)) & 1u);
+        const float4* lu = has_u ? reinterpret_cast<const float4*>(lam + (((size_t)i * 2 * nd + p) * nb + b) * nt)
+                                 : nullptr;
+        const float4* lv = has_v ? reinterpret_cast<const float4*>(lam + (((size_t)i * 2 * nd + nd + p) * nb + b) * nt)
+                                 : nullptr;
+        const float4* ep = e_prev ? reinterpret_cast<const float4*>(e_prev + (((size_t)i * nd + p) * nb + b) * nt)
+                                  : nullptr;
+        float4* mo = reinterpret_cast<float4*>(mu_out + (((size_t)i * (nd + 1) + p) * nb + b) * rs + lead);
+#pragma unroll
+        for (int q = 0; q < kCombine4; ++q) {
+            const int t = threadIdx.x + 256 * q;
+            if (t < nt4) {
+                const float4 u = lu ? __ldg(lu + t) : zero;
+                const float4 v = lv ? __ldg(lv + t) : zero;
+                const float4 mixed = make_float4(sc * u.x + (1.0f - sc) * v.x, sc * u.y + (1.0f - sc) * v.y,
+                                                 sc * u.z + (1.0f - sc) * v.z, sc * u.w + (1.0f - sc) * v.w);
+                float4 m = make_float4(keep * mixed.x, keep * mixed.y, keep * mixed.z, keep * mixed.w);
+                if (g0) m = c4_add(m, __ldg(g0 + t));
+                if (g1) m = c4_add(m, __ldg(g1 + t));
+                mo[t] = m;
+                usum[q] = c4_add(usum[q], m);
+                if (ep) {
+                    const float4 e = __ldg(ep + (nt4 - 1 - t));  // bins 4t .. 4t + 3 read E at nt - 1 - 4t .. nt - 4 - 4t
+                    dot_mix = fmaf(e.w, mixed.x, dot_mix);
+                    dot_mix = fmaf(e.z, mixed.y, dot_mix);
+                    dot_mix = fmaf(e.y, mixed.z, dot_mix);
+                    dot_mix = fmaf(e.x, mixed.w, dot_mix);
+                    dot_diff = fmaf(e.w, u.x - v.x, dot_diff);
+                    dot_diff = fmaf(e.z, u.y - v.y, dot_diff);
+                    dot_diff = fmaf(e.y, u.z - v.z, dot_diff);
+                    dot_diff = fmaf(e.x, u.w - v.w, dot_diff);
+                }
+            }
+        }
+        if (n_hit > 2) add_extra_rows4(p, n_rcv, s_ridx, g_rev, n, i, nb, b, nt, mo);
+    }
+    float4* mu_u = reinterpret_cast<float4*>(mu_out + (((size_t)i * (nd + 1) + nd) * nb + b) * rs + lead);
+#pragma unroll
+    for (int q = 0; q < kCombine4; ++q) {
+        const int t = threadIdx.x + 256 * q;
+        if (t < nt4) mu_u[t] = usum[q];
+    }
+    for (int p = 0; p < nd; ++p) {  // the extra rows' share of U (rare)
+        int hits = 0;
+        for (int r = 0; r < n_rcv; ++r) hits += s_ridx[r] == p;
+        if (hits > 2) add_extra_rows4(p, n_rcv, s_ridx, g_rev, n, i, nb, b, nt, mu_u);
+    }
+    if (!e_prev) return;
     __shared__ float s_red[2][8];
     for (int off = 16; off > 0; off >>= 1) {
         dot_mix += __shfl_xor_sync(0xffffffffu, dot_mix, off);
@@ -433,11 +559,17 @@ int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, siz
             (const float*)L.C.coef, mu_in, L.lam, L.err);
     }
     dim3 cg(nb, n);
-    k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(
-        n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, L.g_rev,
-        S->n_active > 0 ? L.lam : nullptr, L.present, words,
-        L.C.tile_of, (const float*)e_prev, f->wall_of, f->brdf_index, a->alpha, a->scattering, mu_out,
-        a->grad_alpha, a->grad_scattering);
+    if (nt % 4 == 0)
+        k_adjoint_combine4<<<cg, 256, 0, sp_counted(st)>>>(
+            n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, L.g_rev,
+            S->n_active > 0 ? L.lam : nullptr, L.present, words, L.C.tile_of, (const float*)e_prev, f->wall_of,
+            f->brdf_index, a->alpha, a->scattering, mu_out, a->grad_alpha, a->grad_scattering);
+    else
+        k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(
+            n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, L.g_rev,
+            S->n_active > 0 ? L.lam : nullptr, L.present, words,
+            L.C.tile_of, (const float*)e_prev, f->wall_of, f->brdf_index, a->alpha, a->scattering, mu_out,
+            a->grad_alpha, a->grad_scattering);
     S->cur = 1 - S->cur;
     int rc = sp_check_launch();
     if (rc != SP_OK) return rc;

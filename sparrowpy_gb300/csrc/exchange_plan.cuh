@@ -203,7 +203,12 @@ template <typename T, typename Coef>
 __global__ void k_pair_coef(long long n_dir, int nb, Coef pair_coef, T* __restrict__ out) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n_dir) return;
-    for (int b = 0; b < nb; ++b) out[e * nb + b] = (T)pair_coef(e, b);
+    for (int b = 0; b < nb; ++b) {
+        if constexpr (sizeof(T) == 4)
+            out[e * nb + b] = pair_coef.f32(e, b);  // GB300's FP64 pipe is a small fraction of FP32
+        else
+            out[e * nb + b] = pair_coef(e, b);
+    }
 }
 
 // Cells: runs of equal (segment, src) in merged order (<= kTile entries, one
@@ -358,6 +363,12 @@ struct FwdCoef {
         double f = fprime[e];
         if (att) f = f * exp(-att[b] * unit_len[e]);
         return f * slot_scale[(size_t)brdf_index[wall_of[src[e]]] * nb + b];
+    }
+    // the same in FP32 (inputs truncated to 2^-23) for the FP32 plan
+    __device__ float f32(long long e, int b) const {
+        float f = f64_trunc_f32(fprime[e]);
+        if (att) f = f * expf(-f64_trunc_f32(att[b]) * f64_trunc_f32(unit_len[e]));
+        return f * f64_trunc_f32(slot_scale[(size_t)brdf_index[wall_of[src[e]]] * nb + b]);
     }
 };
 

@@ -7,7 +7,7 @@
 // For receiver j and order k:
 //   G_k[j, c, b, t] = sum_{pairs p -> j of class c} w_pb * E_{k-1}[src_p, p2o_p, b, t - n_p]
 //   E_k[j, o, b, t] = sum_c (diff[c, b] + spec[c, b] [o == m_c]) * G_k[j, c, b, t]
-//   E_total += E_k
+//   E_total += E_k  (two orders at a time: see the order loop)
 // with w_pb = F'_p * exp(-att_b |u_p|) * scale[slot(src_p), b].
 //
 // Plan (once per exchange call): receivers are cut into tiles of 16 (a given
@@ -17,15 +17,14 @@
 // n_base .. n_base + 45.  Everything is built in parallel and
 // deterministically (row-wise class sort, merge by binary search, scans).
 //
-// Scatter (per order, FP32): one CTA per (segment, 1024-bin window, band),
-// 128 threads; thread tid owns bins t0 + tid + 128 r (r < 8) of all 16
-// receivers in registers.  Each group's source window (1072 values) is
-// staged in shared memory by a bulk asynchronous copy (cp.async.bulk +
-// mbarrier, 12 stages, refilled by the last warp to finish a stage); every
-// member reads the staged window at its own delay offset, each warp read
-// covering 32 consecutive floats, so one staged window feeds every member
-// of the group.  FP64 uses the same plan with direct loads.  Mix: streams G
-// into E_k and E_total.
+// Scatter (per order, FP32; exchange_scatter.cuh): one CTA per (segment,
+// 1024-bin window, band).  A producer warp stages each group's source window
+// (1072 values), packed member words and coefficients in shared memory with
+// bulk asynchronous copies (cp.async.bulk + mbarrier, 6 stages of 4
+// groups); 8 consumer warps, each owning 2 receiver slots x 1024 bins in
+// registers, read the staged window at each member's delay offset, every
+// warp read covering 32 consecutive floats.  FP64 uses the same plan with
+// direct loads.  Mix: streams G into E_k and E_total.
 #include "exchange_scatter.cuh"
 
 namespace {
@@ -33,13 +32,16 @@ namespace {
 // --------------------------------------------------------------- mix
 // E_k[j, o, b, t] = sum_c diff[c, b] G[j, c, b, t] + sum_{c: m_c = o} spec[c, b] G[j, c, b, t]
 // (the slot scale is folded into the scatter coefficients), written to the
-// padded row of ecur, and E_total += E_k.  One block per (band, receiver),
+// padded row of ecur, and E_total += E_k, or E_total += E_{k-1} + E_k when
+// eadd holds the deferred previous order (padded rows), or nothing when
+// etot is null.  One block per (band, receiver),
 // all bins; only the classes present in the receiver's tile are read.
 template <typename T>
 __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                              const T* __restrict__ cdiff, const T* __restrict__ cspec,
-                                             const T* __restrict__ g, T* __restrict__ ecur, T* __restrict__ etot) {
+                                             const T* __restrict__ g, T* __restrict__ ecur, T* __restrict__ etot,
+                                             const T* __restrict__ eadd) {
     extern __shared__ __align__(16) unsigned char s_mix[];
     const int stride = tile_tab_stride(n_class, nd);
     T* s_cd = reinterpret_cast<T*>(s_mix);  // [n_class] diffuse weight of band b
@@ -61,6 +63,7 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
     const T* gj = g + ((size_t)j * n_class * nb + b) * nt;
     T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;  // padded rows, stride rs
     T* et = etot ? etot + ((size_t)j * nd * nb + b) * nt : nullptr;  // nullptr: E_total not accumulated
+    const T* ea = eadd ? eadd + ((size_t)j * nd * nb + b) * rs + lead : nullptr;  // deferred E_{k-1}, padded
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
         T diffuse = T(0);
         for (int q = 0; q < np; ++q) {
@@ -74,7 +77,11 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
                 v = fma(s_cs[c], gj[c * cstride + t], v);
             }
             ek[(size_t)o * nb * rs + t] = v;
-            if (et) et[o * cstride + t] += v;
+            if (et) {
+                T acc = et[o * cstride + t];
+                if (ea) acc += ea[(size_t)o * nb * rs + t];
+                et[o * cstride + t] = acc + v;
+            }
         }
     }
 }
@@ -92,7 +99,7 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
                                               const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                               const float* __restrict__ cdiff, const float* __restrict__ cspec,
                                               const float* __restrict__ g, float* __restrict__ ecur,
-                                              float* __restrict__ etot) {
+                                              float* __restrict__ etot, const float* __restrict__ eadd) {
     extern __shared__ __align__(16) unsigned char s_mix[];
     const int stride = tile_tab_stride(n_class, nd);
     float* s_cd = reinterpret_cast<float*>(s_mix);
@@ -116,6 +123,7 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
     const float4* gj = reinterpret_cast<const float4*>(g + ((size_t)j * n_class * nb + b) * nt);
     float4* ek = reinterpret_cast<float4*>(ecur + ((size_t)j * nd * nb + b) * rs + lead);
     float4* et = etot ? reinterpret_cast<float4*>(etot + ((size_t)j * nd * nb + b) * nt) : nullptr;
+    const float4* ea = eadd ? reinterpret_cast<const float4*>(eadd + ((size_t)j * nd * nb + b) * rs + lead) : nullptr;
     for (int t = threadIdx.x; t < nt4; t += blockDim.x) {
         float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int q = 0; q < np; ++q) {
@@ -128,6 +136,11 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
 #pragma unroll
             for (int k = 0; k < 8; ++k)
                 if (k < no && et) e[k] = et[(o0 + k) * cs4 + t];
+            if (ea) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (k < no) e[k] = add4(e[k], __ldg(ea + (o0 + k) * ers4 + t));
+            }
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 if (k < no) {
@@ -244,6 +257,15 @@ struct MatCoef {
         if (att) f = f * exp(-att[b] * unit_len[e]);
         const double a = alpha[(size_t)slot * nb + b], s = scat[(size_t)slot * nb + b];
         return cls[t] == 0 ? f * ((1.0 - a) * s) : f * ((1.0 - a) * (1.0 - s) * gain[in_dir[e]]);
+    }
+    __device__ float f32(long long t, int b) const {
+        const long long e = fwd[t];
+        const int slot = brdf_index[wall_of[src[e]]];
+        float f = f64_trunc_f32(fprime[e]);
+        if (att) f = f * expf(-f64_trunc_f32(att[b]) * f64_trunc_f32(unit_len[e]));
+        const float a = f64_trunc_f32(alpha[(size_t)slot * nb + b]), s = f64_trunc_f32(scat[(size_t)slot * nb + b]);
+        return cls[t] == 0 ? f * ((1.0f - a) * s)
+                           : f * ((1.0f - a) * (1.0f - s) * f64_trunc_f32(gain[in_dir[e]]));
     }
 };
 
@@ -382,14 +404,17 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     const int lead = L.R.lead;
     T* states = (T*)a->states_out;
     cudaMemsetAsync(L.err, 0, sizeof(int), st);
-    // eprev: all zero before the starting energies are placed; ecur: only the
-    // leads need zeros (every bin is written each order)
-    cudaMemsetAsync(eprev, 0, (L.rows * L.R.rs + L.R.tail) * sizeof(T), st);
+    // ecur: only the leads need zeros (every bin is written each order);
+    // eprev: the same when a starting state fills its bins, else all zero
+    // before the starting energies are placed
     cudaMemset2DAsync(ecur, L.R.rs * sizeof(T), 0, (size_t)lead * sizeof(T), L.rows, st);
     if (a->state_in) {
+        cudaMemset2DAsync(eprev, L.R.rs * sizeof(T), 0, (size_t)lead * sizeof(T), L.rows, st);
+        cudaMemsetAsync(eprev + L.rows * L.R.rs, 0, L.R.tail * sizeof(T), st);
         copy_rows(eprev + lead, L.R.rs, (const T*)a->state_in, (size_t)nt, nt, L.rows, st);
         if (etot) cudaMemcpyAsync(etot, a->state_in, e * sizeof(T), cudaMemcpyDeviceToDevice, st);
     } else {
+        cudaMemsetAsync(eprev, 0, (L.rows * L.R.rs + L.R.tail) * sizeof(T), st);
         if (etot) cudaMemsetAsync(etot, 0, e * sizeof(T), st);
         long long ne = (long long)n * nd * nb;
         k_init_energy_t<T><<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(
@@ -400,7 +425,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
         if (herr) return SP_ERR_RANGE;
     }
-    if (states) copy_rows(states, (size_t)nt, eprev + lead, L.R.rs, nt, L.rows, st);
+    if (states && !a->state_in) copy_rows(states, (size_t)nt, eprev + lead, L.R.rs, nt, L.rows, st);
     if (a->max_order <= k0 || p == 0) return sp_check_launch();
 
     // ---- plan (or the one a previous call with the same tag left in ws)
@@ -484,14 +509,22 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
                                                                       (const double*)L.C.coef, (const double*)eprev,
                                                                       (double*)L.g);
         }
+        // E_total takes the orders in pairs: the first of a pair is deferred
+        // and added by the second from the scatter's input rows (E_{k-1},
+        // intact until the next mix overwrites them), which saves one read
+        // and one write of E_total per pair; a last unpaired order adds alone.
+        const bool first_of_pair = (k - k0) % 2 == 1;
+        T* et_k = (first_of_pair && k < a->max_order) ? nullptr : etot;
+        const T* ea_k = (etot && !first_of_pair) ? eprev : nullptr;
         if (sizeof(T) == 4 && nt % 4 == 0)
             k_mix4<<<mgrid, 128, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                           (const float*)L.cdiff, (const float*)L.cspec,
-                                                          (const float*)L.g, (float*)ecur, (float*)etot);
+                                                          (const float*)L.g, (float*)ecur, (float*)et_k,
+                                                          (const float*)ea_k);
         else
             k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                             (const T*)L.cdiff, (const T*)L.cspec, (const T*)L.g, ecur,
-                                                            etot);
+                                                            et_k, ea_k);
         if (states && (k - k0) % a->states_every == 0)
             copy_rows(states + (size_t)((k - k0) / a->states_every) * e, (size_t)nt, ecur + lead, L.R.rs, nt, L.rows,
                       st);

@@ -505,7 +505,8 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
 // k_ff_rework), else kStokes32 with ff = base (completed by k_ff_phi).
 __global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, const double* __restrict__ pts,
                           const PatchStokes* __restrict__ pd, double* __restrict__ ff, uint8_t* __restrict__ method,
-                          unsigned long long* __restrict__ n_rework, int64_t* __restrict__ rework) {
+                          float4* __restrict__ geo, unsigned long long* __restrict__ n_rework,
+                          int64_t* __restrict__ rework) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_pairs) return;
     const int i = pairs[2 * q], j = pairs[2 * q + 1];
@@ -534,23 +535,25 @@ __global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, 
     }
     ff[q] = 0.5 * log(D2) * UV + lin / D2 + 0.5 * (qq - 2.0 * pq) / D2;
     method[q] = kStokes32;
+    // what the warp-per-pair phi sum needs, rounded once here (FP64 on every lane of a full warp)
+    geo[q] = make_float4((float)D[0], (float)D[1], (float)D[2], (float)(1.0 / D2));
 }
 
-// One pair per warp: ff = |base + 1/2 sum_ab (u_a.v_b) phi(delta_ab)| / (2 pi A_i).
+// One pair per warp, FP32 only: acc = sum_ab (u_a.v_b) phi(delta_ab) over the
+// 256 sample pairs; k_ff_finish forms ff = |base + acc / 2| / (2 pi A_i).
 __global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t* __restrict__ pairs,
-                                                const PatchStokes* __restrict__ pd, const float* __restrict__ pf,
-                                                const double* __restrict__ areas, double* __restrict__ ff,
-                                                uint8_t* __restrict__ method, unsigned long long* __restrict__ n_rework,
+                                                const float4* __restrict__ geo, const float* __restrict__ pf,
+                                                float* __restrict__ acc_out, uint8_t* __restrict__ method,
+                                                unsigned long long* __restrict__ n_rework,
                                                 int64_t* __restrict__ rework) {
     const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (q >= n_pairs) return;
     if (method[q] != kStokes32) return;  // the same for the whole warp
     const int lane = threadIdx.x & 31;
     const int i = pairs[2 * q], j = pairs[2 * q + 1];
-    const double D[3] = {pd[i].c[0] - pd[j].c[0], pd[i].c[1] - pd[j].c[1], pd[i].c[2] - pd[j].c[2]};
-    const double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
-    const float Df[3] = {(float)D[0], (float)D[1], (float)D[2]};
-    const float invD2 = (float)(1.0 / D2);
+    const float4 g = geo[q];
+    const float Df[3] = {g.x, g.y, g.z};
+    const float invD2 = g.w;
     const int a = lane & 15, half = lane >> 4;
     const float4* fi = reinterpret_cast<const float4*>(pf + (size_t)i * kPatchF) + 2 * a;
     const float4 pa = fi[0], ua = fi[1];
@@ -576,7 +579,16 @@ __global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t
         rework[atomicAdd(n_rework, 1ull)] = q;
         return;
     }
-    ff[q] = fabs((ff[q] + 0.5 * (double)acc) / (2 * SP_PI * areas[i]));
+    acc_out[q] = acc;
+}
+
+// One pair per thread: the FP32 Stokes pairs' form factors from the base term and the phi sum.
+__global__ void k_ff_finish(long long n_pairs, const int32_t* __restrict__ pairs, const float* __restrict__ acc,
+                            const double* __restrict__ areas, const uint8_t* __restrict__ method,
+                            double* __restrict__ ff) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs || method[q] != kStokes32) return;
+    ff[q] = fabs((ff[q] + 0.5 * (double)acc[q]) / (2 * SP_PI * areas[pairs[2 * q]]));
 }
 
 // Set-aside pairs, one warp each: FP64 Stokes or the Nusselt analogue.
@@ -736,7 +748,8 @@ int sp_receiver_factors(const double* rcv, int n, const double* centers, const d
 
 size_t sp_form_factors_workspace(int n_patches, long long n_pairs) {
     return sp_align((size_t)n_patches * sizeof(PatchStokes)) + sp_align((size_t)n_patches * kPatchF * 4) +
-           sp_align(((size_t)n_pairs + 1) * 8) + 256;
+           sp_align(((size_t)n_pairs + 1) * 8) + sp_align((size_t)n_pairs * sizeof(float4)) +
+           sp_align((size_t)n_pairs * sizeof(float)) + 256;
 }
 
 int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
@@ -760,14 +773,19 @@ int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32
     q += sp_align((size_t)n_patches * kPatchF * 4);
     int64_t* rework = (int64_t*)q;
     q += sp_align(((size_t)n_pairs + 1) * 8);
+    float4* geo = (float4*)q;
+    q += sp_align((size_t)n_pairs * sizeof(float4));
+    float* acc = (float*)q;
+    q += sp_align((size_t)n_pairs * sizeof(float));
     unsigned long long* n_rework = (unsigned long long*)q;
     cudaMemsetAsync(n_rework, 0, sizeof(unsigned long long), st);
     const long long warps = ((long long)n_patches + 1) / 2;
     k_ff_patch_data<<<sp_blocks(warps * 32, 256), 256, 0, sp_counted(st)>>>(n_patches, pts, pd, pf);
-    k_ff_base<<<sp_blocks(n_pairs, 128), 128, 0, sp_counted(st)>>>(n_pairs, pairs, pts, pd, ff, method, n_rework,
-                                                                  rework);
-    k_ff_phi<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, pd, pf, areas, ff, method,
+    k_ff_base<<<sp_blocks(n_pairs, 128), 128, 0, sp_counted(st)>>>(n_pairs, pairs, pts, pd, ff, method, geo,
+                                                                  n_rework, rework);
+    k_ff_phi<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, geo, pf, acc, method,
                                                                       n_rework, rework);
+    k_ff_finish<<<sp_blocks(n_pairs, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, acc, areas, method, ff);
     unsigned long long count = 0;
     cudaMemcpyAsync(&count, n_rework, sizeof(count), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;

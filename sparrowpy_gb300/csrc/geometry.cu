@@ -603,18 +603,6 @@ __global__ void k_symmetrize(int n, const uint8_t* __restrict__ v, uint8_t* __re
 // (RadiosityFast.py:402-414), incoming index used by the ff_tilde BRDF row
 // (:1264-1268), centre distance (:538-543), the normalised-vector length
 // used for air attenuation (:1252-1262) and F'_ij (:1255-1256).
-// FP64 -> FP32 by truncating the mantissa with integer operations (the
-// conversion instruction runs on GB300's narrow FP64 pipe).  |error| <
-// 2^-23 |x|; |x| < 2^-126 gives a signed zero; |x| >= 2^128 gives NaN.
-__device__ __forceinline__ float f64_trunc_f32(double x) {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-    const unsigned sign = hi & 0x80000000u;
-    if (e <= 0) return __uint_as_float(sign);
-    if (e >= 255) return __uint_as_float(0x7fc00000u);
-    return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
-}
-
 // The reference argmin (sp_nearest_dir) decided in FP32 where that is
 // provably the same index.  With unit direction vectors:
 // * each FP32 unit(diff) component is within 5.1e-7 of the FP64 one (inputs

@@ -722,21 +722,6 @@ class DirectionalRadiosityFast:
                                    source_groups=int(stats[0]), segments=int(stats[1]), pairs=int(stats[2]),
                                    tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order))
 
-    def _resume_exchange(self, c, dt, n_samples, state_in, k_from, k_to, states):
-        """Orders k_from + 1 .. k_to from E_{k_from} = state_in; states[i] receives E_{k_from + i} (no E_total)."""
-        dummy = torch.empty((1,), dtype=state_in.dtype, device=self.device)
-        a = self._exchange_args(c, dt, n_samples, int(k_to), "structured", dummy)
-        a.state_in = state_in.data_ptr()
-        a.state_order = int(k_from)
-        a.states_out = states.data_ptr()
-        a.states_every = 1
-        a.skip_total = 1
-        n, nd, nb = self._dev["e0dir"].shape
-        wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
-                       a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups * a.n_in_dirs)
-        ws = self._workspace(wsz)
-        nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())
-
     def _workspace(self, nbytes):
         ws = self._dev.get("ws")
         if ws is None or ws.numel() < nbytes:
