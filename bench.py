@@ -40,9 +40,10 @@ import numpy as np  # noqa: E402
 
 METRIC = "ms/solve (bake+exchange) ~5.5k patches FP32 vs FP64 GPU; fwd+bwd ms; HBM GB/s"
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
-# DRAM bytes moved per algorithmic byte by one exchange order (scatter + mix),
-# from the ncu capture summarised in profiles/exchange_street_canyon_small.md
-TRAFFIC_PER_ALGO_BYTE = 1.31
+# DRAM bytes moved per algorithmic byte by one exchange order (scatter + mix,
+# averaged over a deferred and a pairing order), from the single-pass ncu
+# capture summarised in profiles/exchange_street_canyon_small.md
+TRAFFIC_PER_ALGO_BYTE = 1.20
 
 
 def parse():

@@ -27,7 +27,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
 }
 // Bounded wait: gives up after kWaitLimit polls (each poll may suspend
 // briefly) or as soon as another CTA has reported a failure.
-constexpr unsigned kWaitLimit = 1u << 16;
+constexpr unsigned kWaitLimit = 1u << 22;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, const volatile int* err) {
     for (unsigned it = 0; it < kWaitLimit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
@@ -35,6 +35,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, const 
     }
     return false;
 }
+// Wait for a CTA's own bulk copies still in flight before it leaves after a
+// failure: bounded, but not cut short by the error flag (the CTA must not
+// exit while a copy can still write into its shared memory).
+__device__ __forceinline__ bool mbar_drain(uint64_t* bar, unsigned parity) {
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Values of the error flag: which bounded wait gave up first.
+constexpr int kErrConsumerWait = 1;  // a consumer warp waiting for a stage's copies
+constexpr int kErrProducerWait = 2;  // the producer waiting for a stage to be released
+constexpr int kErrDrain = 3;         // the drain of a failed CTA's copies in flight
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -158,7 +170,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                     if (s_abort) {
                         halt = 1;
                     } else if (si >= kStages && !mbar_wait(&empty[st], (unsigned)((si / kStages - 1) & 1), err)) {
-                        atomicExch(err, 1);
+                        atomicCAS(err, 0, kErrProducerWait);
                         s_abort = 1;
                         halt = 1;
                     } else {
@@ -191,7 +203,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
             const bool ok = mbar_wait(&full[st], (unsigned)((si / kStages) & 1), err);
             if (!__all_sync(0xffffffffu, ok)) {  // the whole warp leaves together
                 if (lane == 0) {
-                    atomicExch(err, 1);
+                    atomicCAS(err, 0, kErrConsumerWait);
                     s_abort = 1;
                 }
                 break;
@@ -222,11 +234,12 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
     }
     __syncthreads();
     if (s_abort) {
-        // drain: wait (bounded) until every issued copy has landed
+        // drain: wait (bounded) until every issued copy has landed; only the
+        // last kStages stages can still have copies in flight
         if (threadIdx.x == 0) {
             const int issued = s_issued;
             for (int si = issued - 1; si >= 0 && si >= issued - kStages; --si)
-                mbar_wait(&full[si % kStages], (unsigned)((si / kStages) & 1), err);
+                if (!mbar_drain(&full[si % kStages], (unsigned)((si / kStages) & 1))) atomicCAS(err, 0, kErrDrain);
         }
         return;
     }
