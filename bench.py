@@ -67,10 +67,8 @@ def parse():
 
 # ------------------------------------------------------------------- helpers
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from sparrowpy_gb300.replicas import env_ranks
+    return env_ranks()
 
 
 class ClockSampler:
@@ -272,6 +270,7 @@ def run_gpu(args):
     import torch.distributed as dist
     from sparrowpy_gb300 import _native, scenes
 
+    from sparrowpy_gb300.replicas import max_over_ranks
     world, rank, local = dist_env()
     if world > 1:
         dist.init_process_group("nccl", init_method="env://")
@@ -309,11 +308,7 @@ def run_gpu(args):
     barrier()
     launches = _native.lib().sp_kernel_launches() - launches0
     clk = clocks.stop()
-    ms_step = float(np.mean(times))
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
+    ms_step = max_over_ranks(float(np.mean(times)))
 
     # end to end through the public API from host arrays: upload of the
     # scene and materials, bake, source, exchange, receiver histograms back
@@ -333,11 +328,7 @@ def run_gpu(args):
         h2d = int(r2.host_bytes_uploaded)
         d2h = int(mono.nbytes)
         del r2, mono
-    e2e_ms = float(np.mean(e2e_times)) if e2e_times else None
-    if world > 1 and e2e_ms is not None:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(float(np.mean(e2e_times)) if e2e_times else None)
 
     # roofline of one exchange order (scatter + mix launches of that order)
     stats = r.exchange_stats
@@ -385,9 +376,10 @@ def run_gpu(args):
             fwd_bwd = {"error": f"{type(exc).__name__}: {exc}"}
 
     batch = None
-    if args.batch_rooms > 0 and rank == 0:
+    if args.batch_rooms > 0:
+        barrier()
         try:
-            batch = batch_rooms(args.batch_rooms)
+            batch = batch_rooms(args.batch_rooms, rank=rank, world=world)
         except Exception as exc:  # the batch leg must not hide the solve result
             batch = {"error": f"{type(exc).__name__}: {exc}"}
 
@@ -491,17 +483,24 @@ def fwd_bwd_config4(steps=2, fd_params=2, seed=4):
 
 
 # ------------------------------------------------------------------- batch
-def batch_rooms(n_rooms, seed=5):
+def batch_rooms(n_rooms, seed=5, rank=0, world=1):
     """Seeded shoebox rooms, dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, 1 s, order 30,
-    1 source + 4 receivers each, solved one after another; device time per room."""
+    1 source + 4 receivers each.  Rank r of N solves rooms r, r + N, ... one after another; the job's
+    time is the slowest rank's sum of per-room device times."""
     from sparrowpy_gb300.batch import shoebox_rooms, solve_rooms
+    from sparrowpy_gb300.replicas import gather_in_order, max_over_ranks, shard
     rooms = shoebox_rooms(n_rooms, seed=seed)
-    _, ms, patches = solve_rooms(rooms)
+    idx, mine = shard(rooms, rank, world)
+    _, ms, patches = solve_rooms(mine) if mine else ([], [], [])
+    total = max_over_ranks(float(np.sum(ms)))
+    ms = gather_in_order(n_rooms, idx, [float(x) for x in ms])
+    patches = gather_in_order(n_rooms, idx, [int(x) for x in patches])
     return {"workload": f"{n_rooms} seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, "
-                        "T=1000, order 30, 4 receivers), one after another",
+                        f"T=1000, order 30, 4 receivers), dealt round-robin to {world} GPU(s), one after another "
+                        "on each",
             "rooms": n_rooms, "patches_min": int(min(patches)), "patches_mean": float(np.mean(patches)),
-            "patches_max": int(max(patches)), "total_ms": float(np.sum(ms)),
-            "rooms_per_s": float(n_rooms / (np.sum(ms) * 1e-3)), "ms_per_room": [float(x) for x in ms]}
+            "patches_max": int(max(patches)), "total_ms": total,
+            "rooms_per_s": float(n_rooms / (total * 1e-3)), "ms_per_room": ms}
 
 
 # ----------------------------------------------------------- reference arm
