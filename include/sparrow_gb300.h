@@ -95,6 +95,11 @@ size_t sp_point_visibility_workspace(int n_surf);
 int sp_point_visibility(const double* point, int n, const double* centers, int n_surf, int nv,
                         const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws, size_t ws_bytes,
                         void* stream);
+/* The same for n_points points (3 each) in one launch: out (n_points, n),
+ * row p for points[p] (the receivers of one collection). */
+int sp_points_visibility(int n_points, const double* points, int n, const double* centers, int n_surf, int nv,
+                         const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws,
+                         size_t ws_bytes, void* stream);
 
 /* Row-major list of visible pairs (i < j).  Replaces RadiosityFast.py:377-387.
  * row_counts (n) and row_offset (n+1, int64) are outputs; pairs (n_vis, 2)

@@ -86,6 +86,7 @@ _SIGS = {
     "sp_patch_visibility_static": (I, [I, I, P, P, P, P, P]),
     "sp_point_visibility_workspace": (SZ, [I]),
     "sp_point_visibility": (I, [P, I, P, I, I, P, P, P, P, SZ, P]),
+    "sp_points_visibility": (I, [I, P, I, P, I, I, P, P, P, P, SZ, P]),
     "sp_visible_pairs": (I, [I, P, P, P, P, P, P]),
     "sp_count_directed": (I, [I, P, P, P, P, P]),
     "sp_directed_pairs": (I, [I, P, P, P, P, P]),

@@ -226,7 +226,10 @@ __global__ void k_collect_patchwise(int n, int nd, int nb, int nt, const T* __re
 }
 
 // Mono histogram: sum over patches of the patchwise histogram (RadiosityFast.py:592),
-// one thread per (band, bin), compensated summation.
+// one thread per (band, bin).  Each term is (E * r_k) * a_kb, added with one
+// FP64 fma: the terms are non-negative, so the sum of N of them is within
+// N * 2^-53 of exact (7e-13 relative at N = 6000), and the thread does two
+// FP64 operations per patch on GB300's narrow FP64 pipe.
 template <typename T>
 __global__ void k_collect_mono(int n, int nd, int nb, int nt, const T* __restrict__ etot,
                                const int32_t* __restrict__ ridx, const double* __restrict__ coef,
@@ -234,16 +237,12 @@ __global__ void k_collect_mono(int n, int nd, int nb, int nt, const T* __restric
     int b = blockIdx.y;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nt) return;
-    double s = 0.0, comp = 0.0;
+    double s = 0.0;
     for (int k = 0; k < n; ++k) {
         int src_t = t - shift[k];
         if (src_t < 0) src_t += nt;
-        double v = (double)etot[(((size_t)k * nd + ridx[k]) * nb + b) * nt + src_t];
-        double term = (v * coef[(size_t)k * nb + b]) * coef[(size_t)n * nb + (size_t)k * nb + b];
-        double y = term - comp;
-        double tt = s + y;
-        comp = (tt - s) - y;
-        s = tt;
+        const double v = (double)etot[(((size_t)k * nd + ridx[k]) * nb + b) * nt + src_t];
+        s = fma(v * coef[(size_t)k * nb + b], coef[(size_t)n * nb + (size_t)k * nb + b], s);
     }
     out[(size_t)b * nt + t] = s;
 }

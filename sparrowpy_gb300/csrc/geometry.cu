@@ -471,12 +471,16 @@ __global__ void k_vis_exact(long long count, const int64_t* __restrict__ cand, i
 
 // geometry.py:799-839 `_check_point2patch_visibility`: point -> each patch
 // centre, blockers are the given surfaces (walls), tested in index order.
-__global__ void k_point_visibility(const double* __restrict__ point, int n, const double* __restrict__ centers,
-                                   int n_surf, int nv, const double* __restrict__ surf_pts,
-                                   const double* __restrict__ surf_normals, const float* __restrict__ sbox,
-                                   uint8_t* __restrict__ out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// One thread per (point, patch); out is (n_points, n).
+__global__ void k_point_visibility(long long n_points, const double* __restrict__ points, int n,
+                                   const double* __restrict__ centers, int n_surf, int nv,
+                                   const double* __restrict__ surf_pts, const double* __restrict__ surf_normals,
+                                   const float* __restrict__ sbox, uint8_t* __restrict__ out) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_points * n) return;
+    const long long p = q / n;
+    const int i = (int)(q - p * n);
+    const double* point = points + 3 * p;
     double vp[3] = {point[0], point[1], point[2]};
     double ep[3] = {centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]};
     float a[3], d[6];
@@ -495,7 +499,7 @@ __global__ void k_point_visibility(const double* __restrict__ point, int n, cons
         for (int k = 0; k < nv * 3; ++k) sp[k] = surf_pts[(size_t)s * nv * 3 + k];
         visible = exact_visibility(vp, ep, sp, nv, nn);
     }
-    out[i] = visible ? 1 : 0;
+    out[q] = visible ? 1 : 0;
 }
 
 // Row counts of a 0/1 matrix restricted to columns > row (upper) or all
@@ -844,12 +848,12 @@ size_t sp_point_visibility_workspace(int n_surf) {
     return (size_t)n_surf * 6 * sizeof(float) + groups * 6 * sizeof(float) + 256;
 }
 
-int sp_point_visibility(const double* point, int n, const double* centers, int n_surf, int nv,
-                        const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws,
-                        size_t ws_bytes, void* stream) {
-    if (n < 0 || n_surf < 0 || nv < 3 || nv > kMaxVerts) return SP_ERR_ARG;
-    if (n == 0) return SP_OK;
-    if (!point || !centers || !out || (n_surf > 0 && (!surf_pts || !surf_normals || !ws))) return SP_ERR_ARG;
+int sp_points_visibility(int n_points, const double* points, int n, const double* centers, int n_surf, int nv,
+                         const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws,
+                         size_t ws_bytes, void* stream) {
+    if (n_points < 0 || n < 0 || n_surf < 0 || nv < 3 || nv > kMaxVerts) return SP_ERR_ARG;
+    if (n == 0 || n_points == 0) return SP_OK;
+    if (!points || !centers || !out || (n_surf > 0 && (!surf_pts || !surf_normals || !ws))) return SP_ERR_ARG;
     if (n_surf > 0 && ws_bytes < sp_point_visibility_workspace(n_surf)) return SP_ERR_WORKSPACE;
     cudaStream_t st = (cudaStream_t)stream;
     float* sbox = (float*)ws;
@@ -857,9 +861,16 @@ int sp_point_visibility(const double* point, int n, const double* centers, int n
         int n_groups = (n_surf + kGroup - 1) / kGroup;
         k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n_surf, nv, surf_pts, 1e-3f, sbox, sbox + (size_t)n_surf * 6);
     }
-    k_point_visibility<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(point, n, centers, n_surf, nv, surf_pts, surf_normals,
-                                                          sbox, out);
+    const long long total = (long long)n_points * n;
+    k_point_visibility<<<sp_blocks(total, 128), 128, 0, sp_counted(st)>>>(n_points, points, n, centers, n_surf, nv,
+                                                                          surf_pts, surf_normals, sbox, out);
     return sp_check_launch();
+}
+
+int sp_point_visibility(const double* point, int n, const double* centers, int n_surf, int nv,
+                        const double* surf_pts, const double* surf_normals, uint8_t* out, void* ws,
+                        size_t ws_bytes, void* stream) {
+    return sp_points_visibility(1, point, n, centers, n_surf, nv, surf_pts, surf_normals, out, ws, ws_bytes, stream);
 }
 
 int sp_visible_pairs(int n, const uint8_t* vis, int32_t* row_counts, int64_t* row_offset, int32_t* pairs,

@@ -48,6 +48,50 @@ def _stream():
 
 
 _SIDE_STREAMS = {}
+_PREP_POOL = None
+
+
+def _prep_pool():
+    """One host worker thread for BRDF preparation that runs beside the bake's blocking calls."""
+    global _PREP_POOL
+    if _PREP_POOL is None:
+        import concurrent.futures as cf
+        _PREP_POOL = cf.ThreadPoolExecutor(max_workers=1)
+    return _PREP_POOL
+
+
+_COPY_POOL = None
+
+
+def _copy_pool():
+    global _COPY_POOL
+    if _COPY_POOL is None:
+        import concurrent.futures as cf
+        _COPY_POOL = cf.ThreadPoolExecutor(max_workers=4)
+    return _COPY_POOL
+
+
+def _stack_tables(arrays):
+    """np.stack of equally shaped float64 tables, joined in C (np.concatenate along the first axis).
+
+    A scene with one wall per patch has thousands of BRDF slots; np.stack's
+    per-array Python work would dominate its copy.
+    """
+    first = arrays[0]
+    if first.ndim == 0 or any(a.shape != first.shape for a in arrays):
+        raise ValueError("all BRDF tables must have the same shape")
+    n = len(arrays)
+    out = np.empty((n,) + first.shape)
+    flat = out.reshape((n * first.shape[0],) + first.shape[1:])
+    if n < 256:
+        np.concatenate(arrays, axis=0, out=flat)
+        return out
+    # large tables: four chunks in parallel (numpy releases the GIL while it copies)
+    k = first.shape[0]
+    bounds = [(q * n // 4, (q + 1) * n // 4) for q in range(4)]
+    list(_copy_pool().map(lambda ab: np.concatenate(arrays[ab[0]:ab[1]], axis=0, out=flat[ab[0] * k:ab[1] * k]),
+                          bounds))
+    return out
 
 
 def _side_stream(device):
@@ -230,6 +274,7 @@ class DirectionalRadiosityFast:
         self._bake = None   # device state of the last bake
         self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
         self._device_brdf_key = None  # set while device-built tables are installed
+        self._dirs_xyz = None         # rotated direction sets as arrays (set_wall_brdf)
         self.check()
 
     # ------------------------------------------------------------ validation
@@ -315,6 +360,9 @@ class DirectionalRadiosityFast:
             r._brdf_index = self._brdf_index.copy()
             r._brdf_incoming_directions = self._brdf_incoming_directions.copy()
             r._brdf_outgoing_directions = self._brdf_outgoing_directions.copy()
+            a = self._dirs_xyz
+            if a is not None and self._dirs_belong(a):
+                r._dirs_xyz = dict(a, of=(r._brdf_incoming_directions, r._brdf_outgoing_directions))
         return r
 
     # ---------------------------------------------------------- device state
@@ -358,37 +406,39 @@ class DirectionalRadiosityFast:
         key = self._brdf_key()
         if np.any(self._brdf_index < 0):
             raise ValueError("every wall needs a BRDF (set_wall_brdf) before this step")
-        din = np.array([_cart(c).reshape(-1, 3) for c in self._brdf_incoming_directions])
-        dout = np.array([_cart(c).reshape(-1, 3) for c in self._brdf_outgoing_directions])
+        din, dout = self._direction_arrays()
         slots = []
         for b in self._brdf:
             b = np.asarray(b, dtype=float)
             if b.ndim == 1:  # default BRDF: one value per band (RadiosityFast.py:459-467)
                 b = b.reshape(1, 1, -1)
             slots.append(b)
-        brdf = np.stack(slots)
+        brdf = _stack_tables(slots)
         state = dict(key=key, n_in=din.shape[1], n_out=dout.shape[1], n_slots=brdf.shape[0], brdf_host=brdf,
                      dirs_in=self._t(din, torch.float64), dirs_out=self._t(dout, torch.float64),
                      brdf=self._t(brdf, torch.float64), brdf_index=self._t(self._brdf_index, torch.int32))
         self._dev["brdf_state"] = state
         return state
 
-    def _prepare_brdf(self):
+    def _prepare_brdf(self, consumer=None):
         """Device BRDF tables and their diffuse-plus-mirror structure, made on a side stream.
 
-        Stacking, uploading and grouping new tables is host work; issued right
-        after the visibility kernels it runs while they do, since none of it
-        reads the geometry.  The current stream then waits for the side
-        stream, and the tables are recorded as used on it.
+        Stacking, uploading and grouping new tables is host work; bake_geometry
+        runs it in a worker thread while its own thread waits in the
+        visibility and form-factor calls, since none of it reads the geometry.
+        The consumer stream (the one that uses the tables; default: the
+        calling thread's current stream, which a worker thread must be given)
+        then waits for the side stream, and the tables are recorded as used
+        on it.
         """
         if self._brdf_incoming_directions is None:
             return None
         cached = self._cached_brdf()
         if cached is not None and "structure" in cached:
             return cached
-        main = torch.cuda.current_stream(self.device)
+        main = consumer if consumer is not None else torch.cuda.current_stream(self.device)
         side = _side_stream(self.device)
-        with torch.cuda.stream(side):
+        with torch.cuda.device(self.device), torch.cuda.stream(side):
             bs = self._brdf_device()
             self._brdf_structure(bs)
         main.wait_stream(side)
@@ -462,9 +512,12 @@ class DirectionalRadiosityFast:
         vis = torch.empty((n, n), dtype=torch.uint8, device=dev)
         wsz = nat.size("sp_patch_visibility_workspace", n)
         ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=dev)
+        # the BRDF tables are stacked, uploaded and grouped in a host thread on
+        # a side stream while this thread waits in the visibility and
+        # form-factor calls (ctypes and numpy release the GIL there)
+        brdf_job = _prep_pool().submit(self._prepare_brdf, torch.cuda.current_stream(dev))
         nat.call("sp_patch_visibility", n, nv, _ptr(d["centers"]), _ptr(d["normals"]), _ptr(d["pts"]), _ptr(vis),
                  _ptr(ws), wsz, st)
-        bs = self._prepare_brdf()  # host work while the visibility kernels run
         # visible pair list (RadiosityFast.py:377-387)
         cap = max(n * (n - 1) // 2, 1)
         pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
@@ -493,6 +546,7 @@ class DirectionalRadiosityFast:
         nat.call("sp_directed_pairs", n, _ptr(sym), _ptr(dst_off), _ptr(src), _ptr(dst), st)
         del sym
         # per-pair directions, distances and F' (RadiosityFast.py:402-414, 1234-1272, 538-543)
+        bs = brdf_job.result()
         out_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
         in_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
         dist = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
@@ -561,16 +615,19 @@ class DirectionalRadiosityFast:
         for k in ("distance_patches_to_source", "energy_init_source"):
             self._host.pop(k, None)
 
-    def _point_visibility(self, point_dev):
+    def _point_visibility(self, points_dev):
+        """Patch visibility from one point (3,) -> (N,) or from several (P, 3) -> (P, N), walls as blockers."""
         d = self._geometry()
         n = self.n_patches
-        out = torch.empty((max(n, 1),), dtype=torch.uint8, device=self.device)
+        pts = points_dev.reshape(-1, 3).contiguous()
+        n_p = pts.shape[0]
+        out = torch.empty((n_p, max(n, 1)), dtype=torch.uint8, device=self.device)
         nw = self.n_walls
         wsz = nat.size("sp_point_visibility_workspace", nw)
         ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device=self.device)
-        nat.call("sp_point_visibility", _ptr(point_dev), n, _ptr(d["centers"]), nw, self._walls_points.shape[1],
+        nat.call("sp_points_visibility", n_p, _ptr(pts), n, _ptr(d["centers"]), nw, self._walls_points.shape[1],
                  _ptr(d["walls_pts"]), _ptr(d["walls_normal"]), _ptr(out), _ptr(ws), wsz, _stream())
-        return out
+        return out[0] if points_dev.dim() == 1 else out
 
     # -------------------------------------------------------------- exchange
     def _exchange_plan(self):
@@ -827,10 +884,9 @@ class DirectionalRadiosityFast:
         rfac = torch.empty((n_r, n), dtype=torch.float64, device=dev)
         dist = torch.empty((n_r, n), dtype=torch.float64, device=dev)
         rdev = self._t(rc, torch.float64)
+        rvis = self._point_visibility(rdev)  # every receiver in one launch
         for r in range(n_r):
-            rp = rdev[r]
-            rvis = self._point_visibility(rp)
-            nat.call("sp_receiver_factors", _ptr(rp), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(rvis),
+            nat.call("sp_receiver_factors", _ptr(rdev[r]), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(rvis[r]),
                      _ptr(d["wall_of"]), bs["n_out"], _ptr(bs["dirs_out"]), _ptr(rfac[r]), _ptr(ridx[r]),
                      _ptr(dist[r]), st)
         return ridx, rfac, dist
@@ -856,10 +912,42 @@ class DirectionalRadiosityFast:
                                                    incoming_directions, outgoing_directions)
             self._brdf_incoming_directions[i] = inc
             self._brdf_outgoing_directions[i] = out
+            self._note_wall_dirs(int(i), inc, out)
         self._brdf.append(np.asarray(brdf.freq, dtype=float) * np.pi)
         self._brdf_index[np.atleast_1d(wall_indexes)] = len(self._brdf) - 1
         self._dev.pop("brdf_state", None)
         self._device_brdf_key = None
+
+    def _note_wall_dirs(self, i, inc, out):
+        """Keep (n_walls, n, 3) arrays of the rotated direction sets beside the Coordinates objects.
+
+        They belong to the object arrays they were made for (held and compared
+        by identity), so an assignment of new direction sets leaves them
+        unused.
+        """
+        cin, cout = _cart(inc).reshape(-1, 3), _cart(out).reshape(-1, 3)
+        a = self._dirs_xyz
+        mine = a is not None and self._dirs_belong(a)
+        if not mine or a["in"].shape[1:] != cin.shape or a["out"].shape[1:] != cout.shape:
+            if mine and a["set"].any():
+                self._dirs_xyz = None  # direction sets of different sizes: stacked from the objects
+                return
+            nw = self.n_walls
+            a = dict(of=(self._brdf_incoming_directions, self._brdf_outgoing_directions), set=np.zeros(nw, dtype=bool),
+                     **{"in": np.zeros((nw,) + cin.shape), "out": np.zeros((nw,) + cout.shape)})
+            self._dirs_xyz = a
+        a["in"][i], a["out"][i], a["set"][i] = cin, cout, True
+
+    def _dirs_belong(self, a):
+        return a["of"][0] is self._brdf_incoming_directions and a["of"][1] is self._brdf_outgoing_directions
+
+    def _direction_arrays(self):
+        """(n_walls, n_in, 3) and (n_walls, n_out, 3) rotated direction sets."""
+        a = self._dirs_xyz
+        if a is not None and self._dirs_belong(a) and a["set"].all():
+            return a["in"], a["out"]
+        return (np.array([_cart(c).reshape(-1, 3) for c in self._brdf_incoming_directions]),
+                np.array([_cart(c).reshape(-1, 3) for c in self._brdf_outgoing_directions]))
 
     def _check_set_frequency(self, frequencies):
         frequencies = np.atleast_1d(np.asarray(frequencies))
