@@ -108,6 +108,18 @@ class Coordinates:
         c._weights = None if self._weights is None else self._weights.copy()
         return c
 
+    def __eq__(self, other):
+        """Equal points and weights (content, as pyfar compares Coordinates)."""
+        if not isinstance(other, Coordinates):
+            return NotImplemented
+        if self._pts.shape != other._pts.shape or not np.array_equal(self._pts, other._pts):
+            return False
+        if (self._weights is None) != (other._weights is None):
+            return False
+        return self._weights is None or np.array_equal(self._weights, other._weights)
+
+    __hash__ = None
+
     def __getitem__(self, idx):
         c = Coordinates()
         c._pts = np.atleast_2d(self._pts[idx])

@@ -535,6 +535,20 @@ class DirectionalRadiosityFast:
         nat.call("sp_form_factors", _PREC[self.precision], n, n_vis, _ptr(pairs), _ptr(d["pts"]), _ptr(d["normals"]),
                  _ptr(d["areas"]), _ptr(ff), _ptr(method), _ptr(fws), fsz, st)
         del fws
+        self._bake_pairs(vis, pairs, pair_index, n_vis, ff, method, brdf_job.result)
+        for k in ("visibility_matrix", "visible_patches", "form_factors", "form_factors_tilde",
+                  "patch_2_brdf_outgoing_index"):
+            self._host.pop(k, None)
+
+    def _bake_pairs(self, vis, pairs, pair_index, n_vis, ff, method, brdf_state):
+        """The bake after visibility and form factors: directed pairs, their directions, distances and F'.
+
+        brdf_state: a callable giving the device BRDF state (or None).
+        """
+        d = self._geometry()
+        n = self.n_patches
+        st = _stream()
+        dev = self.device
         # directed pairs, destination-major (RadiosityFast.py:1124-1131)
         sym = torch.empty((n, n), dtype=torch.uint8, device=dev)
         dcounts = torch.empty((max(n, 1),), dtype=torch.int32, device=dev)
@@ -546,7 +560,7 @@ class DirectionalRadiosityFast:
         nat.call("sp_directed_pairs", n, _ptr(sym), _ptr(dst_off), _ptr(src), _ptr(dst), st)
         del sym
         # per-pair directions, distances and F' (RadiosityFast.py:402-414, 1234-1272, 538-543)
-        bs = brdf_job.result()
+        bs = brdf_state()
         out_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
         in_dir = torch.zeros((max(n_dir, 1),), dtype=torch.int32, device=dev)
         dist = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
@@ -563,9 +577,36 @@ class DirectionalRadiosityFast:
                           dst_off=dst_off, src=src, dst=dst, n_dir=n_dir, out_dir=out_dir, in_dir=in_dir, dist=dist,
                           unit_len=unit_len, fprime=fprime, brdf=bs, att=att, n_bins=n_bins,
                           n_out=bs["n_out"] if bs else 1)
-        for k in ("visibility_matrix", "visible_patches", "form_factors", "form_factors_tilde",
-                  "patch_2_brdf_outgoing_index"):
-            self._host.pop(k, None)
+
+    def _restore_bake(self):
+        """Device bake state from a visibility matrix and form factors held on the host (from_dict / from_read).
+
+        The reference restores those attributes and exchanges without baking
+        again; here the visible pairs, directed pairs and pair set-up are
+        rebuilt from them (the O(N^3) visibility and the form factors are
+        not recomputed).  Returns False when the host does not hold both.
+        """
+        vis_h = self._host.get("visibility_matrix")
+        ff_h = self._host.get("form_factors")
+        n = self.n_patches
+        if vis_h is None or ff_h is None or np.shape(vis_h) != (n, n) or np.shape(ff_h) != (n, n):
+            return False
+        dev = self.device
+        st = _stream()
+        vis = self._t(np.triu(np.asarray(vis_h, dtype=bool), 1).astype(np.uint8), torch.uint8)
+        cap = max(n * (n - 1) // 2, 1)
+        pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+        pair_index = torch.full((n, n), -1, dtype=torch.int32, device=dev)
+        row_counts = torch.empty((max(n, 1),), dtype=torch.int32, device=dev)
+        row_off = torch.empty((n + 1,), dtype=torch.int64, device=dev)
+        nat.call("sp_visible_pairs", n, _ptr(vis), _ptr(row_counts), _ptr(row_off), _ptr(pairs), _ptr(pair_index), st)
+        n_vis = int(row_off[n].item()) if n > 0 else 0
+        pairs = pairs[:n_vis].contiguous()
+        ij = pairs.cpu().numpy()
+        ff = self._t(np.asarray(ff_h, dtype=float)[ij[:, 0], ij[:, 1]] if n_vis else np.zeros(1), torch.float64)
+        method = torch.zeros((max(n_vis, 1),), dtype=torch.uint8, device=dev)
+        self._bake_pairs(vis, pairs, pair_index, n_vis, ff, method, self._brdf_device)
+        return True
 
     # ---------------------------------------------------------------- source
     def init_source_energy(self, source):
@@ -631,6 +672,8 @@ class DirectionalRadiosityFast:
 
     # -------------------------------------------------------------- exchange
     def _exchange_plan(self):
+        if self._bake is None:
+            self._restore_bake()
         bk = self._bake
         if bk is None:
             raise ValueError("bake_geometry() must run before calculate_energy_exchange()")
@@ -700,8 +743,8 @@ class DirectionalRadiosityFast:
         return a
 
     def _exchange_args(self, c, dt, n_samples, max_order, algorithm, etc):
+        plan = self._exchange_plan()  # restores the bake from host state where needed
         bk = self._bake
-        plan = self._exchange_plan()
         d = self._geometry()
         e0dir, d0 = self._dev["e0dir"], self._dev["d0"]
         n, nd, nb = e0dir.shape
@@ -958,9 +1001,26 @@ class DirectionalRadiosityFast:
             assert (self._frequencies == frequencies).all(), "Frequencies do not match"
 
     # ------------------------------------------------------------ state I/O
-    def to_dict(self) -> dict:
-        """Convert the object to a dictionary (RadiosityFast.py:841-873)."""
-        out = {
+    def write(self, filename, compress=True):
+        """Write the object to a state file (RadiosityFast.py:828-830): a zip of npy and JSON members (far.py)."""
+        from . import far
+        far.write(filename, self._state_values(), compress=compress)
+
+    @classmethod
+    def from_read(cls, filename, **kwargs):
+        """Read an object from a state file (RadiosityFast.py:832-839); kwargs: precision, device.
+
+        A file that holds the visibility matrix and the form factors needs no
+        bake_geometry() before the next exchange.
+        """
+        from . import far
+        data = far.read(filename)
+        data = {k: (None if isinstance(v, str) and v == 'None' else v) for k, v in data.items()}
+        return cls(**data, **kwargs)
+
+    def _state_values(self):
+        """The to_dict entries with arrays kept as arrays."""
+        return {
             'walls_points': self._walls_points, 'walls_normal': self._walls_normal,
             'walls_up_vector': self._walls_up_vector, 'patches_points': self._patches_points,
             'n_patches': self._n_patches, 'patch_to_wall_ids': self._patch_to_wall_ids,
@@ -975,6 +1035,10 @@ class DirectionalRadiosityFast:
             'distance_patches_to_source': self._distance_patches_to_source,
             'energy_init_source': self._energy_init_source, 'energy_exchange_etc': self._energy_exchange_etc,
         }
+
+    def to_dict(self) -> dict:
+        """Convert the object to a dictionary (RadiosityFast.py:841-873)."""
+        out = self._state_values()
         for key, value in out.items():
             if value is None:
                 out[key] = 'None'

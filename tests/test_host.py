@@ -149,3 +149,43 @@ def test_material_tables_reproduce_create_from_scattering():
         ref = np.asarray(create_from_scattering(dirs, dirs, FrequencyData(scat[k], freqs),
                                                 FrequencyData(alpha[k], freqs)).freq) * np.pi
         np.testing.assert_allclose(tabs[k], ref, rtol=1e-13, atol=1e-15)
+
+
+def test_state_file_round_trip(tmp_path):
+    """write / from_read (RadiosityFast.py:828-839) keep every host input, direction sets included."""
+    r = sp.DirectionalRadiosityFast.from_polygon(sp.shoebox_room_stub(2, 3, 2), 1.0)
+    d = hemisphere_directions(4)
+    f = np.array([500.0, 1000.0])
+    r.set_wall_brdf(np.arange(3), create_from_scattering(d, d, FrequencyData([0.5, 0.4], f)), d, d)
+    r.set_wall_brdf(np.arange(3, 6), create_from_scattering(d, d, FrequencyData([0.2, 0.1], f)), d, d)
+    r.set_air_attenuation(FrequencyData([0.001, 0.002], f))
+    r.write(tmp_path / "state.far")
+    r2 = sp.DirectionalRadiosityFast.from_read(tmp_path / "state.far")
+    assert r2 == r
+    for a, b in zip(r._brdf_outgoing_directions, r2._brdf_outgoing_directions):
+        np.testing.assert_array_equal(np.asarray(a.cartesian), np.asarray(b.cartesian))
+        np.testing.assert_array_equal(a.weights, b.weights)
+    assert len(r2._brdf) == 2 and r2._brdf_index.tolist() == r._brdf_index.tolist()
+
+
+def test_state_file_reads_ndarray_and_builtin_members(tmp_path):
+    """A pyfar-style file holding only ndarray and builtin members (the reference's own layout) reads back."""
+    import io
+    import json
+    import zipfile
+    from sparrowpy_gb300 import far
+    arr = np.arange(12.0).reshape(3, 4)
+    buf = io.BytesIO()
+    np.save(buf, arr)
+    path = tmp_path / "plain.far"
+    with zipfile.ZipFile(path, "w") as z:
+        z.writestr("E_matrix/$ndarray", buf.getvalue())
+        z.writestr("builtin_wrapper/$BuiltinsWrapper", json.dumps({"pyfar.__version__": "0.6.5", "c": 343.0,
+                                                                   "note": "None"}))
+    vals = far.read(path)
+    np.testing.assert_array_equal(vals["E_matrix"], arr)
+    assert vals["c"] == 343.0 and vals["note"] == "None"
+    with zipfile.ZipFile(path, "a") as z:
+        z.writestr("src/$Coordinates", b"{}")
+    with pytest.raises(NotImplementedError):
+        far.read(path)
