@@ -2,7 +2,7 @@
 
 Drop-in for ``sparrowpy.DirectionalRadiosityFast``; see radiosity.py.
 """
-from . import brdf, geometry
+from . import brdf, geometry, sound_object
 from .coords import Coordinates, FrequencyData, TimeData
 from .geometry import Polygon, shoebox_room_stub
 from .radiosity import DirectionalRadiosityFast, analyse_brdf
@@ -11,5 +11,5 @@ __version__ = "0.1.0"
 
 __all__ = [
     "DirectionalRadiosityFast", "Polygon", "shoebox_room_stub", "Coordinates", "FrequencyData", "TimeData",
-    "brdf", "geometry", "analyse_brdf",
+    "brdf", "geometry", "sound_object", "analyse_brdf",
 ]
