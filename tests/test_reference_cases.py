@@ -470,3 +470,39 @@ def test_plane_without_visible_pairs_keeps_source_energy(precision):
         out.append(r.collect_energy_receiver_mono(Coordinates(-0.5, 0.7, 1.5)).time)
     assert np.sum(out[0]) > 0
     np.testing.assert_array_equal(out[0], out[1])
+
+
+@pytest.mark.gpu
+def test_source_delay_beyond_histogram_raises_index_error():
+    """The reference writes E0 at bin int(d0 / c / dt) (RadiosityFast.py:1037-1070); past the end: IndexError."""
+    from sparrowpy_gb300 import DirectionalRadiosityFast
+    from sparrowpy_gb300.coords import Coordinates
+    from sparrowpy_gb300.geometry import shoebox_room_stub
+    r = DirectionalRadiosityFast.from_polygon(shoebox_room_stub(1, 1, 1), 0.5)
+    r.bake_geometry()
+    r.init_source_energy(Coordinates(0.5, 0.5, 0.5))
+    with pytest.raises(IndexError):
+        r.calculate_energy_exchange(343, 1e-3, 1e-3, 2, recalculate=True)  # one bin; delays are >= 1 bin
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_long_histogram_takes_dense_exchange(precision):
+    """More than 65535 bins: the structured kernels' 16-bit delays do not reach; "auto" runs the dense
+    exchange, which matches the oracle (rel L2 <= 1e-10 FP64, 1e-4 FP32)."""
+    from conftest import load_golden, radiosity_from_golden, rel_l2, scene_from_golden
+    from oracle import oracle as orc
+    from sparrowpy_gb300.coords import Coordinates
+    g = load_golden("cube")
+    c, dt, duration, k = 343.0, 1e-5, 0.7, 2  # 70000 bins
+    ref = orc.solve(scene_from_golden(g), g["source"], np.atleast_2d(g["receivers"]), c, dt, duration, k)
+    r = radiosity_from_golden(g, precision)
+    r.bake_geometry()
+    r.init_source_energy(Coordinates(*g["source"]))
+    r.calculate_energy_exchange(c, dt, duration, k)
+    assert r.exchange_stats["algorithm"] == "dense"
+    rcv = np.atleast_2d(g["receivers"])
+    mono = r.collect_energy_receiver_mono(Coordinates(rcv[:, 0], rcv[:, 1], rcv[:, 2])).time
+    assert rel_l2(mono, ref["mono"]) <= (1e-10 if precision == "fp64" else 1e-4)
+    with pytest.raises(ValueError):
+        r.calculate_energy_exchange(c, dt, duration, k, recalculate=True, algorithm="structured")
