@@ -270,37 +270,13 @@ __global__ void __launch_bounds__(256) k_patch_visibility(int n, int nv, const d
 // Patch visibility in steps that keep the FP64 predicate on full warps:
 // k_vis_self (the pair's own patches as blockers), then k_vis_cull (one
 // 16 x 16 pair tile per block, one pair per thread) writes, after the FP32
-// box culling, the (pair, blocker) candidates to a buffer, each block reserving a slice
-// with one atomic; k_vis_exact evaluates one candidate per thread and clears
-// the pair when the blocker hides it (visibility is the AND over blockers,
-// so the order of evaluation does not change the result).  A block whose
-// slice does not fit records its tile and is culled again in a later round.
+// box culling, the (pair, blocker) candidates to a buffer, each warp
+// reserving room per blocker group with one atomic; k_vis_exact evaluates
+// one candidate per thread and clears the pair when the blocker hides it
+// (visibility is the AND over blockers, so the order of evaluation does not
+// change the result).  A tile whose candidates do not all fit is culled
+// again in a later round.
 constexpr int kCandBits = 20;  // i, j, s < 2^20
-// Box hits of one segment against blocker groups g0 .. g0 + cnt - 1, the
-// pair's own patches excluded (one compiled copy, so the counting and the
-// writing pass agree); writes at most `limit` candidates when `out` is given.
-__device__ __noinline__ int vis_cull_pair(bool active, const float* a, const float* d, const float* gb, int g0,
-                                          int cnt, int n, const float* __restrict__ box, int64_t code, int64_t* out,
-                                          int limit, int self_i, int self_j) {
-    int hits = 0;
-    if (!active) return 0;
-    for (int g = 0; g < cnt; ++g) {
-        if (!seg_hits_box(a, d, gb + 6 * g, gb + 6 * g + 3)) continue;
-        const int s_end = min(n, (g0 + g + 1) * kGroup);
-        for (int s = (g0 + g) * kGroup; s < s_end; ++s) {
-            const float* bx = box + 6 * s;
-            float lo[3] = {bx[0], bx[1], bx[2]}, hi[3] = {bx[3], bx[4], bx[5]};
-            if (s == self_i || s == self_j || !seg_hits_box(a, d, lo, hi)) continue;
-            if (out) {
-                if (hits >= limit) return hits;
-                out[hits] = code | s;
-            }
-            ++hits;
-        }
-    }
-    return hits;
-}
-
 // Per patch: whether its centre lies inside it (the winding test of
 // `_point_in_polygon`) and within eta of its plane, each in the reference
 // predicate's arithmetic.  Both hold for every non-degenerate patch.
@@ -383,6 +359,13 @@ __global__ void __launch_bounds__(256) k_vis_self(int n, int nv, const int32_t* 
     vis[(size_t)i * n + j] = visible ? 1 : 0;
 }
 
+// One pass: the warps of a 16 x 16 pair tile walk the blocker groups
+// together.  Per group, a lane whose segment meets the group's box tests its
+// 32 blockers (bit mask of box hits, the pair's own patches left out); the
+// warp then reserves room for all its lanes' hits with one atomic (shuffle
+// prefix sum) and writes them.  A reservation that would pass `cap` is not
+// written and marks the tile for the next round, where it is culled again
+// in full (candidates written twice are harmless: visibility is an AND).
 __global__ void __launch_bounds__(256) k_vis_cull(int n, const int32_t* __restrict__ tiles,
                                                   const double* __restrict__ centers, const float* __restrict__ box,
                                                   const float* __restrict__ gbox, int n_groups,
@@ -390,12 +373,12 @@ __global__ void __launch_bounds__(256) k_vis_cull(int n, const int32_t* __restri
                                                   long long cap, unsigned long long* __restrict__ counter,
                                                   int32_t* __restrict__ overflow, int* __restrict__ n_overflow) {
     extern __shared__ float s_gbox[];
-    __shared__ int s_scan[256];
-    __shared__ long long s_base;
+    __shared__ int s_over;
     const int tile = tiles[blockIdx.x];
     const int tile_i = tile >> 16, tile_j = tile & 0xffff;
     const int i = tile_i * 16 + (threadIdx.x >> 4);
     const int j = tile_j * 16 + (threadIdx.x & 15);
+    const int lane = threadIdx.x & 31;
     // pairs the own-patch pass (k_vis_self) already hid need no candidates
     const bool active = (i < n) && (j < n) && (i < j) && vis[(size_t)i * n + j] != 0;
     float a[3] = {0, 0, 0}, d[6] = {0, 0, 0, 0, 0, 0};
@@ -407,45 +390,48 @@ __global__ void __launch_bounds__(256) k_vis_cull(int n, const int32_t* __restri
         seg_reciprocals(d);
     }
     const int64_t code = ((int64_t)i << (2 * kCandBits)) | ((int64_t)j << kCandBits);
-    // pass 1: count
-    int hits = 0;
+    if (threadIdx.x == 0) s_over = 0;
     for (int g0 = 0; g0 < n_groups; g0 += 1024) {
         const int cnt = min(1024, n_groups - g0);
         __syncthreads();
         for (int t = threadIdx.x; t < cnt * 6; t += blockDim.x) s_gbox[t] = gbox[6 * g0 + t];
         __syncthreads();
-        hits += vis_cull_pair(active, a, d, s_gbox, g0, cnt, n, box, code, nullptr, 0, i, j);
-    }
-    // block prefix sum and one reservation
-    s_scan[threadIdx.x] = hits;
-    __syncthreads();
-    for (int off = 1; off < 256; off <<= 1) {
-        const int x = threadIdx.x >= (unsigned)off ? s_scan[threadIdx.x - off] : 0;
-        __syncthreads();
-        s_scan[threadIdx.x] += x;
-        __syncthreads();
-    }
-    if (threadIdx.x == 255) {
-        const long long total = s_scan[255];
-        long long base = total > 0 ? (long long)atomicAdd(counter, (unsigned long long)total) : 0;
-        if (base + total > cap) {
-            overflow[atomicAdd(n_overflow, 1)] = tile;
-            base = -1;
+        for (int g = 0; g < cnt; ++g) {
+            const int s0 = (g0 + g) * kGroup;
+            uint32_t mask = 0;
+            if (active && seg_hits_box(a, d, s_gbox + 6 * g, s_gbox + 6 * g + 3)) {
+                const int s_end = min(n, s0 + kGroup);
+                for (int s = s0; s < s_end; ++s) {
+                    const float* bx = box + 6 * s;
+                    const float lo[3] = {bx[0], bx[1], bx[2]}, hi[3] = {bx[3], bx[4], bx[5]};
+                    if (s != i && s != j && seg_hits_box(a, d, lo, hi)) mask |= 1u << (s - s0);
+                }
+            }
+            if (__ballot_sync(0xffffffffu, mask != 0u) == 0u) continue;  // the same for the whole warp
+            const int h = __popc(mask);
+            int incl = h;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += y;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            unsigned long long base = 0;
+            if (lane == 31) base = atomicAdd(counter, (unsigned long long)total);
+            base = __shfl_sync(0xffffffffu, base, 31);
+            if (base + (unsigned long long)total > (unsigned long long)cap) {
+                if (lane == 0) s_over = 1;
+                continue;
+            }
+            long long pos = (long long)base + incl - h;
+            while (mask) {
+                const int b = __ffs(mask) - 1;
+                mask &= mask - 1u;
+                cand[pos++] = code | (int64_t)(s0 + b);
+            }
         }
-        s_base = base;
     }
     __syncthreads();
-    const long long base = s_base;
-    if (base < 0 || hits == 0) return;  // no further barriers below
-    int64_t* out = cand + base + (s_scan[threadIdx.x] - hits);
-    // pass 2: write (the group boxes are read from global memory here)
-    int left = hits;
-    for (int g0 = 0; g0 < n_groups && left > 0; g0 += 1024) {
-        const int cnt = min(1024, n_groups - g0);
-        const int w = min(left, vis_cull_pair(active, a, d, gbox + 6 * g0, g0, cnt, n, box, code, out, left, i, j));
-        out += w;
-        left -= w;
-    }
+    if (threadIdx.x == 0 && s_over) overflow[atomicAdd(n_overflow, 1)] = tile;
 }
 
 __global__ void k_vis_exact(long long count, const int64_t* __restrict__ cand, int n, int nv,
