@@ -127,6 +127,105 @@ __device__ bool exact_visibility(const double* vp, const double* ep, const doubl
     return !(fabs(xdot3(a, n)) < eta && fabs(xdot3(b, n)) < eta);
 }
 
+// The blocker-only part of point_in_polygon, computed once per patch with
+// the same FP64 operations: the first two rows of the rotation to the
+// horizontal plane, the rotated vertices, and per edge the unit normal nl
+// and the length |a1 - a0|.
+struct PolyPre {
+    double r[6];
+    double a[kMaxVerts][2];
+    double nl[kMaxVerts][2];
+    double ns[kMaxVerts];
+};
+
+__device__ void poly_pre(const double* poly3, int nv, const double* n, PolyPre& P) {
+    double rot[9];
+    rotation_matrix(n, rot);
+    for (int k = 0; k < 6; ++k) P.r[k] = rot[k];
+    for (int i = 0; i < nv; ++i) {
+        P.a[i][0] = xdot3(rot, poly3 + 3 * i);
+        P.a[i][1] = xdot3(rot + 3, poly3 + 3 * i);
+    }
+    for (int i = 0; i < nv; ++i) {
+        const double* a1 = P.a[(i + 1) % nv];
+        const double* a0 = P.a[i];
+        const double side[2] = {xsub(a1[0], a0[0]), xsub(a1[1], a0[1])};
+        const double ns = xnorm2(side);
+        P.ns[i] = ns;
+        P.nl[i][0] = xdiv(-side[1], ns);
+        P.nl[i][1] = xdiv(side[0], ns);
+    }
+}
+
+// point_in_polygon with the blocker part from poly_pre (bit-identical).
+__device__ bool point_in_polygon_pre(const double* p3, const double* v0, const double* n, const PolyPre& P, int nv) {
+    const double eta = 1e-6;
+    const double d0[3] = {xsub(p3[0], v0[0]), xsub(p3[1], v0[1]), xsub(p3[2], v0[2])};
+    if (fabs(xdot3(d0, n)) > eta) return false;
+    const double pt[2] = {xdot3(P.r, p3), xdot3(P.r + 3, p3)};
+    int count = 0;
+    for (int i = 0; i < nv; ++i) {
+        const double* a1 = P.a[(i + 1) % nv];
+        const double* a0 = P.a[i];
+        const double* nl = P.nl[i];
+        const double point[2] = {xadd(pt[0], 1.0), xadd(pt[1], 0.0)};
+        const double v[2] = {xsub(point[0], pt[0]), xsub(point[1], pt[1])};
+        const double dp = xdot2(v, nl);
+        if (!(fabs(dp) > 1e-6)) continue;
+        const double w[2] = {xsub(point[0], a1[0]), xsub(point[1], a1[1])};
+        const double fac = -xdiv(xdot2(nl, w), dp);
+        const double b[2] = {xadd(xadd(w[0], a1[0]), xmul(fac, v[0])), xadd(xadd(w[1], a1[1]), xmul(fac, v[1]))};
+        if (b[0] > pt[0]) {
+            const double ba0[2] = {xsub(b[0], a0[0]), xsub(b[1], a0[1])};
+            const double ba1[2] = {xsub(b[0], a1[0]), xsub(b[1], a1[1])};
+            if (fabs(xsub(xadd(xnorm2(ba0), xnorm2(ba1)), P.ns[i])) <= eta) {
+                const double bp[2] = {xsub(b[0], pt[0]), xsub(b[1], pt[1])};
+                const double sgn = xdot2(bp, nl);
+                if (sgn > 0)
+                    count += 1;
+                else if (sgn < 0)
+                    count -= 1;
+            }
+        }
+    }
+    return count != 0;
+}
+
+// exact_visibility with the blocker part from poly_pre (bit-identical); v0 =
+// the blocker's first vertex.
+__device__ bool exact_visibility_pre(const double* vp, const double* ep, const double* v0, const double* n,
+                                     const PolyPre& P, int nv) {
+    const double eta = 1e-6;
+    const bool vis_in = point_in_polygon_pre(vp, v0, n, P, nv);
+    const bool eval_in = point_in_polygon_pre(ep, v0, n, P, nv);
+    if (!vis_in && !eval_in) {
+        const double v[3] = {xsub(ep[0], vp[0]), xsub(ep[1], vp[1]), xsub(ep[2], vp[2])};
+        const double dp = xdot3(v, n);
+        if (fabs(dp) > 1e-6) {
+            const double w[3] = {xsub(ep[0], v0[0]), xsub(ep[1], v0[1]), xsub(ep[2], v0[2])};
+            const double fac = -xdiv(xdot3(n, w), dp);
+            double pt[3];
+            for (int d = 0; d < 3; ++d) pt[d] = xadd(xadd(w[d], v0[d]), xmul(fac, v[d]));
+            if (point_in_polygon_pre(pt, v0, n, P, nv)) {
+                const double a[3] = {xsub(pt[0], vp[0]), xsub(pt[1], vp[1]), xsub(pt[2], vp[2])};
+                const double b[3] = {xsub(pt[0], ep[0]), xsub(pt[1], ep[1]), xsub(pt[2], ep[2])};
+                if (xdot3(a, b) < 0) return false;
+            }
+        }
+        return true;
+    }
+    if (vis_in && !eval_in) {
+        const double d[3] = {xsub(ep[0], vp[0]), xsub(ep[1], vp[1]), xsub(ep[2], vp[2])};
+        if (xdot3(n, d) < 0) return false;
+    } else if (!vis_in && eval_in) {
+        const double d[3] = {xsub(vp[0], ep[0]), xsub(vp[1], ep[1]), xsub(vp[2], ep[2])};
+        if (xdot3(n, d) < 0) return false;
+    }
+    const double a[3] = {xsub(vp[0], v0[0]), xsub(vp[1], v0[1]), xsub(vp[2], v0[2])};
+    const double b[3] = {xsub(ep[0], v0[0]), xsub(ep[1], v0[1]), xsub(ep[2], v0[2])};
+    return !(fabs(xdot3(a, n)) < eta && fabs(xdot3(b, n)) < eta);
+}
+
 // Conservative segment/box overlap in FP32.  Boxes are already enlarged by a
 // margin that covers the predicate's 1e-6 tolerances and the FP32 rounding
 // of the segment end points, so a miss here proves the exact predicate
@@ -434,9 +533,23 @@ __global__ void __launch_bounds__(256) k_vis_cull(int n, const int32_t* __restri
     if (threadIdx.x == 0 && s_over) overflow[atomicAdd(n_overflow, 1)] = tile;
 }
 
+// Per patch: the blocker part of the predicate (poly_pre).
+__global__ void k_poly_pre(int n, int nv, const double* __restrict__ normals, const double* __restrict__ pts,
+                           PolyPre* __restrict__ pre) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    double nn[3] = {normals[3 * s], normals[3 * s + 1], normals[3 * s + 2]};
+    double sp[kMaxVerts * 3];
+    for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)s * nv * 3 + q];
+    PolyPre P;
+    poly_pre(sp, nv, nn, P);
+    pre[s] = P;
+}
+
 __global__ void k_vis_exact(long long count, const int64_t* __restrict__ cand, int n, int nv,
                             const double* __restrict__ centers, const double* __restrict__ normals,
-                            const double* __restrict__ pts, uint8_t* __restrict__ vis) {
+                            const double* __restrict__ pts, const PolyPre* __restrict__ pre,
+                            uint8_t* __restrict__ vis) {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
     const int64_t c = cand[k];
@@ -445,14 +558,14 @@ __global__ void k_vis_exact(long long count, const int64_t* __restrict__ cand, i
     const int i = (int)(c >> (2 * kCandBits)), j = (int)((c >> kCandBits) & mask), s = (int)(c & mask);
     uint8_t* v = vis + (size_t)i * n + j;
     if (*v == 0) return;  // already hidden by another blocker
-    double ci[3], cj[3], nn[3], sp[kMaxVerts * 3];
+    double ci[3], cj[3], nn[3], v0[3];
     for (int q = 0; q < 3; ++q) {
         ci[q] = centers[3 * i + q];
         cj[q] = centers[3 * j + q];
         nn[q] = normals[3 * s + q];
+        v0[q] = pts[(size_t)s * nv * 3 + q];
     }
-    for (int q = 0; q < nv * 3; ++q) sp[q] = pts[(size_t)s * nv * 3 + q];
-    if (!exact_visibility(ci, cj, sp, nv, nn)) *v = 0;
+    if (!exact_visibility_pre(ci, cj, v0, nn, pre[s], nv)) *v = 0;
 }
 
 // geometry.py:799-839 `_check_point2patch_visibility`: point -> each patch
@@ -768,7 +881,7 @@ size_t sp_patch_visibility_workspace(int n) {
     size_t groups = ((size_t)n + kGroup - 1) / kGroup;
     return sp_align((size_t)n * 6 * sizeof(float) + groups * 6 * sizeof(float)) +
            sp_align((size_t)vis_cand_capacity(n) * 8) + 2 * sp_align((size_t)vis_tile_count(n) * 4) +
-           sp_align((size_t)n) + 256;
+           sp_align((size_t)n) + sp_align((size_t)n * sizeof(PolyPre)) + 256;
 }
 
 int sp_patch_visibility(int n, int nv, const double* centers, const double* normals, const double* pts,
@@ -794,6 +907,8 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
     q += sp_align((size_t)n_tiles * 4);
     uint8_t* own_ok = (uint8_t*)q;
     q += sp_align((size_t)n);
+    PolyPre* pre = (PolyPre*)q;
+    q += sp_align((size_t)n * sizeof(PolyPre));
     unsigned long long* counter = (unsigned long long*)q;
     int* n_overflow = (int*)(q + 8);
     k_blocker_boxes<<<n_groups, kGroup, 0, sp_counted(st)>>>(n, nv, pts, 1e-3f, box, gbox);
@@ -807,6 +922,7 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
     cudaMemcpyAsync(list[0], h_tiles.data(), h_tiles.size() * 4, cudaMemcpyHostToDevice, st);
     long long todo = (long long)h_tiles.size();
     k_own_patch<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(n, nv, centers, normals, pts, own_ok);
+    k_poly_pre<<<sp_blocks(n, 128), 128, 0, sp_counted(st)>>>(n, nv, normals, pts, pre);
     k_vis_self<<<(unsigned)todo, 256, 0, sp_counted(st)>>>(n, nv, list[0], centers, normals, pts, own_ok, vis);
     int cur = 0;
     for (int round = 0; todo > 0; ++round) {
@@ -821,7 +937,7 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
         const int overflowed = (int)(h[1] & 0xffffffffull);
         if (used > 0)
             k_vis_exact<<<sp_blocks(used, 256), 256, 0, sp_counted(st)>>>(used, cand, n, nv, centers, normals, pts,
-                                                                         vis);
+                                                                         pre, vis);
         if (overflowed >= todo) return SP_ERR_CUDA;  // no progress: cannot happen with cap >= 256 n
         todo = overflowed;
         cur = 1 - cur;
