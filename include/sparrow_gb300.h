@@ -242,6 +242,8 @@ size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches,
                                     int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs,
                                     int n_classes);
 int sp_energy_exchange(const sp_exchange_args* args, void* ws, size_t ws_bytes, void* stream);
+/* sizeof(sp_exchange_args), for bindings that mirror the struct. */
+size_t sp_exchange_args_size(void);
 
 /* ------------------------------------------------------------------ adjoint */
 
@@ -287,6 +289,8 @@ size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples
 int sp_adjoint_begin(const sp_adjoint_args* args, void* ws, size_t ws_bytes, void* stream);
 int sp_adjoint_order(const sp_adjoint_args* args, const void* e_prev, void* ws, size_t ws_bytes, void* stream);
 int sp_adjoint_finish(const sp_adjoint_args* args, double* grad_e0dir, void* ws, size_t ws_bytes, void* stream);
+/* sizeof(sp_adjoint_args), for bindings that mirror the struct. */
+size_t sp_adjoint_args_size(void);
 
 /* ------------------------------------------------------ BRDF structure / collection */
 

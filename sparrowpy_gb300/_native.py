@@ -80,6 +80,8 @@ class AdjointArgs(ctypes.Structure):
 _SIGS = {
     "sp_version": (ctypes.c_char_p, []),
     "sp_kernel_launches": (LL, []),
+    "sp_exchange_args_size": (SZ, []),
+    "sp_adjoint_args_size": (SZ, []),
     "sp_patch_geometry": (I, [I, I, P, P, P, P]),
     "sp_patch_visibility_workspace": (SZ, [I]),
     "sp_patch_visibility": (I, [I, I, P, P, P, P, P, SZ, P]),

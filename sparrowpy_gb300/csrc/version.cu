@@ -1,4 +1,4 @@
-// Library identification and the kernel launch counter.
+// Library identification, the kernel launch counter and the sizes of the argument structs.
 #include <atomic>
 
 #include "common.cuh"
@@ -10,3 +10,6 @@ void sp_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 extern "C" const char* sp_version(void) { return "sparrowpy_gb300 0.1.0 (sm_103a)"; }
 
 extern "C" long long sp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+extern "C" size_t sp_exchange_args_size(void) { return sizeof(sp_exchange_args); }
+extern "C" size_t sp_adjoint_args_size(void) { return sizeof(sp_adjoint_args); }

@@ -64,3 +64,14 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "nope.so"))
     with pytest.raises(ImportError):
         _native.lib()
+
+
+def test_struct_mirrors_match_the_library():
+    """The ctypes mirrors have the C structs' sizes (a missing trailing field would be read as garbage)."""
+    import ctypes as ct
+    from sparrowpy_gb300 import _native
+    if not os.path.exists(_native.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _native.lib()
+    assert lib.sp_exchange_args_size() == ct.sizeof(_native.ExchangeArgs)
+    assert lib.sp_adjoint_args_size() == ct.sizeof(_native.AdjointArgs)
