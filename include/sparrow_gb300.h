@@ -231,6 +231,7 @@ typedef struct sp_exchange_args {
        materials to every call with the same tag; the plan left in `ws` by the
        previous call with this tag (and these sizes) is then reused */
     long long plan_tag;
+    float* scatter_ms;      /* HOST float or NULL: CUDA-event time of the scatter launches alone (all orders) */
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070

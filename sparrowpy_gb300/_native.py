@@ -57,7 +57,7 @@ class ExchangeArgs(ctypes.Structure):
         ("order_ms", ctypes.POINTER(ctypes.c_float)),
         ("state_in", P), ("state_order", I), ("states_out", P), ("states_every", I), ("skip_total", I),
         ("mat_alpha", P), ("mat_scattering", P), ("mat_mirror", P), ("mat_gain", P),
-        ("plan_tag", LL),
+        ("plan_tag", LL), ("scatter_ms", ctypes.POINTER(ctypes.c_float)),
     ]
 
 

@@ -492,7 +492,9 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     dim3 mgrid(nb, n);
     size_t msmem = (size_t)2 * n_class * sizeof(T) + (size_t)tile_tab_stride(n_class, nd) * sizeof(int);
     SpEventTimer timer(a->order_ms != nullptr, st);
+    SpIntervalTimer scatter_timer(a->scatter_ms != nullptr, a->max_order - k0);
     for (int k = k0 + 1; k <= a->max_order; ++k) {
+        scatter_timer.start(st);
         if constexpr (sizeof(T) == 4) {
             if (k == k0 + 1)
                 cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
@@ -516,6 +518,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         const bool first_of_pair = (k - k0) % 2 == 1;
         T* et_k = (first_of_pair && k < a->max_order) ? nullptr : etot;
         const T* ea_k = (etot && !first_of_pair) ? eprev : nullptr;
+        scatter_timer.stop(st);
         if (sizeof(T) == 4 && nt % 4 == 0)
             k_mix4<<<mgrid, 128, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                           (const float*)L.cdiff, (const float*)L.cspec,
@@ -539,6 +542,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     cudaMemcpyAsync(&herr, L.err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
     if (a->order_ms) *a->order_ms = timer.elapsed_ms();
+    if (a->scatter_ms) *a->scatter_ms = scatter_timer.total_ms();
     return herr ? SP_ERR_TIMEOUT : SP_OK;
 }
 

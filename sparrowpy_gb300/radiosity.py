@@ -809,6 +809,8 @@ class DirectionalRadiosityFast:
         a.plan_stats = stats
         order_ms = ctypes.c_float(-1.0)
         a.order_ms = ctypes.pointer(order_ms)
+        scatter_ms = ctypes.c_float(-1.0)
+        a.scatter_ms = ctypes.pointer(scatter_ms)
         wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
                        a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups * a.n_in_dirs)
         ws = self._workspace(wsz)
@@ -820,7 +822,8 @@ class DirectionalRadiosityFast:
         self._dev["etc"] = etc
         self.exchange_stats = dict(algorithm="structured" if a.algorithm == nat.SP_EXCHANGE_STRUCTURED else "dense",
                                    source_groups=int(stats[0]), segments=int(stats[1]), pairs=int(stats[2]),
-                                   tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order))
+                                   tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order),
+                                   scatter_ms=float(scatter_ms.value))
 
     def _workspace(self, nbytes):
         ws = self._dev.get("ws")
