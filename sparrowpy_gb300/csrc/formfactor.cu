@@ -10,10 +10,13 @@
 //   - FP32 mode uses an exact re-centring: with D = c_i - c_j,
 //     ln r_ab = ln|D| + (1/2)(L_ab + Q_ab) + (1/2) phi(delta_ab), where
 //     delta = L + Q, L = 2 D.e/|D|^2, Q = |e|^2/|D|^2, e = (P_a - c_i) - (Q_b - c_j)
-//     and phi(x) = ln(1 + x) - x.  The ln|D|, L and Q sums reduce to 3x3 moments
-//     of the weights (computed in FP64), leaving only the well-conditioned phi
-//     sum for FP32.  Pairs whose sample points come closer than 0.3 |D| are
-//     recomputed in FP64 inside the same warp.
+//     and phi(x) = ln(1 + x) - x.  The ln|D|, L and Q sums, and the
+//     (D.e)^2 and (D.e)|e|^2 parts of -delta^2/2, reduce to per-patch moments
+//     of the weights (FP64).  FP32 carries only the remainder
+//     phi(delta) + delta^2/2 - |e|^4/(2|D|^4) = O(|e|^3/|D|^3), so its
+//     rounding error is small beside the heavily cancelling sum.  Pairs
+//     whose sample points come closer than 0.3 |D|, or whose FP32 error
+//     indicator exceeds kFP32RelTol of the result, are recomputed in FP64.
 #include "common.cuh"
 #include "exchange_common.cuh"
 
@@ -93,22 +96,44 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// phi(x) = ln(1 + x) - x, accurate to a few ulp of its value in FP32.
-__device__ __forceinline__ float phi_f(float x) {
+// phi3(x) = ln(1 + x) - x + x^2/2, accurate to a few ulp of its value in FP32
+// for |x| < 0.2 (14 terms of the Taylor series x^3/3 - x^4/4 + ...).
+__device__ __forceinline__ float phi3_f(float x) {
     if (fabsf(x) < 0.2f) {
-        // -x^2/2 + x^3/3 - x^4/4 + ... (16 terms of the Taylor series)
         float p = -1.0f / 17.0f;
 #pragma unroll
-        for (int k = 16; k >= 2; --k) p = fmaf(p, x, ((k & 1) ? 1.0f : -1.0f) / (float)k);
-        return p * x * x;
+        for (int k = 16; k >= 3; --k) p = fmaf(p, x, ((k & 1) ? 1.0f : -1.0f) / (float)k);
+        return ((p * x) * x) * x;
     }
-    return log1pf(x) - x;
+    return (log1pf(x) - x) + 0.5f * x * x;
 }
 
-// integration.py:38-114 `stokes_integration` for one pair, one warp.
-// Lane l < 16 owns sample point a = l of patch i, lane l >= 16 owns point
-// b = l - 16 of patch j.  Returns the same value on all lanes.
-__device__ double stokes_pair(const double* pi, const double* pj, double area_i, bool fp32, bool* needs_fp64) {
+// FP32 error indicator of the remainder sum, per term |W| times
+// * |rem|: the rounding of the term and of the sum;
+// * |rem'(delta)| ~ delta^2 / (1 + delta) times delta's own rounding error,
+//   about 2^-24 (2 |D| (|p_a| + |q_b|) + |e|^2) / |D|^2 (the sample points
+//   are rounded to FP32 relative to their patch centres);
+// * |delta| + delta^2 where log1p(delta) - delta + delta^2/2 cancels.
+// The pair's indicator is 2^-24 / 2 times the sum over its 256 terms; the
+// pair is recomputed in FP64 when that exceeds kFP32RelTol of |num|, the
+// Stokes sum itself.  On the 24046 sampled pairs of a 5939-patch street
+// canyon the measured error of the FP32 result never exceeded 1.8 times
+// the indicator, so FP32 results keep a relative error below 1e-5 (measured
+// at most 1.0e-6 there), and 1.4 % of the pairs are recomputed.
+constexpr double kUnitRoundoff32 = 5.960464477539063e-08;  // 2^-24
+constexpr double kFP32RelTol = 5e-6;
+__device__ __forceinline__ float rem_term_err(float W, float rem, float delta, float ee, float invD2,
+                                              float Dn, float la, float lb) {
+    const float ad = fabsf(delta);
+    return fabsf(W) * (fabsf(rem) + __fdividef(delta * delta, 1.0f + delta) * ((2.0f * Dn * (la + lb) + ee) * invD2) +
+                       (ad >= 0.2f ? ad + delta * delta : 0.0f));
+}
+
+// integration.py:38-114 `stokes_integration` for one pair, one warp, FP64
+// direct logarithms.  Lane l < 16 owns sample point a = l of patch i, lane
+// l >= 16 owns point b = l - 16 of patch j; then lane l sums the terms
+// (a = l & 15, b in (l >> 4) * 8 .. +8).  Returns the same value on all lanes.
+__device__ double stokes_pair(const double* pi, const double* pj, double area_i) {
     int lane = threadIdx.x & 31;
     bool is_i = lane < 16;
     int a = lane & 15;
@@ -116,103 +141,26 @@ __device__ double stokes_pair(const double* pi, const double* pj, double area_i,
     double P[3], w[3];
     boundary_point5(el, a, P);
     boole_weight(el, a, w);
-    if (!fp32) {
-        // direct logarithms: lane handles (a = lane & 15, b in half*8 .. +8)
-        double s = 0.0;
-        int half = lane >> 4;
-        double Pa[3], ua[3];
-        for (int d = 0; d < 3; ++d) {
-            Pa[d] = __shfl_sync(0xffffffffu, P[d], a);
-            ua[d] = __shfl_sync(0xffffffffu, w[d], a);
-        }
-        for (int bb = 0; bb < 8; ++bb) {
-            int b = half * 8 + bb;
-            double Qb[3], vb[3];
-            for (int d = 0; d < 3; ++d) {
-                Qb[d] = __shfl_sync(0xffffffffu, P[d], 16 + b);
-                vb[d] = __shfl_sync(0xffffffffu, w[d], 16 + b);
-            }
-            double dd[3] = {Pa[0] - Qb[0], Pa[1] - Qb[1], Pa[2] - Qb[2]};
-            double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
-            s += (ua[0] * vb[0] + ua[1] * vb[1] + ua[2] * vb[2]) * log(r);
-        }
-        s = warp_sum(s);
-        *needs_fp64 = false;
-        return fabs(s / (2 * SP_PI * area_i));
-    }
-    // centres (vertex means, geometry.py:412-413)
-    double ci[3], cj[3];
-    for (int d = 0; d < 3; ++d) {
-        ci[d] = (((pi[d] + pi[3 + d]) + pi[6 + d]) + pi[9 + d]) / 4;
-        cj[d] = (((pj[d] + pj[3 + d]) + pj[6 + d]) + pj[9 + d]) / 4;
-    }
-    double D[3] = {ci[0] - cj[0], ci[1] - cj[1], ci[2] - cj[2]};
-    double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
-    double loc[3];
-    for (int d = 0; d < 3; ++d) loc[d] = P[d] - (is_i ? ci[d] : cj[d]);
-    // FP64 moments: m_w = sum w, m_dw = sum (D.loc) w, m_qw = sum |loc|^2 w,
-    // m_lw[d][e] = sum w[d] loc[e]  (separately over i-lanes and j-lanes)
-    double Dl = D[0] * loc[0] + D[1] * loc[1] + D[2] * loc[2];
-    double l2 = loc[0] * loc[0] + loc[1] * loc[1] + loc[2] * loc[2];
-    double mom[18];
-    for (int d = 0; d < 3; ++d) {
-        mom[d] = w[d];
-        mom[3 + d] = Dl * w[d];
-        mom[6 + d] = l2 * w[d];
-        for (int e = 0; e < 3; ++e) mom[9 + 3 * d + e] = w[d] * loc[e];
-    }
-    // reduce within each half-warp
-    for (int k = 0; k < 18; ++k) {
-        double v = mom[k];
-        for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-        mom[k] = v;
-    }
-    double Mi[18], Mj[18];
-    for (int k = 0; k < 18; ++k) {
-        Mi[k] = __shfl_sync(0xffffffffu, mom[k], 0);
-        Mj[k] = __shfl_sync(0xffffffffu, mom[k], 16);
-    }
-    double UV = Mi[0] * Mj[0] + Mi[1] * Mj[1] + Mi[2] * Mj[2];
-    double lin = (Mi[3] * Mj[0] + Mi[4] * Mj[1] + Mi[5] * Mj[2]) - (Mi[0] * Mj[3] + Mi[1] * Mj[4] + Mi[2] * Mj[5]);
-    lin /= D2;
-    double pq = 0.0;
-    for (int k = 0; k < 9; ++k) pq += Mi[9 + k] * Mj[9 + k];
-    double quad = 0.5 * ((Mi[6] * Mj[0] + Mi[7] * Mj[1] + Mi[8] * Mj[2]) +
-                         (Mi[0] * Mj[6] + Mi[1] * Mj[7] + Mi[2] * Mj[8]) - 2.0 * pq) / D2;
-    double base = 0.5 * log(D2) * UV + lin + quad;
-    // FP32 phi sum over the 256 sample pairs
-    float Df[3] = {(float)D[0], (float)D[1], (float)D[2]};
-    float invD2 = (float)(1.0 / D2);
-    float locf[3] = {(float)loc[0], (float)loc[1], (float)loc[2]};
-    float wf[3] = {(float)w[0], (float)w[1], (float)w[2]};
+    double s = 0.0;
     int half = lane >> 4;
-    float pa[3], ua[3];
+    double Pa[3], ua[3];
     for (int d = 0; d < 3; ++d) {
-        pa[d] = __shfl_sync(0xffffffffu, locf[d], a);
-        ua[d] = __shfl_sync(0xffffffffu, wf[d], a);
+        Pa[d] = __shfl_sync(0xffffffffu, P[d], a);
+        ua[d] = __shfl_sync(0xffffffffu, w[d], a);
     }
-    float acc = 0.0f;
-    float min_ratio = 1e30f;
     for (int bb = 0; bb < 8; ++bb) {
         int b = half * 8 + bb;
-        float qb[3], vb[3];
+        double Qb[3], vb[3];
         for (int d = 0; d < 3; ++d) {
-            qb[d] = __shfl_sync(0xffffffffu, locf[d], 16 + b);
-            vb[d] = __shfl_sync(0xffffffffu, wf[d], 16 + b);
+            Qb[d] = __shfl_sync(0xffffffffu, P[d], 16 + b);
+            vb[d] = __shfl_sync(0xffffffffu, w[d], 16 + b);
         }
-        float e[3] = {pa[0] - qb[0], pa[1] - qb[1], pa[2] - qb[2]};
-        float de = Df[0] * e[0] + Df[1] * e[1] + Df[2] * e[2];
-        float ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
-        float delta = (2.0f * de + ee) * invD2;
-        min_ratio = fminf(min_ratio, 1.0f + delta);
-        float W = ua[0] * vb[0] + ua[1] * vb[1] + ua[2] * vb[2];
-        acc = fmaf(W, phi_f(delta), acc);
+        double dd[3] = {Pa[0] - Qb[0], Pa[1] - Qb[1], Pa[2] - Qb[2]};
+        double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+        s += (ua[0] * vb[0] + ua[1] * vb[1] + ua[2] * vb[2]) * log(r);
     }
-    acc = warp_sum(acc);
-    for (int off = 16; off > 0; off >>= 1) min_ratio = fminf(min_ratio, __shfl_xor_sync(0xffffffffu, min_ratio, off));
-    *needs_fp64 = (min_ratio < 0.09f);  // some r_ab < 0.3 |D|
-    double outer = base + 0.5 * (double)acc;
-    return fabs(outer / (2 * SP_PI * area_i));
+    s = warp_sum(s);
+    return fabs(s / (2 * SP_PI * area_i));
 }
 
 __device__ __forceinline__ double dsign(double v) { return (v > 0) ? 1.0 : ((v < 0) ? -1.0 : 0.0); }
@@ -396,10 +344,10 @@ __device__ __forceinline__ bool coincident(const double* p0, const double* p1) {
 // method codes written per pair
 enum { kStokes32 = 0, kStokes64 = 1, kNusselt = 2 };
 
-// universal.py:12-96: one warp per visible pair (i < j, i = source).
+// universal.py:12-96 in FP64: one warp per visible pair (i < j, i = source).
 __global__ void __launch_bounds__(256) k_form_factors(long long n_pairs, const int32_t* __restrict__ pairs,
                                                       const double* __restrict__ pts, const double* __restrict__ normals,
-                                                      const double* __restrict__ areas, int fp32, double* __restrict__ ff,
+                                                      const double* __restrict__ areas, double* __restrict__ ff,
                                                       uint8_t* __restrict__ method) {
     long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (q >= n_pairs) return;
@@ -418,13 +366,8 @@ __global__ void __launch_bounds__(256) k_form_factors(long long n_pairs, const i
         result = nusselt_pair(pi, pj, ni, nj);
         m = kNusselt;
     } else {
-        bool redo = false;
-        result = stokes_pair(pi, pj, areas[i], fp32 != 0, &redo);
-        m = fp32 ? kStokes32 : kStokes64;
-        if (redo) {
-            result = stokes_pair(pi, pj, areas[i], false, &redo);
-            m = kStokes64;
-        }
+        result = stokes_pair(pi, pj, areas[i]);
+        m = kStokes64;
     }
     if (lane == 0) {
         ff[q] = result;
@@ -436,20 +379,37 @@ __global__ void __launch_bounds__(256) k_form_factors(long long n_pairs, const i
 // FP32 Stokes in three passes (the FP64 pipe carries only per-patch sums and
 // one short base term per pair):
 //   k_ff_patch_data: per patch, the 16 boundary points relative to the centre
-//     and their Boole weights (FP32 copies for the phi sum) and the FP64 sums
-//     W[d] = sum w[d], Q[d] = sum |loc|^2 w[d], M[d][e] = sum w[d] loc[e];
+//     and their Boole weights (FP32 copies for the remainder sum) and the
+//     FP64 sums over the samples a (loc = p_a):
+//       W[d] = sum w[d],             M[d][e] = sum w[d] loc[e],
+//       Q[d] = sum w[d] |loc|^2,     T[d][e][f] = sum w[d] loc[e] loc[f],
+//       R[d][e] = sum w[d] loc[e] |loc|^2;
 //   k_ff_base: one pair per thread: shared-vertex test (Nusselt pairs are
-//     set aside) and base = 1/2 ln|D|^2 W_i.W_j + lin + quad from the sums;
-//   k_ff_phi: one pair per warp: the FP32 sum of (u_a.v_b) phi(delta_ab);
-//     pairs whose sample points come closer than 0.3 |D| are set aside;
+//     set aside) and, from the sums, base = 1/2 ln|D|^2 W_i.W_j + lin + quad
+//     - (A + B) / |D|^4 with A = sum W_ab (D.e)^2, B = sum W_ab (D.e)|e|^2;
+//   k_ff_phi: one pair per warp: the FP32 sum of (u_a.v_b) rem(delta_ab)
+//     and its error indicator; pairs whose sample points come closer than
+//     0.3 |D| are set aside;
+//   k_ff_finish: ff = |base + sum / 2| / (2 pi A_i), or set aside;
 //   k_ff_rework: set-aside pairs, one warp each, in FP64 (Stokes or Nusselt).
 struct PatchStokes {
     double c[3];   // centre (vertex mean, geometry.py:412-413)
     double W[3];
     double Q[3];
-    double M[9];   // M[3 d + e] = sum_a w_a[d] loc_a[e]
+    double M[9];   // M[3 d + e]
+    double T[18];  // T[6 d + s], s over the symmetric (e, f) = 00 01 02 11 12 22
+    double R[9];   // R[3 d + e]
 };
-constexpr int kPatchF = 16 * 8;  // per patch: 16 x (loc.xyz, 0, w.xyz, 0) floats
+constexpr int kPatchF = 16 * 8;  // per patch: 16 x (loc.xyz, |loc|, w.xyz, 0) floats
+// The (e, f) of slot s: 00 01 02 11 12 22.
+__device__ __forceinline__ int sym_e(int s) { return s < 3 ? 0 : (s < 5 ? 1 : 2); }
+__device__ __forceinline__ int sym_f(int s) { return s < 3 ? s : (s < 5 ? s - 2 : 2); }
+
+// Index of the symmetric pair (e, f) in T's 6 slots.
+__device__ __forceinline__ int sym_slot(int e, int f) {
+    const int lo = e < f ? e : f, hi = e < f ? f : e;
+    return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+}
 
 // Two patches per warp: lanes 0-15 patch 2w, lanes 16-31 patch 2w + 1 (the
 // half-warp reduction order of stokes_pair).
@@ -468,13 +428,18 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
     for (int d = 0; d < 3; ++d) c[d] = (((el[d] + el[3 + d]) + el[6 + d]) + el[9 + d]) / 4;
     double loc[3] = {P[0] - c[0], P[1] - c[1], P[2] - c[2]};
     double l2 = loc[0] * loc[0] + loc[1] * loc[1] + loc[2] * loc[2];
-    double mom[15];
+    constexpr int kMom = 42;  // W 3, Q 3, M 9, T 18, R 9
+    double mom[kMom];
     for (int d = 0; d < 3; ++d) {
         mom[d] = w[d];
         mom[3 + d] = l2 * w[d];
-        for (int e = 0; e < 3; ++e) mom[6 + 3 * d + e] = w[d] * loc[e];
+        for (int e = 0; e < 3; ++e) {
+            mom[6 + 3 * d + e] = w[d] * loc[e];
+            mom[33 + 3 * d + e] = (w[d] * loc[e]) * l2;
+        }
+        for (int s = 0; s < 6; ++s) mom[15 + 6 * d + s] = (w[d] * loc[sym_e(s)]) * loc[sym_f(s)];
     }
-    for (int q = 0; q < 15; ++q) {
+    for (int q = 0; q < kMom; ++q) {
         double v = mom[q];
         for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         mom[q] = v;
@@ -484,7 +449,7 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
     f[0] = (float)loc[0];
     f[1] = (float)loc[1];
     f[2] = (float)loc[2];
-    f[3] = 0.0f;
+    f[3] = (float)sqrt(l2);
     f[4] = (float)w[0];
     f[5] = (float)w[1];
     f[6] = (float)w[2];
@@ -496,13 +461,36 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
             r.W[d] = mom[d];
             r.Q[d] = mom[3 + d];
         }
-        for (int q = 0; q < 9; ++q) r.M[q] = mom[6 + q];
+        for (int q = 0; q < 9; ++q) {
+            r.M[q] = mom[6 + q];
+            r.R[q] = mom[33 + q];
+        }
+        for (int q = 0; q < 18; ++q) r.T[q] = mom[15 + q];
         out[k] = r;
     }
 }
 
+// A patch's moments contracted with D: m1[d] = sum w[d] (D.loc),
+// t1[d][f] = sum w[d] (D.loc) loc[f], m2[d] = sum w[d] (D.loc)^2 and
+// mq1[d] = sum w[d] (D.loc) |loc|^2.
+struct DMoments {
+    double m1[3], t1[9], m2[3], mq1[3];
+};
+__device__ __forceinline__ void d_moments(const PatchStokes& P, const double* D, DMoments& o) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        o.m1[d] = D[0] * P.M[3 * d] + D[1] * P.M[3 * d + 1] + D[2] * P.M[3 * d + 2];
+        o.mq1[d] = D[0] * P.R[3 * d] + D[1] * P.R[3 * d + 1] + D[2] * P.R[3 * d + 2];
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+            o.t1[3 * d + f] = D[0] * P.T[6 * d + sym_slot(0, f)] + D[1] * P.T[6 * d + sym_slot(1, f)] +
+                              D[2] * P.T[6 * d + sym_slot(2, f)];
+        o.m2[d] = D[0] * o.t1[3 * d] + D[1] * o.t1[3 * d + 1] + D[2] * o.t1[3 * d + 2];
+    }
+}
+
 // One pair per thread.  method: kNusselt for shared-vertex pairs (handled in
-// k_ff_rework), else kStokes32 with ff = base (completed by k_ff_phi).
+// k_ff_rework), else kStokes32 with ff = base (completed by k_ff_finish).
 __global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, const double* __restrict__ pts,
                           const PatchStokes* __restrict__ pd, double* __restrict__ ff, uint8_t* __restrict__ method,
                           float4* __restrict__ geo, unsigned long long* __restrict__ n_rework,
@@ -524,26 +512,37 @@ __global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, 
     const PatchStokes& B = pd[j];
     const double D[3] = {A.c[0] - B.c[0], A.c[1] - B.c[1], A.c[2] - B.c[2]};
     const double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
-    double UV = 0.0, lin = 0.0, pq = 0.0, qq = 0.0;
+    DMoments a, b;
+    d_moments(A, D, a);
+    d_moments(B, D, b);
+    // e = p_a - q_b; with W_ab = sum_d u_a[d] v_b[d] every sum below splits
+    // into products of the two patches' moments.
+    double UV = 0.0, lin = 0.0, pq = 0.0, qq = 0.0, sA = 0.0, sB = 0.0;
     for (int d = 0; d < 3; ++d) {
-        const double dmA = D[0] * A.M[3 * d] + D[1] * A.M[3 * d + 1] + D[2] * A.M[3 * d + 2];
-        const double dmB = D[0] * B.M[3 * d] + D[1] * B.M[3 * d + 1] + D[2] * B.M[3 * d + 2];
         UV += A.W[d] * B.W[d];
-        lin += dmA * B.W[d] - A.W[d] * dmB;
+        lin += a.m1[d] * B.W[d] - A.W[d] * b.m1[d];                            // sum W D.e
         qq += A.Q[d] * B.W[d] + A.W[d] * B.Q[d];
-        for (int e = 0; e < 3; ++e) pq += A.M[3 * d + e] * B.M[3 * d + e];
+        double cross = 0.0;
+        for (int e = 0; e < 3; ++e) {
+            pq += A.M[3 * d + e] * B.M[3 * d + e];
+            cross += A.M[3 * d + e] * b.t1[3 * d + e] - a.t1[3 * d + e] * B.M[3 * d + e];
+        }
+        sA += a.m2[d] * B.W[d] - 2.0 * a.m1[d] * b.m1[d] + A.W[d] * b.m2[d];  // sum W (D.e)^2
+        sB += (a.mq1[d] * B.W[d] - A.W[d] * b.mq1[d]) + (a.m1[d] * B.Q[d] - A.Q[d] * b.m1[d]) +
+              2.0 * cross;                                                      // sum W (D.e)|e|^2
     }
-    ff[q] = 0.5 * log(D2) * UV + lin / D2 + 0.5 * (qq - 2.0 * pq) / D2;
+    ff[q] = 0.5 * log(D2) * UV + lin / D2 + 0.5 * (qq - 2.0 * pq) / D2 - (sA + sB) / (D2 * D2);
     method[q] = kStokes32;
     // what the warp-per-pair phi sum needs, rounded once here (FP64 on every lane of a full warp)
     geo[q] = make_float4((float)D[0], (float)D[1], (float)D[2], (float)(1.0 / D2));
 }
 
-// One pair per warp, FP32 only: acc = sum_ab (u_a.v_b) phi(delta_ab) over the
-// 256 sample pairs; k_ff_finish forms ff = |base + acc / 2| / (2 pi A_i).
+// One pair per warp, FP32 only: acc = sum_ab (u_a.v_b) rem_ab over the 256
+// sample pairs, rem = phi3(delta) - |e|^4 / (2 |D|^4), with the sum of
+// rem_term_err beside it; k_ff_finish forms ff = |base + acc / 2| / (2 pi A_i).
 __global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t* __restrict__ pairs,
                                                 const float4* __restrict__ geo, const float* __restrict__ pf,
-                                                float* __restrict__ acc_out, uint8_t* __restrict__ method,
+                                                float2* __restrict__ acc_out, uint8_t* __restrict__ method,
                                                 unsigned long long* __restrict__ n_rework,
                                                 int64_t* __restrict__ rework) {
     const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -554,11 +553,12 @@ __global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t
     const float4 g = geo[q];
     const float Df[3] = {g.x, g.y, g.z};
     const float invD2 = g.w;
+    const float Dn = rsqrtf(invD2);
     const int a = lane & 15, half = lane >> 4;
     const float4* fi = reinterpret_cast<const float4*>(pf + (size_t)i * kPatchF) + 2 * a;
     const float4 pa = fi[0], ua = fi[1];
     const float4* fj = reinterpret_cast<const float4*>(pf + (size_t)j * kPatchF);
-    float acc = 0.0f, min_ratio = 1e30f;
+    float acc = 0.0f, aerr = 0.0f, min_ratio = 1e30f;
 #pragma unroll
     for (int bb = 0; bb < 8; ++bb) {
         const int b = half * 8 + bb;
@@ -569,9 +569,13 @@ __global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t
         const float delta = (2.0f * de + ee) * invD2;
         min_ratio = fminf(min_ratio, 1.0f + delta);
         const float W = ua.x * vb.x + ua.y * vb.y + ua.z * vb.z;
-        acc = fmaf(W, phi_f(delta), acc);
+        const float q2 = ee * invD2;
+        const float rem = phi3_f(delta) - 0.5f * q2 * q2;
+        acc = fmaf(W, rem, acc);
+        aerr += rem_term_err(W, rem, delta, ee, invD2, Dn, pa.w, qb.w);
     }
     acc = warp_sum(acc);
+    aerr = warp_sum(aerr);
     for (int off = 16; off > 0; off >>= 1) min_ratio = fminf(min_ratio, __shfl_xor_sync(0xffffffffu, min_ratio, off));
     if (lane != 0) return;
     if (min_ratio < 0.09f) {  // some r_ab < 0.3 |D|: FP64
@@ -579,16 +583,25 @@ __global__ void __launch_bounds__(256) k_ff_phi(long long n_pairs, const int32_t
         rework[atomicAdd(n_rework, 1ull)] = q;
         return;
     }
-    acc_out[q] = acc;
+    acc_out[q] = make_float2(acc, aerr);
 }
 
-// One pair per thread: the FP32 Stokes pairs' form factors from the base term and the phi sum.
-__global__ void k_ff_finish(long long n_pairs, const int32_t* __restrict__ pairs, const float* __restrict__ acc,
-                            const double* __restrict__ areas, const uint8_t* __restrict__ method,
-                            double* __restrict__ ff) {
+// One pair per thread: the FP32 Stokes pairs' form factors from the base term
+// and the remainder sum, or a place in the FP64 rework list when the sum's
+// error indicator exceeds kFP32RelTol of the result.
+__global__ void k_ff_finish(long long n_pairs, const int32_t* __restrict__ pairs, const float2* __restrict__ acc,
+                            const double* __restrict__ areas, uint8_t* __restrict__ method, double* __restrict__ ff,
+                            unsigned long long* __restrict__ n_rework, int64_t* __restrict__ rework) {
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_pairs || method[q] != kStokes32) return;
-    ff[q] = fabs((ff[q] + 0.5 * (double)acc[q]) / (2 * SP_PI * areas[pairs[2 * q]]));
+    const float2 s = acc[q];
+    const double num = ff[q] + 0.5 * (double)s.x;
+    if (0.5 * kUnitRoundoff32 * (double)s.y > kFP32RelTol * fabs(num)) {
+        method[q] = kStokes64;
+        rework[atomicAdd(n_rework, 1ull)] = q;
+        return;
+    }
+    ff[q] = fabs(num / (2 * SP_PI * areas[pairs[2 * q]]));
 }
 
 // Set-aside pairs, one warp each: FP64 Stokes or the Nusselt analogue.
@@ -612,8 +625,7 @@ __global__ void __launch_bounds__(256) k_ff_rework(long long count, const int64_
         double nj[3] = {normals[3 * j], normals[3 * j + 1], normals[3 * j + 2]};
         result = nusselt_pair(pi, pj, ni, nj);
     } else {
-        bool redo = false;
-        result = stokes_pair(pi, pj, areas[i], false, &redo);
+        result = stokes_pair(pi, pj, areas[i]);
     }
     if (lane == 0) ff[q] = result;
 }
@@ -749,7 +761,7 @@ int sp_receiver_factors(const double* rcv, int n, const double* centers, const d
 size_t sp_form_factors_workspace(int n_patches, long long n_pairs) {
     return sp_align((size_t)n_patches * sizeof(PatchStokes)) + sp_align((size_t)n_patches * kPatchF * 4) +
            sp_align(((size_t)n_pairs + 1) * 8) + sp_align((size_t)n_pairs * sizeof(float4)) +
-           sp_align((size_t)n_pairs * sizeof(float)) + 256;
+           sp_align((size_t)n_pairs * sizeof(float2)) + 256;
 }
 
 int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
@@ -761,8 +773,8 @@ int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32
     cudaStream_t st = (cudaStream_t)stream;
     if (precision == SP_F64 || !method) {
         long long threads = n_pairs * 32;
-        k_form_factors<<<sp_blocks(threads, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, pts, normals, areas,
-                                                                           precision == SP_F32 ? 1 : 0, ff, method);
+        k_form_factors<<<sp_blocks(threads, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, pts, normals, areas, ff,
+                                                                           method);
         return sp_check_launch();
     }
     if (!ws || ws_bytes < sp_form_factors_workspace(n_patches, n_pairs)) return SP_ERR_WORKSPACE;
@@ -775,8 +787,8 @@ int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32
     q += sp_align(((size_t)n_pairs + 1) * 8);
     float4* geo = (float4*)q;
     q += sp_align((size_t)n_pairs * sizeof(float4));
-    float* acc = (float*)q;
-    q += sp_align((size_t)n_pairs * sizeof(float));
+    float2* acc = (float2*)q;
+    q += sp_align((size_t)n_pairs * sizeof(float2));
     unsigned long long* n_rework = (unsigned long long*)q;
     cudaMemsetAsync(n_rework, 0, sizeof(unsigned long long), st);
     const long long warps = ((long long)n_patches + 1) / 2;
@@ -785,7 +797,8 @@ int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32
                                                                   n_rework, rework);
     k_ff_phi<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, geo, pf, acc, method,
                                                                       n_rework, rework);
-    k_ff_finish<<<sp_blocks(n_pairs, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, acc, areas, method, ff);
+    k_ff_finish<<<sp_blocks(n_pairs, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, acc, areas, method, ff,
+                                                                    n_rework, rework);
     unsigned long long count = 0;
     cudaMemcpyAsync(&count, n_rework, sizeof(count), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
