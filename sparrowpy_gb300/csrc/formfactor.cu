@@ -399,6 +399,7 @@ struct PatchStokes {
     double M[9];   // M[3 d + e]
     double T[18];  // T[6 d + s], s over the symmetric (e, f) = 00 01 02 11 12 22
     double R[9];   // R[3 d + e]
+    double rad;    // largest vertex distance from the centre
 };
 constexpr int kPatchF = 16 * 8;  // per patch: 16 x (loc.xyz, |loc|, w.xyz, 0) floats
 // The (e, f) of slot s: 00 01 02 11 12 22.
@@ -466,6 +467,12 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
             r.R[q] = mom[33 + q];
         }
         for (int q = 0; q < 18; ++q) r.T[q] = mom[15 + q];
+        double rad2 = 0.0;
+        for (int v = 0; v < 4; ++v) {
+            const double dv[3] = {el[3 * v] - c[0], el[3 * v + 1] - c[1], el[3 * v + 2] - c[2]};
+            rad2 = fmax(rad2, dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+        }
+        r.rad = sqrt(rad2);
         out[k] = r;
     }
 }
@@ -498,20 +505,26 @@ __global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, 
     const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_pairs) return;
     const int i = pairs[2 * q], j = pairs[2 * q + 1];
-    double pi[12], pj[12];
-    for (int k = 0; k < 12; ++k) {
-        pi[k] = pts[(size_t)i * 12 + k];
-        pj[k] = pts[(size_t)j * 12 + k];
-    }
-    if (coincident(pj, pi)) {
-        method[q] = kNusselt;
-        rework[atomicAdd(n_rework, 1ull)] = q;
-        return;
-    }
     const PatchStokes& A = pd[i];
     const PatchStokes& B = pd[j];
     const double D[3] = {A.c[0] - B.c[0], A.c[1] - B.c[1], A.c[2] - B.c[2]};
     const double D2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    // Every vertex distance is at least |D| - rad_i - rad_j: beyond 1e-5 no
+    // vertex pair can pass the shared-vertex test (distance < 1e-6), which
+    // then runs only for the remaining pairs.
+    const double reach = A.rad + B.rad + 1e-5;
+    if (D2 <= reach * reach) {
+        double pi[12], pj[12];
+        for (int k = 0; k < 12; ++k) {
+            pi[k] = pts[(size_t)i * 12 + k];
+            pj[k] = pts[(size_t)j * 12 + k];
+        }
+        if (coincident(pj, pi)) {
+            method[q] = kNusselt;
+            rework[atomicAdd(n_rework, 1ull)] = q;
+            return;
+        }
+    }
     DMoments a, b;
     d_moments(A, D, a);
     d_moments(B, D, b);
