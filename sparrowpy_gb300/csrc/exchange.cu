@@ -225,26 +225,42 @@ __global__ void k_collect_patchwise(int n, int nd, int nb, int nt, const T* __re
     out[((size_t)k * nb + b) * nt + dst] = (v * r) * a;
 }
 
-// Mono histogram: sum over patches of the patchwise histogram (RadiosityFast.py:592),
-// one thread per (band, bin).  Each term is (E * r_k) * a_kb, added with one
-// FP64 fma: the terms are non-negative, so the sum of N of them is within
-// N * 2^-53 of exact (7e-13 relative at N = 6000), and the thread does two
-// FP64 operations per patch on GB300's narrow FP64 pipe.
+// Mono histogram: sum over patches of the patchwise histogram (RadiosityFast.py:592).
+// A block holds 32 bins of one band; its kMonoWarps warps split the patches
+// (warp w takes k = w, w + kMonoWarps, ...) and their partial sums are added
+// in warp order through shared memory, so the result does not depend on
+// scheduling.  Each term is (E * r_k) * a_kb, added with one FP64 fma: the
+// terms are non-negative, so the sum of N of them is within N * 2^-53 of
+// exact (7e-13 relative at N = 6000).
+constexpr int kMonoWarps = 8;
 template <typename T>
-__global__ void k_collect_mono(int n, int nd, int nb, int nt, const T* __restrict__ etot,
-                               const int32_t* __restrict__ ridx, const double* __restrict__ coef,
-                               const int32_t* __restrict__ shift, double* __restrict__ out) {
-    int b = blockIdx.y;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nt) return;
+__global__ void __launch_bounds__(kMonoWarps * 32) k_collect_mono(int n, int nd, int nb, int nt,
+                                                                  const T* __restrict__ etot,
+                                                                  const int32_t* __restrict__ ridx,
+                                                                  const double* __restrict__ coef,
+                                                                  const int32_t* __restrict__ shift,
+                                                                  double* __restrict__ out) {
+    __shared__ double part[kMonoWarps][32];
+    const int b = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int t = blockIdx.x * 32 + lane;
     double s = 0.0;
-    for (int k = 0; k < n; ++k) {
-        int src_t = t - shift[k];
-        if (src_t < 0) src_t += nt;
-        const double v = (double)etot[(((size_t)k * nd + ridx[k]) * nb + b) * nt + src_t];
-        s = fma(v * coef[(size_t)k * nb + b], coef[(size_t)n * nb + (size_t)k * nb + b], s);
+    if (t < nt) {
+#pragma unroll 4
+        for (int k = warp; k < n; k += kMonoWarps) {
+            int src_t = t - shift[k];
+            if (src_t < 0) src_t += nt;
+            const double v = (double)etot[(((size_t)k * nd + ridx[k]) * nb + b) * nt + src_t];
+            s = fma(v * coef[(size_t)k * nb + b], coef[(size_t)n * nb + (size_t)k * nb + b], s);
+        }
     }
-    out[(size_t)b * nt + t] = s;
+    part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && t < nt) {
+        double tot = part[0][lane];
+        for (int w = 1; w < kMonoWarps; ++w) tot += part[w][lane];
+        out[(size_t)b * nt + t] = tot;
+    }
 }
 
 template <typename T>
@@ -261,8 +277,9 @@ int run_collect(int n, int nd, int nb, int nt, const void* etot, const int32_t* 
         k_collect_patchwise<T><<<g, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift, patchwise);
     }
     if (mono) {
-        dim3 g((nt + 127) / 128, nb);
-        k_collect_mono<T><<<g, 128, 0, sp_counted(st)>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift, mono);
+        dim3 g((nt + 31) / 32, nb);
+        k_collect_mono<T><<<g, kMonoWarps * 32, 0, sp_counted(st)>>>(n, nd, nb, nt, (const T*)etot, ridx, coef, shift,
+                                                                    mono);
     }
     return sp_check_launch();
 }
