@@ -95,7 +95,8 @@ __global__ void k_double_offsets(int n, const int64_t* __restrict__ off, int64_t
     if (i <= n) t_off[i] = 2 * off[i];
 }
 
-// Coefficient of transposed pair t in band b: w_e,b (U kind) or w_e,b K_c(e) (V kind).
+// Coefficient of transposed pair t in band b: w_e,b (U kind) or w_e,b K_c(e)
+// (V kind).  The adjoint runs in FP32 only, so only the FP32 form exists.
 struct AdjCoef {
     const int32_t* fwd;
     const int32_t* cls;
@@ -105,12 +106,6 @@ struct AdjCoef {
     const double* unit_len;
     const double* att;
     int nd;
-    __device__ double operator()(long long t, int b) const {
-        const long long e = fwd[t];
-        double f = fprime[e];
-        if (att) f = f * exp(-att[b] * unit_len[e]);
-        return cls[t] >= nd ? f * gain[in_dir[e]] : f;
-    }
     __device__ float f32(long long t, int b) const {
         const long long e = fwd[t];
         float f = f64_trunc_f32(fprime[e]);
