@@ -273,7 +273,6 @@ class DirectionalRadiosityFast:
         self._dev = {}      # device tensors of the current geometry / results
         self._bake = None   # device state of the last bake
         self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
-        self._device_brdf_key = None  # set while device-built tables are installed
         self._dirs_xyz = None         # rotated direction sets as arrays (set_wall_brdf)
         self.check()
 
@@ -392,7 +391,7 @@ class DirectionalRadiosityFast:
     def _cached_brdf(self):
         """The device BRDF state if it still matches the object's tables, else None."""
         cached = self._dev.get("brdf_state")
-        if cached is not None and (cached["key"] == self._brdf_key() or cached["key"] == self._device_brdf_key):
+        if cached is not None and cached["key"] == self._brdf_key():
             return cached
         return None
 
@@ -446,30 +445,6 @@ class DirectionalRadiosityFast:
             if isinstance(v, torch.Tensor) and v.is_cuda:
                 v.record_stream(main)
         return bs
-
-    def _install_device_brdf(self, tables, brdf_index):
-        """Use device-built BRDF tables (S, n_in, n_out, B) float64 with the current direction sets.
-
-        For solvers that build the tables on the GPU (the differentiable
-        exchange); set_wall_brdf replaces them again.  Keeps the baked
-        geometry; the next exchange re-plans for the new tables.
-        """
-        base = self._brdf_device()
-        if base is None:
-            raise ValueError("set the BRDF direction sets (set_wall_brdf) first")
-        if tuple(tables.shape[1:3]) != (base["n_in"], base["n_out"]):
-            raise ValueError("tables must be (n_slots, n_in, n_out, n_bins) for the current direction sets")
-        state = dict(base)
-        state.pop("structure", None)
-        key = ("device", id(tables))
-        state.update(key=key, brdf=tables.contiguous(), n_slots=int(tables.shape[0]), brdf_host=None,
-                     brdf_index=self._t(brdf_index, torch.int32))
-        self._dev["brdf_state"] = state
-        self._device_brdf_key = key
-        if self._bake is not None:
-            self._bake["brdf"] = state
-            self._bake.pop("plan", None)
-        return state
 
     def _brdf_structure(self, bs):
         """Diffuse-plus-mirror structure of the current BRDF tables (None if absent), kept with them.
@@ -962,7 +937,6 @@ class DirectionalRadiosityFast:
         self._brdf.append(np.asarray(brdf.freq, dtype=float) * np.pi)
         self._brdf_index[np.atleast_1d(wall_indexes)] = len(self._brdf) - 1
         self._dev.pop("brdf_state", None)
-        self._device_brdf_key = None
 
     def _note_wall_dirs(self, i, inc, out):
         """Keep (n_walls, n, 3) arrays of the rotated direction sets beside the Coordinates objects.

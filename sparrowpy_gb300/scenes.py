@@ -206,7 +206,3 @@ def config(name, precision="fp32"):
         return dict(radiosity=r, source=src, receivers=rcv, c=343.0, dt=1e-3, duration=2.0, max_order=50)
     raise ValueError(name)
 
-
-def as_coordinates(xyz):
-    xyz = np.atleast_2d(np.asarray(xyz, float))
-    return Coordinates(xyz[:, 0], xyz[:, 1], xyz[:, 2])
