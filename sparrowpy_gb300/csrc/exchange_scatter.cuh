@@ -59,61 +59,91 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
-// --------------------------------------------------------- FP32 scatter
+// ------------------------------------------------------- scatter (FP32, FP64)
 // Warp-specialised pipeline.  One producer warp streams the groups of a
 // segment through kStages shared-memory stages of kGps groups each, with
 // bulk copies (per group the source window; per stage the groups' packed
 // per-warp words and their 16 coefficients of this band).  kConsumers consumer
 // warps, warp w owning receiver slots 2w and 2w + 1 of the tile, accumulate
-// those slots' 1024-bin windows in registers (lane l owns bins t0 + l + 32 r).
+// those slots' windows in registers (lane l owns bins t0 + l + 32 r).
 // Stage hand-off: `full` (producer arrival + transaction bytes) and `empty`
 // (one arrival per consumer warp); every wait is bounded.
-constexpr int kThreads = 128;                        // FP64 scatter block
+//
+// FP32 windows are 1024 bins (32 per lane): the kernel is bound by
+// shared-memory bandwidth, one window value per FMA.  FP64 windows are 256
+// bins (8 per lane, 16 accumulator registers per slot): the kernel is bound
+// by the FP64 pipe, and shorter windows keep registers low and the grid large.
 constexpr int kSlotsPerWarp = 2;
 constexpr int kConsumers = kTile / kSlotsPerWarp;    // 8 consumer warps
 constexpr int kWsThreads = (kConsumers + 1) * 32;    // + one producer warp
-constexpr int kBins = 32;                            // bins per lane, strided by 32
-constexpr int kTW = 32 * kBins;                      // 1024 bins per window
-constexpr int kStageF = kTW + kMaxSpan + 3;          // staged floats per group (multiple of 4)
-static_assert(kStageF % 4 == 0, "staged window must be a whole number of 16-byte chunks");
 constexpr int kGps = 4;                              // groups per stage
-constexpr int kWinBytes = kStageF * 4;
-constexpr int kPackOff = kGps * kWinBytes;           // kGps x kPackWarps packed words
-constexpr int kCoefOff = kPackOff + kGps * kPackWarps * 4;  // kGps x 16 coefficients
-constexpr int kStageBytes = kCoefOff + kGps * kTile * 4;
-static_assert(kWinBytes % 16 == 0 && kPackOff % 16 == 0 && kCoefOff % 16 == 0 && kStageBytes % 16 == 0,
-              "stage parts must stay 16-byte aligned");
-static_assert(kPackWarps == kConsumers, "one packed word per consumer warp");
 constexpr int kStages = 6;
 constexpr int kBarBytes = 128;                       // full[kStages], empty[kStages]
 static_assert(2 * kStages * 8 <= kBarBytes, "barrier area too small");
-constexpr size_t kScatterSmem = (size_t)kBarBytes + (size_t)kStages * kStageBytes;
+static_assert(kPackWarps == kConsumers, "one packed word per consumer warp");
+
+template <typename T>
+struct WsLayout {
+    static constexpr int kBins = sizeof(T) == 4 ? 32 : 8;   // bins per lane, strided by 32
+    static constexpr int kTW = 32 * kBins;                   // bins per window
+    static constexpr int kAlign = 16 / (int)sizeof(T);       // elements per 16 bytes
+    static constexpr int kStageF = kTW + kMaxSpan + kAlign - 1;  // staged elements per group
+    static constexpr int kWinBytes = kStageF * (int)sizeof(T);
+    static constexpr int kPackOff = kGps * kWinBytes;        // kGps x kPackWarps packed words
+    static constexpr int kCoefOff = kPackOff + kGps * kPackWarps * 4;  // kGps x 16 coefficients
+    static constexpr int kStageBytes = kCoefOff + kGps * kTile * (int)sizeof(T);
+    static constexpr size_t kSmem = (size_t)kBarBytes + (size_t)kStages * kStageBytes;
+    static_assert(kStageF % kAlign == 0, "staged window must be a whole number of 16-byte chunks");
+    static_assert(kWinBytes % 16 == 0 && kPackOff % 16 == 0 && kCoefOff % 16 == 0 && kStageBytes % 16 == 0,
+                  "stage parts must stay 16-byte aligned");
+};
+// FP32 names used by the callers
+constexpr int kBins = WsLayout<float>::kBins;
+constexpr int kTW = WsLayout<float>::kTW;
+constexpr int kStageF = WsLayout<float>::kStageF;    // also bounds the FP64 window (the row tail)
+constexpr size_t kScatterSmem = WsLayout<float>::kSmem;
+static_assert(WsLayout<double>::kStageF <= kStageF, "the row tail is sized for the longer window");
+
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+    using type = float2;
+};
+template <>
+struct Vec2<double> {
+    using type = double2;
+};
+
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
 // acc[r] += cf * staged[lane + 32 r + base - off] for one member slot, with
-// base = kMaxSpan + mu (mu: floats the staged start was rounded down by).
-__device__ __forceinline__ void slot_window(float (&acc)[kBins], const float* win, float cf, int off, int base,
-                                            int lane) {
-    const float* p = win + lane + base - off;
+// base = kMaxSpan + mu (mu: elements the staged start was rounded down by).
+template <typename T, int kN>
+__device__ __forceinline__ void slot_window(T (&acc)[kN], const T* win, T cf, int off, int base, int lane) {
+    const T* p = win + lane + base - off;
 #pragma unroll
-    for (int r = 0; r < kBins; ++r) acc[r] = fmaf(cf, p[32 * r], acc[r]);
+    for (int r = 0; r < kN; ++r) acc[r] = fma_t(cf, p[32 * r], acc[r]);
 }
 
-// One order, one band, one 1024-bin window: G[j, c, b, window] for the 16
-// receivers of a segment.  Histogram rows of eprev are padded: row r starts
-// at r * rs with bin 0 at offset `lead` (>= nt + kMaxSpan + 4 zeros before
-// it), so a staged window reaching before bin 0 reads zeros and needs no
-// masking, and no window starts before the buffer.  Every shared-memory read
-// of a consumer warp covers 32 consecutive floats (no bank conflict at any
+// One order, one band, one window: G[j, c, b, window] for the 16 receivers
+// of a segment.  Histogram rows of eprev are padded: row r starts at r * rs
+// with bin 0 at offset `lead` (>= nt + kMaxSpan + 4 zeros before it), so a
+// staged window reaching before bin 0 reads zeros and needs no masking, and
+// no window starts before the buffer.  Every shared-memory read of a
+// consumer warp covers 32 consecutive elements (no bank conflict at any
 // offset).
-__global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int nb, int nt, long long rs, int lead,
-                                                               long long cap, const int32_t* __restrict__ tile_recv,
-                                                               const int32_t* __restrict__ seg_order,
-                                                               const int64_t* __restrict__ seg_off,
-                                                               const Group* __restrict__ groups,
-                                                               const uint32_t* __restrict__ wpack,
-                                                               const float* __restrict__ coef,
-                                                               const float* __restrict__ eprev,
-                                                               float* __restrict__ gout, int* __restrict__ err) {
+template <typename T>
+__device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long long rs, int lead, long long cap,
+                                           const int32_t* __restrict__ tile_recv,
+                                           const int32_t* __restrict__ seg_order,
+                                           const int64_t* __restrict__ seg_off, const Group* __restrict__ groups,
+                                           const uint32_t* __restrict__ wpack, const T* __restrict__ coef,
+                                           const T* __restrict__ eprev, T* __restrict__ gout,
+                                           int* __restrict__ err) {
+    using L = WsLayout<T>;
+    using T2 = typename Vec2<T>::type;
     extern __shared__ __align__(128) unsigned char s_raw[];
     uint64_t* full = reinterpret_cast<uint64_t*>(s_raw);
     uint64_t* empty = full + kStages;
@@ -123,7 +153,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
 
     const long long seg = seg_order[blockIdx.x];
     const int b = blockIdx.z;
-    const int t0 = blockIdx.y * kTW;
+    const int t0 = blockIdx.y * L::kTW;
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
     const int n_grp = (int)(g_end - g_beg);  // groups of one segment (< 2^31)
     if (n_grp == 0) return;                   // the same for every thread of the block
@@ -142,11 +172,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
     __syncthreads();
     if (s_abort) return;
 
-    float acc0[kBins], acc1[kBins];
+    T acc0[L::kBins], acc1[L::kBins];
 #pragma unroll
-    for (int r = 0; r < kBins; ++r) {
-        acc0[r] = 0.0f;
-        acc1[r] = 0.0f;
+    for (int r = 0; r < L::kBins; ++r) {
+        acc0[r] = T(0);
+        acc1[r] = T(0);
     }
 
     if (warp == kConsumers) {
@@ -158,7 +188,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
             if (base + lane < n_grp) {
                 const int2 h = __ldg(reinterpret_cast<const int2*>(groups + g_beg + base + lane));
                 const long long row = ((long long)h.x * nb + b) * rs + lead;
-                a0 = (row + t0 - h.y - kMaxSpan) & ~3LL;  // 16-byte aligned start of the window
+                a0 = (row + t0 - h.y - kMaxSpan) & ~(long long)(L::kAlign - 1);  // 16-byte aligned start
             }
             const int cnt = min(32, n_grp - base);
             for (int k0 = 0; k0 < cnt; k0 += kGps) {
@@ -175,7 +205,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                         halt = 1;
                     } else {
                         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                        mbar_expect_tx(&full[st], (unsigned)(ng * (kWinBytes + kPackWarps * 4 + kTile * 4)));
+                        mbar_expect_tx(&full[st],
+                                       (unsigned)(ng * (L::kWinBytes + kPackWarps * 4 + kTile * (int)sizeof(T))));
                     }
                 }
                 halt = __shfl_sync(0xffffffffu, halt, 0);
@@ -183,14 +214,14 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                     stop = true;
                     break;
                 }
-                unsigned char* sp = stages + (size_t)st * kStageBytes;
+                unsigned char* sp = stages + (size_t)st * L::kStageBytes;
                 const int q = lane - k0;  // this lane's group within the stage
-                if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * kWinBytes, eprev + a0, kWinBytes, &full[st]);
+                if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * L::kWinBytes, eprev + a0, L::kWinBytes, &full[st]);
                 if (lane == 0) {
                     const long long g0 = g_beg + base + k0;
-                    bulk_copy_g2s(sp + kPackOff, wpack + g0 * kPackWarps, (unsigned)(ng * kPackWarps * 4), &full[st]);
-                    bulk_copy_g2s(sp + kCoefOff, coef + ((size_t)b * cap + g0) * kTile, (unsigned)(ng * kTile * 4),
-                                  &full[st]);
+                    bulk_copy_g2s(sp + L::kPackOff, wpack + g0 * kPackWarps, (unsigned)(ng * kPackWarps * 4), &full[st]);
+                    bulk_copy_g2s(sp + L::kCoefOff, coef + ((size_t)b * cap + g0) * kTile,
+                                  (unsigned)(ng * kTile * (int)sizeof(T)), &full[st]);
                     s_issued = si + 1;
                 }
             }
@@ -208,23 +239,24 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
                 }
                 break;
             }
-            const unsigned char* sp = stages + (size_t)st * kStageBytes;
+            const unsigned char* sp = stages + (size_t)st * L::kStageBytes;
             const int ng = min(kGps, n_grp - si * kGps);
-            const uint32_t* packs = reinterpret_cast<const uint32_t*>(sp + kPackOff) + warp;
-            const float* coefs = reinterpret_cast<const float*>(sp + kCoefOff) + sh;
+            const uint32_t* packs = reinterpret_cast<const uint32_t*>(sp + L::kPackOff) + warp;
+            const T* coefs = reinterpret_cast<const T*>(sp + L::kCoefOff) + sh;
             // the stage's words first (independent loads), then the windows
             uint32_t pk[kGps];
-            float2 cf[kGps];
+            T2 cf[kGps];
 #pragma unroll
             for (int q = 0; q < kGps; ++q) {
                 pk[q] = q < ng ? packs[q * kPackWarps] : 0u;  // 0: no member of this warp
-                cf[q] = *reinterpret_cast<const float2*>(coefs + q * kTile);
+                cf[q] = *reinterpret_cast<const T2*>(coefs + q * kTile);
             }
 #pragma unroll
             for (int q = 0; q < kGps; ++q) {
                 const unsigned bits = (pk[q] >> 12) & 3u;
-                const int base_off = kMaxSpan + (int)((pk[q] >> 14) & 3u);
-                const float* win = reinterpret_cast<const float*>(sp + q * kWinBytes);
+                // the word's alignment field holds (-n_base - kMaxSpan) mod 4
+                const int base_off = kMaxSpan + (int)((pk[q] >> 14) & (unsigned)(L::kAlign - 1));
+                const T* win = reinterpret_cast<const T*>(sp + q * L::kWinBytes);
                 if (bits & 1u) slot_window(acc0, win, cf[q].x, (int)(pk[q] & 63u), base_off, lane);
                 if (bits & 2u) slot_window(acc1, win, cf[q].y, (int)((pk[q] >> 6) & 63u), base_off, lane);
             }
@@ -249,83 +281,27 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(int n_class, int 
         for (int h = 0; h < kSlotsPerWarp; ++h) {
             const int j = tile_recv[tile * kTile + kSlotsPerWarp * warp + h];
             if (j < 0) continue;
-            float* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + lane;
+            T* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + lane;
 #pragma unroll
-            for (int r = 0; r < kBins; ++r)
+            for (int r = 0; r < L::kBins; ++r)
                 if (t0 + lane + 32 * r < nt) out[32 * r] = h == 0 ? acc0[r] : acc1[r];
         }
     }
 }
 
-// --------------------------------------------------------- FP64 scatter
-constexpr int kR64 = 4;
-constexpr int kTW64 = kThreads * kR64;
-
-template <int W>
-__device__ __forceinline__ void slot_f64(double (&acc)[kTile][kR64], const Group& g, const double* sp, const double* cf) {
-    if (g.mask & (1u << W)) {
-        const double cfw = cf[W];
-        const double* p = sp - g.off[W];
-#pragma unroll
-        for (int r = 0; r < kR64; ++r) acc[W][r] = fma(cfw, __ldg(p + kThreads * r), acc[W][r]);
-    }
+#define SP_SCATTER_ARGS(T)                                                                                 \
+    int n_class, int nb, int nt, long long rs, int lead, long long cap, const int32_t *__restrict__ tile_recv, \
+        const int32_t *__restrict__ seg_order, const int64_t *__restrict__ seg_off,                           \
+        const Group *__restrict__ groups, const uint32_t *__restrict__ wpack, const T *__restrict__ coef,      \
+        const T *__restrict__ eprev, T *__restrict__ gout, int *__restrict__ err
+__global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(SP_SCATTER_ARGS(float)) {
+    scatter_ws<float>(n_class, nb, nt, rs, lead, cap, tile_recv, seg_order, seg_off, groups, wpack, coef, eprev, gout,
+                      err);
 }
-__device__ __forceinline__ void group_f64(double (&acc)[kTile][kR64], const Group& g, const double* sp, const double* cf) {
-    slot_f64<0>(acc, g, sp, cf);
-    slot_f64<1>(acc, g, sp, cf);
-    slot_f64<2>(acc, g, sp, cf);
-    slot_f64<3>(acc, g, sp, cf);
-    slot_f64<4>(acc, g, sp, cf);
-    slot_f64<5>(acc, g, sp, cf);
-    slot_f64<6>(acc, g, sp, cf);
-    slot_f64<7>(acc, g, sp, cf);
-    slot_f64<8>(acc, g, sp, cf);
-    slot_f64<9>(acc, g, sp, cf);
-    slot_f64<10>(acc, g, sp, cf);
-    slot_f64<11>(acc, g, sp, cf);
-    slot_f64<12>(acc, g, sp, cf);
-    slot_f64<13>(acc, g, sp, cf);
-    slot_f64<14>(acc, g, sp, cf);
-    slot_f64<15>(acc, g, sp, cf);
+__global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f64(SP_SCATTER_ARGS(double)) {
+    scatter_ws<double>(n_class, nb, nt, rs, lead, cap, tile_recv, seg_order, seg_off, groups, wpack, coef, eprev, gout,
+                       err);
 }
-
-// FP64: same plan, direct (L1-cached) loads, thread owns bins t0 + tid + 128 r.
-__global__ void __launch_bounds__(kThreads) k_scatter_f64(int n_class, int nb, int nt, long long rs, int lead,
-                                                          long long cap, const int32_t* __restrict__ tile_recv,
-                                                          const int32_t* __restrict__ seg_order,
-                                                          const int64_t* __restrict__ seg_off,
-                                                          const Group* __restrict__ groups,
-                                                          const double* __restrict__ coef,
-                                                          const double* __restrict__ eprev,
-                                                          double* __restrict__ gout) {
-    const long long seg = seg_order[blockIdx.x];
-    const int b = blockIdx.z;
-    const int t0 = blockIdx.y * kTW64;
-    const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
-    if (g_beg == g_end) return;
-    const int tid = threadIdx.x;
-    const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
-    double acc[kTile][kR64];
-#pragma unroll
-    for (int w = 0; w < kTile; ++w)
-#pragma unroll
-        for (int r = 0; r < kR64; ++r) acc[w][r] = 0.0;
-    for (long long gidx = g_beg; gidx < g_end; ++gidx) {
-        const Group& g = groups[gidx];  // read in place (no local copy)
-        const double* cf = coef + ((size_t)b * cap + gidx) * kTile;
-        // padded rows: the zero lead covers source indices below 0
-        const double* sp = eprev + ((long long)g.srcrow * nb + b) * rs + lead + t0 + tid - g.n_base;
-        group_f64(acc, g, sp, cf);
-    }
-#pragma unroll
-    for (int w = 0; w < kTile; ++w) {
-        int j = tile_recv[tile * kTile + w];
-        if (j < 0) continue;
-        double* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + tid;
-#pragma unroll
-        for (int r = 0; r < kR64; ++r)
-            if (t0 + tid + kThreads * r < nt) out[kThreads * r] = acc[w][r];
-    }
-}
+#undef SP_SCATTER_ARGS
 
 }  // namespace

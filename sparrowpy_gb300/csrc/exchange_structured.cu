@@ -495,21 +495,20 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     SpIntervalTimer scatter_timer(a->scatter_ms != nullptr, a->max_order - k0);
     for (int k = k0 + 1; k <= a->max_order; ++k) {
         scatter_timer.start(st);
-        if constexpr (sizeof(T) == 4) {
-            if (k == k0 + 1)
-                cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
-            dim3 sgrid(n_active, (nt + kTW - 1) / kTW, nb);
+        {
+            using WL = WsLayout<T>;
+            auto kern = [] {
+                if constexpr (sizeof(T) == 4)
+                    return k_scatter_f32;
+                else
+                    return k_scatter_f64;
+            }();
+            if (k == k0 + 1) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WL::kSmem);
+            dim3 sgrid(n_active, (nt + WL::kTW - 1) / WL::kTW, nb);
             if (n_active > 0)
-                k_scatter_f32<<<sgrid, kWsThreads, kScatterSmem, sp_counted(st)>>>(
+                kern<<<sgrid, kWsThreads, WL::kSmem, sp_counted(st)>>>(
                     n_class, nb, nt, rs, lead, pp, L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups, L.C.wpack,
-                    (const float*)L.C.coef, (const float*)eprev, (float*)L.g, L.err);
-        } else {
-            dim3 sgrid(n_active, (nt + kTW64 - 1) / kTW64, nb);
-            if (n_active > 0)
-                k_scatter_f64<<<sgrid, kThreads, 0, sp_counted(st)>>>(n_class, nb, nt, rs, lead, pp, L.C.tile_recv,
-                                                                      L.C.seg_order, L.C.seg_off, L.C.groups,
-                                                                      (const double*)L.C.coef, (const double*)eprev,
-                                                                      (double*)L.g);
+                    (const T*)L.C.coef, (const T*)eprev, (T*)L.g, L.err);
         }
         // E_total takes the orders in pairs: the first of a pair is deferred
         // and added by the second from the scatter's input rows (E_{k-1},
