@@ -122,14 +122,67 @@ def create_patches(polygon_points, max_size):
     return out
 
 
+def axis_patchable(polygon_points, max_size):
+    """True where the reference's patching applies: some axis spans less than max_size."""
+    size = np.ptp(np.asarray(polygon_points, dtype=float), axis=0)
+    return bool(np.any(np.array([int(n) for n in size / max_size]) == 0))
+
+
+def create_patches_general(polygon_points, max_size):
+    """Patches of a planar convex quadrilateral wall in any orientation.
+
+    The reference patches walls that are aligned with the coordinate axes
+    (geometry.py:373-410) and fails on others.  Here the wall is split along
+    its own edges p0 -> p1 (u) and p0 -> p3 (v) into n_u x n_v
+    quadrilaterals, n = max(1, int(edge length / max_size)) as the reference
+    counts patches per axis.  Corners are bilinear in (u, v) and keep the
+    wall's vertex order; u runs in the outer loop, v in the inner, as the
+    reference's loops do.
+    """
+    p = np.asarray(polygon_points, dtype=float)
+    if p.shape != (4, 3):
+        raise ValueError("general patching takes quadrilateral walls (4 vertices)")
+    n = np.cross(p[1] - p[0], p[3] - p[0])
+    nn = np.sqrt(np.sum(n * n))
+    extent = float(np.max(np.ptp(p, axis=0)))
+    if nn <= 1e-12 * max(extent, 1.0) ** 2:
+        raise ValueError("degenerate wall")
+    n = n / nn
+    if np.max(np.abs((p - p[0]) @ n)) > 1e-9 * max(extent, 1.0):
+        raise ValueError("the wall's vertices are not coplanar")
+    for k in range(4):
+        turn = np.cross(p[(k + 1) % 4] - p[k], p[(k + 2) % 4] - p[(k + 1) % 4]) @ n
+        if turn <= 0:
+            raise ValueError("the wall is not a convex quadrilateral")
+    # 1e-9 of a patch absorbs the rounding of rotated coordinates, so that an
+    # edge of exactly k patch sizes gives k patches as on an axis-aligned wall
+    n_u = max(1, int(np.sqrt(np.sum((p[1] - p[0]) ** 2)) / max_size + 1e-9))
+    n_v = max(1, int(np.sqrt(np.sum((p[3] - p[0]) ** 2)) / max_size + 1e-9))
+
+    def at(s, t):
+        return (1 - s) * (1 - t) * p[0] + s * (1 - t) * p[1] + s * t * p[2] + (1 - s) * t * p[3]
+
+    out = np.empty((n_u * n_v, 4, 3))
+    k = 0
+    for a in range(n_u):
+        for b in range(n_v):
+            s0, s1, t0, t1 = a / n_u, (a + 1) / n_u, b / n_v, (b + 1) / n_v
+            out[k] = (at(s0, t0), at(s1, t0), at(s1, t1), at(s0, t1))
+            k += 1
+    return out
+
+
 def process_patches(walls_points, walls_normal, patch_size):
     """sparrowpy/geometry.py:290-339 `_process_patches`.
 
-    Returns patches_points (n, 4, 3), patches_normal (n, 3), n_patches and
-    patch_to_wall_ids (n,).
+    Axis-aligned walls are patched as the reference does, with its
+    arithmetic; any other wall (where the reference fails) by
+    create_patches_general.  Returns patches_points (n, 4, 3), patches_normal
+    (n, 3), n_patches and patch_to_wall_ids (n,).
     """
     walls_points = np.asarray(walls_points, dtype=float)
-    parts = [create_patches(walls_points[i], patch_size) for i in range(walls_points.shape[0])]
+    parts = [create_patches(w, patch_size) if axis_patchable(w, patch_size) else create_patches_general(w, patch_size)
+             for w in walls_points]
     patches_points = np.concatenate(parts, axis=0) if parts else np.zeros((0, 4, 3))
     patch_to_wall_ids = np.concatenate(
         [np.full(p.shape[0], i, dtype=np.int64) for i, p in enumerate(parts)]) if parts else np.zeros(0, np.int64)
