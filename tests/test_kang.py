@@ -1,0 +1,113 @@
+"""Kang radiosity (sparrowpy/classes/RadiosityKang.py; tests/test_Radiosity.py).
+
+Golden vectors (tests/golden/kang.npz) hold the reference's own stored
+results and a run of the reference here (make_kang_golden.py).  The CPU
+tests pin the oracle (oracle/kang.py) to them; the GPU tests run
+sparrowpy_gb300.kang (CUDA, FP64) against the same vectors and against the
+oracle.  The reference compares its stored results to 2-7 decimals; the
+restatements here agree to 1e-12 relative where the arithmetic is the
+reference's (the FP64 library functions exp and arctan may differ in the
+last bit).
+"""
+import os
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+from oracle import kang as ok
+from sparrowpy_gb300.geometry import shoebox_room_stub
+
+GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "kang.npz"))
+ROOM = eval(str(GOLD["room_config"]))  # written by make_kang_golden.py
+PARALLEL = [[0, 1], [1, 0], [2, 3], [3, 2], [4, 5], [5, 4]]
+PERPENDICULAR = [[i, j] for i in range(6) for j in range(6) if i // 2 != j // 2]
+
+
+def cube_pair(i, j, size):
+    """Two unit-cube walls as the reference's tests build them: PatchesKang(w_i, size, [1], 0), (w_j, size, [0], 1)."""
+    walls = shoebox_room_stub(1, 1, 1)
+    out = []
+    for k, (w, other) in enumerate(((walls[i], [1]), (walls[j], [0]))):
+        out.append(dict(pts=np.asarray(w.pts, float), normal=np.asarray(w.normal, float), max_size=size, other=other,
+                        scattering=np.ones(1), absorption=np.full(1, 0.1), attenuation=np.zeros(1),
+                        patches=ok.kang_patches(w.pts, size)))
+    return out
+
+
+def room_walls():
+    walls = shoebox_room_stub(*ROOM["dims"])
+    return ok.make_walls([(w.pts, w.normal) for w in walls], ROOM["patch_size"], ROOM["scattering"],
+                         ROOM["absorption"], ROOM["attenuation"])
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+@pytest.mark.parametrize("size", [0.5, 1])
+@pytest.mark.parametrize("pair", PARALLEL)
+def test_oracle_ff_parallel(pair, size):
+    walls = cube_pair(*pair, size)
+    npt.assert_allclose(ok.kang_ff(walls, 0), GOLD[f"ff_parallel_size{size:g}"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("pair", PERPENDICULAR)
+def test_oracle_ff_perpendicular(pair):
+    npt.assert_allclose(ok.kang_ff(cube_pair(*pair, 0.5), 0), GOLD[f"ff_perpendicular_{pair[0]}_{pair[1]}_size0.5"],
+                        rtol=1e-12)
+    ff = np.sort(ok.kang_ff(cube_pair(*pair, 0.5), 0).reshape(-1))
+    npt.assert_allclose(ff, GOLD["ff_perpendicular_sorted_size0.5"], rtol=1e-12)
+    npt.assert_allclose(ok.kang_ff(cube_pair(*pair, 1), 0), GOLD["ff_perpendicular_0_0_size1"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("size", [0.5, 1])
+@pytest.mark.parametrize("wall", range(6))
+def test_oracle_init_energy(wall, size):
+    w = cube_pair(wall, wall, size)[0]
+    E = ok.kang_init(w, 3, 5, [0.5, 0.5, 0.5], 1.0, 1000, 346.18)
+    npt.assert_allclose(E, GOLD[f"E_init_size{size:g}"], rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("size", [0.5, 1])
+def test_oracle_energy_exchange(size):
+    walls = cube_pair(0, 2, size)
+    E = [ok.kang_init(w, 3, 5, [0.5, 0.5, 0.5], 1.0, 1000, 346.18) for w in walls]
+    FF = [ok.kang_ff(walls, 0), ok.kang_ff(walls, 1)]
+    for k in range(1, 4):
+        ok.kang_exchange(walls, E, FF, 0, k, 346.18, 1000)
+        ok.kang_exchange(walls, E, FF, 1, k, 346.18, 1000)
+    npt.assert_allclose(E[0], GOLD[f"E_exchange_size{size:g}"], rtol=1e-12, atol=1e-300)
+
+
+def test_oracle_room_matches_reference_run():
+    walls = room_walls()
+    E, FF = ok.kang_run(walls, ROOM["max_order_k"], ROOM["ir_length_s"], ROOM["source"], ROOM["speed_of_sound"],
+                        ROOM["sampling_rate"])
+    for i in range(6):
+        npt.assert_allclose(FF[i], GOLD[f"room_ff_{i}"], rtol=1e-12, atol=1e-300)
+        assert rel(E[i], GOLD[f"room_E_{i}"]) < 1e-12
+    args = (walls, E, ROOM["max_order_k"], ROOM["receiver"], ROOM["source"], ROOM["speed_of_sound"],
+            ROOM["sampling_rate"])
+    assert rel(ok.kang_energy_at_receiver(*args), GOLD["room_ir"]) < 1e-12
+    assert rel(ok.kang_energy_at_receiver(*args, ignore_direct=True), GOLD["room_ir_no_direct"]) < 1e-12
+    args2 = (walls, E, 2) + args[3:]
+    assert rel(ok.kang_energy_at_receiver(*args2), GOLD["room_ir_k2"]) < 1e-12
+
+
+def x10_walls():
+    """The reference's 10 x 20 x 15 m ground + two facades (test_Radiosity.py:236-283)."""
+    X, Y, Z = 10, 20, 15
+    polys = [([[0, 0, 0], [X, 0, 0], [X, Y, 0], [0, Y, 0]], [0, 0, 1]),
+             ([[0, 0, 0], [X, 0, 0], [X, 0, Z], [0, 0, Z]], [0, 1, 0]),
+             ([[0, Y, 0], [X, Y, 0], [X, Y, Z], [0, Y, Z]], [0, -1, 0])]
+    return ok.make_walls(polys, 5, [1.0, 1.0, 1.0], [0.1], [0.0])
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_oracle_x10_simulation(k):
+    walls = x10_walls()
+    E, _ = ok.kang_run(walls, k, 5, [10, 6, 1], 343, 50)
+    ir = ok.kang_energy_at_receiver(walls, E, k, [20, 2, 1], [10, 6, 1], 343, 50)
+    ir = ir / np.max(np.abs(ir))
+    npt.assert_almost_equal(GOLD[f"sim_X10_k{k}_time"][0], ir[0], decimal=2)
