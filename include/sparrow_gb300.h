@@ -319,6 +319,52 @@ int sp_collect_receiver(int precision, int n, int nd, int nb, int nt, const void
                         const double* rfac, const double* dist, double c, double dt, const double* att,
                         double* patchwise, double* mono, void* ws, size_t ws_bytes, void* stream);
 
+/* ------------------------------------------------------------ Kang solver
+ * The legacy Kang radiosity of sparrowpy/classes/RadiosityKang.py in FP64,
+ * per wall as the reference runs it.  A wall's histograms are E (nb,
+ * n_orders, n, nt) (the reference's E_matrix, n_orders = max order + 1);
+ * centres, sizes (Polygon.size) and normals are (.., 3).  `err` (one int,
+ * zeroed by the caller) receives 1 when a source delay falls outside the
+ * histogram (the reference's IndexError) and 2 when an exchange or receiver
+ * delay exceeds it (the ValueError of `_add_delay`). */
+
+/* Replaces RadiosityKang.py:141-207 `init_energy_exchange` with :812-849
+ * `_init_energy_exchange`: adds the source energy of each patch at its delay
+ * into order 0 of E. */
+int sp_kang_init_energy(int n, const double* centers, const double* sizes, const double* normal, const double* src,
+                        double sound_power, int nb, const double* absorption, const double* attenuation,
+                        double speed_of_sound, double sampling_rate, int n_orders, int nt, double* E, int* err,
+                        void* stream);
+
+/* Replaces RadiosityKang.py:269-408 `calculate_form_factor`: ff (n_src,
+ * n_rcv) from the source wall's patches to the receiver columns (the other
+ * walls' patches in the wall's order); rcv_normals and rcv_wall_centers are
+ * per column; max_size is the wall's patch size (used as the patch extent,
+ * as the reference does). */
+int sp_kang_form_factors(int n_src, const double* src_centers, const double* src_normal, const double* src_wall_center,
+                         int n_rcv, const double* rcv_centers, const double* rcv_normals,
+                         const double* rcv_wall_centers, double max_size, double* ff, void* stream);
+
+/* Replaces RadiosityKang.py:209-267 `calculate_energy_exchange` for one
+ * (receiver wall, source wall) pair at order `order`: adds into E_rcv[:,
+ * order] the delayed E_src[:, order - 1] times the source wall's form factors
+ * (columns ff_col0 .. ff_col0 + n_rcv of rows of ff_stride) and the receiver
+ * wall's scattering, 1 - absorption and exp(-attenuation d).  Calls for the
+ * source walls in the receiver wall's order reproduce the reference's sums.
+ * ws: sp_kang_exchange_workspace(n_rcv, n_src, nb) bytes. */
+size_t sp_kang_exchange_workspace(int n_rcv, int n_src, int nb);
+int sp_kang_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const double* rcv_centers, double* E_rcv,
+                     const double* scattering, const double* absorption, const double* attenuation, int n_src,
+                     const double* src_centers, const double* E_src, const double* ff_src, long long ff_stride,
+                     long long ff_col0, double speed_of_sound, double sampling_rate, void* ws, size_t ws_bytes,
+                     int* err, void* stream);
+
+/* Replaces RadiosityKang.py:443-498 `energy_at_receiver` of one wall: adds
+ * the wall's response (nb, nt) over orders 0 .. max_order into out. */
+int sp_kang_receiver(int n, const double* centers, const double* normal, int nb, int n_orders, int nt,
+                     const double* E, int max_order, const double* receiver, const double* attenuation,
+                     double speed_of_sound, double sampling_rate, double* out, int* err, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

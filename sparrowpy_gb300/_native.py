@@ -110,6 +110,11 @@ _SIGS = {
     "sp_brdf_structure": (I, [I, I, I, I, P, D, P, P, P, P, P, P, SZ, P]),
     "sp_collect_workspace": (SZ, [I, I]),
     "sp_collect_receiver": (I, [I, I, I, I, I, P, P, P, P, D, D, P, P, P, P, SZ, P]),
+    "sp_kang_init_energy": (I, [I, P, P, P, P, D, I, P, P, D, D, I, I, P, P, P]),
+    "sp_kang_form_factors": (I, [I, P, P, P, I, P, P, P, D, P, P]),
+    "sp_kang_exchange_workspace": (SZ, [I, I, I]),
+    "sp_kang_exchange": (I, [I, I, I, I, I, P, P, P, P, P, I, P, P, P, LL, LL, D, D, P, SZ, P, P]),
+    "sp_kang_receiver": (I, [I, P, P, I, I, I, P, I, P, P, D, D, P, P, P]),
 }
 
 

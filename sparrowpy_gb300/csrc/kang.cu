@@ -1,0 +1,286 @@
+// Kang radiosity (sparrowpy/classes/RadiosityKang.py) in FP64: closed-form
+// source energy and form factors for axis-aligned rectangular patches, the
+// delayed energy exchange between walls per order, and the energy at a
+// receiver.  Arithmetic follows the reference's evaluation order with
+// unfused operations (x* helpers), so results agree with it up to the last
+// bit of exp / atan / pow.  Histograms are E (n_bins, n_orders, n, nt) per
+// wall, as the reference's E_matrix.
+#include "common.cuh"
+#include "exchange_common.cuh"
+
+namespace {
+
+enum { kKangErrIndex = 1, kKangErrDelay = 2 };  // IndexError (init), ValueError (_add_delay)
+
+__device__ __forceinline__ double sq(double a) { return xmul(a, a); }
+
+// np.linalg.norm(a - b) for 3-vectors.
+__device__ __forceinline__ double dist3(const double* a, const double* b) {
+    const double d[3] = {xsub(a[0], b[0]), xsub(a[1], b[1]), xsub(a[2], b[2])};
+    return xnorm3(d);
+}
+
+// RadiosityKang.py:812-849 `_init_energy_exchange` without the per-band
+// constant: |sin_phi_delta - sin_phi| and beta.
+__device__ void kang_init_geom(double dl, double dm, double dn, double dd_l, double dd_m, double sx, double sy,
+                               double sz, double* dphi, double* beta_out) {
+    const double half_l = xdiv(dd_l, 2.0), half_m = xdiv(dd_m, 2.0);
+    const double a = xsub(xadd(dl, half_l), sx);
+    const double sin_phi_delta = xdiv(a, __dsqrt_rn(xadd(xadd(sq(a), sq(xsub(dm, sy))), sq(xsub(dn, sz)))));
+    const double k_phi = (xsub(dl, half_l) <= sx && sx <= xadd(dl, half_l)) ? -1.0 : 1.0;
+    const double b = xsub(xsub(dl, half_l), sx);
+    double sin_phi = xdiv(xmul(k_phi, b), __dsqrt_rn(xadd(xadd(sq(b), sq(xsub(dm, sy))), sq(xsub(dn, sz)))));
+    if (xsub(sin_phi_delta, sin_phi) < 1e-11) sin_phi = -sin_phi;
+    const double plus = atan(fabs(xdiv(xsub(xadd(dm, half_m), sy), fabs(sz))));
+    const double minus = atan(fabs(xdiv(xsub(xsub(dm, half_m), sy), fabs(sz))));
+    const double k_beta = (xsub(dm, half_m) <= sy && sy <= xadd(dm, half_m)) ? -1.0 : 1.0;
+    *beta_out = fabs(xsub(plus, xmul(k_beta, minus)));
+    *dphi = fabs(xsub(sin_phi_delta, sin_phi));
+}
+
+// RadiosityKang.py:141-207 `init_energy_exchange`, one patch per thread:
+// E[b, 0, i, delay] += energy_b.
+__global__ void k_kang_init(int n, const double* __restrict__ centers, const double* __restrict__ sizes,
+                            const double* __restrict__ normal, const double* __restrict__ src, double power, int nb,
+                            const double* __restrict__ absorption, const double* __restrict__ attenuation, double c,
+                            double fs, int n_orders, int nt, double* __restrict__ E, int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s[3] = {src[0], src[1], src[2]};
+    double r[3] = {centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]};
+    const double distance = dist3(r, s);
+    const long long delay = (long long)xmul(xdiv(distance, c), fs);
+    int ax, idx[3];
+    if (fabs(normal[2]) > 0.99) {
+        ax = 2, idx[0] = 0, idx[1] = 1, idx[2] = 2;
+    } else if (fabs(normal[1]) > 0.99) {
+        ax = 1, idx[0] = 2, idx[1] = 0, idx[2] = 1;
+    } else {  // |normal[0]| > 0.99, checked by the host
+        ax = 0, idx[0] = 1, idx[1] = 2, idx[2] = 0;
+    }
+    const double off = r[ax];
+    s[ax] = fabs(xsub(s[ax], off));
+    r[ax] = fabs(xsub(r[ax], off));
+    const double* sz = sizes + 3 * i;
+    double dphi, beta;
+    kang_init_geom(r[idx[0]], r[idx[1]], r[idx[2]], sz[idx[0]], sz[idx[1]], s[idx[0]], s[idx[1]], s[idx[2]], &dphi,
+                   &beta);
+    if (delay < 0 || delay >= nt) {
+        atomicCAS(err, 0, kKangErrIndex);
+        return;
+    }
+    for (int b = 0; b < nb; ++b) {
+        const double cst = xmul(xmul(power, xsub(1.0, absorption[b])), exp(xmul(-attenuation[b], distance)));
+        const double e = xdiv(xmul(xmul(cst, dphi), beta), 4 * SP_PI);
+        double* p = E + (((size_t)b * n_orders) * n + i) * nt + delay;
+        *p = xadd(*p, e);
+    }
+}
+
+// In-plane axes of a patch by its normal, in the reference's order of tests
+// (RadiosityKang.py:301-322); returned as a bit set.
+__device__ __forceinline__ int plane_axes(const double* nrm) {
+    if (fabs(nrm[0]) > 1e-5) return (1 << 2) | (1 << 1);
+    if (fabs(nrm[1]) > 1e-5) return (1 << 2) | (1 << 0);
+    return (1 << 0) | (1 << 1);
+}
+__device__ __forceinline__ int only_axis(int bits) { return bits == 1 ? 0 : (bits == 2 ? 1 : 2); }
+
+// RadiosityKang.py:269-408 `calculate_form_factor`: one (source patch,
+// receiver column) per thread; ff is (n_src, n_rcv) row-major.
+__global__ void k_kang_ff(int n_src, const double* __restrict__ src_c, const double* __restrict__ src_n,
+                          const double* __restrict__ src_wc, int n_rcv, const double* __restrict__ rcv_c,
+                          const double* __restrict__ rcv_n, const double* __restrict__ rcv_wc, double dd,
+                          double* __restrict__ ff) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)n_src * n_rcv) return;
+    const int i = (int)(q / n_rcv), j = (int)(q % n_rcv);
+    const double* sc = src_c + 3 * i;
+    const double* rc = rcv_c + 3 * j;
+    const double* rn = rcv_n + 3 * j;
+    const double dot = xadd(xadd(xmul(rn[0], src_n[0]), xmul(rn[1], src_n[1])), xmul(rn[2], src_n[2]));
+    double out;
+    if (dot == 0.0) {  // perpendicular
+        const int s_ax = plane_axes(src_n), r_ax = plane_axes(rn);
+        const int l = only_axis(s_ax & r_ax), sa = only_axis(s_ax & ~(s_ax & r_ax)),
+                  ra = only_axis(r_ax & ~(s_ax & r_ax));
+        const double dm = fabs(xsub(sc[sa], rc[sa]));
+        const double dl = sc[l], dlp = rc[l];
+        const double dnp = fabs(xsub(sc[ra], rc[ra]));
+        const double h = xmul(0.5, dd);
+        const double A = xdiv(xsub(dm, h), __dsqrt_rn(xadd(xadd(sq(xsub(dl, dlp)), sq(xsub(dm, h))), sq(dnp))));
+        const double B = xdiv(xadd(dm, h), __dsqrt_rn(xadd(xadd(sq(xsub(dl, dlp)), sq(xadd(dm, h))), sq(dnp))));
+        const double one = atan(fabs(xdiv(xsub(xsub(dl, h), dlp), dnp)));
+        const double two = atan(fabs(xdiv(xsub(xadd(dl, h), dlp), dnp)));
+        const double k = fabs(xsub(dl, dlp)) < 1e-12 ? -1.0 : 1.0;
+        const double theta = fabs(xsub(one, xmul(k, two)));
+        out = xmul(xmul(xdiv(1.0, 2 * SP_PI), fabs(xsub(sq(A), sq(B)))), theta);
+    } else {  // parallel: axes by the walls' centre difference
+        const double* rw = rcv_wc + 3 * j;
+        double dif[3];
+        for (int d = 0; d < 3; ++d) dif[d] = fabs(xsub(rw[d], src_wc[d]));
+        int a, m, b;
+        if (dif[0] > 1e-5)
+            a = 1, m = 0, b = 2;
+        else if (dif[1] > 1e-5)
+            a = 0, m = 1, b = 2;
+        else  // dif[2] > 1e-5, checked by the host
+            a = 1, m = 2, b = 0;
+        const double d = __dsqrt_rn(xadd(xadd(sq(xsub(rc[a], sc[a])), sq(xsub(rc[b], sc[b]))), sq(xsub(rc[m], sc[m]))));
+        out = xdiv(xmul(xmul(dd, dd), sq(xsub(rc[m], sc[m]))), xmul(SP_PI, pow(d, 4.0)));
+    }
+    ff[q] = out;
+}
+
+// Per (receiver r, source s) of one wall pair: the delay and, per band, the
+// factor exp(-m_b d) of RadiosityKang.py:240-262.
+__global__ void k_kang_pair(int n_rcv, const double* __restrict__ rcv_c, int n_src, const double* __restrict__ src_c,
+                            int nb, const double* __restrict__ attenuation, double c, double fs, int nt,
+                            int32_t* __restrict__ delay, double* __restrict__ expo, int* __restrict__ err) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)n_rcv * n_src) return;
+    const int r = (int)(q / n_src), s = (int)(q % n_src);
+    const double d = dist3(rcv_c + 3 * r, src_c + 3 * s);
+    const long long dl = (long long)xmul(xdiv(d, c), fs);
+    if (dl > nt) atomicCAS(err, 0, kKangErrDelay);
+    delay[q] = (int32_t)(dl % (nt > 0 ? nt : 1));  // np.roll by delay == nt is the identity
+    for (int b = 0; b < nb; ++b) expo[(size_t)b * n_rcv * n_src + q] = exp(xmul(-attenuation[b], d));
+}
+
+// RadiosityKang.py:209-267 for one source wall: E_rcv[b, k, r, t] +=
+// sum_s (((roll(E_src[b, k-1, s], delay)[t] * ff) * scattering_b) * (1 - alpha_b)) * expo,
+// sources in order, one (band, receiver patch, bin) per thread.
+__global__ void k_kang_exchange(int k, int nb, int n_orders, int nt, int n_rcv, double* __restrict__ E_rcv,
+                                const double* __restrict__ scattering, const double* __restrict__ absorption,
+                                int n_src, const double* __restrict__ E_src, const double* __restrict__ ff,
+                                long long ff_stride, long long ff_col0, const int32_t* __restrict__ delay,
+                                const double* __restrict__ expo) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y, b = blockIdx.z;
+    if (t >= nt) return;
+    const double scat = scattering[b], om = xsub(1.0, absorption[b]);
+    const double* prev = E_src + (((size_t)b * n_orders + (k - 1)) * n_src) * nt;
+    double* out = E_rcv + (((size_t)b * n_orders + k) * n_rcv + r) * nt + t;
+    double acc = *out;
+    for (int s = 0; s < n_src; ++s) {
+        const long long q = (long long)r * n_src + s;
+        int src_t = t - delay[q];
+        if (src_t < 0) src_t += nt;
+        const double v = prev[(size_t)s * nt + src_t];
+        const double f = ff[(size_t)s * ff_stride + ff_col0 + r];
+        acc = xadd(acc, xmul(xmul(xmul(xmul(v, f), scat), om), expo[(size_t)b * n_rcv * n_src + q]));
+    }
+    *out = acc;
+}
+
+// RadiosityKang.py:443-498 `energy_at_receiver` of one wall, added to out
+// (n_bins, nt): out[b, t] += sum_s sum_k roll(E[b, k, s], delay_s)[t] * factor_sb,
+// one (band, bin) per thread.
+__global__ void k_kang_receiver(int n, const double* __restrict__ centers, const double* __restrict__ normal, int nb,
+                                int n_orders, int nt, const double* __restrict__ E, int max_order,
+                                const double* __restrict__ rcv, const double* __restrict__ attenuation, double c,
+                                double fs, double* __restrict__ out, int* __restrict__ err) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (t >= nt) return;
+    double resp = 0.0;
+    for (int s = 0; s < n; ++s) {
+        const double* sp = centers + 3 * s;
+        const double dif[3] = {fabs(xsub(rcv[0], sp[0])), fabs(xsub(rcv[1], sp[1])), fabs(xsub(rcv[2], sp[2]))};
+        const double R = dist3(sp, rcv);
+        const long long dl = (long long)xmul(xdiv(R, c), fs);
+        if (dl > nt) {
+            if (t == 0 && b == 0) atomicCAS(err, 0, kKangErrDelay);
+            continue;
+        }
+        const int delay = (int)(dl % nt);
+        const double cos_xi =
+            xdiv(fabs(xadd(xadd(xmul(normal[0], dif[0]), xmul(normal[1], dif[1])), xmul(normal[2], dif[2]))), R);
+        const double factor = xdiv(xmul(cos_xi, exp(xmul(-attenuation[b], R))), xmul(SP_PI, xmul(R, R)));
+        int src_t = t - delay;
+        if (src_t < 0) src_t += nt;
+        for (int k = 0; k <= max_order; ++k)
+            resp = xadd(resp, xmul(E[(((size_t)b * n_orders + k) * n + s) * nt + src_t], factor));
+    }
+    double* o = out + (size_t)b * nt + t;
+    *o = xadd(*o, resp);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sp_kang_init_energy(int n, const double* centers, const double* sizes, const double* normal, const double* src,
+                        double sound_power, int nb, const double* absorption, const double* attenuation,
+                        double speed_of_sound, double sampling_rate, int n_orders, int nt, double* E, int* err,
+                        void* stream) {
+    if (n < 0 || nb < 1 || n_orders < 1 || nt < 1 || !(speed_of_sound > 0) || !(sampling_rate > 0)) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!centers || !sizes || !normal || !src || !absorption || !attenuation || !E || !err) return SP_ERR_ARG;
+    k_kang_init<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        n, centers, sizes, normal, src, sound_power, nb, absorption, attenuation, speed_of_sound, sampling_rate,
+        n_orders, nt, E, err);
+    return sp_check_launch();
+}
+
+int sp_kang_form_factors(int n_src, const double* src_centers, const double* src_normal, const double* src_wall_center,
+                         int n_rcv, const double* rcv_centers, const double* rcv_normals,
+                         const double* rcv_wall_centers, double max_size, double* ff, void* stream) {
+    if (n_src < 0 || n_rcv < 0) return SP_ERR_ARG;
+    if (n_src == 0 || n_rcv == 0) return SP_OK;
+    if (!src_centers || !src_normal || !src_wall_center || !rcv_centers || !rcv_normals || !rcv_wall_centers || !ff)
+        return SP_ERR_ARG;
+    const long long total = (long long)n_src * n_rcv;
+    k_kang_ff<<<sp_blocks(total, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        n_src, src_centers, src_normal, src_wall_center, n_rcv, rcv_centers, rcv_normals, rcv_wall_centers, max_size,
+        ff);
+    return sp_check_launch();
+}
+
+size_t sp_kang_exchange_workspace(int n_rcv, int n_src, int nb) {
+    const size_t pairs = (size_t)(n_rcv > 0 ? n_rcv : 0) * (size_t)(n_src > 0 ? n_src : 0);
+    return sp_align(pairs * 4) + sp_align(pairs * (size_t)(nb > 0 ? nb : 0) * 8) + 256;
+}
+
+int sp_kang_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const double* rcv_centers, double* E_rcv,
+                     const double* scattering, const double* absorption, const double* attenuation, int n_src,
+                     const double* src_centers, const double* E_src, const double* ff_src, long long ff_stride,
+                     long long ff_col0, double speed_of_sound, double sampling_rate, void* ws, size_t ws_bytes,
+                     int* err, void* stream) {
+    if (order < 1 || order >= n_orders || nb < 1 || nt < 1 || n_rcv < 0 || n_src < 0 || ff_stride < 0 ||
+        ff_col0 < 0 || !(speed_of_sound > 0) || !(sampling_rate > 0))
+        return SP_ERR_ARG;
+    if (n_rcv == 0 || n_src == 0) return SP_OK;
+    if (ff_col0 + n_rcv > ff_stride) return SP_ERR_ARG;
+    if (!rcv_centers || !E_rcv || !scattering || !absorption || !attenuation || !src_centers || !E_src || !ff_src ||
+        !err)
+        return SP_ERR_ARG;
+    if (!ws || ws_bytes < sp_kang_exchange_workspace(n_rcv, n_src, nb)) return SP_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t pairs = (size_t)n_rcv * n_src;
+    int32_t* delay = (int32_t*)ws;
+    double* expo = (double*)((char*)ws + sp_align(pairs * 4));
+    k_kang_pair<<<sp_blocks((long long)pairs, 128), 128, 0, sp_counted(st)>>>(
+        n_rcv, rcv_centers, n_src, src_centers, nb, attenuation, speed_of_sound, sampling_rate, nt, delay, expo, err);
+    dim3 grid((nt + 127) / 128, n_rcv, nb);
+    k_kang_exchange<<<grid, 128, 0, sp_counted(st)>>>(order, nb, n_orders, nt, n_rcv, E_rcv, scattering, absorption,
+                                                      n_src, E_src, ff_src, ff_stride, ff_col0, delay, expo);
+    return sp_check_launch();
+}
+
+int sp_kang_receiver(int n, const double* centers, const double* normal, int nb, int n_orders, int nt,
+                     const double* E, int max_order, const double* receiver, const double* attenuation,
+                     double speed_of_sound, double sampling_rate, double* out, int* err, void* stream) {
+    if (n < 0 || nb < 1 || n_orders < 1 || nt < 1 || max_order < 0 || max_order >= n_orders ||
+        !(speed_of_sound > 0) || !(sampling_rate > 0))
+        return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!centers || !normal || !E || !receiver || !attenuation || !out || !err) return SP_ERR_ARG;
+    dim3 grid((nt + 127) / 128, nb);
+    k_kang_receiver<<<grid, 128, 0, sp_counted((cudaStream_t)stream)>>>(n, centers, normal, nb, n_orders, nt, E,
+                                                                        max_order, receiver, attenuation,
+                                                                        speed_of_sound, sampling_rate, out, err);
+    return sp_check_launch();
+}
+
+}  // extern "C"
