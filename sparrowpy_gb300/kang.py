@@ -17,8 +17,9 @@ arrays (csrc/kang.cu):
   (:1028-1046) on the host.
 
 E_matrix and form_factors read back to NumPy on access.  The directional
-variant (PatchesDirectionalKang, DirectionalRadiosityKang) reads its BRDFs
-from SOFA files and is not provided: sofar is not installed here.
+variant (PatchesDirectionalKang, DirectionalRadiosityKang) is not provided:
+its BRDFs come from SOFA files or pyfar objects rotated by pyfar's
+Orientations, neither of which is available here.
 """
 import ctypes
 
