@@ -93,3 +93,29 @@ def test_canyon_rows_match_oracle():
     assert np.all(err[s64] <= bound), "FP64 Stokes"
     # most pairs stay on the FP32 path
     assert np.mean(m == 0) > 0.9
+
+
+def test_canyon_fp32_solve_matches_fp64():
+    """The whole 5939-patch solve (8 bands, 32 directions, 2000 bins, order 50): the FP32 receiver histograms
+    within the 1e-4 relative L2 tolerance of the FP64 solve, itself parity-tested against the oracle at 1e-10."""
+    import torch
+    from sparrowpy_gb300 import scenes
+    from sparrowpy_gb300.coords import Coordinates
+
+    def run(precision):
+        c = scenes.config("cfg3", precision=precision)
+        r = c["radiosity"]
+        r.bake_geometry()
+        r.init_source_energy(Coordinates(*c["source"]))
+        r.calculate_energy_exchange(c["c"], c["dt"], c["duration"], c["max_order"])
+        rc = c["receivers"]
+        out = r.collect_energy_receiver_mono(Coordinates(rc[:, 0], rc[:, 1], rc[:, 2])).time
+        del r, c
+        torch.cuda.empty_cache()
+        return out
+
+    m32 = run("fp32")
+    m64 = run("fp64")
+    assert m32.shape == m64.shape == (8, 8, 2000)
+    assert np.all(np.isfinite(m32)) and np.sum(m64) > 0
+    assert np.linalg.norm(m32 - m64) / np.linalg.norm(m64) < 1e-4
