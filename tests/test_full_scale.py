@@ -13,8 +13,8 @@ rows of it in seconds:
     the sum of its terms' magnitudes.  Two FP64 summation orders (the
     reference's and the warp's) then differ by about sqrt(256) 2^-53 times
     that magnitude sum; the test allows 4 sqrt(256) 2^-53 sum |W ln r|.
-The whole-solve comparison at this size is the benchmark's FP32-vs-FP64
-receiver error.
+and the whole solve at this size: the FP32 receiver histograms against the
+FP64 solve's (the benchmark reports the same error).
 """
 import numpy as np
 import pytest
