@@ -150,14 +150,14 @@ __global__ void k_kang_pair(int n_rcv, const double* __restrict__ rcv_c, int n_s
 // RadiosityKang.py:209-267 for one source wall: E_rcv[b, k, r, t] +=
 // sum_s (((roll(E_src[b, k-1, s], delay)[t] * ff) * scattering_b) * (1 - alpha_b)) * expo,
 // sources in order, one (band, receiver patch, bin) per thread.
-__global__ void k_kang_exchange(int k, int nb, int n_orders, int nt, int n_rcv, double* __restrict__ E_rcv,
+__global__ void k_kang_exchange(int k, int nb, int n_orders, int nt, int n_rcv, int r0, double* __restrict__ E_rcv,
                                 const double* __restrict__ scattering, const double* __restrict__ absorption,
                                 int n_src, const double* __restrict__ E_src, const double* __restrict__ ff,
                                 long long ff_stride, long long ff_col0, const int32_t* __restrict__ delay,
                                 const double* __restrict__ expo) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r = blockIdx.y, b = blockIdx.z;
-    if (t >= nt) return;
+    const int r = r0 + (int)blockIdx.y, b = blockIdx.z;
+    if (t >= nt || r >= n_rcv) return;
     const double scat = scattering[b], om = xsub(1.0, absorption[b]);
     const double* prev = E_src + (((size_t)b * n_orders + (k - 1)) * n_src) * nt;
     double* out = E_rcv + (((size_t)b * n_orders + k) * n_rcv + r) * nt + t;
@@ -262,9 +262,13 @@ int sp_kang_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const d
     double* expo = (double*)((char*)ws + sp_align(pairs * 4));
     k_kang_pair<<<sp_blocks((long long)pairs, 128), 128, 0, sp_counted(st)>>>(
         n_rcv, rcv_centers, n_src, src_centers, nb, attenuation, speed_of_sound, sampling_rate, nt, delay, expo, err);
-    dim3 grid((nt + 127) / 128, n_rcv, nb);
-    k_kang_exchange<<<grid, 128, 0, sp_counted(st)>>>(order, nb, n_orders, nt, n_rcv, E_rcv, scattering, absorption,
-                                                      n_src, E_src, ff_src, ff_stride, ff_col0, delay, expo);
+    constexpr int kMaxGridY = 65535;  // receiver patches per launch (grid y limit)
+    for (int r0 = 0; r0 < n_rcv; r0 += kMaxGridY) {
+        dim3 grid((nt + 127) / 128, (unsigned)(n_rcv - r0 < kMaxGridY ? n_rcv - r0 : kMaxGridY), nb);
+        k_kang_exchange<<<grid, 128, 0, sp_counted(st)>>>(order, nb, n_orders, nt, n_rcv, r0, E_rcv, scattering,
+                                                          absorption, n_src, E_src, ff_src, ff_stride, ff_col0,
+                                                          delay, expo);
+    }
     return sp_check_launch();
 }
 
