@@ -15,6 +15,7 @@ Usage:  python tests/golden/make_kang_golden.py [--ref /path/to/sparrowpy]
 """
 import argparse
 import io
+import json
 import os
 import sys
 import zipfile
@@ -100,7 +101,7 @@ def main():
     a = ap.parse_args()
     out = stored_results(os.path.join(a.ref, "tests", "test_data"))
     out.update(reference_room(a.ref))
-    out["room_config"] = np.array(repr(ROOM))
+    out["room_config"] = np.array(json.dumps(ROOM))
     np.savez_compressed(os.path.join(HERE, "kang.npz"), **out)
     print("wrote", os.path.join(HERE, "kang.npz"), len(out), "arrays")
 

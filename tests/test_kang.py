@@ -9,6 +9,7 @@ restatements here agree to 1e-12 relative where the arithmetic is the
 reference's (the FP64 library functions exp and arctan may differ in the
 last bit).
 """
+import json
 import os
 
 import numpy as np
@@ -19,7 +20,7 @@ from oracle import kang as ok
 from sparrowpy_gb300.geometry import shoebox_room_stub
 
 GOLD = np.load(os.path.join(os.path.dirname(__file__), "golden", "kang.npz"))
-ROOM = eval(str(GOLD["room_config"]))  # written by make_kang_golden.py
+ROOM = json.loads(str(GOLD["room_config"]))  # written by make_kang_golden.py
 PARALLEL = [[0, 1], [1, 0], [2, 3], [3, 2], [4, 5], [5, 4]]
 PERPENDICULAR = [[i, j] for i in range(6) for j in range(6) if i // 2 != j // 2]
 
