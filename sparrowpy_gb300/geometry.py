@@ -8,6 +8,7 @@ per solve.
 import numpy as np
 
 from .coords import Coordinates, _cart
+from .sound_object import Receiver, SoundSource  # noqa: F401  (sparrowpy/geometry.py:12 re-exports them)
 
 
 def _norm(v):

@@ -258,3 +258,71 @@ def test_gpu_source_delay_past_histogram_raises():
     p = sp.PatchesKang(shoebox_room_stub(1, 1, 1)[0], 0.5, [], 0)
     with pytest.raises(IndexError):
         p.init_energy_exchange(1, 0.01, SoundSource([0.5, 100.0, 0.5], [0, 1, 0], [0, 0, 1]), 1000, 343.0)
+
+
+# ------------------------------------------------ the reference's properties
+def _kang_room(dims, patch_size, max_order, src, sampling_rate=1, ir_length_s=1, shift=(0.0, 0.0, 0.0)):
+    import sparrowpy_gb300 as sp
+    from sparrowpy_gb300.geometry import SoundSource
+    walls = shoebox_room_stub(*dims)
+    for w in walls:
+        w.pts += np.asarray(shift)
+    radi = sp.RadiosityKang(walls, patch_size, max_order, ir_length_s, speed_of_sound=343,
+                            sampling_rate=sampling_rate, absorption=0.1)
+    radi.run(SoundSource(np.asarray(src, float) + np.asarray(shift), [0, 1, 0], [0, 0, 1]))
+    return radi
+
+
+@pytest.mark.gpu
+def test_gpu_small_room_and_shift():
+    """test_Radiosity.py:16-80: a shifted room gives identical E_matrix, form factors and response."""
+    from sparrowpy_gb300.geometry import Receiver
+    out = []
+    for shift in ((0.0, 0.0, 0.0), (2.0, 4.0, 5.0)):
+        radi = _kang_room((5, 6, 4), 1, 10, [2, 2, 2], shift=shift)
+        E = np.concatenate([p.E_matrix for p in radi.patch_list], axis=-2)
+        ff = [p.form_factors for p in radi.patch_list]
+        ir = radi.energy_at_receiver(Receiver(np.array([3.0, 2.0, 3.0]) + shift, [0, 1, 0], [0, 0, 1]),
+                                     ignore_direct=True)
+        out.append((E, ff, ir))
+    npt.assert_array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        npt.assert_array_equal(a, b)
+    npt.assert_array_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.gpu
+def test_gpu_small_room_and_rotate():
+    """test_Radiosity.py:82-141: the six axis permutations of a room give the same response (4 decimals)."""
+    from sparrowpy_gb300.geometry import Receiver
+    X, Y, Z = 5, 3, 4
+    r = (1, 2, 1.5)
+    perms = [(0, 1, 2), (0, 2, 1), (1, 2, 0), (1, 0, 2), (2, 0, 1), (2, 1, 0)]
+    irs = []
+    for p in perms:
+        dims = [(X, Y, Z)[k] for k in p]
+        radi = _kang_room(dims, 1, 10, [2, 2, 2])
+        irs.append(radi.energy_at_receiver(Receiver([r[k] for k in p], [0, 1, 0], [0, 0, 1]),
+                                           ignore_direct=True).squeeze())
+    irs = np.array(irs)
+    npt.assert_array_almost_equal(irs, irs[0], decimal=4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("patch_size", [1, 0.5, 0.2, 1 / 3])
+def test_gpu_init_energy_larger_0(patch_size):
+    """test_Radiosity.py:635-660: a cube's patches receive energy from a central source (and match the oracle)."""
+    import sparrowpy_gb300 as sp
+    from sparrowpy_gb300.geometry import SoundSource
+    radi = sp.RadiosityKang(shoebox_room_stub(1, 1, 1), patch_size, 0, 1, speed_of_sound=343, sampling_rate=1,
+                            absorption=0.1)
+    source = SoundSource([0.5, 0.5, 0.5], [0, 1, 0], [0, 0, 1])
+    for p in radi.patch_list:
+        p.init_energy_exchange(radi.max_order_k, radi.ir_length_s, source, sampling_rate=radi.sampling_rate,
+                               speed_of_sound=343)
+    E = np.concatenate([p.E_matrix for p in radi.patch_list], axis=-2)
+    assert E.flatten()[0] > 0
+    walls = ok.make_walls([(w.pts, w.normal) for w in shoebox_room_stub(1, 1, 1)], patch_size, [1.0] * 6, [0.1],
+                          [0.0])
+    ref = np.concatenate([ok.kang_init(w, 0, 1, [0.5, 0.5, 0.5], 1.0, 1, 343) for w in walls], axis=-2)
+    npt.assert_allclose(E, ref, rtol=1e-12, atol=1e-300)
