@@ -856,6 +856,21 @@ class DirectionalRadiosityFast:
         """Per-patch energy at the receivers (RadiosityFast.py:660-684)."""
         return self._collect(receivers, patchwise=True)
 
+    def _collect_energy_patches(self, receiver_pos, propagation_fx=False):
+        """Patch histograms as the receivers see them (RadiosityFast.py:686-752): (R, N, B, T) FP64.
+
+        With propagation_fx each patch's histogram is delayed and attenuated
+        towards the receiver (the patchwise collection); without, it is the
+        patch's histogram in the receiver's direction times the point factor.
+        """
+        rc = np.atleast_2d(np.asarray(receiver_pos, dtype=float).reshape(-1, 3))
+        if propagation_fx:
+            return self._collect_device(rc, patchwise=True).cpu().numpy()
+        etc = self._etc_device()
+        ridx, rfac, _ = self._receiver_factors(rc)
+        rows = etc[torch.arange(etc.shape[0], device=etc.device)[None, :], ridx.long()]  # (R, N, B, T)
+        return (rows.double() * rfac[:, :, None, None]).cpu().numpy()
+
     def _collect(self, receivers, patchwise):
         if not is_coordinates(receivers):
             raise ValueError("Receiver positions must be of type pf.Coordinates")

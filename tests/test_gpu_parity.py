@@ -90,6 +90,18 @@ def test_patchwise_and_direct_sound(golden):
     rcv = Coordinates(rc[:, 0], rc[:, 1], rc[:, 2])
     pw = r.collect_energy_receiver_patchwise(rcv).time
     np.testing.assert_allclose(pw.sum(axis=1), golden["mono"], rtol=1e-9, atol=1e-300)
+    # the private helper behind it (RadiosityFast.py:686-752): with propagation it is the patchwise
+    # result; without, delaying each patch by ceil(d / c / dt) and attenuating it gives that result
+    np.testing.assert_array_equal(r._collect_energy_patches(rc, propagation_fx=True), pw)
+    raw = r._collect_energy_patches(rc)
+    att = np.zeros(r.n_bins) if r._air_attenuation is None else np.asarray(r._air_attenuation, float)
+    c, dt = r.speed_of_sound, r._etc_time_resolution
+    expect = np.empty_like(raw)
+    for i in range(rc.shape[0]):
+        for k in range(r.n_patches):
+            d = np.linalg.norm(r.patches_center[k] - rc[i])
+            expect[i, k] = np.roll(raw[i, k] * np.exp(-att * d)[:, None], int(np.ceil(d / c / dt)), axis=-1)
+    assert rel_l2(expect, pw) < 1e-12
     ds, delay = r.calculate_direct_sound(rcv)
     np.testing.assert_allclose(ds, golden["direct"], rtol=1e-14)
     np.testing.assert_array_equal(delay, golden["direct_delay"])
