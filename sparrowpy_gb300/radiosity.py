@@ -47,6 +47,24 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def _pair_dir_tables(bs):
+    """The BRDF state's direction tables with identical ones merged: (table of each wall, dirs_in, dirs_out).
+
+    Walls of the same orientation have the same rotated direction sets.  The
+    pair set-up looks a table up for every directed pair; with the tables
+    merged (exact comparison) it reads a few small, cache-resident ones
+    instead of one per wall, with the same results.
+    """
+    if "pair_tables" not in bs:
+        n_w = bs["dirs_in"].shape[0]
+        both = torch.cat([bs["dirs_in"].reshape(n_w, -1), bs["dirs_out"].reshape(n_w, -1)], dim=1)
+        uniq, inv = torch.unique(both, dim=0, return_inverse=True)
+        k = bs["n_in"] * 3
+        bs["pair_tables"] = (inv.to(torch.int32), uniq[:, :k].reshape(-1, bs["n_in"], 3).contiguous(),
+                             uniq[:, k:].reshape(-1, bs["n_out"], 3).contiguous())
+    return bs["pair_tables"]
+
+
 _SIDE_STREAMS = {}
 _PREP_POOL = None
 
@@ -541,10 +559,13 @@ class DirectionalRadiosityFast:
         dist = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
         unit_len = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
         fprime = torch.empty((max(n_dir, 1),), dtype=torch.float64, device=dev)
+        if bs:
+            tab_of_wall, din_u, dout_u = _pair_dir_tables(bs)
+            tab_of_patch = tab_of_wall[d["wall_of"].long()].contiguous()
         nat.call("sp_pair_setup", n_dir, n, _ptr(src), _ptr(dst), _ptr(d["centers"]), _ptr(d["areas"]),
-                 _ptr(pair_index), _ptr(ff), _ptr(d["wall_of"]),
-                 bs["n_in"] if bs else 0, _ptr(bs["dirs_in"]) if bs else _ptr(None),
-                 bs["n_out"] if bs else 0, _ptr(bs["dirs_out"]) if bs else _ptr(None),
+                 _ptr(pair_index), _ptr(ff), _ptr(tab_of_patch) if bs else _ptr(d["wall_of"]),
+                 bs["n_in"] if bs else 0, _ptr(din_u) if bs else _ptr(None),
+                 bs["n_out"] if bs else 0, _ptr(dout_u) if bs else _ptr(None),
                  _ptr(out_dir), _ptr(in_dir), _ptr(dist), _ptr(unit_len), _ptr(fprime), st)
         att = None if self._air_attenuation is None else self._t(self._air_attenuation, torch.float64)
         n_bins = 1 if self._frequencies is None else self.n_bins
