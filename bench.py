@@ -430,7 +430,9 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": TRAFFIC_PER_ALGO_BYTE * bytes_order,
                          "kernel": "one exchange order: k_scatter_f32 + k_mix launches", "peak_of": peak_kind,
-                         "algorithmic_bytes": bytes_order, "ms_per_launch": ms_order},
+                         "algorithmic_bytes": bytes_order, "ms_per_launch": ms_order,
+                         "binding": "shared-memory bandwidth of k_scatter_f32 (roofline_smem); the order's HBM "
+                                    "traffic is a byproduct"},
             "roofline_smem": smem,
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
