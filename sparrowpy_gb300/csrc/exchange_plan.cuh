@@ -142,15 +142,32 @@ __global__ void k_scan_blocks(long long n, const int64_t* __restrict__ in, int64
     if (i < n) out[i] = s[threadIdx.x] - v;
     if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[kScanBlock - 1];
 }
+// Exclusive scan of the block sums in one block of kScanBlock threads: each
+// thread takes a contiguous chunk, the chunk totals are scanned in shared
+// memory, then each chunk is written from its prefix (integers: exact).
 __global__ void k_scan_sums(long long nblocks, int64_t* __restrict__ sums, int64_t* __restrict__ total) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int64_t run = 0;
-    for (long long k = 0; k < nblocks; ++k) {
-        int64_t v = sums[k];
+    __shared__ int64_t s[kScanBlock];
+    const int t = threadIdx.x;
+    const long long per = (nblocks + kScanBlock - 1) / kScanBlock;
+    const long long b0 = (long long)t * per;
+    const long long b1 = b0 + per < nblocks ? b0 + per : nblocks;
+    int64_t local = 0;
+    for (long long k = b0; k < b1; ++k) local += sums[k];
+    s[t] = local;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        const int64_t x = (t >= off) ? s[t - off] : 0;
+        __syncthreads();
+        s[t] += x;
+        __syncthreads();
+    }
+    int64_t run = s[t] - local;
+    for (long long k = b0; k < b1; ++k) {
+        const int64_t v = sums[k];
         sums[k] = run;
         run += v;
     }
-    *total = run;
+    if (t == kScanBlock - 1) *total = s[kScanBlock - 1];
 }
 __global__ void k_scan_add(long long n, int64_t* __restrict__ out, const int64_t* __restrict__ sums) {
     long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
@@ -211,32 +228,55 @@ __global__ void k_pair_coef(long long n_dir, int nb, Coef pair_coef, T* __restri
     }
 }
 
+// 1 where merged position q starts a cell (a new (src, tile, class) run), else 0.
+__global__ void k_cell_flags(long long n_dir, const int64_t* __restrict__ merged, const int32_t* __restrict__ src,
+                             const int32_t* __restrict__ dst, const int32_t* __restrict__ tile_of,
+                             const int32_t* __restrict__ cls, int64_t* __restrict__ flag) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_dir) return;
+    int start = 1;
+    if (q > 0) {
+        const long long e = merged[q], ep = merged[q - 1];
+        start = !(src[ep] == src[e] && tile_of[dst[ep]] == tile_of[dst[e]] && cls[ep] == cls[e]);
+    }
+    flag[q] = start;
+}
+
+// starts[c] = merged position of cell c (fscan: exclusive scan of the flags).
+__global__ void k_cell_compact(long long n_dir, const int64_t* __restrict__ flag, const int64_t* __restrict__ fscan,
+                               int64_t* __restrict__ starts) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n_dir && flag[q]) starts[fscan[q]] = q;
+}
+
 // Cells: runs of equal (segment, src) in merged order (<= kTile entries, one
-// per destination).  For each cell start: sort members by (p2o, delay), cut into
-// groups; write == 0 counts, write == 1 emits with the coefficients of
-// k_pair_coef.
+// per destination), one thread per cell (the compacted cell starts, so that
+// every lane works).  Per cell: sort members by (p2o, delay), cut into
+// groups; write == 0 counts (cell_count[c]), write == 1 emits at
+// cell_base[c] with the coefficients of k_pair_coef.
+// n_cells is read on the device (the flag scan's total), so the launch covers
+// all n_dir slots; slots past it count zero groups.
 template <typename T>
-__global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* __restrict__ merged,
-                        const int32_t* __restrict__ src, const int32_t* __restrict__ dst, const int32_t* __restrict__ out_dir,
+__global__ void k_cells(const int64_t* __restrict__ n_cells_p, const int64_t* __restrict__ starts, long long n_dir,
+                        int nd, int nb, int nt, const int64_t* __restrict__ merged, const int32_t* __restrict__ src,
+                        const int32_t* __restrict__ dst, const int32_t* __restrict__ out_dir,
                         const int32_t* __restrict__ delay, const int32_t* __restrict__ cls,
                         const int32_t* __restrict__ tile_of, const int32_t* __restrict__ slot_of,
                         const T* __restrict__ pair_coef,
                         int write, int64_t* __restrict__ cell_count, const int64_t* __restrict__ cell_base,
                         long long cap, Group* __restrict__ groups, T* __restrict__ coef,
                         uint32_t* __restrict__ wpack) {
-    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n_dir) return;
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_dir) return;
+    if (c >= *n_cells_p) {
+        if (!write) cell_count[c] = 0;
+        return;
+    }
+    const long long q = starts[c];
     long long e = merged[q];
     int s_src = src[e];
     int s_tile = tile_of[dst[e]];
     int s_cls = cls[e];
-    if (q > 0) {
-        long long ep = merged[q - 1];
-        if (src[ep] == s_src && tile_of[dst[ep]] == s_tile && cls[ep] == s_cls) {
-            if (!write) cell_count[q] = 0;
-            return;
-        }
-    }
     int mo[kTile], md[kTile], mw[kTile];
     long long me[kTile];
     int m = 0;
@@ -267,7 +307,7 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
         mw[r + 1] = tw;
         me[r + 1] = te;
     }
-    long long g_out = write ? cell_base[q] : 0;
+    long long g_out = write ? cell_base[c] : 0;
     long long n_groups = 0;
     int a = 0;
     while (a < m) {
@@ -299,16 +339,17 @@ __global__ void k_cells(long long n_dir, int nd, int nb, int nt, const int64_t* 
         ++n_groups;
         a = r + 1;
     }
-    if (!write) cell_count[q] = n_groups;
+    if (!write) cell_count[c] = n_groups;
 }
 
-// seg_off[s] = group index of the first cell of segment s.
-__global__ void k_seg_offsets(long long n_seg, long long n_dir, const int64_t* __restrict__ seg_base,
+// seg_off[s] = group index of the first cell of segment s: its first merged
+// position starts a cell (or, for an empty segment, the next one does), and
+// fscan turns positions into cell numbers (fscan[n_dir] = number of cells).
+__global__ void k_seg_offsets(long long n_seg, const int64_t* __restrict__ seg_base, const int64_t* __restrict__ fscan,
                               const int64_t* __restrict__ cell_base, int64_t* __restrict__ seg_off) {
     long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (s > n_seg) return;
-    long long q = seg_base[s];
-    seg_off[s] = (q < n_dir) ? cell_base[q] : cell_base[n_dir];
+    seg_off[s] = cell_base[fscan[seg_base[s]]];
 }
 
 // Per tile: the classes present (segments with groups) and, per outgoing
@@ -344,7 +385,7 @@ void scan64(long long n, const int64_t* in, int64_t* out, int64_t* tmp, cudaStre
     long long nblocks = (n + kScanBlock - 1) / kScanBlock;
     if (nblocks < 1) nblocks = 1;
     k_scan_blocks<<<(unsigned)nblocks, kScanBlock, 0, sp_counted(st)>>>(n, in, out, tmp);
-    k_scan_sums<<<1, 32, 0, sp_counted(st)>>>(nblocks, tmp, out + n);
+    k_scan_sums<<<1, kScanBlock, 0, sp_counted(st)>>>(nblocks, tmp, out + n);
     k_scan_add<<<(unsigned)nblocks, kScanBlock, 0, sp_counted(st)>>>(n, out, tmp);
 }
 
@@ -401,6 +442,9 @@ struct PlanCore {
     int32_t* seg_order;
     int64_t* cell_count;
     int64_t* cell_base;
+    int64_t* cell_flag;   // [pairs + 1] start flags, then their exclusive scan in cell_fscan
+    int64_t* cell_fscan;  // [pairs + 1]
+    int64_t* cell_start;  // [pairs] merged position of each cell
     int64_t* scan_tmp;
     Group* groups;
     uint32_t* wpack;  // [cap][kPackWarps]
@@ -427,6 +471,9 @@ PlanCore plan_core_layout(Take& take, int esz, int n, int nb, long long p, int n
     C.seg_order = (int32_t*)take((size_t)n_seg * 4);
     C.cell_count = (int64_t*)take(((size_t)p + 1) * 8);
     C.cell_base = (int64_t*)take(((size_t)p + 1) * 8);
+    C.cell_flag = (int64_t*)take(((size_t)p + 1) * 8);
+    C.cell_fscan = (int64_t*)take(((size_t)p + 1) * 8);
+    C.cell_start = (int64_t*)take(((size_t)p + 1) * 8);
     long long big = p > n_seg ? p : n_seg;
     C.scan_tmp = (int64_t*)take(((size_t)(big / kScanBlock) + 2) * 8);
     C.groups = (Group*)take((size_t)(p + 1) * sizeof(Group));
@@ -458,15 +505,21 @@ int build_groups(int n, int nb, int nt, const PairSet& ps, const int32_t* order,
                                                                      C.rco, C.tile_of, C.slot_of, C.tile_recv,
                                                                      C.seg_base, C.merged);
     k_pair_coef<T, Coef><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(p, nb, coef, (T*)C.pcoef);
+    // cell starts, compacted so that one thread per cell builds its groups
+    k_cell_flags<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, C.merged, ps.src, ps.dst, C.tile_of, ps.cls,
+                                                                C.cell_flag);
+    scan64(p, C.cell_flag, C.cell_fscan, C.scan_tmp, st);
+    k_cell_compact<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, C.cell_flag, C.cell_fscan, C.cell_start);
+    const int64_t* n_cells = C.cell_fscan + p;
     k_cells<T><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
-        p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of,
-        (const T*)C.pcoef, 0, C.cell_count, nullptr, p, nullptr, nullptr, nullptr);
+        n_cells, C.cell_start, p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls,
+        C.tile_of, C.slot_of, (const T*)C.pcoef, 0, C.cell_count, nullptr, p, nullptr, nullptr, nullptr);
     scan64(p, C.cell_count, C.cell_base, C.scan_tmp, st);
     k_cells<T><<<sp_blocks(p, 128), 128, 0, sp_counted(st)>>>(
-        p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls, C.tile_of, C.slot_of,
-        (const T*)C.pcoef, 1, nullptr, C.cell_base, p, C.groups, (T*)C.coef, C.wpack);
-    k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, sp_counted(st)>>>(n_seg, p, C.seg_base, C.cell_base,
-                                                                         C.seg_off);
+        n_cells, C.cell_start, p, ps.rows_per_src, nb, nt, C.merged, ps.src, ps.dst, ps.row, ps.delay, ps.cls,
+        C.tile_of, C.slot_of, (const T*)C.pcoef, 1, nullptr, C.cell_base, p, C.groups, (T*)C.coef, C.wpack);
+    k_seg_offsets<<<sp_blocks(n_seg + 1, 256), 256, 0, sp_counted(st)>>>(n_seg, C.seg_base, C.cell_fscan,
+                                                                         C.cell_base, C.seg_off);
     // scatter blocks visit the non-empty segments longest first, so the
     // longest blocks do not end up in the tail of the grid
     std::vector<int64_t> h_off((size_t)n_seg + 1);
