@@ -189,3 +189,34 @@ def test_state_file_reads_ndarray_and_builtin_members(tmp_path):
         z.writestr("src/$Coordinates", b"{}")
     with pytest.raises(NotImplementedError):
         far.read(path)
+
+
+def test_pair_dir_tables_merge_identical_walls():
+    """The pair set-up's merged direction tables: every wall maps to a table equal to its own."""
+    import torch
+    from sparrowpy_gb300.radiosity import _pair_dir_tables
+    rng = np.random.default_rng(0)
+    base_in = rng.standard_normal((3, 5, 3))
+    base_out = rng.standard_normal((3, 7, 3))
+    which = np.array([2, 0, 0, 1, 2, 2, 1, 0])  # 8 walls, 3 distinct orientations
+    bs = dict(n_in=5, n_out=7, dirs_in=torch.tensor(base_in[which]), dirs_out=torch.tensor(base_out[which]))
+    tab, din, dout = _pair_dir_tables(bs)
+    assert din.shape == (3, 5, 3) and dout.shape == (3, 7, 3)
+    tab = tab.numpy()
+    np.testing.assert_array_equal(din.numpy()[tab], base_in[which])
+    np.testing.assert_array_equal(dout.numpy()[tab], base_out[which])
+    assert _pair_dir_tables(bs)[0] is bs["pair_tables"][0]  # cached with the state
+
+
+def test_kang_form_factor_columns():
+    """PatchesKang._column: offsets of the other walls' patches in other_wall_ids order (RadiosityKang.py:410-441)."""
+    walls = geometry.shoebox_room_stub(2, 1, 1)
+    radi = sp.RadiosityKang(walls, 0.5, 1, 0.1)
+    p0 = radi.patch_list[0]
+    sizes = [len(p.patches) for p in radi.patch_list]
+    off = 0
+    for w in p0.other_wall_ids:
+        assert p0._column(radi.patch_list, w) == off
+        off += sizes[w]
+    with pytest.raises(KeyError):
+        p0._column(radi.patch_list, 0)
