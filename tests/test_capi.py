@@ -75,3 +75,23 @@ def test_struct_mirrors_match_the_library():
     lib = _native.lib()
     assert lib.sp_exchange_args_size() == ct.sizeof(_native.ExchangeArgs)
     assert lib.sp_adjoint_args_size() == ct.sizeof(_native.AdjointArgs)
+
+
+def declared_prototypes():
+    """name -> number of parameters, from the header's prototypes."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(sp_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_binding_argument_counts_match_header():
+    """Every ctypes signature has as many arguments as its C prototype."""
+    from sparrowpy_gb300 import _native
+    protos = declared_prototypes()
+    bad = {name: (len(args), protos[name]) for name, (_, args) in _native._SIGS.items()
+           if name in protos and len(args) != protos[name]}
+    assert not bad, bad
+    assert len(protos) >= 30
