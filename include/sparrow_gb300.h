@@ -150,11 +150,14 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
 /* Universal patch-to-patch form factor for each listed pair (i = source).
  * Replaces universal.py:12-52 `patch2patch_ff_universal` (+ :54-96,
  * integration.py:38-114 Stokes, :116-289 Nusselt).  Quadrilateral patches.
- * precision SP_F64: FP64 throughout; SP_F32: Stokes in re-centred FP32 with
- * FP64 for vertex-sharing and near-coincident pairs.  ff (n_pairs) FP64;
- * method (n_pairs): 0 Stokes FP32, 1 Stokes FP64, 2 Nusselt FP64.  pts holds
- * n_patches patches; SP_F32 with method needs ws (sp_form_factors_workspace
- * bytes) and synchronises `stream` once; SP_F64 or method == NULL uses no ws. */
+ * precision SP_F64: FP64 throughout.  SP_F32: Stokes re-centred on the patch
+ * centres, the second-order terms from FP64 moments and the remainder sum in
+ * FP32; FP64 for vertex-sharing pairs (Nusselt), near pairs and pairs whose
+ * FP32 error indicator exceeds 5e-6 of the sum.  ff (n_pairs) FP64; method
+ * (n_pairs): 0 Stokes FP32, 1 Stokes FP64, 2 Nusselt FP64.  pts holds
+ * n_patches patches.  SP_F32 with method needs ws (sp_form_factors_workspace
+ * bytes) and synchronises `stream` once; SP_F64, or SP_F32 with method ==
+ * NULL, computes FP64 throughout and uses no ws. */
 size_t sp_form_factors_workspace(int n_patches, long long n_pairs);
 int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
                     const double* normals, const double* areas, double* ff, uint8_t* method, void* ws,
