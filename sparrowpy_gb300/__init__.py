@@ -2,7 +2,7 @@
 
 Drop-in for ``sparrowpy.DirectionalRadiosityFast``; see radiosity.py.
 """
-from . import brdf, geometry, kang, sound_object
+from . import brdf, geometry, kang, mesh, sound_object
 from .coords import Coordinates, FrequencyData, TimeData
 from .geometry import Polygon, shoebox_room_stub
 from .kang import PatchesKang, RadiosityKang
@@ -12,5 +12,5 @@ __version__ = "0.1.0"
 
 __all__ = [
     "DirectionalRadiosityFast", "Polygon", "shoebox_room_stub", "Coordinates", "FrequencyData", "TimeData",
-    "brdf", "geometry", "sound_object", "analyse_brdf", "kang", "PatchesKang", "RadiosityKang",
+    "brdf", "geometry", "sound_object", "analyse_brdf", "kang", "mesh", "PatchesKang", "RadiosityKang",
 ]

@@ -155,10 +155,11 @@ def create_patches_general(polygon_points, max_size):
         turn = np.cross(p[(k + 1) % 4] - p[k], p[(k + 2) % 4] - p[(k + 1) % 4]) @ n
         if turn <= 0:
             raise ValueError("the wall is not a convex quadrilateral")
-    # 1e-9 of a patch absorbs the rounding of rotated coordinates, so that an
-    # edge of exactly k patch sizes gives k patches as on an axis-aligned wall
-    n_u = max(1, int(np.sqrt(np.sum((p[1] - p[0]) ** 2)) / max_size + 1e-9))
-    n_v = max(1, int(np.sqrt(np.sum((p[3] - p[0]) ** 2)) / max_size + 1e-9))
+    # 1e-6 of a patch absorbs the rounding of rotated coordinates (also of
+    # float32 ones, as STL files store them), so that an edge of k patch
+    # sizes gives k patches as on an axis-aligned wall
+    n_u = max(1, int(np.sqrt(np.sum((p[1] - p[0]) ** 2)) / max_size + 1e-6))
+    n_v = max(1, int(np.sqrt(np.sum((p[3] - p[0]) ** 2)) / max_size + 1e-6))
 
     def at(s, t):
         return (1 - s) * (1 - t) * p[0] + s * (1 - t) * p[1] + s * t * p[2] + (1 - s) * t * p[3]

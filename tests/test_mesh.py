@@ -1,0 +1,108 @@
+"""STL geometry import (sparrowpy/utils/blender.py; tests/test_blender_import.py).
+
+The reference reads STL through Blender and checks, for a cube, that the
+rough mesh keeps the fine mesh's vertices and has half as many faces.  The
+same checks run here on cubes written as binary and ASCII STL (the
+reference's cube.stl is a binary STL of the cube [-1, 1]^3 with 12
+triangles), and the meshes feed DirectionalRadiosityFast.from_polygon.
+"""
+import struct
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+from sparrowpy_gb300 import DirectionalRadiosityFast
+from sparrowpy_gb300.mesh import polygons_from_mesh, read_geometry_file
+from sparrowpy_gb300.scenes import rotation_matrix_xyz
+
+
+def cube_triangles(half=1.0, split_top=False):
+    """Outward-wound triangles of the cube [-half, half]^3; the top face optionally as a 2 x 2 grid."""
+    h = half
+    quads = [  # counter-clockwise seen from outside
+        [(-h, -h, h), (h, -h, h), (h, h, h), (-h, h, h)],
+        [(-h, -h, -h), (-h, h, -h), (h, h, -h), (h, -h, -h)],
+        [(-h, -h, -h), (h, -h, -h), (h, -h, h), (-h, -h, h)],
+        [(-h, h, -h), (-h, h, h), (h, h, h), (h, h, -h)],
+        [(-h, -h, -h), (-h, -h, h), (-h, h, h), (-h, h, -h)],
+        [(h, -h, -h), (h, h, -h), (h, h, h), (h, -h, h)],
+    ]
+    tris = []
+    for qi, q in enumerate(quads):
+        q = np.asarray(q, float)
+        if split_top and qi == 0:
+            for a in range(2):
+                for b in range(2):
+                    x0, x1 = -h + a * h, -h + (a + 1) * h
+                    y0, y1 = -h + b * h, -h + (b + 1) * h
+                    sq = np.array([(x0, y0, h), (x1, y0, h), (x1, y1, h), (x0, y1, h)])
+                    tris += [sq[[0, 1, 2]], sq[[0, 2, 3]]]
+        else:
+            tris += [q[[0, 1, 2]], q[[0, 2, 3]]]
+    return np.array(tris)
+
+
+def write_binary_stl(path, tris):
+    with open(path, "wb") as f:
+        f.write(b"written by the test".ljust(80, b"\0"))
+        f.write(struct.pack("<I", len(tris)))
+        for t in tris:
+            f.write(struct.pack("<12fH", 0.0, 0.0, 0.0, *t.reshape(-1), 0))
+
+
+def write_ascii_stl(path, tris):
+    lines = ["solid cube"]
+    for t in tris:
+        lines += ["  facet normal 0 0 0", "    outer loop"]
+        lines += [f"      vertex {v[0]:.9g} {v[1]:.9g} {v[2]:.9g}" for v in t]
+        lines += ["    endloop", "  endfacet"]
+    lines.append("endsolid cube")
+    open(path, "w").write("\n".join(lines) + "\n")
+
+
+@pytest.mark.parametrize("writer", [write_binary_stl, write_ascii_stl])
+def test_mesh_simplification(tmp_path, writer):
+    """tests/test_blender_import.py:8-15 for the STL cube."""
+    path = tmp_path / "cube.stl"
+    writer(path, cube_triangles())
+    fine, rough = read_geometry_file(path)
+    npt.assert_array_equal(fine["verts"], rough["verts"])
+    assert len(fine["conn"]) == len(rough["conn"]) * 2
+    assert fine["verts"].shape == (8, 3) and len(fine["conn"]) == 12
+    assert all(len(p) == 4 for p in rough["conn"])
+
+
+def test_rough_polygons_are_the_cube_faces(tmp_path):
+    path = tmp_path / "cube.stl"
+    write_binary_stl(path, cube_triangles(split_top=True))
+    fine, rough = read_geometry_file(path)
+    assert len(fine["conn"]) == 18 and fine["verts"].shape == (13, 3)
+    assert len(rough["conn"]) == 6
+    polys = polygons_from_mesh(rough)
+    assert all(p.pts.shape == (4, 3) for p in polys)  # the split face's edge midpoints are left out
+    npt.assert_allclose(sorted(p.area for p in polys), [4.0] * 6, rtol=1e-12)
+    for p in polys:  # outward normals from the STL winding
+        assert np.dot(p.normal, p.center) > 0
+    inward = polygons_from_mesh(rough, flip=True)
+    assert all(np.dot(p.normal, p.center) < 0 for p in inward)
+
+
+@pytest.mark.parametrize("rotate", [False, True])
+def test_stl_room_patches(tmp_path, rotate):
+    """An STL room through from_polygon: 4 x 4 patches per 2 m face at 0.5 m, in any orientation."""
+    tris = cube_triangles()
+    if rotate:
+        tris = tris @ rotation_matrix_xyz(0.3, 0.7, 1.1).T
+    path = tmp_path / "room.stl"
+    write_binary_stl(path, tris)  # float32 coordinates: a rotated face is planar to about 1e-7
+    _, rough = read_geometry_file(path)
+    r = DirectionalRadiosityFast.from_polygon(polygons_from_mesh(rough, flip=True), 0.5)
+    assert r.n_patches == 6 * 16
+
+
+def test_blend_files_need_blender(tmp_path):
+    with pytest.raises(NotImplementedError):
+        read_geometry_file(tmp_path / "room.blend")
+    with pytest.raises(NotImplementedError):
+        read_geometry_file(tmp_path / "room.obj")
