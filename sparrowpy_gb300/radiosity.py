@@ -23,8 +23,9 @@ collect_energy_receiver_*      sp_point_visibility, sp_receiver_factors,
 attribute is materialised on access (sp_form_factors_tilde).
 
 Extra keyword (not in the reference): ``precision`` = "fp32" (default; FP32
-exchange and Stokes form factors, FP64 for shared-vertex and near pairs) or
-"fp64" (FP64 throughout).
+exchange and Stokes form factors, FP64 for shared-vertex and near pairs and
+for pairs whose FP32 error indicator is too large) or "fp64" (FP64
+throughout).
 """
 import ctypes
 
