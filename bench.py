@@ -41,8 +41,9 @@ import numpy as np  # noqa: E402
 METRIC = "ms/solve (bake+exchange) ~5.5k patches FP32 vs FP64 GPU; fwd+bwd ms; HBM GB/s"
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 # DRAM bytes moved per algorithmic byte by one exchange order (scatter + mix,
-# averaged over a deferred and a pairing order), from the single-pass ncu
-# capture summarised in profiles/exchange_street_canyon_small.md
+# averaged over a deferred and a pairing order), from a single-pass ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 1759-patch
+# canyon
 TRAFFIC_PER_ALGO_BYTE = 1.20
 
 
@@ -59,6 +60,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fwd-bwd", action="store_true", help="skip the gradient (forward + backward) leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the cfg1 / cfg2 legs")
     ap.add_argument("--batch-rooms", type=int, default=8, help="seeded shoebox rooms for the batch leg (0: skip)")
     ap.add_argument("--fwd-bwd-only", action="store_true",
                     help="print only the gradient leg (shoebox, 2016 patches) as one JSON line")
@@ -146,20 +148,24 @@ def peak_hbm():
 
 
 # -------------------------------------------------------------- CPU baseline
-def cpu_baseline(cfg, rows_per_thread=1):
+def cpu_baseline(cfg, rows_per_thread=1, exchange_rows=8):
     """FP64 CPU restatement (oracle/) on bounded samples, extrapolated to one solve.
 
-    GPU-free.  Samples, all on the same scene and its own pair lists:
+    GPU-free.  Each part runs on the threads the reference's numba code uses
+    for it: visibility and form factors on every host thread (numba
+    parallel=True, geometry.py:919, universal.py:164), the exchange on one
+    (RadiosityFast.py:1396 compiles _energy_exchange with numba.njit(), not
+    parallel).  Samples, all on the same scene and its own pair lists:
       visibility - full rows of the visibility matrix at evenly spaced
                    patches (every pair against every blocker, as
                    geometry.py:750-797), scaled by N(N-1)/2 / pairs evaluated;
       form factors - the visible pairs (i < j) of those rows (universal.py),
                    scaled by the visible-pair count those rows imply;
-      exchange   - one order of RadiosityFast.py:1121-1143 for the sampled
-                   patches as destinations, their visible partners as sources
-                   (true delays; source rows read from a 64-row buffer, the
-                   cost does not depend on the values), times N / rows and
-                   the number of orders.
+      exchange   - one order of RadiosityFast.py:1121-1143 for
+                   `exchange_rows` of the sampled patches as destinations,
+                   their visible partners as sources (true delays; source
+                   rows read from a 64-row buffer, the cost does not depend on
+                   the values), times N / rows and the number of orders.
     Returns (ms_per_solve, threads, description).
     """
     from oracle import oracle as orc
@@ -194,7 +200,9 @@ def cpu_baseline(cfg, rows_per_thread=1):
     t0 = time.perf_counter()
     orc.form_factors(pts, normals, area, pairs)
     t_ff = (time.perf_counter() - t0) * total_visible / max(pairs.shape[0], 1)
-    # one exchange order for the sampled rows as destinations
+    # one exchange order for some of the sampled rows as destinations
+    keep_rows = np.linspace(0, rows.shape[0] - 1, min(exchange_rows, rows.shape[0])).astype(int)
+    rows, row_ids = rows[keep_rows], row_ids[keep_rows]
     nd = sc["dirs_out"].shape[1]
     nb = sc["brdf"].shape[-1]
     n_in = sc["brdf"].shape[1]
@@ -214,17 +222,57 @@ def cpu_baseline(cfg, rows_per_thread=1):
     att = np.ones((m, nb))
     slot = np.asarray(sc["brdf_index"])[wall_of[src]].astype(np.int32)
     prev = rng.uniform(0, 1e-3, size=(64, nd * nb * nt))
-    t0 = time.perf_counter()
-    orc.exchange_rows_sample(nd, nb, nt, prev, dst_off, src, p2o, delay, fprime, att, slot, s_in, sc["brdf"],
-                             row_ids.astype(np.int32))
-    t_order = (time.perf_counter() - t0) * n / rows.shape[0]
+    orc.set_threads(1)  # the reference's exchange is serial numba
+    try:
+        t0 = time.perf_counter()
+        orc.exchange_rows_sample(nd, nb, nt, prev, dst_off, src, p2o, delay, fprime, att, slot, s_in, sc["brdf"],
+                                 row_ids.astype(np.int32))
+        t_order = (time.perf_counter() - t0) * n / rows.shape[0]
+    finally:
+        orc.set_threads(threads)
     total = t_vis + t_ff + cfg["max_order"] * t_order
-    desc = (f"oracle C++/OpenMP FP64 on {threads} threads: visibility of {rows.shape[0]} full patch rows "
+    desc = (f"EXTRAPOLATED from samples (no complete solve at this size): oracle C++/OpenMP FP64, visibility and "
+            f"form factors on {threads} threads (numba parallel=True in the reference), the exchange on 1 thread "
+            f"(serial numba.njit in the reference, RadiosityFast.py:1396): visibility of {n_rows} full patch rows "
             f"({pairs_evaluated} pairs x {n} blockers), form factors of {pairs.shape[0]} of their visible pairs, "
-            f"one exchange order for those {rows.shape[0]} destination patches ({m} incoming pairs); "
+            f"one exchange order for {rows.shape[0]} destination patches ({m} incoming pairs); "
             f"extrapolated by pair/row counts to one solve: visibility {t_vis:.1f} s, form factors {t_ff:.1f} s, "
             f"{cfg['max_order']} orders x {t_order:.1f} s")
     return total * 1e3, threads, desc
+
+
+def cpu_full_solve_cfg1():
+    """One complete oracle solve of the 126-patch shoebox (cfg1), timed, no extrapolation.
+
+    Bake (visibility and form factors on every host thread, as the
+    reference's parallel numba loops), source energy, the 20 exchange orders
+    on one thread (serial in the reference) and the receiver histogram.
+    Returns (ms, threads, description, mono).
+    """
+    from oracle import oracle as orc
+    from oracle.scene import scene_from_radiosity
+    from sparrowpy_gb300 import scenes
+    cfg = scenes.config("cfg1", precision="fp64")
+    sc = scene_from_radiosity(cfg["radiosity"])
+    threads = orc.num_threads()
+    src, rcv = cfg["source"], cfg["receivers"]
+    nt = int(cfg["duration"] / cfg["dt"])
+    t0 = time.perf_counter()
+    bk = orc.bake(sc)
+    e0dir, d0, _ = orc.init_source(sc, bk, src)
+    t1 = time.perf_counter()
+    orc.set_threads(1)
+    try:
+        etot = orc.exchange(sc, bk, e0dir, d0, cfg["c"], cfg["dt"], nt, cfg["max_order"])
+    finally:
+        orc.set_threads(threads)
+    t2 = time.perf_counter()
+    mono = orc.collect(sc, bk, etot, rcv, cfg["c"], cfg["dt"])
+    t3 = time.perf_counter()
+    desc = (f"complete oracle FP64 solve of cfg1 (126 patches, {bk['src'].size} directed pairs, 16 directions, "
+            f"1 band, T={nt}, order {cfg['max_order']}): bake + source {1e3 * (t1 - t0):.0f} ms on {threads} threads, "
+            f"exchange {1e3 * (t2 - t1):.0f} ms on 1 thread, collection {1e3 * (t3 - t2):.0f} ms")
+    return 1e3 * (t2 - t0), threads, desc, mono
 
 
 # ----------------------------------------------------------------- GPU arm
@@ -402,6 +450,17 @@ def run_gpu(args):
         except Exception as exc:  # the gradient leg must not hide the solve result
             fwd_bwd = {"error": f"{type(exc).__name__}: {exc}"}
 
+    configs = None
+    if not args.no_configs and rank == 0:
+        r._dev.clear()
+        r._bake = None
+        torch.cuda.empty_cache()
+        try:
+            cfg1_cpu = None if args.no_cpu else cpu_full_solve_cfg1()
+            configs = config_legs(cfg1_cpu)
+        except Exception as exc:  # the config legs must not hide the solve result
+            configs = {"error": f"{type(exc).__name__}: {exc}"}
+
     batch = None
     if args.batch_rooms > 0:
         barrier()
@@ -437,6 +496,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
             "fwd_bwd": fwd_bwd,
+            "configs": configs,
             "batch": batch,
             "clocks": clk,
             "gpu_launches": int(launches),
@@ -449,67 +509,195 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------ per-config legs
+def _gpu_solve_timed(cfg, precision, repeats=2):
+    """Solve a config through the public API on the GPU: (ms per solve, mono histograms, radiosity)."""
+    import torch
+    from sparrowpy_gb300 import scenes
+    c = scenes.config(cfg, precision=precision)
+    r = c["radiosity"]
+    st = torch.cuda.current_stream()
+    ms = []
+    for k in range(repeats + 1):  # the first solve warms up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        solve(r, c, as_coords)
+        e1.record(st)
+        e1.synchronize()
+        if k > 0:
+            ms.append(e0.elapsed_time(e1))
+    mono = r.collect_energy_receiver_mono(as_coords(c["receivers"])).time
+    return float(np.mean(ms)), mono, r
+
+
+def config_legs(cpu_cfg1=None):
+    """cfg1 and cfg2 at FP32 and FP64 on the GPU, with their errors and the FP64 energy check.
+
+    cfg1 (126 patches) is also solved completely by the oracle on the host
+    (cpu_cfg1: the result of cpu_full_solve_cfg1), which gives the error
+    against the FP64 oracle and a measured CPU/GPU ratio; cfg2 (2016 patches)
+    is too large for a complete oracle solve, so its FP32 error is stated
+    against the FP64 GPU solve (itself oracle-checked at 1e-10 on smaller
+    scenes).
+    """
+    import torch
+    out = {}
+    for name in ("cfg1", "cfg2"):
+        leg = {}
+        ms32, m32, r32 = _gpu_solve_timed(name, "fp32")
+        eb32 = r32.energy_balance()
+        del r32
+        torch.cuda.empty_cache()
+        ms64, m64, r64 = _gpu_solve_timed(name, "fp64", repeats=1)
+        eb64 = r64.energy_balance()
+        del r64
+        torch.cuda.empty_cache()
+        leg.update(fp32_ms_per_solve=ms32, fp64_ms_per_solve=ms64, fp64_over_fp32=ms64 / ms32,
+                   receiver_rel_l2_fp32_vs_fp64_gpu=float(np.linalg.norm(m32 - m64) / np.linalg.norm(m64)),
+                   energy_check={"fp32_max_rel_dev": float(eb32["rel_dev"].max()),
+                                 "fp64_max_rel_dev": float(eb64["rel_dev"].max()),
+                                 "check_ms": eb32["ms"],
+                                 "meaning": "per-band FP64 sum of E_total against the time-free energy budget of "
+                                            "the orders; nothing is delayed past this histogram"})
+        if name == "cfg1" and cpu_cfg1 is not None:
+            cpu_ms, cores, desc, mono_ref = cpu_cfg1
+            leg.update(receiver_rel_l2_fp32_vs_oracle=float(np.linalg.norm(m32 - mono_ref) / np.linalg.norm(mono_ref)),
+                       receiver_rel_l2_fp64_vs_oracle=float(np.linalg.norm(m64 - mono_ref) / np.linalg.norm(mono_ref)),
+                       cpu_measured={"ms": cpu_ms, "cores": cores, "sample": desc},
+                       cpu_over_gpu_fp32=cpu_ms / ms32)
+        out[name] = leg
+    return out
+
+
 # ------------------------------------------------------- forward + backward
-def fwd_bwd_config4(steps=2, fd_params=2, seed=4):
+def fwd_bwd_config4(steps=2, fd_params=64, seed=4, fp64_reference=True):
     """Energy-decay-loss gradient w.r.t. per-patch, per-band absorption and scattering.
 
-    Shoebox 5 x 6 x 3 m, 0.25 m patches, one wall per patch (2016 patches), 6
-    bands, 64 directions, 1 ms x 2 s, order 50, 1 source, 1 receiver; the
-    target comes from a second seeded material set.  Times the forward solve
-    (with checkpoints) and forward + backward with CUDA events; checks the
-    largest gradients against central differences of the FP32 forward.
+    Timing: shoebox 5 x 6 x 3 m, 0.25 m patches, one wall per patch (2016
+    patches), 6 bands, 64 directions, 1 ms x 2 s, order 50, 1 source, 1
+    receiver; the target comes from a second seeded material set.  Times the
+    FP32 forward solve (with checkpoints) and forward + backward with CUDA
+    events.  References (fp64_reference):
+      * the FP64 adjoint of the same room (FP64 forward, checkpoints and
+        adjoint), against which every one of the 24,192 FP32 gradients is
+        compared;
+      * central differences (h = 1e-4) of the FP64 forward on `fd_params`
+        seeded random parameters, on the same materials model over config
+        1's geometry (the 5 x 6 x 3 m room at 1 m patches, 126 patches, same
+        bands, directions, histogram and order): 128 FP64 solves there take
+        seconds, where the 2016-patch room's would take about 15 minutes.
     """
     import torch
     from sparrowpy_gb300.adjoint import DifferentiableExchange, as_source, energy_decay_loss, per_patch_room
     from sparrowpy_gb300.brdf import hemisphere_directions
     dirs = hemisphere_directions(64)
-    r = per_patch_room((5.0, 6.0, 3.0), 0.25, dirs, 6)
     src, rcv = np.array([2.0, 2.0, 1.5]), np.array([[3.0, 4.0, 1.5]])
-    solver = DifferentiableExchange(r, dirs, as_source(src), rcv, 343.0, 1e-3, 2.0, 50)
-    rng = np.random.default_rng(seed)
-    S = solver.n_slots
     dev = "cuda"
     t = lambda x, g=False: torch.tensor(x, dtype=torch.float64, device=dev, requires_grad=g)
-    alpha0, scat0 = rng.uniform(0.02, 0.6, (S, 6)), rng.uniform(0.1, 0.9, (S, 6))
-    target = solver.forward_only(t(rng.uniform(0.02, 0.6, (S, 6))), t(rng.uniform(0.1, 0.9, (S, 6))))
     st = torch.cuda.current_stream()
-    fwd_ms, both_ms = [], []
-    for k in range(steps + 1):  # first pass warms up
+
+    def room(patch, precision):
+        r = per_patch_room((5.0, 6.0, 3.0), patch, dirs, 6, precision=precision)
+        return r, DifferentiableExchange(r, dirs, as_source(src), rcv, 343.0, 1e-3, 2.0, 50)
+
+    def grads(solver, alpha0, scat0, target, n_steps):
+        fwd_ms, both_ms = [], []
+        for k in range(n_steps + 1):  # the first pass warms up
+            a_t, s_t = t(alpha0, True), t(scat0, True)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(st)
+            loss = energy_decay_loss(solver(a_t, s_t), target)
+            e1.record(st)
+            loss.backward()
+            e2.record(st)
+            e2.synchronize()
+            if k > 0 or n_steps == 0:
+                fwd_ms.append(e0.elapsed_time(e1))
+                both_ms.append(e0.elapsed_time(e2))
+        return a_t.grad.cpu().numpy(), s_t.grad.cpu().numpy(), fwd_ms, both_ms
+
+    rng = np.random.default_rng(seed)
+    r, solver = room(0.25, "fp32")
+    S = solver.n_slots
+    alpha0, scat0 = rng.uniform(0.02, 0.6, (S, 6)), rng.uniform(0.1, 0.9, (S, 6))
+    alpha_t, scat_t = rng.uniform(0.02, 0.6, (S, 6)), rng.uniform(0.1, 0.9, (S, 6))
+    target = solver.forward_only(t(alpha_t), t(scat_t))
+    ga, gs, fwd_ms, both_ms = grads(solver, alpha0, scat0, target, steps)
+    out = {"workload": "shoebox 5x6x3 m, 0.25 m patches, one wall per patch: 2016 patches, 6 bands, 64 directions, "
+                       "T=2000, order 50; loss = sum (log EDC - log EDC_target)^2",
+           "params": int(ga.size + gs.size), "fwd_ms": float(np.mean(fwd_ms)), "fwd_bwd_ms": float(np.mean(both_ms)),
+           "fwd_bwd_over_fwd": float(np.mean(both_ms) / np.mean(fwd_ms)), "checkpoint_every": solver.m}
+    del solver, r
+    torch.cuda.empty_cache()
+    if fp64_reference:
+        r64, s64 = room(0.25, "fp64")
+        ga64, gs64, f64_ms, b64_ms = grads(s64, alpha0, scat0, s64.forward_only(t(alpha_t), t(scat_t)), 0)
+        del s64, r64
+        torch.cuda.empty_cache()
+        g32 = np.concatenate([ga.ravel(), gs.ravel()])
+        g64 = np.concatenate([ga64.ravel(), gs64.ravel()])
+        big = np.abs(g64) > 1e-3 * np.abs(g64).max()
+        out["fp64_adjoint"] = {
+            "fwd_bwd_ms": float(b64_ms[0]),
+            "max_abs_err_over_max_grad": float(np.abs(g32 - g64).max() / np.abs(g64).max()),
+            "rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
+            "max_rel_err_where_grad_above_1e-3_max": float((np.abs(g32 - g64)[big] / np.abs(g64)[big]).max())}
+    if fd_params > 0:
+        out["fd_check"] = fd_check_cfg1_geometry(fd_params, seed=seed + 1)
+    return out
+
+
+def fd_check_cfg1_geometry(n_params, seed=5, h=1e-4):
+    """FP32 and FP64 adjoint gradients against central differences of the FP64 forward (h = 1e-4).
+
+    Per-patch materials over config 1's geometry (5 x 6 x 3 m, 1 m patches,
+    126 patches), 6 bands, 64 directions, T = 2000, order 50; `n_params`
+    seeded random (absorption or scattering, patch, band) entries.
+    """
+    import torch
+    from sparrowpy_gb300.adjoint import DifferentiableExchange, as_source, energy_decay_loss, per_patch_room
+    from sparrowpy_gb300.brdf import hemisphere_directions
+    dirs = hemisphere_directions(64)
+    src, rcv = np.array([2.0, 2.0, 1.5]), np.array([[3.0, 4.0, 1.5]])
+    t = lambda x, g=False: torch.tensor(x, dtype=torch.float64, device="cuda", requires_grad=g)
+    rng = np.random.default_rng(seed)
+    solvers = {}
+    for prec in ("fp32", "fp64"):
+        r = per_patch_room((5.0, 6.0, 3.0), 1.0, dirs, 6, precision=prec)
+        solvers[prec] = DifferentiableExchange(r, dirs, as_source(src), rcv, 343.0, 1e-3, 2.0, 50)
+    S = solvers["fp64"].n_slots
+    alpha0, scat0 = rng.uniform(0.02, 0.6, (S, 6)), rng.uniform(0.1, 0.9, (S, 6))
+    target = solvers["fp64"].forward_only(t(rng.uniform(0.02, 0.6, (S, 6))), t(rng.uniform(0.1, 0.9, (S, 6))))
+    g = {}
+    for prec, sv in solvers.items():
         a_t, s_t = t(alpha0, True), t(scat0, True)
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-        e0.record(st)
-        loss = energy_decay_loss(solver(a_t, s_t), target)
-        e1.record(st)
-        loss.backward()
-        e2.record(st)
-        e2.synchronize()
-        if k > 0:
-            fwd_ms.append(e0.elapsed_time(e1))
-            both_ms.append(e0.elapsed_time(e2))
-    ga, gs = a_t.grad.cpu().numpy(), s_t.grad.cpu().numpy()
-    fd = []
-    h = 1e-3
-    flat = np.abs(np.concatenate([ga.ravel(), gs.ravel()]))
-    for q in np.argsort(flat)[::-1][:fd_params]:
-        which, k = (0, q) if q < ga.size else (1, q - ga.size)
-        idx = np.unravel_index(k, ga.shape)
+        energy_decay_loss(sv(a_t, s_t), target).backward()
+        g[prec] = (a_t.grad.cpu().numpy(), s_t.grad.cpu().numpy())
+    flat = rng.choice(2 * S * 6, size=n_params, replace=False)
+    entries = []
+    for q in flat:
+        which, k = int(q >= S * 6), int(q % (S * 6))
+        idx = np.unravel_index(k, (S, 6))
         vals = []
         for sign in (1, -1):
             a, s_ = alpha0.copy(), scat0.copy()
             (a if which == 0 else s_)[idx] += sign * h
-            vals.append(float(energy_decay_loss(solver.forward_only(t(a), t(s_)), target)))
-        fdv = (vals[0] - vals[1]) / (2 * h)
-        g = float((ga if which == 0 else gs)[idx])
-        fd.append({"param": ["absorption", "scattering"][which], "index": [int(x) for x in idx], "adjoint": g,
-                   "central_difference": fdv, "rel_err": abs(g - fdv) / max(abs(fdv), 1e-300)})
-    out = {"workload": "shoebox 5x6x3 m, 0.25 m patches, one wall per patch: 2016 patches, 6 bands, 64 directions, "
-                       "T=2000, order 50; loss = sum (log EDC - log EDC_target)^2",
-           "params": int(ga.size + gs.size), "fwd_ms": float(np.mean(fwd_ms)), "fwd_bwd_ms": float(np.mean(both_ms)),
-           "fwd_bwd_over_fwd": float(np.mean(both_ms) / np.mean(fwd_ms)), "checkpoint_every": solver.m,
-           "fd_check_h": h, "fd_check": fd}
-    del solver, r, target
-    torch.cuda.empty_cache()
-    return out
+            vals.append(float(energy_decay_loss(solvers["fp64"].forward_only(t(a), t(s_)), target)))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        entries.append({"param": ["absorption", "scattering"][which], "index": [int(x) for x in idx],
+                        "central_difference_fp64": fd, "adjoint_fp64": float(g["fp64"][which][idx]),
+                        "adjoint_fp32": float(g["fp32"][which][idx])})
+    fd = np.array([e["central_difference_fp64"] for e in entries])
+    a64 = np.array([e["adjoint_fp64"] for e in entries])
+    a32 = np.array([e["adjoint_fp32"] for e in entries])
+    scale = np.abs(fd).max()
+    return {"workload": "per-patch materials over cfg1's geometry (5x6x3 m, 1 m patches: 126 patches), 6 bands, "
+                        "64 directions, T=2000, order 50", "h": h, "params": int(n_params),
+            "max_rel_err_fp64_adjoint": float(np.max(np.abs(a64 - fd) / np.maximum(np.abs(fd), 1e-300))),
+            "max_err_over_scale_fp64_adjoint": float(np.abs(a64 - fd).max() / scale),
+            "max_err_over_scale_fp32_adjoint": float(np.abs(a32 - fd).max() / scale),
+            "median_rel_err_fp32_adjoint": float(np.median(np.abs(a32 - fd) / np.maximum(np.abs(fd), 1e-300))),
+            "entries": entries}
 
 
 # ------------------------------------------------------------------- batch
@@ -565,8 +753,7 @@ if __name__ == "__main__":
     if a.fwd_bwd_only:
         import torch
         torch.cuda.set_device(dist_env()[2])
-        print(json.dumps({"metric": "fwd+bwd ms", "fwd_bwd": fwd_bwd_config4(steps=a.steps, fd_params=0)}),
-              flush=True)
+        print(json.dumps({"metric": "fwd+bwd ms", "fwd_bwd": fwd_bwd_config4(steps=a.steps)}), flush=True)
     elif a.impl == "reference":
         run_reference(a)
     else:

@@ -6,7 +6,7 @@
  * function interface; each entry point below replaces one of its numba or
  * numpy routines, named in the comment as file:line inside the sparrowpy
  * source tree.  The Python class sparrowpy_gb300.DirectionalRadiosityFast
- * binds these symbols with ctypes; INTEGRATION.md shows the binding.
+ * binds these symbols with ctypes (sparrowpy_gb300/_native.py).
  *
  * Conventions
  *  - Every pointer argument is a DEVICE pointer unless stated otherwise.
@@ -41,7 +41,13 @@ typedef enum {
 } sp_status;
 
 enum { SP_F32 = 0, SP_F64 = 1 };
-enum { SP_EXCHANGE_DENSE = 0, SP_EXCHANGE_STRUCTURED = 1, SP_EXCHANGE_MATERIAL = 2 };
+enum {
+    SP_EXCHANGE_DENSE = 0,
+    SP_EXCHANGE_STRUCTURED = 1,
+    SP_EXCHANGE_MATERIAL = 2,
+    SP_EXCHANGE_SLOTWISE = 3,
+    SP_EXCHANGE_GENERAL = 4
+};
 
 /* Library version string (static storage). */
 const char* sp_version(void);
@@ -69,17 +75,24 @@ int sp_patch_visibility(int n, int nv, const double* centers, const double* norm
  * For callers that cannot allocate device memory when visibility is
  * recomputed, e.g. an engine that reserves its whole device budget up front
  * and re-bakes after geometry edits, or a binding without a device allocator
- * of its own, so it has no workspace to pass.  Same arguments, results and
- * kernels as sp_patch_visibility, without ws/ws_bytes: the blocker-box
- * scratch is a fixed 405,504-byte array inside this library's device image
- * (reserved when the module loads).  This call allocates nothing.
+ * of its own, so it has no workspace to pass.  Same arguments and results
+ * as sp_patch_visibility, without ws/ws_bytes: the blocker-box scratch is a
+ * fixed 405,504-byte array inside this library's device image (reserved
+ * when the module loads).  This call allocates nothing.
  *
+ * Cost: it runs the single-pass kernel (one pair per thread, the exact FP64
+ *   predicate against every blocker box the pair's segment crosses), not
+ *   the three-pass form of sp_patch_visibility, whose own-patch pass and
+ *   compacted candidate lists need the workspace.  On the 5939-patch street
+ *   canyon it takes about 240 ms against about 19 ms.
  * Limit: n <= 16384 patches; larger n returns SP_ERR_WORKSPACE before any
  *   device work (use sp_patch_visibility there).
  * Set-up: the first call on each device, made with that device current,
- *   looks up the array's address (cudaGetSymbolAddress) and keeps it; make
- *   that first call before any stream capture.  A failed lookup returns
- *   SP_ERR_CUDA.
+ *   looks up the array's address (cudaGetSymbolAddress) and keeps it per
+ *   device ordinal; make that first call before any stream capture.  A
+ *   failed lookup returns SP_ERR_CUDA.  The kept address belongs to the
+ *   device's primary context: after cudaDeviceReset, or from a context
+ *   made with the driver API, it is stale; use sp_patch_visibility there.
  * Zeroing: nothing has to start at zero (every box read is written earlier
  *   in the same call; vis is cleared on the stream as in sp_patch_visibility).
  * Concurrency: all calls on a device share the one scratch array, so calls
@@ -225,7 +238,7 @@ typedef struct sp_exchange_args {
     int skip_total;         /* 1: etc_total is neither cleared nor written */
     /* SP_EXCHANGE_MATERIAL only: per-slot create_from_scattering materials
        BRDF_s[c, o, b] = (1 - alpha[s, b]) (scat[s, b] + (1 - scat[s, b]) gain[c] [o == mirror[c]])
-       (brdf, slot_group, slot_scale and class_* are not used; FP32 only) */
+       (brdf, slot_group, slot_scale and class_* are not used; FP32 or FP64) */
     const double* mat_alpha;        /* (n_slots, B) */
     const double* mat_scattering;   /* (n_slots, B) */
     const int32_t* mat_mirror;      /* (n_in) mirror outgoing direction, -1: none */
@@ -235,13 +248,29 @@ typedef struct sp_exchange_args {
        previous call with this tag (and these sizes) is then reused */
     long long plan_tag;
     float* scatter_ms;      /* HOST float or NULL: CUDA-event time of the scatter launches alone (all orders) */
+    /* structured / material, FP32: E_total's late bins (t >= n_samples / 4, rounded down to a multiple of 4)
+       are accumulated over the orders with Kahan compensation; 1 = plain FP32 sums instead */
+    int plain_total;
+    /* SP_EXCHANGE_GENERAL only: (n_groups * n_in_dirs, D, B) normalised table rows of the classes, with
+       BRDF[slot, s, o, b] = slot_scale[slot, b] class_table[slot_group[slot] * n_in + s, o, b] */
+    const double* class_table;
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070
  * `_energy_exchange_init_energy` (max_order < 1).  Synchronises `stream` once
  * (to report SP_ERR_RANGE for a source delay outside the histogram).
- * n_classes = n_groups * n_in_dirs for SP_EXCHANGE_STRUCTURED (<= 256),
- * 1 + n_in_dirs for SP_EXCHANGE_MATERIAL. */
+ * Algorithms: SP_EXCHANGE_DENSE (any BRDF table, D FMAs per pair and bin);
+ * SP_EXCHANGE_STRUCTURED (diffuse-plus-mirror rows, pairs scattered per class
+ * (material group, incoming direction), n_classes = n_groups * n_in_dirs <=
+ * 256); SP_EXCHANGE_SLOTWISE (the same tables with any number of groups,
+ * e.g. per-patch scattering: each pair scattered into a diffuse class and
+ * its mirror direction's class, n_classes = 1 + n_dirs; reads the same
+ * slot_group / slot_scale / class_* fields); SP_EXCHANGE_GENERAL (any
+ * tables, grouped by proportional tables: pairs scattered per class as in
+ * the structured algorithm, then each receiver's classes contracted with
+ * the full table rows, on the tensor cores for FP32 with n_dirs >= 32;
+ * n_classes = n_groups * n_in_dirs <= 256); SP_EXCHANGE_MATERIAL (per-slot
+ * absorption and scattering, n_classes = 1 + n_in_dirs). */
 size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins,
                                     int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs,
                                     int n_classes);
@@ -249,9 +278,32 @@ int sp_energy_exchange(const sp_exchange_args* args, void* ws, size_t ws_bytes, 
 /* sizeof(sp_exchange_args), for bindings that mirror the struct. */
 size_t sp_exchange_args_size(void);
 
+/* ------------------------------------------------------------ energy check */
+
+/* Per-band total energy of E_total (N, D, B, T) in `precision`: out[b] (FP64,
+ * device) = sum over patches, directions and bins, accumulated in FP64 in a
+ * fixed order (no counterpart in the reference; the FP64 per-band
+ * total-energy check).  n_rows = N * D.  ws: sp_energy_totals_workspace(B). */
+size_t sp_energy_totals_workspace(int n_bins);
+int sp_energy_totals(int precision, long long n_rows, int n_bins, int n_samples, const void* etot, double* out,
+                     void* ws, size_t ws_bytes, void* stream);
+
+/* The same totals predicted without time, in FP64: the orders of
+ * RadiosityFast.py:1121-1143 summed over t map e_{k-1}[i, o, b] = sum_t
+ * E_{k-1} linearly through ff_tilde (:1234-1272), starting from E0dir; the
+ * budget is sum_{k <= max_order} sum_{j, o} e_k[j, o, b] -> totals (B, device).
+ * It equals sp_energy_totals of the solve's E_total when no contribution is
+ * delayed past the histogram (the reference drops those, :1137-1143).  Uses
+ * the dense BRDF tables and pair data of `a` (n_dirs * n_bins <= 512);
+ * precision, algorithm and the histogram fields are not read.
+ * ws: sp_energy_budget_workspace bytes. */
+size_t sp_energy_budget_workspace(int n_patches, int n_dirs, int n_bins, long long n_dir_pairs);
+int sp_energy_budget(const sp_exchange_args* a, double* totals, void* ws, size_t ws_bytes, void* stream);
+
 /* ------------------------------------------------------------------ adjoint */
 
-/* Reverse-mode gradient of the FP32 structured exchange (no counterpart in
+/* Reverse-mode gradient of the structured exchange, FP32 or FP64 (the
+ * precision of the forward arguments `fwd`; no counterpart in
  * the reference, which is not differentiable).  Materials: every slot s uses
  * the create_from_scattering table stored x pi (sparrowpy/brdf.py:8-130,
  * RadiosityFast.py:815): BRDF_s[c, o, b] = (1 - alpha[s, b]) (scattering[s, b]
@@ -260,8 +312,9 @@ size_t sp_exchange_args_size(void);
  * of the exchange orders and returns dL/dE0dir for the source term.
  *
  * Use: sp_adjoint_begin once (transposed plan, mu_K = dL/dE_total), then
- * sp_adjoint_order for k = K, K-1, ..., 1 with e_prev = E_{k-1} (FP32,
- * (N, D, B, T), e.g. from sp_energy_exchange states_out), then
+ * sp_adjoint_order for k = K, K-1, ..., 1 with e_prev = E_{k-1} (in the
+ * forward's precision, (N, D, B, T), e.g. from sp_energy_exchange
+ * states_out), then
  * sp_adjoint_finish.  The workspace carries the state between the calls;
  * `state` is a HOST struct owned by the caller (zeroed before begin). */
 typedef struct sp_adjoint_state {
@@ -288,8 +341,8 @@ typedef struct sp_adjoint_args {
     sp_adjoint_state* state;      /* HOST */
 } sp_adjoint_args;
 
-size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs,
-                            int n_receivers);
+size_t sp_adjoint_workspace(int precision, int n_patches, int n_dirs, int n_bins, int n_samples,
+                            long long n_dir_pairs, int n_receivers);
 int sp_adjoint_begin(const sp_adjoint_args* args, void* ws, size_t ws_bytes, void* stream);
 int sp_adjoint_order(const sp_adjoint_args* args, const void* e_prev, void* ws, size_t ws_bytes, void* stream);
 int sp_adjoint_finish(const sp_adjoint_args* args, double* grad_e0dir, void* ws, size_t ws_bytes, void* stream);

@@ -706,6 +706,39 @@ double orc_exchange_rows_sample(int nd, int nb, int nt, const double* prev, int 
     return total;
 }
 
+// One order of RadiosityFast.py:1121-1143 for the listed destination rows,
+// written out: out (n_rows, nd, nb, nt) FP64.  The previous order's
+// histograms come as FP32 rows (the GPU's own state): the source row of pair
+// e is prev[prev_row[e]] (nb * nt values, bands then bins), so a caller can
+// pass only the rows the sampled destinations read.  Same loop and summation
+// order as orc_exchange.
+int orc_exchange_rows_out(int nd, int nb, int nt, const float* prev, const int64_t* prev_row,
+                          const int64_t* dst_off, const int32_t* delay, const double* fprime, const double* att_fac,
+                          const int32_t* slot, const int32_t* s_in, const double* brdf, int n_in, int n_rows,
+                          const int32_t* rows, double* out) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int q = 0; q < n_rows; ++q) {
+        const int j = rows[q];
+        double* o_row = out + (size_t)q * nd * nb * nt;
+        std::memset(o_row, 0, sizeof(double) * (size_t)nd * nb * nt);
+        std::vector<double> in(nt);
+        for (int64_t e = dst_off[j]; e < dst_off[j + 1]; ++e) {
+            const int64_t nsh = delay[e];
+            const double* brow = brdf + (((size_t)slot[e] * n_in + s_in[e]) * nd) * nb;
+            for (int b = 0; b < nb; ++b) {
+                const float* src = prev + ((size_t)prev_row[e] * nb + b) * nt;
+                for (int t = 0; t < nt; ++t) in[t] = (double)src[t];
+                for (int o = 0; o < nd; ++o) {
+                    double f = (fprime[e] * att_fac[(size_t)e * nb + b]) * brow[(size_t)o * nb + b];
+                    double* o_ = o_row + ((size_t)o * nb + b) * nt;
+                    for (int64_t t = nsh; t < nt; ++t) o_[t] += f * in[t - nsh];
+                }
+            }
+        }
+    }
+    return 0;
+}
+
 // RadiosityFast.py:686-752 `_collect_energy_patches` + :1148-1185
 // `_collect_receiver_energy` for one receiver: out is (N, B, T).
 int orc_collect(int n, int nd, int nb, int nt, const double* etot, const int32_t* ridx, const double* rfac,

@@ -293,6 +293,24 @@ def visibility_rows_sample(ctr, normals, points, i0, i1, stride, full=False):
     return cnt, rows
 
 
+def exchange_rows_out(nd, nb, nt, prev_rows, prev_row_of_pair, dst_off, delay, fprime, att_fac, slot, s_in, brdf,
+                      rows):
+    """One exchange order (RadiosityFast.py:1121-1143) for destination `rows`, written out (R, nd, nb, nt) FP64.
+
+    prev_rows: float32 (M, nb, nt) source rows of the previous order;
+    prev_row_of_pair[e] is the row pair e reads (its source patch and
+    outgoing direction).  Pairs are destination-major (dst_off, (N + 1,)).
+    """
+    rows = _c(rows, np.int32)
+    out = np.zeros((rows.size, nd, nb, nt))
+    args = [_c(prev_rows, np.float32), _c(prev_row_of_pair, np.int64), _c(dst_off, np.int64), _c(delay, np.int32),
+            _c(fprime, float), _c(att_fac, float), _c(slot, np.int32), _c(s_in, np.int32), _c(brdf, float)]
+    lib().orc_exchange_rows_out(nd, nb, nt, _p(args[0]), _p(args[1]), _p(args[2]), _p(args[3]), _p(args[4]),
+                                _p(args[5]), _p(args[6]), _p(args[7]), _p(args[8]), brdf.shape[1], rows.size,
+                                _p(rows), _p(out))
+    return out
+
+
 def exchange_rows_sample(nd, nb, nt, prev, dst_off, src, p2o, delay, fprime, att_fac, slot, s_in, brdf, rows):
     """One exchange order for the given destination rows (RadiosityFast.py:1121-1143 loop)."""
     lib().orc_exchange_rows_sample.restype = ctypes.c_double

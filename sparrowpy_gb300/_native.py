@@ -21,6 +21,8 @@ SP_F64 = 1
 SP_EXCHANGE_DENSE = 0
 SP_EXCHANGE_STRUCTURED = 1
 SP_EXCHANGE_MATERIAL = 2
+SP_EXCHANGE_SLOTWISE = 3
+SP_EXCHANGE_GENERAL = 4
 
 _ERRORS = {
     SP_ERR_ARG: "invalid argument",
@@ -57,7 +59,8 @@ class ExchangeArgs(ctypes.Structure):
         ("order_ms", ctypes.POINTER(ctypes.c_float)),
         ("state_in", P), ("state_order", I), ("states_out", P), ("states_every", I), ("skip_total", I),
         ("mat_alpha", P), ("mat_scattering", P), ("mat_mirror", P), ("mat_gain", P),
-        ("plan_tag", LL), ("scatter_ms", ctypes.POINTER(ctypes.c_float)),
+        ("plan_tag", LL), ("scatter_ms", ctypes.POINTER(ctypes.c_float)), ("plain_total", I),
+        ("class_table", P),
     ]
 
 
@@ -102,7 +105,11 @@ _SIGS = {
     "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
     "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I, I]),
     "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
-    "sp_adjoint_workspace": (SZ, [I, I, I, I, LL, I]),
+    "sp_energy_totals_workspace": (SZ, [I]),
+    "sp_energy_totals": (I, [I, LL, I, I, P, P, P, SZ, P]),
+    "sp_energy_budget_workspace": (SZ, [I, I, I, LL]),
+    "sp_energy_budget": (I, [ctypes.POINTER(ExchangeArgs), P, P, SZ, P]),
+    "sp_adjoint_workspace": (SZ, [I, I, I, I, I, LL, I]),
     "sp_adjoint_begin": (I, [ctypes.POINTER(AdjointArgs), P, SZ, P]),
     "sp_adjoint_order": (I, [ctypes.POINTER(AdjointArgs), P, P, SZ, P]),
     "sp_adjoint_finish": (I, [ctypes.POINTER(AdjointArgs), P, P, SZ, P]),

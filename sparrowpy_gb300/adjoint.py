@@ -8,9 +8,11 @@ per-band absorption a and scattering s:
 
 (m_c: mirror direction of incoming direction c, K_c = pi / (cos w) as in
 brdf.py:110-118).  `DifferentiableExchange` runs the forward solve (the
-same CUDA path as DirectionalRadiosityFast, FP32 histograms) and, behind a
+same CUDA path as DirectionalRadiosityFast, FP32 histograms, or FP64 when
+the radiosity object's precision is "fp64") and, behind a
 torch.autograd.Function, the hand-written adjoint of the exchange
-(libsparrow_gb300: sp_adjoint_*).  Exchange states are checkpointed every m
+(libsparrow_gb300: sp_adjoint_*) in the same precision.  The FP64 form
+serves as the reference gradient of the FP32 one.  Exchange states are checkpointed every m
 orders on the forward pass (the smallest m whose states fit in device
 memory; sqrt(K) when memory is short) and recomputed segment by segment on
 the backward pass.  The reference has no differentiable path.
@@ -67,7 +69,7 @@ def energy_decay_loss(mono, target, eps=1e-30):
 class DifferentiableExchange:
     """Receiver histograms as a differentiable function of per-slot absorption and scattering.
 
-    radiosity: a DirectionalRadiosityFast (precision "fp32") whose walls use
+    radiosity: a DirectionalRadiosityFast (precision "fp32" or "fp64") whose walls use
     one direction set `directions` (the unrotated Coordinates their tables
     were built from); bake_geometry is run here once.  slot_of_wall maps each
     wall to its material slot (default: wall index).  Calling the object
@@ -78,9 +80,10 @@ class DifferentiableExchange:
     def __init__(self, radiosity, directions, source, receivers, speed_of_sound, etc_time_resolution, etc_duration,
                  max_reflection_order, slot_of_wall=None, checkpoint_every=None):
         r = radiosity
-        if r.precision != "fp32":
-            raise ValueError("the adjoint runs on the FP32 exchange")
         self.r = r
+        self.prec = nat.SP_F64 if r.precision == "fp64" else nat.SP_F32
+        self.dtype = torch.float64 if r.precision == "fp64" else torch.float32
+        self.esz = 8 if r.precision == "fp64" else 4
         self.source = source
         self.receivers = np.atleast_2d(np.asarray(receivers, dtype=float).reshape(-1, 3))
         self.c = float(speed_of_sound)
@@ -117,11 +120,11 @@ class DifferentiableExchange:
         """
         r = self.r
         n, nd, nb = r._dev["e0dir"].shape
-        h = n * nd * nb * self.nt * 4
+        h = n * nd * nb * self.nt * self.esz
         p = int(r._bake["n_dir"])
-        fw = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_MATERIAL, n, nd, nb, self.nt, p,
+        fw = nat.size("sp_energy_exchange_workspace", self.prec, nat.SP_EXCHANGE_MATERIAL, n, nd, nb, self.nt, p,
                       self.n_slots, self.mirror_np.size, 1 + self.mirror_np.size)
-        adj = nat.size("sp_adjoint_workspace", n, nd, nb, self.nt, p, int(self.receivers.shape[0]))
+        adj = nat.size("sp_adjoint_workspace", self.prec, n, nd, nb, self.nt, p, int(self.receivers.shape[0]))
         free, _ = torch.cuda.mem_get_info(r.device)
         avail = free + torch.cuda.memory_reserved(r.device) - torch.cuda.memory_allocated(r.device)
         for m in range(1, self.K + 1):
@@ -151,7 +154,7 @@ class DifferentiableExchange:
 
     def _workspace(self, a):
         n, nd, nb = self._e0dir.shape
-        wsz = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_MATERIAL, n, nd, nb, self.nt,
+        wsz = nat.size("sp_energy_exchange_workspace", self.prec, nat.SP_EXCHANGE_MATERIAL, n, nd, nb, self.nt,
                        a.n_dir_pairs, a.n_slots, a.n_in_dirs, 1 + a.n_in_dirs)
         return self.r._workspace(wsz), wsz
 
@@ -178,12 +181,12 @@ class DifferentiableExchange:
         scat64 = scattering.detach().to(torch.float64).contiguous()
         self._e0dir = self._source_dir(alpha64, scat64).contiguous()
         n, nd, nb = self._e0dir.shape
-        etc = torch.empty((n, nd, nb, self.nt), dtype=torch.float32, device=r.device)
+        etc = torch.empty((n, nd, nb, self.nt), dtype=self.dtype, device=r.device)
         a = self._args(alpha64, scat64, etc)
         states = None
         if keep_states:
             n_ck = self.K // self.m + 1
-            states = torch.empty((n_ck, n, nd, nb, self.nt), dtype=torch.float32, device=r.device)
+            states = torch.empty((n_ck, n, nd, nb, self.nt), dtype=self.dtype, device=r.device)
             a.states_out = states.data_ptr()
             a.states_every = self.m
         ws, wsz = self._workspace(a)
@@ -197,7 +200,7 @@ class DifferentiableExchange:
     def _resume(self, alpha64, scat64, state_in, k_from, k_to, states):
         """Orders k_from + 1 .. k_to from E_{k_from}; states[i] = E_{k_from + i} for i >= 1 (states[0] is not
         written: it would repeat state_in)."""
-        dummy = torch.empty((1,), dtype=torch.float32, device=self.r.device)
+        dummy = torch.empty((1,), dtype=self.dtype, device=self.r.device)
         a = self._args(alpha64, scat64, dummy)
         a.max_order = int(k_to)
         a.state_in = state_in.data_ptr()
@@ -230,7 +233,7 @@ class DifferentiableExchange:
         gs = torch.zeros_like(scat64)
         ridx, rfac, rdist = r._receiver_factors(self.receivers)
         gm = grad_mono.detach().to(torch.float64).contiguous()
-        etc_dummy = torch.empty((1,), dtype=torch.float32, device=dev)
+        etc_dummy = torch.empty((1,), dtype=self.dtype, device=dev)
         fwd = self._args(alpha64, scat64, etc_dummy)
         state = nat.AdjointState()
         a = nat.AdjointArgs()
@@ -247,11 +250,12 @@ class DifferentiableExchange:
         a.grad_alpha = ga.data_ptr()
         a.grad_scattering = gs.data_ptr()
         a.state = ctypes.pointer(state)
-        wsz = nat.size("sp_adjoint_workspace", n, nd, nb, nt, fwd.n_dir_pairs, int(self.receivers.shape[0]))
+        wsz = nat.size("sp_adjoint_workspace", self.prec, n, nd, nb, nt, fwd.n_dir_pairs,
+                       int(self.receivers.shape[0]))
         ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
         st = _stream()
         nat.call("sp_adjoint_begin", ctypes.byref(a), _ptr(ws), wsz, st)
-        seg_states = torch.empty((m, n, nd, nb, nt), dtype=torch.float32, device=dev) if m > 1 else None
+        seg_states = torch.empty((m, n, nd, nb, nt), dtype=self.dtype, device=dev) if m > 1 else None
         for seg in range((K - 1) // m, -1, -1):
             k_lo = seg * m                      # checkpointed state E_{k_lo}
             k_hi = min(k_lo + m, K)             # orders k_hi .. k_lo + 1 need E_{k_hi - 1} .. E_{k_lo}

@@ -291,7 +291,8 @@ extern "C" {
 size_t sp_energy_exchange_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins,
                                     int n_samples, long long n_dir_pairs, int n_slots, int n_in_dirs,
                                     int n_classes) {
-    if (algorithm == SP_EXCHANGE_STRUCTURED || algorithm == SP_EXCHANGE_MATERIAL)
+    if (algorithm == SP_EXCHANGE_STRUCTURED || algorithm == SP_EXCHANGE_MATERIAL || algorithm == SP_EXCHANGE_SLOTWISE ||
+        algorithm == SP_EXCHANGE_GENERAL)
         return sp_structured_workspace(precision, algorithm, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs,
                                        n_classes);
     if (precision == SP_F64)
@@ -312,7 +313,8 @@ int sp_energy_exchange(const sp_exchange_args* a, void* ws, size_t ws_bytes, voi
                                !a->pair_distance || !a->pair_fprime || !a->pair_unit_len))
         return SP_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    if (a->algorithm == SP_EXCHANGE_STRUCTURED || a->algorithm == SP_EXCHANGE_MATERIAL)
+    if (a->algorithm == SP_EXCHANGE_STRUCTURED || a->algorithm == SP_EXCHANGE_MATERIAL ||
+        a->algorithm == SP_EXCHANGE_SLOTWISE || a->algorithm == SP_EXCHANGE_GENERAL)
         return sp_run_structured(a, ws, ws_bytes, st);
     if (a->precision == SP_F64) return run_exchange_dense<double>(a, ws, ws_bytes, st);
     return run_exchange_dense<float>(a, ws, ws_bytes, st);

@@ -1,4 +1,4 @@
-// Adjoint (reverse mode) of the structured energy exchange, FP32.
+// Adjoint (reverse mode) of the structured energy exchange, FP32 or FP64.
 //
 // Forward, order k (RadiosityFast.py:1121-1143, pair e: i -> j, sender slot
 // s(i), incoming direction c(e), outgoing index p(e) of i toward j):
@@ -96,7 +96,7 @@ __global__ void k_double_offsets(int n, const int64_t* __restrict__ off, int64_t
 }
 
 // Coefficient of transposed pair t in band b: w_e,b (U kind) or w_e,b K_c(e)
-// (V kind).  The adjoint runs in FP32 only, so only the FP32 form exists.
+// (V kind), in FP64 (the FP64 adjoint) or from inputs truncated to FP32.
 struct AdjCoef {
     const int32_t* fwd;
     const int32_t* cls;
@@ -106,6 +106,12 @@ struct AdjCoef {
     const double* unit_len;
     const double* att;
     int nd;
+    __device__ double operator()(long long t, int b) const {
+        const long long e = fwd[t];
+        double f = fprime[e];
+        if (att) f = f * exp(-att[b] * unit_len[e]);
+        return cls[t] >= nd ? f * gain[in_dir[e]] : f;
+    }
     __device__ float f32(long long t, int b) const {
         const long long e = fwd[t];
         float f = f64_trunc_f32(fprime[e]);
@@ -118,9 +124,10 @@ struct AdjCoef {
 // mono[r, b, t] = sum_k E[k, ridx_rk, b, (t - s_rk) mod T] f_rk a_rkb (k_collect_mono),
 // so that row of g, reversed, is g_r[k, b, tau] = f_rk a_rkb gm[r, b, (T - 1 - tau + s_rk) mod T].
 // One block per (band, patch); g_rev is (R, N, B, T).
+template <typename T>
 __global__ void k_adjoint_g(int n, int nb, int nt, int n_rcv, const double* __restrict__ rfac,
                             const double* __restrict__ rdist, double c, double dt, const double* __restrict__ att,
-                            const double* __restrict__ gm, float* __restrict__ g_rev) {
+                            const double* __restrict__ gm, T* __restrict__ g_rev) {
     const int b = blockIdx.x, k = blockIdx.y;
     for (int r = 0; r < n_rcv; ++r) {
         const size_t rk = (size_t)r * n + k;
@@ -129,12 +136,12 @@ __global__ void k_adjoint_g(int n, int nb, int nt, int n_rcv, const double* __re
         s %= nt;
         if (s < 0) s += nt;
         const double f = rfac[rk] * (att ? exp(-att[b] * rdist[rk]) : 1.0);
-        float* out = g_rev + (rk * nb + b) * nt;
+        T* out = g_rev + (rk * nb + b) * nt;
         const double* src = gm + ((size_t)r * nb + b) * nt;
         for (int tau = threadIdx.x; tau < nt; tau += blockDim.x) {
             long long t = nt - 1 - tau + s;
             if (t >= nt) t -= nt;
-            out[tau] = (float)(f * src[t]);
+            out[tau] = (T)(f * src[t]);
         }
     }
 }
@@ -149,75 +156,77 @@ constexpr int kCombineBins = 16;   // bins per thread in k_adjoint_combine: nt <
 // Rows of dL/dE_total beyond the first two that fall on direction p of patch i
 // (three or more receivers seen along one direction): added to `out` (a mu
 // row, or the U row) at the bins this thread owns.
-__device__ __noinline__ void add_extra_rows(int p, int n_rcv, const int* s_ridx, const float* __restrict__ g_rev,
-                                            int n, int i, int nb, int b, int nt, float* out) {
+template <typename T>
+__device__ __noinline__ void add_extra_rows(int p, int n_rcv, const int* s_ridx, const T* __restrict__ g_rev,
+                                            int n, int i, int nb, int b, int nt, T* out) {
     for (int r = 0, h = 0; r < n_rcv; ++r) {
         if (s_ridx[r] != p || h++ < 2) continue;
-        const float* row = g_rev + (((size_t)r * n + i) * nb + b) * nt;
+        const T* row = g_rev + (((size_t)r * n + i) * nb + b) * nt;
         for (int tau = threadIdx.x; tau < nt; tau += 256) out[tau] += row[tau];
     }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(256) k_adjoint_combine(
     int n, int nd, int nb, int nt, long long rs, int lead, int n_rcv, const int32_t* __restrict__ ridx,
-    const float* __restrict__ g_rev, const float* __restrict__ lam, const uint32_t* __restrict__ present, int words, const int32_t* __restrict__ tile_of,
-    const float* __restrict__ e_prev, const int32_t* __restrict__ wall_of, const int32_t* __restrict__ brdf_index,
-    const double* __restrict__ alpha, const double* __restrict__ scat, float* __restrict__ mu_out,
-    double* __restrict__ grad_a, double* __restrict__ grad_s) {
+    const T* __restrict__ g_rev, const T* __restrict__ lam, const uint32_t* __restrict__ present, int words,
+    const int32_t* __restrict__ tile_of, const T* __restrict__ e_prev, const int32_t* __restrict__ wall_of,
+    const int32_t* __restrict__ brdf_index, const double* __restrict__ alpha, const double* __restrict__ scat,
+    T* __restrict__ mu_out, double* __restrict__ grad_a, double* __restrict__ grad_s) {
     const int b = blockIdx.x, i = blockIdx.y;
     __shared__ int s_ridx[kMaxReceivers];
     for (int r = threadIdx.x; r < n_rcv; r += blockDim.x) s_ridx[r] = ridx[(size_t)r * n + i];
     __syncthreads();
     const int slot = brdf_index[wall_of[i]];
-    const float a = (float)alpha[(size_t)slot * nb + b];
-    const float sc = (float)scat[(size_t)slot * nb + b];
-    const float keep = 1.0f - a;
+    const T a = (T)alpha[(size_t)slot * nb + b];
+    const T sc = (T)scat[(size_t)slot * nb + b];
+    const T keep = T(1) - a;
     const uint32_t* pres = lam ? present + (size_t)tile_of[i] * words : nullptr;
     constexpr int kMaxPerThread = kCombineBins;
-    float usum[kMaxPerThread];
+    T usum[kMaxPerThread];
 #pragma unroll
-    for (int q = 0; q < kMaxPerThread; ++q) usum[q] = 0.0f;
-    float dot_mix = 0.0f, dot_diff = 0.0f;
+    for (int q = 0; q < kMaxPerThread; ++q) usum[q] = T(0);
+    T dot_mix = T(0), dot_diff = T(0);
     for (int p = 0; p < nd; ++p) {
         // rows of dL/dE_total in direction p of this patch (one per receiver seeing it along p)
-        const float* g0 = nullptr;
-        const float* g1 = nullptr;
+        const T* g0 = nullptr;
+        const T* g1 = nullptr;
         int n_hit = 0;
         for (int r = 0; r < n_rcv; ++r)
             if (s_ridx[r] == p) {
-                const float* row = g_rev + (((size_t)r * n + i) * nb + b) * nt;
+                const T* row = g_rev + (((size_t)r * n + i) * nb + b) * nt;
                 if (n_hit == 0) g0 = row;
                 else if (n_hit == 1) g1 = row;
                 ++n_hit;
             }
         const bool has_u = pres && ((pres[p >> 5] >> (p & 31)) & 1u);
         const bool has_v = pres && ((pres[(nd + p) >> 5] >> ((nd + p) & 31)) & 1u);
-        const float* lu = has_u ? lam + (((size_t)i * 2 * nd + p) * nb + b) * nt : nullptr;
-        const float* lv = has_v ? lam + (((size_t)i * 2 * nd + nd + p) * nb + b) * nt : nullptr;
-        const float* ep = e_prev ? e_prev + (((size_t)i * nd + p) * nb + b) * nt : nullptr;
-        float* mo = mu_out + (((size_t)i * (nd + 1) + p) * nb + b) * rs + lead;
+        const T* lu = has_u ? lam + (((size_t)i * 2 * nd + p) * nb + b) * nt : nullptr;
+        const T* lv = has_v ? lam + (((size_t)i * 2 * nd + nd + p) * nb + b) * nt : nullptr;
+        const T* ep = e_prev ? e_prev + (((size_t)i * nd + p) * nb + b) * nt : nullptr;
+        T* mo = mu_out + (((size_t)i * (nd + 1) + p) * nb + b) * rs + lead;
 #pragma unroll
         for (int q = 0; q < kMaxPerThread; ++q) {
             const int tau = threadIdx.x + 256 * q;
             if (tau < nt) {
-                const float u = lu ? lu[tau] : 0.0f;
-                const float v = lv ? lv[tau] : 0.0f;
-                const float mixed = sc * u + (1.0f - sc) * v;
-                float m = keep * mixed;
+                const T u = lu ? lu[tau] : T(0);
+                const T v = lv ? lv[tau] : T(0);
+                const T mixed = sc * u + (T(1) - sc) * v;
+                T m = keep * mixed;
                 if (g0) m += g0[tau];
                 if (g1) m += g1[tau];
                 mo[tau] = m;
                 usum[q] += m;
                 if (ep) {
-                    const float e = ep[nt - 1 - tau];
-                    dot_mix = fmaf(e, mixed, dot_mix);
-                    dot_diff = fmaf(e, u - v, dot_diff);
+                    const T e = ep[nt - 1 - tau];
+                    dot_mix = fma(e, mixed, dot_mix);
+                    dot_diff = fma(e, u - v, dot_diff);
                 }
             }
         }
         if (n_hit > 2) add_extra_rows(p, n_rcv, s_ridx, g_rev, n, i, nb, b, nt, mo);
     }
-    float* mu_u = mu_out + (((size_t)i * (nd + 1) + nd) * nb + b) * rs + lead;
+    T* mu_u = mu_out + (((size_t)i * (nd + 1) + nd) * nb + b) * rs + lead;
 #pragma unroll
     for (int q = 0; q < kMaxPerThread; ++q) {
         const int tau = threadIdx.x + 256 * q;
@@ -230,7 +239,7 @@ __global__ void __launch_bounds__(256) k_adjoint_combine(
     }
     if (!e_prev) return;
     // block reduction of the two dot products
-    __shared__ float s_red[2][8];
+    __shared__ T s_red[2][8];
     for (int off = 16; off > 0; off >>= 1) {
         dot_mix += __shfl_xor_sync(0xffffffffu, dot_mix, off);
         dot_diff += __shfl_xor_sync(0xffffffffu, dot_diff, off);
@@ -388,7 +397,8 @@ __global__ void k_present_bits(int n_tiles, int n_class, int words, const int64_
 }
 
 // dL/dE0dir[i, o, b] = mu_0[i, o, b, n0_i] (E_0 sits at bin n0 = int(d0 / c / dt)).
-__global__ void k_adjoint_e0(int n, int nd, int nb, int nt, long long rs, int lead, const float* __restrict__ mu,
+template <typename T>
+__global__ void k_adjoint_e0(int n, int nd, int nb, int nt, long long rs, int lead, const T* __restrict__ mu,
                              const double* __restrict__ d0, double c, double dt, double* __restrict__ out) {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (long long)n * nd * nb) return;
@@ -406,9 +416,9 @@ struct AdjLayout {
     int lead;
     size_t rs;
     size_t rows;  // N * (D + 1) * B
-    float* mu[2];
-    float* lam;   // (N, 2D, B, T)
-    float* g_rev; // (R, N, B, T): the receivers' rows of dL/dE_total, reversed
+    void* mu[2];
+    void* lam;    // (N, 2D, B, T)
+    void* g_rev;  // (R, N, B, T): the receivers' rows of dL/dE_total, reversed
     int32_t* rev;
     int32_t* delay;
     int64_t* t_off;
@@ -418,7 +428,8 @@ struct AdjLayout {
     int* err;
 };
 
-AdjLayout adj_layout(void* base, int n, int nd, int nb, int nt, long long p, int n_rcv) {
+// esz: element size of the histograms and of the arithmetic (4: FP32, 8: FP64)
+AdjLayout adj_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p, int n_rcv) {
     AdjLayout L;
     char* q = (char*)base;
     auto take = [&](size_t bytes) {
@@ -432,9 +443,9 @@ AdjLayout adj_layout(void* base, int n, int nd, int nb, int nt, long long p, int
     L.rs = (((size_t)nt + L.lead) + 3) & ~(size_t)3;
     L.rows = (size_t)n * (nd + 1) * nb;
     const size_t tail = (size_t)kStageF + 64;
-    for (int k = 0; k < 2; ++k) L.mu[k] = (float*)take((L.rows * L.rs + tail) * 4);
-    L.lam = (float*)take((size_t)n * n_class * nb * nt * 4);
-    L.g_rev = (float*)take((size_t)(n_rcv > 0 ? n_rcv : 1) * n * nb * nt * 4);
+    for (int k = 0; k < 2; ++k) L.mu[k] = take((L.rows * L.rs + tail) * esz);
+    L.lam = take((size_t)n * n_class * nb * nt * esz);
+    L.g_rev = take((size_t)(n_rcv > 0 ? n_rcv : 1) * n * nb * nt * esz);
     L.rev = (int32_t*)take((size_t)p * 4);
     L.delay = (int32_t*)take((size_t)p * 4);
     L.t_off = (int64_t*)take(((size_t)n + 1) * 8);
@@ -446,16 +457,19 @@ AdjLayout adj_layout(void* base, int n, int nd, int nb, int nt, long long p, int
     L.t_delay = (int32_t*)take((size_t)tp * 4);
     L.t_fwd = (int32_t*)take((size_t)tp * 4);
     L.present = (uint32_t*)take((size_t)n_tiles * ((n_class + 31) / 32) * 4);
-    L.C = plan_core_layout(take, 4, n, nb, tp, n_class);
+    L.C = plan_core_layout(take, esz, n, nb, tp, n_class);
     L.err = (int*)take(16);
     L.bytes = (size_t)(q - (char*)base);
     return L;
 }
 
+inline int adj_esz(int precision) { return precision == SP_F64 ? 8 : 4; }
+
 bool adj_args_ok(const sp_adjoint_args* a) {
     if (!a || !a->fwd) return false;
     const sp_exchange_args* f = a->fwd;
-    return f->precision == SP_F32 && f->n_patches > 0 && f->n_dirs > 0 && f->n_bins > 0 && f->n_samples > 0 &&
+    return (f->precision == SP_F32 || f->precision == SP_F64) && f->n_patches > 0 && f->n_dirs > 0 &&
+           f->n_bins > 0 && f->n_samples > 0 &&
            f->n_samples <= 256 * 16 && f->n_dir_pairs >= 0 && 2 * f->n_dir_pairs < (1LL << 31) && f->dst_offset &&
            f->pair_src && f->pair_dst && f->pair_out_dir && f->pair_in_dir && f->pair_distance && f->pair_fprime &&
            f->pair_unit_len && f->wall_of && f->brdf_index && a->mirror_of_in && a->mirror_gain && a->alpha &&
@@ -463,26 +477,14 @@ bool adj_args_ok(const sp_adjoint_args* a) {
            a->n_receivers <= kMaxReceivers && (a->n_receivers == 0 || a->recv_dir);
 }
 
-}  // namespace
-
-extern "C" {
-
-size_t sp_adjoint_workspace(int n_patches, int n_dirs, int n_bins, int n_samples, long long n_dir_pairs,
-                            int n_receivers) {
-    return adj_layout(nullptr, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_receivers).bytes;
-}
-
-int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* stream) {
-    if (!adj_args_ok(a) || !ws || a->n_receivers < 0 || (a->n_receivers > 0 && (!a->recv_dir || !a->recv_factor ||
-                                                                               !a->recv_dist || !a->grad_mono)))
-        return SP_ERR_ARG;
+template <typename T>
+int adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, cudaStream_t st) {
     const sp_exchange_args* f = a->fwd;
     const int n = f->n_patches, nd = f->n_dirs, nb = f->n_bins, nt = f->n_samples;
     const long long p = f->n_dir_pairs;
-    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, p, a->n_receivers);
+    AdjLayout L = adj_layout(nullptr, sizeof(T), n, nd, nb, nt, p, a->n_receivers);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = adj_layout(ws, n, nd, nb, nt, p, a->n_receivers);
-    cudaStream_t st = (cudaStream_t)stream;
+    L = adj_layout(ws, sizeof(T), n, nd, nb, nt, p, a->n_receivers);
     sp_adjoint_state* S = a->state;
     S->ready = 0;
     S->cur = 0;
@@ -506,7 +508,7 @@ int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* 
                      f->air_attenuation, nd};
         unsigned n_active = 0;
         long long n_groups = 0;
-        int rc = build_groups<float>(n, nb, nt, ps, f->receiver_order, coef, L.C, &n_active, &n_groups, st);
+        int rc = build_groups<T>(n, nb, nt, ps, f->receiver_order, coef, L.C, &n_active, &n_groups, st);
         if (rc != SP_OK) return rc;
         const int n_tiles = (n + kTile - 1) / kTile;
         const int words = (2 * nd + 31) / 32;
@@ -518,52 +520,63 @@ int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* 
     // g and mu_K = g
     if (a->n_receivers > 0) {
         dim3 gg(nb, n);
-        k_adjoint_g<<<gg, 256, 0, sp_counted(st)>>>(n, nb, nt, a->n_receivers, a->recv_factor, a->recv_dist,
-                                                    f->speed_of_sound, f->time_resolution, f->air_attenuation,
-                                                    a->grad_mono, L.g_rev);
+        k_adjoint_g<T><<<gg, 256, 0, sp_counted(st)>>>(n, nb, nt, a->n_receivers, a->recv_factor, a->recv_dist,
+                                                       f->speed_of_sound, f->time_resolution, f->air_attenuation,
+                                                       a->grad_mono, (T*)L.g_rev);
     }
-    for (int k = 0; k < 2; ++k) cudaMemsetAsync(L.mu[k], 0, (L.rows * L.rs + kStageF + 64) * 4, st);
+    for (int k = 0; k < 2; ++k) cudaMemsetAsync(L.mu[k], 0, (L.rows * L.rs + kStageF + 64) * sizeof(T), st);
     dim3 cg(nb, n);
-    k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers,
-                                                      a->recv_dir, L.g_rev, nullptr,
-                                                      nullptr, 0, L.C.tile_of, nullptr, f->wall_of, f->brdf_index,
-                                                      a->alpha, a->scattering, L.mu[0], a->grad_alpha,
-                                                      a->grad_scattering);
+    k_adjoint_combine<T><<<cg, 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers,
+                                                         a->recv_dir, (const T*)L.g_rev, nullptr, nullptr, 0,
+                                                         L.C.tile_of, nullptr, f->wall_of, f->brdf_index, a->alpha,
+                                                         a->scattering, (T*)L.mu[0], a->grad_alpha,
+                                                         a->grad_scattering);
     S->ready = 1;
     return sp_check_launch();
 }
 
-int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, size_t ws_bytes, void* stream) {
-    if (!adj_args_ok(a) || !ws || !e_prev || !a->state->ready) return SP_ERR_ARG;
+template <typename T>
+int adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, size_t ws_bytes, cudaStream_t st) {
+    using WL = WsLayout<T>;
     const sp_exchange_args* f = a->fwd;
     const int n = f->n_patches, nd = f->n_dirs, nb = f->n_bins, nt = f->n_samples;
     const long long p = f->n_dir_pairs;
-    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, p, a->n_receivers);
+    AdjLayout L = adj_layout(nullptr, sizeof(T), n, nd, nb, nt, p, a->n_receivers);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = adj_layout(ws, n, nd, nb, nt, p, a->n_receivers);
-    cudaStream_t st = (cudaStream_t)stream;
+    L = adj_layout(ws, sizeof(T), n, nd, nb, nt, p, a->n_receivers);
     sp_adjoint_state* S = a->state;
     const int words = (2 * nd + 31) / 32;
-    float* mu_in = L.mu[S->cur];
-    float* mu_out = L.mu[1 - S->cur];
+    T* mu_in = (T*)L.mu[S->cur];
+    T* mu_out = (T*)L.mu[1 - S->cur];
     if (S->n_active > 0) {
-        cudaFuncSetAttribute(k_scatter_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kScatterSmem);
-        dim3 sgrid(S->n_active, (nt + kTW - 1) / kTW, nb);
-        k_scatter_f32<<<sgrid, kWsThreads, kScatterSmem, sp_counted(st)>>>(
-            2 * nd, nb, nt, (long long)L.rs, L.lead, 2 * p, L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups, L.C.wpack,
-            (const float*)L.C.coef, mu_in, L.lam, L.err);
+        auto kern = [] {
+            if constexpr (sizeof(T) == 4)
+                return k_scatter_f32;
+            else
+                return k_scatter_f64;
+        }();
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WL::kSmem);
+        dim3 sgrid(S->n_active, (nt + WL::kTW - 1) / WL::kTW, nb);
+        kern<<<sgrid, kWsThreads, WL::kSmem, sp_counted(st)>>>(2 * nd, nb, nt, (long long)L.rs, L.lead, 2 * p,
+                                                               L.C.tile_recv, L.C.seg_order, L.C.seg_off, L.C.groups,
+                                                               L.C.wpack, (const T*)L.C.coef, mu_in, (T*)L.lam, L.err);
     }
     dim3 cg(nb, n);
-    if (nt % 4 == 0)
-        k_adjoint_combine4<<<cg, 256, 0, sp_counted(st)>>>(
-            n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, L.g_rev,
-            S->n_active > 0 ? L.lam : nullptr, L.present, words, L.C.tile_of, (const float*)e_prev, f->wall_of,
-            f->brdf_index, a->alpha, a->scattering, mu_out, a->grad_alpha, a->grad_scattering);
-    else
-        k_adjoint_combine<<<cg, 256, 0, sp_counted(st)>>>(
-            n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, L.g_rev,
-            S->n_active > 0 ? L.lam : nullptr, L.present, words,
-            L.C.tile_of, (const float*)e_prev, f->wall_of, f->brdf_index, a->alpha, a->scattering, mu_out,
+    const T* lam = S->n_active > 0 ? (const T*)L.lam : nullptr;
+    bool vec4 = false;  // FP32 with nt % 4 == 0: the float4 combine
+    if constexpr (sizeof(T) == 4) {
+        if (nt % 4 == 0) {
+            k_adjoint_combine4<<<cg, 256, 0, sp_counted(st)>>>(
+                n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, (const float*)L.g_rev, lam,
+                L.present, words, L.C.tile_of, (const float*)e_prev, f->wall_of, f->brdf_index, a->alpha,
+                a->scattering, mu_out, a->grad_alpha, a->grad_scattering);
+            vec4 = true;
+        }
+    }
+    if (!vec4)
+        k_adjoint_combine<T><<<cg, 256, 0, sp_counted(st)>>>(
+            n, nd, nb, nt, (long long)L.rs, L.lead, a->n_receivers, a->recv_dir, (const T*)L.g_rev, lam, L.present,
+            words, L.C.tile_of, (const T*)e_prev, f->wall_of, f->brdf_index, a->alpha, a->scattering, mu_out,
             a->grad_alpha, a->grad_scattering);
     S->cur = 1 - S->cur;
     int rc = sp_check_launch();
@@ -574,18 +587,50 @@ int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, siz
     return herr ? SP_ERR_TIMEOUT : SP_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+size_t sp_adjoint_workspace(int precision, int n_patches, int n_dirs, int n_bins, int n_samples,
+                            long long n_dir_pairs, int n_receivers) {
+    return adj_layout(nullptr, adj_esz(precision), n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_receivers)
+        .bytes;
+}
+
+int sp_adjoint_begin(const sp_adjoint_args* a, void* ws, size_t ws_bytes, void* stream) {
+    if (!adj_args_ok(a) || !ws || a->n_receivers < 0 || (a->n_receivers > 0 && (!a->recv_dir || !a->recv_factor ||
+                                                                               !a->recv_dist || !a->grad_mono)))
+        return SP_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (a->fwd->precision == SP_F64) return adjoint_begin<double>(a, ws, ws_bytes, st);
+    return adjoint_begin<float>(a, ws, ws_bytes, st);
+}
+
+int sp_adjoint_order(const sp_adjoint_args* a, const void* e_prev, void* ws, size_t ws_bytes, void* stream) {
+    if (!adj_args_ok(a) || !ws || !e_prev || !a->state->ready) return SP_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (a->fwd->precision == SP_F64) return adjoint_order<double>(a, e_prev, ws, ws_bytes, st);
+    return adjoint_order<float>(a, e_prev, ws, ws_bytes, st);
+}
+
 int sp_adjoint_finish(const sp_adjoint_args* a, double* grad_e0dir, void* ws, size_t ws_bytes, void* stream) {
     if (!adj_args_ok(a) || !ws || !grad_e0dir || !a->state->ready || !a->fwd->distance_0) return SP_ERR_ARG;
     const sp_exchange_args* f = a->fwd;
     const int n = f->n_patches, nd = f->n_dirs, nb = f->n_bins, nt = f->n_samples;
-    AdjLayout L = adj_layout(nullptr, n, nd, nb, nt, f->n_dir_pairs, a->n_receivers);
+    const int esz = adj_esz(f->precision);
+    AdjLayout L = adj_layout(nullptr, esz, n, nd, nb, nt, f->n_dir_pairs, a->n_receivers);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = adj_layout(ws, n, nd, nb, nt, f->n_dir_pairs, a->n_receivers);
+    L = adj_layout(ws, esz, n, nd, nb, nt, f->n_dir_pairs, a->n_receivers);
     cudaStream_t st = (cudaStream_t)stream;
     const long long ne = (long long)n * nd * nb;
-    k_adjoint_e0<<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(n, nd, nb, nt, (long long)L.rs, L.lead,
-                                                                 L.mu[a->state->cur], f->distance_0,
-                                                                 f->speed_of_sound, f->time_resolution, grad_e0dir);
+    if (esz == 8)
+        k_adjoint_e0<double><<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(
+            n, nd, nb, nt, (long long)L.rs, L.lead, (const double*)L.mu[a->state->cur], f->distance_0,
+            f->speed_of_sound, f->time_resolution, grad_e0dir);
+    else
+        k_adjoint_e0<float><<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(
+            n, nd, nb, nt, (long long)L.rs, L.lead, (const float*)L.mu[a->state->cur], f->distance_0,
+            f->speed_of_sound, f->time_resolution, grad_e0dir);
     return sp_check_launch();
 }
 

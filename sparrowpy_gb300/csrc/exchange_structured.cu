@@ -36,12 +36,27 @@ namespace {
 // eadd holds the deferred previous order (padded rows), or nothing when
 // etot is null.  One block per (band, receiver),
 // all bins; only the classes present in the receiver's tile are read.
+//
+// Late bins (t >= t_late) of an FP32 E_total are added with Kahan
+// compensation when comp is given: comp holds, per row, the compensation of
+// bins t_late .. nt - 1 (rows of nt - t_late values), zero before the first
+// order.  With x the order's addend (E_{k-1} + E_k, or E_k):
+//   y = x - c;  s' = s + y;  c' = (s' - s) - y
+// and the last update of a solve (fold) stores s' - c', the compensated sum.
+template <typename T>
+__device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
+    const T y = x - c;
+    const T t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                              const T* __restrict__ cdiff, const T* __restrict__ cspec,
                                              const T* __restrict__ g, T* __restrict__ ecur, T* __restrict__ etot,
-                                             const T* __restrict__ eadd) {
+                                             const T* __restrict__ eadd, T* __restrict__ comp, int t_late, int fold) {
     extern __shared__ __align__(16) unsigned char s_mix[];
     const int stride = tile_tab_stride(n_class, nd);
     T* s_cd = reinterpret_cast<T*>(s_mix);  // [n_class] diffuse weight of band b
@@ -60,10 +75,12 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
     const int* inv_off = cls + n_class;
     const int* inv = inv_off + nd + 1;
     const size_t cstride = (size_t)nb * nt;
+    const int nl = nt - t_late;  // compensated bins per row
     const T* gj = g + ((size_t)j * n_class * nb + b) * nt;
     T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;  // padded rows, stride rs
     T* et = etot ? etot + ((size_t)j * nd * nb + b) * nt : nullptr;  // nullptr: E_total not accumulated
     const T* ea = eadd ? eadd + ((size_t)j * nd * nb + b) * rs + lead : nullptr;  // deferred E_{k-1}, padded
+    T* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
         T diffuse = T(0);
         for (int q = 0; q < np; ++q) {
@@ -79,11 +96,98 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
             ek[(size_t)o * nb * rs + t] = v;
             if (et) {
                 T acc = et[o * cstride + t];
-                if (ea) acc += ea[(size_t)o * nb * rs + t];
-                et[o * cstride + t] = acc + v;
+                if (cj && t >= t_late) {
+                    T* cp = cj + (size_t)o * nb * nl + (t - t_late);
+                    T cc = *cp;
+                    kahan_add(acc, cc, ea ? ea[(size_t)o * nb * rs + t] + v : v);
+                    if (fold) {
+                        et[o * cstride + t] = acc - cc;
+                    } else {
+                        et[o * cstride + t] = acc;
+                        *cp = cc;
+                    }
+                } else {
+                    if (ea) acc += ea[(size_t)o * nb * rs + t];
+                    et[o * cstride + t] = acc + v;
+                }
             }
         }
     }
+}
+
+// SP_EXCHANGE_GENERAL: E_k[j, o, b, t] = sum_c tab[c, o, b] G[j, c, b, t] over
+// the classes present in j's tile (any BRDF table rows; the slot scale is in
+// the scatter coefficients), on CUDA cores: one block per (band, receiver),
+// one bin per thread, the D outputs of a bin in registers, each class value
+// read once and broadcast weights from shared memory.  E_total as in k_mix.
+constexpr int kGeneralMaxDirs = 64;
+template <typename T>
+__global__ void __launch_bounds__(128) k_mix_general(int n_class, int nd, int nb, int nt, long long rs, int lead,
+                                                     const int32_t* __restrict__ tile_of,
+                                                     const int32_t* __restrict__ tab, const T* __restrict__ ctab,
+                                                     const T* __restrict__ g, T* __restrict__ ecur,
+                                                     T* __restrict__ etot, const T* __restrict__ eadd,
+                                                     T* __restrict__ comp, int t_late, int fold) {
+    extern __shared__ __align__(16) unsigned char s_mix[];
+    const int stride = tile_tab_stride(n_class, nd);
+    int* s_tab = reinterpret_cast<int*>(s_mix);
+    T* s_w = reinterpret_cast<T*>(s_mix + (((size_t)stride * sizeof(int) + 15) & ~(size_t)15));  // [np][nd]
+    const int b = blockIdx.x, j = blockIdx.y;
+    const int tile = tile_of[j];
+    for (int k = threadIdx.x; k < stride; k += blockDim.x) s_tab[k] = tab[(size_t)tile * stride + k];
+    __syncthreads();
+    const int np = s_tab[0];
+    const int* cls = s_tab + 1;
+    for (int k = threadIdx.x; k < np * nd; k += blockDim.x) {
+        const int q = k / nd, o = k % nd;
+        s_w[k] = ctab[((size_t)cls[q] * nd + o) * nb + b];
+    }
+    __syncthreads();
+    const size_t cstride = (size_t)nb * nt;
+    const int nl = nt - t_late;
+    const T* gj = g + ((size_t)j * n_class * nb + b) * nt;
+    T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;
+    T* et = etot ? etot + ((size_t)j * nd * nb + b) * nt : nullptr;
+    const T* ea = eadd ? eadd + ((size_t)j * nd * nb + b) * rs + lead : nullptr;
+    T* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        T v[kGeneralMaxDirs];
+#pragma unroll
+        for (int o = 0; o < kGeneralMaxDirs; ++o) v[o] = T(0);
+        for (int q = 0; q < np; ++q) {
+            const T x = gj[(size_t)cls[q] * cstride + t];
+            const T* w = s_w + (size_t)q * nd;
+#pragma unroll
+            for (int o = 0; o < kGeneralMaxDirs; ++o)
+                if (o < nd) v[o] = fma(w[o], x, v[o]);
+        }
+#pragma unroll
+        for (int o = 0; o < kGeneralMaxDirs; ++o) {
+            if (o >= nd) break;
+            ek[(size_t)o * nb * rs + t] = v[o];
+            if (!et) continue;
+            T acc = et[o * cstride + t];
+            if (cj && t >= t_late) {
+                T* cp = cj + (size_t)o * nb * nl + (t - t_late);
+                T cc = *cp;
+                kahan_add(acc, cc, ea ? ea[(size_t)o * nb * rs + t] + v[o] : v[o]);
+                if (fold) {
+                    et[o * cstride + t] = acc - cc;
+                } else {
+                    et[o * cstride + t] = acc;
+                    *cp = cc;
+                }
+            } else {
+                if (ea) acc += ea[(size_t)o * nb * rs + t];
+                et[o * cstride + t] = acc + v[o];
+            }
+        }
+    }
+}
+
+constexpr size_t kMixGeneralMaxSmem = 200 * 1024;
+inline size_t mix_general_smem(int n_class, int nd, int esz) {
+    return (((size_t)tile_tab_stride(n_class, nd) * sizeof(int) + 15) & ~(size_t)15) + (size_t)n_class * nd * esz;
 }
 
 // k_mix for FP32 with nt % 4 == 0: four bins per thread (16-byte accesses),
@@ -95,11 +199,23 @@ __device__ __forceinline__ float4 add4(float4 x, float4 y) {
     return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
 }
 
+__device__ __forceinline__ float4 sub4(float4 x, float4 y) {
+    return make_float4(x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w);
+}
+// Kahan step on four lanes: s += x with compensation c (see k_mix)
+__device__ __forceinline__ void kahan_add4(float4& s, float4& c, float4 x) {
+    const float4 y = sub4(x, c);
+    const float4 t = add4(s, y);
+    c = sub4(sub4(t, s), y);
+    s = t;
+}
+
 __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                               const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                               const float* __restrict__ cdiff, const float* __restrict__ cspec,
                                               const float* __restrict__ g, float* __restrict__ ecur,
-                                              float* __restrict__ etot, const float* __restrict__ eadd) {
+                                              float* __restrict__ etot, const float* __restrict__ eadd,
+                                              float* __restrict__ comp, int t_late, int fold) {
     extern __shared__ __align__(16) unsigned char s_mix[];
     const int stride = tile_tab_stride(n_class, nd);
     float* s_cd = reinterpret_cast<float*>(s_mix);
@@ -118,28 +234,32 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
     const int* inv_off = cls + n_class;
     const int* inv = inv_off + nd + 1;
     const int nt4 = nt >> 2;
+    const int tl4 = t_late >> 2;  // t_late is a multiple of 4
     const size_t cs4 = (size_t)nb * nt4;  // class (G) and direction (E_total) stride, in float4
     const size_t ers4 = (size_t)nb * (size_t)(rs >> 2);  // direction stride of the padded ecur rows
+    const size_t cc4 = (size_t)nb * (nt4 - tl4);        // direction stride of the compensation rows
     const float4* gj = reinterpret_cast<const float4*>(g + ((size_t)j * n_class * nb + b) * nt);
     float4* ek = reinterpret_cast<float4*>(ecur + ((size_t)j * nd * nb + b) * rs + lead);
     float4* et = etot ? reinterpret_cast<float4*>(etot + ((size_t)j * nd * nb + b) * nt) : nullptr;
     const float4* ea = eadd ? reinterpret_cast<const float4*>(eadd + ((size_t)j * nd * nb + b) * rs + lead) : nullptr;
+    float4* cj = (comp && et) ? reinterpret_cast<float4*>(comp + ((size_t)j * nd * nb + b) * (nt - t_late)) : nullptr;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int t = threadIdx.x; t < nt4; t += blockDim.x) {
-        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 d = zero;
         for (int q = 0; q < np; ++q) {
             const int c = cls[q];
             if (s_cd[c] != 0.0f) d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);  // skip pure mirror classes
         }
+        const bool late = cj != nullptr && t >= tl4;
         for (int o0 = 0; o0 < nd; o0 += 8) {
             const int no = min(8, nd - o0);
-            float4 e[8];
+            // every load of the 8 directions (E_total, deferred E_{k-1}, compensation) before any store
+            float4 e[8], x[8], c[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (k < no && et) e[k] = et[(o0 + k) * cs4 + t];
-            if (ea) {
-#pragma unroll
-                for (int k = 0; k < 8; ++k)
-                    if (k < no) e[k] = add4(e[k], __ldg(ea + (o0 + k) * ers4 + t));
+            for (int k = 0; k < 8; ++k) {
+                e[k] = (k < no && et) ? et[(o0 + k) * cs4 + t] : zero;
+                x[k] = (k < no && ea) ? __ldg(ea + (o0 + k) * ers4 + t) : zero;
+                c[k] = (k < no && late) ? cj[(o0 + k) * cc4 + (t - tl4)] : zero;
             }
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
@@ -147,11 +267,23 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
                     const int o = o0 + k;
                     float4 v = d;
                     for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
-                        const int c = inv[q];
-                        v = fma4(s_cs[c], __ldg(gj + c * cs4 + t), v);
+                        const int cl = inv[q];
+                        v = fma4(s_cs[cl], __ldg(gj + cl * cs4 + t), v);
                     }
                     ek[o * ers4 + t] = v;
-                    if (et) et[o * cs4 + t] = add4(e[k], v);
+                    if (!et) continue;
+                    if (late) {
+                        float4 s_ = e[k], cc = c[k];
+                        kahan_add4(s_, cc, ea ? add4(x[k], v) : v);
+                        if (fold) {
+                            et[o * cs4 + t] = sub4(s_, cc);
+                        } else {
+                            et[o * cs4 + t] = s_;
+                            cj[o * cc4 + (t - tl4)] = cc;
+                        }
+                    } else {
+                        et[o * cs4 + t] = add4(ea ? add4(e[k], x[k]) : e[k], v);
+                    }
                 }
             }
         }
@@ -236,6 +368,90 @@ __global__ void k_material_classes(int n_in, int nb, const int32_t* __restrict__
     ctarget[c] = c == 0 ? -1 : mirror[c - 1];
 }
 
+// SP_EXCHANGE_SLOTWISE: tables of the diffuse-plus-mirror form with any
+// number of material groups (e.g. per-patch scattering, where every slot's
+// normalised rows differ):
+//   BRDF[slot, s, o, b] = scale[slot, b] (diff[c, b] + spec[c, b] [o == m_c]),
+// c = group(slot) n_in + s.  Each pair e enters twice: the diffuse part
+// (class 0, coefficient w scale diff_c) and the mirror part (class 1 + m_c,
+// coefficient w scale spec_c; none when m_c < 0).  The mix adds class 0 to
+// every outgoing row and class 1 + o to row o, so the class count is 1 + D
+// whatever the number of groups.
+__global__ void k_expand_slotwise_pairs(long long p, int nt, const int64_t* __restrict__ off,
+                                        const int32_t* __restrict__ src, const int32_t* __restrict__ dst,
+                                        const int32_t* __restrict__ out_dir, const int32_t* __restrict__ pcls,
+                                        const int32_t* __restrict__ delay, const int32_t* __restrict__ ctarget,
+                                        int32_t* __restrict__ x_src, int32_t* __restrict__ x_dst,
+                                        int32_t* __restrict__ x_row, int32_t* __restrict__ x_cls,
+                                        int32_t* __restrict__ x_delay, int32_t* __restrict__ x_fwd) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p) return;
+    const int j = dst[e];
+    const long long deg = off[j + 1] - off[j];
+    const long long t0 = 2 * off[j] + (e - off[j]);
+    const long long t1 = t0 + deg;
+    const int m = ctarget[pcls[e]];
+    x_src[t0] = src[e];
+    x_src[t1] = src[e];
+    x_dst[t0] = j;
+    x_dst[t1] = j;
+    x_row[t0] = out_dir[e];
+    x_row[t1] = out_dir[e];
+    x_cls[t0] = 0;
+    x_cls[t1] = m >= 0 ? 1 + m : 0;
+    x_delay[t0] = delay[e];
+    x_delay[t1] = m >= 0 ? delay[e] : nt;  // no mirror term: dropped by the planner
+    x_fwd[t0] = (int32_t)e;
+    x_fwd[t1] = (int32_t)e;
+}
+
+// Class tables of the slot-wise mode: class 0 diffuse (to every row), class 1 + o mirror (to row o).
+template <typename T>
+__global__ void k_slotwise_classes(int nd, int nb, T* __restrict__ cdiff, T* __restrict__ cspec,
+                                   int32_t* __restrict__ ctarget) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > nd) return;
+    for (int b = 0; b < nb; ++b) {
+        cdiff[(size_t)c * nb + b] = c == 0 ? T(1) : T(0);
+        cspec[(size_t)c * nb + b] = c == 0 ? T(0) : T(1);
+    }
+    ctarget[c] = c - 1;
+}
+
+struct SlotCoef {
+    const int32_t* fwd;
+    const int32_t* xcls;
+    const int32_t* pcls;  // structured class of each pair
+    const int32_t* src;
+    const int32_t* wall_of;
+    const int32_t* brdf_index;
+    const double* slot_scale;
+    const double* cdiff;
+    const double* cspec;
+    const double* fprime;
+    const double* unit_len;
+    const double* att;
+    int nb;
+    __device__ double operator()(long long t, int b) const {
+        const long long e = fwd[t];
+        const int slot = brdf_index[wall_of[src[e]]];
+        const size_t cb = (size_t)pcls[e] * nb + b;
+        double f = fprime[e];
+        if (att) f = f * exp(-att[b] * unit_len[e]);
+        f = f * slot_scale[(size_t)slot * nb + b];
+        return xcls[t] == 0 ? f * cdiff[cb] : f * cspec[cb];
+    }
+    __device__ float f32(long long t, int b) const {
+        const long long e = fwd[t];
+        const int slot = brdf_index[wall_of[src[e]]];
+        const size_t cb = (size_t)pcls[e] * nb + b;
+        float f = f64_trunc_f32(fprime[e]);
+        if (att) f = f * expf(-f64_trunc_f32(att[b]) * f64_trunc_f32(unit_len[e]));
+        f = f * f64_trunc_f32(slot_scale[(size_t)slot * nb + b]);
+        return xcls[t] == 0 ? f * f64_trunc_f32(cdiff[cb]) : f * f64_trunc_f32(cspec[cb]);
+    }
+};
+
 struct MatCoef {
     const int32_t* fwd;
     const int32_t* cls;
@@ -301,14 +517,21 @@ struct Plan {
     void* cdiff;
     void* cspec;
     int32_t* ctarget;
+    void* ctab;  // SP_EXCHANGE_GENERAL: (n_class, D, B) class table rows in T
     // material mode: the expanded pair list
     int64_t* x_off;
     int32_t *x_src, *x_dst, *x_row, *x_cls, *x_delay, *x_fwd;
     int64_t* info;  // [signature, n_active, n_groups, 0]
     int* err;
+    int t_late;     // first compensated E_total bin (FP32): nt / 4, rounded down to a multiple of 4
+    void* comp;     // FP32: (N * D * B, nt - t_late) Kahan compensation of E_total's late bins
 };
 
-Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p, int n_class, bool material) {
+// First late bin of E_total: a quarter of the histogram, on a float4 boundary.
+inline int late_bin(int nt) { return (nt / 4) & ~3; }
+
+Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p, int n_class, bool material,
+                 bool general) {
     Plan L;
     char* q = (char*)base;
     auto take = [&](size_t bytes) {
@@ -330,6 +553,7 @@ Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p
     L.cdiff = take((size_t)n_class * nb * esz);
     L.cspec = take((size_t)n_class * nb * esz);
     L.ctarget = (int32_t*)take((size_t)n_class * 4);
+    L.ctab = general ? take((size_t)n_class * nd * nb * esz) : nullptr;
     L.x_off = nullptr;
     L.x_src = L.x_dst = L.x_row = L.x_cls = L.x_delay = L.x_fwd = nullptr;
     if (material) {
@@ -343,6 +567,8 @@ Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p
     }
     L.info = (int64_t*)take(32);
     L.err = (int*)take(16);
+    L.t_late = late_bin(nt);
+    L.comp = esz == 4 ? take(L.rows * (size_t)(nt - L.t_late) * 4) : nullptr;
     L.bytes = (size_t)(q - (char*)base);
     return L;
 }
@@ -378,23 +604,28 @@ template <typename T>
 int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t st) {
     const int n = a->n_patches, nd = a->n_dirs, nb = a->n_bins, nt = a->n_samples;
     const long long p = a->n_dir_pairs;
-    const bool material = a->algorithm == SP_EXCHANGE_MATERIAL;
-    if (material) {
-        if (sizeof(T) != 4 || !a->mat_alpha || !a->mat_scattering || !a->mat_mirror || !a->mat_gain ||
-            a->n_in_dirs < 1)
+    const bool slotwise = a->algorithm == SP_EXCHANGE_SLOTWISE;
+    const bool general = a->algorithm == SP_EXCHANGE_GENERAL;
+    const bool material = a->algorithm == SP_EXCHANGE_MATERIAL || slotwise;  // pairs enter twice
+    if (a->algorithm == SP_EXCHANGE_MATERIAL) {
+        if (!a->mat_alpha || !a->mat_scattering || !a->mat_mirror || !a->mat_gain || a->n_in_dirs < 1)
             return SP_ERR_ARG;
+    } else if (general) {
+        if (!a->slot_group || !a->slot_scale || !a->class_table || a->n_groups < 1) return SP_ERR_ARG;
+        if (nd > kGeneralMaxDirs) return SP_ERR_UNSUPPORTED;
     } else if (!a->slot_group || !a->slot_scale || !a->class_diff || !a->class_spec || !a->class_target ||
                a->n_groups < 1) {
         return SP_ERR_ARG;
     }
-    const int n_class = material ? 1 + a->n_in_dirs : a->n_groups * a->n_in_dirs;
+    const int n_class = slotwise ? 1 + nd : material ? 1 + a->n_in_dirs : a->n_groups * a->n_in_dirs;
     if (n_class > kMaxClasses) return SP_ERR_UNSUPPORTED;
     const int k0 = a->state_in ? a->state_order : 0;
     if (k0 < 0 || (a->states_out && a->states_every < 1)) return SP_ERR_ARG;
     if (nt > 65535) return SP_ERR_UNSUPPORTED;  // base delays are packed in 16 bits
-    Plan L = plan_layout(nullptr, sizeof(T), n, nd, nb, nt, p, n_class, material);
+    if (general && mix_general_smem(n_class, nd, sizeof(T)) > kMixGeneralMaxSmem) return SP_ERR_UNSUPPORTED;
+    Plan L = plan_layout(nullptr, sizeof(T), n, nd, nb, nt, p, n_class, material, general);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
-    L = plan_layout(ws, sizeof(T), n, nd, nb, nt, p, n_class, material);
+    L = plan_layout(ws, sizeof(T), n, nd, nb, nt, p, n_class, material, general);
     const int n_tiles = (n + kTile - 1) / kTile;
     const size_t e = (size_t)n * nd * nb * nt;
     T* etot = a->skip_total ? nullptr : (T*)a->etc_total;
@@ -403,7 +634,10 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     const long long rs = (long long)L.R.rs;
     const int lead = L.R.lead;
     T* states = (T*)a->states_out;
+    // Kahan compensation of E_total's late bins (FP32, unless switched off)
+    float* comp = (sizeof(T) == 4 && etot && !a->plain_total) ? (float*)L.comp : nullptr;
     cudaMemsetAsync(L.err, 0, sizeof(int), st);
+    if (comp) cudaMemsetAsync(comp, 0, L.rows * (size_t)(nt - L.t_late) * sizeof(float), st);
     // ecur: only the leads need zeros (every bin is written each order);
     // eprev: the same when a starting state fills its bins, else all zero
     // before the starting energies are placed
@@ -448,7 +682,22 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     if (!reuse) {
     k_delays_t<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, a->pair_distance, a->speed_of_sound,
                                                               a->time_resolution, L.delay);
-    if (material) {
+    if (slotwise) {
+        k_pair_class_t<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(p, a->pair_src, a->pair_in_dir, a->wall_of,
+                                                                      a->brdf_index, a->slot_group, a->n_in_dirs,
+                                                                      L.cls);
+        k_expand_slotwise_pairs<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(
+            p, nt, a->dst_offset, a->pair_src, a->pair_dst, a->pair_out_dir, L.cls, L.delay, a->class_target,
+            L.x_src, L.x_dst, L.x_row, L.x_cls, L.x_delay, L.x_fwd);
+        k_double_offsets_fwd<<<sp_blocks(n + 1, 256), 256, 0, sp_counted(st)>>>(n, a->dst_offset, L.x_off);
+        PairSet ps{pp, L.x_off, L.x_src, L.x_dst, L.x_row, L.x_cls, L.x_delay, nd, n_class};
+        SlotCoef coef{L.x_fwd, L.x_cls, L.cls, a->pair_src, a->wall_of, a->brdf_index, a->slot_scale, a->class_diff,
+                      a->class_spec, a->pair_fprime, a->pair_unit_len, a->air_attenuation, nb};
+        rc = build_groups<T>(n, nb, nt, ps, a->receiver_order, coef, L.C, &n_active, &n_groups, st);
+        if (rc != SP_OK) return rc;
+        k_slotwise_classes<T><<<sp_blocks(n_class, 128), 128, 0, sp_counted(st)>>>(nd, nb, (T*)L.cdiff,
+                                                                                  (T*)L.cspec, L.ctarget);
+    } else if (material) {
         k_expand_material_pairs<<<sp_blocks(p, 256), 256, 0, sp_counted(st)>>>(
             p, nt, a->dst_offset, a->pair_src, a->pair_dst, a->pair_out_dir, a->pair_in_dir, L.delay, a->mat_mirror,
             L.x_src, L.x_dst, L.x_row, L.x_cls, L.x_delay, L.x_fwd);
@@ -469,11 +718,17 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
                      a->slot_scale, a->pair_src, nb};
         rc = build_groups<T>(n, nb, nt, ps, a->receiver_order, coef, L.C, &n_active, &n_groups, st);
         if (rc != SP_OK) return rc;
-        long long nc = (long long)n_class * nb;
-        k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_diff, (T*)L.cdiff);
-        k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_spec, (T*)L.cspec);
-        cudaMemcpyAsync(L.ctarget, a->class_target, (size_t)n_class * sizeof(int32_t), cudaMemcpyDeviceToDevice,
-                        st);
+        if (general) {
+            long long nc = (long long)n_class * nd * nb;
+            k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_table, (T*)L.ctab);
+            cudaMemsetAsync(L.ctarget, 0xff, (size_t)n_class * sizeof(int32_t), st);  // -1: no mirror lists
+        } else {
+            long long nc = (long long)n_class * nb;
+            k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_diff, (T*)L.cdiff);
+            k_convert_t<T><<<sp_blocks(nc, 256), 256, 0, sp_counted(st)>>>(nc, a->class_spec, (T*)L.cspec);
+            cudaMemcpyAsync(L.ctarget, a->class_target, (size_t)n_class * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                            st);
+        }
     }
     k_tile_table<<<sp_blocks(n_tiles, 128), 128, 0, sp_counted(st)>>>(n_tiles, n_class, nd, L.C.seg_off,
                                                                       L.ctarget, L.tile_tab);
@@ -517,16 +772,24 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         const bool first_of_pair = (k - k0) % 2 == 1;
         T* et_k = (first_of_pair && k < a->max_order) ? nullptr : etot;
         const T* ea_k = (etot && !first_of_pair) ? eprev : nullptr;
+        const int fold = k == a->max_order;  // the last E_total update folds the compensation in
         scatter_timer.stop(st);
-        if (sizeof(T) == 4 && nt % 4 == 0)
+        if (general) {
+            const size_t gsmem = mix_general_smem(n_class, nd, sizeof(T));
+            if (k == k0 + 1)
+                cudaFuncSetAttribute(k_mix_general<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
+            k_mix_general<T><<<mgrid, 128, gsmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of,
+                                                                    L.tile_tab, (const T*)L.ctab, (const T*)L.g, ecur,
+                                                                    et_k, ea_k, (T*)comp, L.t_late, fold);
+        } else if (sizeof(T) == 4 && nt % 4 == 0)
             k_mix4<<<mgrid, 128, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                           (const float*)L.cdiff, (const float*)L.cspec,
                                                           (const float*)L.g, (float*)ecur, (float*)et_k,
-                                                          (const float*)ea_k);
+                                                          (const float*)ea_k, comp, L.t_late, fold);
         else
             k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                             (const T*)L.cdiff, (const T*)L.cspec, (const T*)L.g, ecur,
-                                                            et_k, ea_k);
+                                                            et_k, ea_k, (T*)comp, L.t_late, fold);
         if (states && (k - k0) % a->states_every == 0)
             copy_rows(states + (size_t)((k - k0) / a->states_every) * e, (size_t)nt, ecur + lead, L.R.rs, nt, L.rows,
                       st);
@@ -551,7 +814,8 @@ size_t sp_structured_workspace(int precision, int algorithm, int n_patches, int 
                                long long n_dir_pairs, int n_class) {
     int esz = precision == SP_F64 ? 8 : 4;
     return plan_layout(nullptr, esz, n_patches, n_dirs, n_bins, n_samples, n_dir_pairs, n_class,
-                       algorithm == SP_EXCHANGE_MATERIAL)
+                       algorithm == SP_EXCHANGE_MATERIAL || algorithm == SP_EXCHANGE_SLOTWISE,
+                       algorithm == SP_EXCHANGE_GENERAL)
         .bytes;
 }
 

@@ -1033,9 +1033,11 @@ int sp_outgoing_index_map(long long n_dir, int n, const int32_t* src, const int3
 }  // extern "C"
 
 // ------------------------------------------------ allocation-free variant
-// sp_patch_visibility_static: the same kernels as sp_patch_visibility with
-// the blocker-box scratch in a fixed array of this library's device image
-// instead of a caller-provided workspace.
+// sp_patch_visibility_static: the results of sp_patch_visibility with the
+// blocker-box scratch in a fixed array of this library's device image
+// instead of a caller-provided workspace.  It runs the single-pass
+// k_patch_visibility (one pair per thread), which needs no scratch beyond the
+// boxes; the three-pass form needs the workspace for its candidate lists.
 namespace {
 constexpr int kStaticVisMaxPatches = 16384;
 constexpr size_t kStaticVisScratchFloats =

@@ -92,25 +92,34 @@ def _merge_coplanar(verts, faces, angular_tolerance):
     polys = []
     for root in sorted(regions):
         members = regions[root]
-        # directed boundary edges: edges of the region's faces whose reverse is not in the region
-        directed = {}
-        inner = set()
+        # boundary edges: edges used by one face of the region (counted without
+        # direction, so that faces wound inconsistently still share their
+        # inner edges), each in its face's direction
+        uses = {}
         for fi in members:
             f = faces[fi]
             for k in range(3):
-                directed[(f[k], f[(k + 1) % 3])] = True
-        for (a, b) in list(directed):
-            if (b, a) in directed:
-                inner.add((a, b))
-        nxt = {a: b for (a, b) in directed if (a, b) not in inner}
+                a, b = int(f[k]), int(f[(k + 1) % 3])
+                uses.setdefault((min(a, b), max(a, b)), []).append((a, b))
+        nxt = {}
+        for used in uses.values():
+            if len(used) != 1:
+                continue
+            a, b = used[0]
+            if a in nxt:
+                raise ValueError("a merged region's boundary has a vertex with two outgoing edges "
+                                 "(faces wound inconsistently, or regions touching at a vertex)")
+            nxt[a] = b
         if not nxt:
             continue
         start = min(nxt)
-        loop, v = [start], nxt[start]
-        while v != start and len(loop) <= len(nxt):
+        loop, v = [start], nxt.get(start)
+        while v is not None and v != start and len(loop) <= len(nxt):
             loop.append(v)
-            v = nxt[v]
-        if v != start:
+            v = nxt.get(v)
+        if v != start or len(loop) != len(nxt):
+            # an open chain, or boundary edges left over after one closed loop:
+            # a hole (a second loop) or an inconsistently wound face
             raise ValueError("a merged region's boundary is not one simple loop (holes are not supported)")
         # leave out loop vertices where the boundary runs straight on
         keep = []

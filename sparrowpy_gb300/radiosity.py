@@ -212,6 +212,26 @@ def group_brdf_rows(diff, spec, target, scale):
                 class_target=class_target.astype(np.int32))
 
 
+def group_brdf_tables(brdf):
+    """Group slots whose whole tables agree up to a per-slot, per-band scale: BRDF[slot] = scale[slot, b] T_g.
+
+    brdf: (n_slots, n_in, n_out, n_bins), any values.  Returns slot_group
+    (S,), slot_scale (S, B) (max |brdf| per slot and band), n_groups and
+    class_table (G * n_in, n_out, B): the normalised table row of class
+    c = g * n_in + s.  For tables without the diffuse-plus-mirror structure
+    (the general exchange contracts these rows on the device).
+    """
+    brdf = np.asarray(brdf, dtype=float)
+    S, Din, Dout, B = brdf.shape
+    scale = np.max(np.abs(brdf), axis=(1, 2)) if brdf.size else np.zeros((S, B))
+    scale = np.where(scale > 0, scale, 1.0)
+    norm = brdf / scale[:, None, None, :]
+    first, inverse = _unique_rows(np.round(norm.reshape(S, -1), 12))
+    G = first.size
+    return dict(slot_group=inverse.astype(np.int32), slot_scale=scale, n_groups=int(G),
+                class_table=np.ascontiguousarray(norm[first].reshape(G * Din, Dout, B)))
+
+
 def analyse_brdf(brdf, rel_tol=1e-12):
     """Factor BRDF tables as scale[slot, b] * (diff[g, s, b] + spec[g, s, b] [o == m[g, s]]) on the host.
 
@@ -293,6 +313,10 @@ class DirectionalRadiosityFast:
         self._bake = None   # device state of the last bake
         self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
         self._dirs_xyz = None         # rotated direction sets as arrays (set_wall_brdf)
+        # FP32 exchange: E_total's late bins (the last three quarters of the
+        # histogram) are summed over the orders with Kahan compensation
+        self.compensated_total = True
+        self._max_order = None
         self.check()
 
     # ------------------------------------------------------------ validation
@@ -686,16 +710,40 @@ class DirectionalRadiosityFast:
             plan = dict(brdf=bs["brdf"], brdf_index=bs["brdf_index"], n_slots=bs["n_slots"], n_in=bs["n_in"],
                         n_out=bs["n_out"], host=bs["brdf_host"])
         st = analyse_brdf(plan["host"]) if bs is None else self._brdf_structure(bs)
-        if st is not None and st["n_groups"] * plan["n_in"] <= 256:
+        # diffuse-plus-mirror tables: per (group, incoming direction) class when
+        # the classes fit, else slot-wise (diffuse class + mirror-direction class)
+        mode = None
+        if st is not None:
+            mode = "structured" if st["n_groups"] * plan["n_in"] <= 256 else \
+                "slotwise" if 1 + plan["n_out"] <= 256 else None
+        general = None
+        if mode is None:
+            # any other tables: per (group of proportional tables, incoming
+            # direction) class, contracted with the full table rows
+            general = group_brdf_tables(plan["host"])
+            n_class = general["n_groups"] * plan["n_in"]
+            # the contraction keeps a tile's table rows in shared memory (at most 200 KB) and a bin's
+            # outgoing directions in registers (at most 64)
+            if n_class <= 256 and plan["n_out"] <= 64 and n_class * plan["n_out"] * 8 <= 190 * 1024:
+                mode = "general"
+        if mode is not None:
+            plan["mode"] = mode
             if "receiver_order" not in self._dev:
                 self._dev["receiver_order"] = self._t(
                     receiver_tile_order(self.patches_center, self.patches_normal), torch.int32)
             plan["receiver_order"] = self._dev["receiver_order"]
-            plan["structured"] = dict(
-                slot_group=self._t(st["slot_group"], torch.int32), slot_scale=self._t(st["slot_scale"], torch.float64),
-                n_groups=st["n_groups"], class_diff=self._t(st["class_diff"], torch.float64),
-                class_spec=self._t(st["class_spec"], torch.float64),
-                class_target=self._t(st["class_target"], torch.int32))
+            if mode == "general":
+                plan["structured"] = dict(
+                    slot_group=self._t(general["slot_group"], torch.int32),
+                    slot_scale=self._t(general["slot_scale"], torch.float64), n_groups=general["n_groups"],
+                    class_table=self._t(general["class_table"], torch.float64))
+            else:
+                plan["structured"] = dict(
+                    slot_group=self._t(st["slot_group"], torch.int32),
+                    slot_scale=self._t(st["slot_scale"], torch.float64),
+                    n_groups=st["n_groups"], class_diff=self._t(st["class_diff"], torch.float64),
+                    class_spec=self._t(st["class_spec"], torch.float64),
+                    class_target=self._t(st["class_target"], torch.int32))
         bk["plan"] = plan
         return plan
 
@@ -712,6 +760,7 @@ class DirectionalRadiosityFast:
             self._run_exchange(float(speed_of_sound), float(etc_time_resolution), n_samples,
                                int(max_reflection_order), algorithm)
             self._host.pop("energy_exchange_etc", None)
+            self._max_order = int(max_reflection_order)
         self._etc_time_resolution = float(etc_time_resolution)
         self._speed_of_sound = float(speed_of_sound)
         self._etc_duration = float(etc_duration)
@@ -749,14 +798,25 @@ class DirectionalRadiosityFast:
             raise ValueError("the BRDF directions/bands changed after bake_geometry(); bake again")
         # the structured kernels pack base delays in 16 bits; longer histograms take the dense kernel
         fits = n_samples <= STRUCTURED_MAX_SAMPLES
-        use_struct = "structured" in plan and (algorithm == "structured" or (algorithm == "auto" and fits))
-        if algorithm == "structured" and "structured" not in plan:
-            raise ValueError("BRDF tables are not of the diffuse-plus-mirror form")
-        if algorithm == "structured" and not fits:
+        if algorithm not in ("auto", "dense", "structured", "slotwise", "general"):
+            raise ValueError("algorithm must be 'auto', 'dense', 'structured', 'slotwise' or 'general'")
+        tiled = algorithm in ("structured", "slotwise", "general")
+        use_struct = "structured" in plan and (tiled or (algorithm == "auto" and fits))
+        if tiled and "structured" not in plan:
+            raise ValueError("BRDF tables have more than 256 (table group, incoming direction) classes")
+        if tiled and not fits:
             raise ValueError(f"the structured exchange holds at most {STRUCTURED_MAX_SAMPLES} time bins")
+        mode = plan.get("mode")
+        if algorithm in ("structured", "slotwise") and mode == "general":
+            raise ValueError("BRDF tables are not of the diffuse-plus-mirror form: use 'general'")
+        if algorithm == "structured" and mode == "slotwise":
+            raise ValueError("more than 256 (material group, incoming direction) classes: use 'slotwise'")
+        if use_struct and algorithm in ("slotwise", "general"):
+            mode = algorithm
         a = nat.ExchangeArgs()
         a.precision = _PREC[self.precision]
-        a.algorithm = nat.SP_EXCHANGE_STRUCTURED if use_struct else nat.SP_EXCHANGE_DENSE
+        a.algorithm = {"slotwise": nat.SP_EXCHANGE_SLOTWISE, "general": nat.SP_EXCHANGE_GENERAL}.get(
+            mode, nat.SP_EXCHANGE_STRUCTURED) if use_struct else nat.SP_EXCHANGE_DENSE
         a.n_patches, a.n_dirs, a.n_bins, a.n_samples, a.max_order = n, nd, nb, n_samples, max_order
         a.energy_0_dir = e0dir.data_ptr()
         a.distance_0 = d0.data_ptr()
@@ -775,14 +835,18 @@ class DirectionalRadiosityFast:
         a.brdf = plan["brdf"].data_ptr()
         a.speed_of_sound, a.time_resolution = c, dt
         a.etc_total = etc.data_ptr()
+        a.plain_total = 0 if self.compensated_total else 1
         if use_struct:
             s = plan["structured"]
             a.slot_group = s["slot_group"].data_ptr()
             a.slot_scale = s["slot_scale"].data_ptr()
             a.n_groups = s["n_groups"]
-            a.class_diff = s["class_diff"].data_ptr()
-            a.class_spec = s["class_spec"].data_ptr()
-            a.class_target = s["class_target"].data_ptr()
+            if "class_table" in s:
+                a.class_table = s["class_table"].data_ptr()
+            else:
+                a.class_diff = s["class_diff"].data_ptr()
+                a.class_spec = s["class_spec"].data_ptr()
+                a.class_target = s["class_target"].data_ptr()
             a.receiver_order = plan["receiver_order"].data_ptr()
             a.pair_dst = bk["dst"].data_ptr()
         return a
@@ -798,7 +862,7 @@ class DirectionalRadiosityFast:
         else:
             a = self._exchange_args(c, dt, n_samples, max_order, algorithm, etc)
         if states is not None:
-            if a.algorithm != nat.SP_EXCHANGE_STRUCTURED:
+            if a.algorithm not in (nat.SP_EXCHANGE_STRUCTURED, nat.SP_EXCHANGE_SLOTWISE, nat.SP_EXCHANGE_GENERAL):
                 raise ValueError("saving exchange states needs the structured exchange")
             a.states_out = states.data_ptr()
             a.states_every = int(states_every)
@@ -808,8 +872,9 @@ class DirectionalRadiosityFast:
         a.order_ms = ctypes.pointer(order_ms)
         scatter_ms = ctypes.c_float(-1.0)
         a.scatter_ms = ctypes.pointer(scatter_ms)
+        n_class = 1 + nd if a.algorithm == nat.SP_EXCHANGE_SLOTWISE else a.n_groups * a.n_in_dirs
         wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, n_samples,
-                       a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups * a.n_in_dirs)
+                       a.n_dir_pairs, a.n_slots, a.n_in_dirs, n_class)
         ws = self._workspace(wsz)
         rc = nat.lib().sp_energy_exchange(ctypes.byref(a), _ptr(ws), wsz, _stream())
         if rc == nat.SP_ERR_RANGE:
@@ -817,10 +882,55 @@ class DirectionalRadiosityFast:
         if rc != nat.SP_OK:
             raise nat.NativeError("sp_energy_exchange", rc)
         self._dev["etc"] = etc
-        self.exchange_stats = dict(algorithm="structured" if a.algorithm == nat.SP_EXCHANGE_STRUCTURED else "dense",
+        names = {nat.SP_EXCHANGE_STRUCTURED: "structured", nat.SP_EXCHANGE_SLOTWISE: "slotwise",
+                 nat.SP_EXCHANGE_GENERAL: "general"}
+        self.exchange_stats = dict(algorithm=names.get(a.algorithm, "dense"),
                                    source_groups=int(stats[0]), segments=int(stats[1]), pairs=int(stats[2]),
                                    tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order),
                                    scatter_ms=float(scatter_ms.value))
+
+    def energy_balance(self):
+        """FP64 per-band energy check of the last exchange (no counterpart in the reference).
+
+        Returns a dict of per-band arrays: ``histogram`` = sum of E_total
+        over patches, directions and bins (accumulated in FP64 on the GPU,
+        sp_energy_totals), ``budget`` = the same total predicted without
+        time by the orders' energy recursion through ff_tilde, from the
+        source energy (sp_energy_budget, FP64), and ``rel_dev`` =
+        |histogram - budget| / budget.  The two agree up to rounding when
+        no contribution is delayed past the histogram's last bin (a closed
+        room whose histogram outlasts the orders); otherwise the deviation
+        is the energy beyond the histogram, which the reference drops
+        (RadiosityFast.py:1137-1143).  Also ``ms``, the check's GPU time.
+        """
+        etc = self._etc_device()
+        if self._max_order is None or self._max_order < 0 or "e0dir" not in self._dev:
+            raise ValueError("calculate_energy_exchange() with max_reflection_order >= 0 must run first")
+        n, nd, nb, nt = etc.shape
+        dev = self.device
+        st = _stream()
+        stream = torch.cuda.current_stream(dev)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        hist = torch.empty((nb,), dtype=torch.float64, device=dev)
+        wsz = nat.size("sp_energy_totals_workspace", nb)
+        ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
+        prec = nat.SP_F32 if etc.dtype == torch.float32 else nat.SP_F64
+        nat.call("sp_energy_totals", prec, n * nd, nb, nt, _ptr(etc), _ptr(hist), _ptr(ws), wsz, st)
+        budget = torch.empty((nb,), dtype=torch.float64, device=dev)
+        if self._max_order >= 1:
+            a = self._exchange_args(self._speed_of_sound, self._etc_time_resolution, nt, self._max_order, "dense",
+                                    etc)
+        else:
+            a = self._init_only_args(self._speed_of_sound, self._etc_time_resolution, nt, etc)
+        bsz = nat.size("sp_energy_budget_workspace", n, nd, nb, a.n_dir_pairs)
+        bws = torch.empty((max(bsz, 1),), dtype=torch.uint8, device=dev)
+        nat.call("sp_energy_budget", ctypes.byref(a), _ptr(budget), _ptr(bws), bsz, st)
+        ev1.record(stream)
+        ev1.synchronize()
+        h, b = hist.cpu().numpy(), budget.cpu().numpy()
+        return dict(histogram=h, budget=b, rel_dev=np.abs(h - b) / np.where(b > 0, b, 1.0),
+                    ms=float(ev0.elapsed_time(ev1)))
 
     def _workspace(self, nbytes):
         ws = self._dev.get("ws")

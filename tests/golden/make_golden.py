@@ -174,9 +174,12 @@ def run_reference(mods, sc, setup, brdf_inputs):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', default=os.environ.get('SPARROWPY_SRC'),
+                    help='sparrowpy source tree (default: $SPARROWPY_SRC)')
     ap.add_argument('scenes', nargs='*', default=list(SCENES))
     args = ap.parse_args()
+    if not args.ref:
+        ap.error('give --ref or set SPARROWPY_SRC')
     mods = import_reference(args.ref)
     for name in args.scenes:
         r, setup, bi = SCENES[name]()

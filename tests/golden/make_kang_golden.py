@@ -97,8 +97,11 @@ def reference_room(ref_path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("SPARROWPY_SRC"),
+                    help="sparrowpy source tree (default: $SPARROWPY_SRC)")
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give --ref or set SPARROWPY_SRC")
     out = stored_results(os.path.join(a.ref, "tests", "test_data"))
     out.update(reference_room(a.ref))
     out["room_config"] = np.array(json.dumps(ROOM))

@@ -106,3 +106,38 @@ def test_blend_files_need_blender(tmp_path):
         read_geometry_file(tmp_path / "room.blend")
     with pytest.raises(NotImplementedError):
         read_geometry_file(tmp_path / "room.obj")
+
+
+def _grid_triangles(cells, flip=()):
+    """Triangles of unit squares (x, y) on z = 0, two per cell, counter-clockwise from +z; cells in `flip` have
+    their first triangle wound the other way."""
+    tris = []
+    for k, (x, y) in enumerate(cells):
+        sq = np.array([(x, y, 0.0), (x + 1, y, 0.0), (x + 1, y + 1, 0.0), (x, y + 1, 0.0)])
+        t0 = sq[[0, 2, 1]] if k in flip else sq[[0, 1, 2]]
+        tris += [t0, sq[[0, 2, 3]]]
+    return np.array(tris)
+
+
+def test_merged_face_with_a_hole_is_refused(tmp_path):
+    """A 3 x 3 square with the middle cell missing: two boundary loops, which no single polygon holds."""
+    ring = [(x, y) for x in range(3) for y in range(3) if (x, y) != (1, 1)]
+    path = str(tmp_path / "ring.stl")
+    write_binary_stl(path, _grid_triangles(ring))
+    with pytest.raises(ValueError, match="holes are not supported"):
+        read_geometry_file(path)
+    # without the hole the same square merges into one quadrilateral
+    path = str(tmp_path / "square.stl")
+    write_binary_stl(path, _grid_triangles([(x, y) for x in range(3) for y in range(3)]))
+    _, rough = read_geometry_file(path)
+    assert len(rough["conn"]) == 1 and len(rough["conn"][0]) == 4
+
+
+def test_inconsistent_winding_stays_a_face_of_its_own(tmp_path):
+    """A triangle wound against its neighbours has the opposite normal, so it is not merged with them: the
+    rest of the square merges into one polygon around it, and the triangle stays a face of its own."""
+    path = str(tmp_path / "flipped.stl")
+    write_binary_stl(path, _grid_triangles([(x, y) for x in range(2) for y in range(2)], flip=(3,)))
+    _, rough = read_geometry_file(path)
+    sizes = sorted(len(c) for c in rough["conn"])
+    assert sizes[0] == 3 and len(sizes) == 2

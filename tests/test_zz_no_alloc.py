@@ -1,7 +1,10 @@
 """Allocation-free patch visibility (sp_patch_visibility_static) against sp_patch_visibility.
 
 Collected last (file name) so that it also runs after every other GPU test
-has used the device.  Tolerance: exact (visibility is boolean).
+has used the device.  Tolerance: exact (visibility is boolean).  The
+allocation-free entry point runs the single-pass kernel, so besides the
+small golden scenes it is compared on the 5939-patch street canyon, with
+both entry points' times printed.
 """
 import os
 
@@ -42,3 +45,33 @@ def test_static_visibility_matches_workspace_entry_point():
             torch.cuda.synchronize()
             assert torch.equal(out, ref)
         np.testing.assert_array_equal(ref.cpu().numpy(), g["V"])
+
+
+@pytest.mark.gpu
+def test_static_visibility_matches_on_the_street_canyon():
+    import torch
+    from sparrowpy_gb300 import _native as nat
+    from sparrowpy_gb300 import scenes
+    st = torch.cuda.current_stream()
+    r = scenes.street_canyon(seed=3)
+    d = r._geometry()
+    n, nv = r.n_patches, r._patches_points.shape[1]
+    args = (n, nv, d["centers"].data_ptr(), d["normals"].data_ptr(), d["pts"].data_ptr())
+    ref = torch.empty((n, n), dtype=torch.uint8, device="cuda")
+    out = torch.empty((n, n), dtype=torch.uint8, device="cuda")
+    wsz = nat.size("sp_patch_visibility_workspace", n)
+    ws = torch.empty((wsz,), dtype=torch.uint8, device="cuda")
+    ms = {}
+    for name, call in (("sp_patch_visibility", lambda: nat.call("sp_patch_visibility", *args, ref.data_ptr(),
+                                                               ws.data_ptr(), wsz, st.cuda_stream)),
+                       ("sp_patch_visibility_static", lambda: nat.call("sp_patch_visibility_static", *args,
+                                                                      out.data_ptr(), st.cuda_stream))):
+        call()  # first call (and the static array's address lookup) untimed
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        call()
+        e1.record(st)
+        e1.synchronize()
+        ms[name] = e0.elapsed_time(e1)
+    print(f"street canyon, {n} patches: " + ", ".join(f"{k} {v:.1f} ms" for k, v in ms.items()))
+    assert torch.equal(out, ref)
