@@ -254,6 +254,9 @@ typedef struct sp_exchange_args {
     /* SP_EXCHANGE_GENERAL only: (n_groups * n_in_dirs, D, B) normalised table rows of the classes, with
        BRDF[slot, s, o, b] = slot_scale[slot, b] class_table[slot_group[slot] * n_in + s, o, b] */
     const double* class_table;
+    /* SP_EXCHANGE_GENERAL, FP32 with 32 <= D <= 64 and D % 16 == 0: the contraction runs on the tensor cores
+       (tcgen05, TF32 with a hi/lo split); 1 = on the CUDA cores instead */
+    int no_tensor_cores;
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070

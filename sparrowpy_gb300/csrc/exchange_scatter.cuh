@@ -115,6 +115,16 @@ struct Vec2<double> {
     using type = double2;
 };
 
+// One Kahan step: s += x with the running compensation c (the exchange's
+// late-bin E_total sums).  y = x - c; t = s + y; c = (t - s) - y; s = t.
+template <typename T>
+__device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
+    const T y = x - c;
+    const T t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 

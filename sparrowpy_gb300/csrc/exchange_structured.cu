@@ -26,6 +26,7 @@
 // warp read covering 32 consecutive floats.  FP64 uses the same plan with
 // direct loads.  Mix: streams G into E_k and E_total.
 #include "exchange_scatter.cuh"
+#include "exchange_tc.cuh"
 
 namespace {
 
@@ -43,14 +44,6 @@ namespace {
 // order.  With x the order's addend (E_{k-1} + E_k, or E_k):
 //   y = x - c;  s' = s + y;  c' = (s' - s) - y
 // and the last update of a solve (fold) stores s' - c', the compensated sum.
-template <typename T>
-__device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
-    const T y = x - c;
-    const T t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
-
 template <typename T>
 __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
@@ -623,6 +616,9 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     if (k0 < 0 || (a->states_out && a->states_every < 1)) return SP_ERR_ARG;
     if (nt > 65535) return SP_ERR_UNSUPPORTED;  // base delays are packed in 16 bits
     if (general && mix_general_smem(n_class, nd, sizeof(T)) > kMixGeneralMaxSmem) return SP_ERR_UNSUPPORTED;
+    // the receiver-side contraction on tensor cores: FP32, 32 <= D <= 64 (a multiple of 16, the MMA's N)
+    const bool tensor_mix = general && sizeof(T) == 4 && !a->no_tensor_cores && nd >= 32 && nd <= 64 &&
+                            nd % 16 == 0 && tc_smem_bytes(n_class, nd) <= kTcSmem;
     Plan L = plan_layout(nullptr, sizeof(T), n, nd, nb, nt, p, n_class, material, general);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
     L = plan_layout(ws, sizeof(T), n, nd, nb, nt, p, n_class, material, general);
@@ -774,7 +770,13 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         const T* ea_k = (etot && !first_of_pair) ? eprev : nullptr;
         const int fold = k == a->max_order;  // the last E_total update folds the compensation in
         scatter_timer.stop(st);
-        if (general) {
+        if (general && tensor_mix) {
+            if (k == k0 + 1)
+                cudaFuncSetAttribute(k_mix_general_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+            k_mix_general_tc<<<mgrid, kTcThreads, kTcSmem, sp_counted(st)>>>(
+                n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab, (const float*)L.ctab, (const float*)L.g,
+                (float*)ecur, (float*)et_k, (const float*)ea_k, comp, L.t_late, fold, L.err);
+        } else if (general) {
             const size_t gsmem = mix_general_smem(n_class, nd, sizeof(T));
             if (k == k0 + 1)
                 cudaFuncSetAttribute(k_mix_general<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);

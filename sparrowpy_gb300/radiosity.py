@@ -316,6 +316,9 @@ class DirectionalRadiosityFast:
         # FP32 exchange: E_total's late bins (the last three quarters of the
         # histogram) are summed over the orders with Kahan compensation
         self.compensated_total = True
+        # general BRDF tables, FP32, 32 <= directions <= 64: the receiver-side
+        # contraction on the tensor cores (False: on the CUDA cores)
+        self.tensor_cores = True
         self._max_order = None
         self.check()
 
@@ -836,6 +839,7 @@ class DirectionalRadiosityFast:
         a.speed_of_sound, a.time_resolution = c, dt
         a.etc_total = etc.data_ptr()
         a.plain_total = 0 if self.compensated_total else 1
+        a.no_tensor_cores = 0 if self.tensor_cores else 1
         if use_struct:
             s = plan["structured"]
             a.slot_group = s["slot_group"].data_ptr()

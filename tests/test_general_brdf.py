@@ -88,3 +88,15 @@ def test_random_table_general_exchange(precision, tol, n_dirs):
     ref = orc.solve(scene_from_radiosity(r), SRC, RCV, c, dt, dur, k)
     assert rel_l2(mono, ref["mono"]) < tol
     assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
+
+
+def test_tensor_core_contraction_matches_cuda_cores():
+    """The tcgen05 contraction (TF32 hi/lo split) against the CUDA-core one on the same solve: 64 directions,
+    FP32; histograms within 1e-6 rel L2 of each other."""
+    out = {}
+    for tc in (True, False):
+        r = random_table_room("fp32", 64)
+        r.tensor_cores = tc
+        out[tc] = _solve(r)[0]
+        assert r.exchange_stats["algorithm"] == "general"
+    assert rel_l2(out[True], out[False]) < 1e-6
