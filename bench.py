@@ -461,6 +461,13 @@ def run_gpu(args):
         except Exception as exc:  # the config legs must not hide the solve result
             configs = {"error": f"{type(exc).__name__}: {exc}"}
 
+    general = None
+    if not args.no_configs and rank == 0:
+        try:
+            general = general_brdf_leg()
+        except Exception as exc:  # must not hide the solve result
+            general = {"error": f"{type(exc).__name__}: {exc}"}
+
     batch = None
     if args.batch_rooms > 0:
         barrier()
@@ -497,6 +504,7 @@ def run_gpu(args):
             "fp64_gpu": fp64,
             "fwd_bwd": fwd_bwd,
             "configs": configs,
+            "general_brdf": general,
             "batch": batch,
             "clocks": clk,
             "gpu_launches": int(launches),
@@ -569,6 +577,55 @@ def config_legs(cpu_cfg1=None):
     return out
 
 
+# ------------------------------------------------------------ general BRDF
+def general_brdf_leg(orders=50, dense_orders=5):
+    """A table without diffuse-plus-mirror structure on every wall: cfg2's geometry and histogram.
+
+    5 x 6 x 3 m shoebox at 0.25 m (2016 patches), one seeded random positive
+    64 x 64 x 6 table (as create_from_directional_scattering tables are
+    dense), T = 2000, FP32.  The general exchange (class scatter, then the
+    receiver-side contraction of the 64 table rows) with the contraction on
+    the tensor cores and on the CUDA cores, `orders` orders each, and the
+    dense kernel (D FMAs per pair and bin) for `dense_orders` orders; per
+    order ms from CUDA events around the order loop.
+    """
+    import torch
+    from sparrowpy_gb300 import scenes
+    from sparrowpy_gb300.brdf import hemisphere_directions
+    from sparrowpy_gb300.coords import FrequencyData
+
+    def room():
+        r = scenes.shoebox(0.25, n_dirs=64, n_bins=6, scattering=0.3, absorption=0.1, precision="fp32")
+        rng = np.random.default_rng(9)
+        dirs = hemisphere_directions(64)
+        tab = rng.uniform(0.05, 0.25, size=(64, 64, 6)) / 8.0
+        r.set_wall_brdf(np.arange(r.n_walls), FrequencyData(tab, np.asarray(r._frequencies, float)), dirs, dirs)
+        return r
+
+    out = {"workload": "cfg2 geometry (2016 patches), a seeded random positive 64 x 64 x 6 BRDF table on every wall, "
+                       "6 bands, T=2000, FP32"}
+    monos = {}
+    for name, algo, tc, k in (("general_tensor_cores", "general", True, orders),
+                              ("general_cuda_cores", "general", False, orders),
+                              ("dense", "dense", True, dense_orders)):
+        r = room()
+        r.tensor_cores = tc
+        src = np.array([2.0, 2.0, 1.5])
+        r.bake_geometry()
+        r.init_source_energy(as_coords(src))
+        for _ in range(2):  # the first call warms up
+            r.calculate_energy_exchange(343.0, 1e-3, 2.0, k, recalculate=True, algorithm=algo)
+        st = r.exchange_stats
+        out[name] = {"orders": k, "ms_per_order": st["order_ms"] / k, "algorithm": st["algorithm"]}
+        if k == orders:
+            monos[name] = r.collect_energy_receiver_mono(as_coords(np.array([[3.0, 4.0, 1.5]]))).time
+        del r
+        torch.cuda.empty_cache()
+    a, b = monos["general_tensor_cores"], monos["general_cuda_cores"]
+    out["receiver_rel_l2_tensor_vs_cuda_cores"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return out
+
+
 # ------------------------------------------------------- forward + backward
 def fwd_bwd_config4(steps=2, fd_params=64, seed=4, fp64_reference=True):
     """Energy-decay-loss gradient w.r.t. per-patch, per-band absorption and scattering.
@@ -630,15 +687,24 @@ def fwd_bwd_config4(steps=2, fd_params=64, seed=4, fp64_reference=True):
     del solver, r
     torch.cuda.empty_cache()
     if fp64_reference:
-        r64, s64 = room(0.25, "fp64")
-        ga64, gs64, f64_ms, b64_ms = grads(s64, alpha0, scat0, s64.forward_only(t(alpha_t), t(scat_t)), 0)
-        del s64, r64
-        torch.cuda.empty_cache()
-        g32 = np.concatenate([ga.ravel(), gs.ravel()])
-        g64 = np.concatenate([ga64.ravel(), gs64.ravel()])
+        # the FP64 adjoint of the 2016-patch room would hold about 340 GB (FP64 checkpoints, exchange and adjoint
+        # workspaces): the reference gradient runs on the same room at 0.5 m patches (504 patches, 6048 params)
+        grad = {}
+        for prec in ("fp32", "fp64"):
+            rr, sv = room(0.5, prec)
+            Sm = sv.n_slots
+            rng_m = np.random.default_rng(seed + 7)
+            a0, s0 = rng_m.uniform(0.02, 0.6, (Sm, 6)), rng_m.uniform(0.1, 0.9, (Sm, 6))
+            tgt = sv.forward_only(t(rng_m.uniform(0.02, 0.6, (Sm, 6))), t(rng_m.uniform(0.1, 0.9, (Sm, 6))))
+            grad[prec] = grads(sv, a0, s0, tgt, 0)
+            del sv, rr
+            torch.cuda.empty_cache()
+        g32 = np.concatenate([grad["fp32"][0].ravel(), grad["fp32"][1].ravel()])
+        g64 = np.concatenate([grad["fp64"][0].ravel(), grad["fp64"][1].ravel()])
         big = np.abs(g64) > 1e-3 * np.abs(g64).max()
         out["fp64_adjoint"] = {
-            "fwd_bwd_ms": float(b64_ms[0]),
+            "workload": "the same room and loss at 0.5 m patches: 504 patches, 6048 parameters",
+            "fp32_fwd_bwd_ms": float(grad["fp32"][3][0]), "fp64_fwd_bwd_ms": float(grad["fp64"][3][0]),
             "max_abs_err_over_max_grad": float(np.abs(g32 - g64).max() / np.abs(g64).max()),
             "rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
             "max_rel_err_where_grad_above_1e-3_max": float((np.abs(g32 - g64)[big] / np.abs(g64)[big]).max())}

@@ -257,6 +257,9 @@ typedef struct sp_exchange_args {
     /* SP_EXCHANGE_GENERAL, FP32 with 32 <= D <= 64 and D % 16 == 0: the contraction runs on the tensor cores
        (tcgen05, TF32 with a hi/lo split); 1 = on the CUDA cores instead */
     int no_tensor_cores;
+    /* structured / slot-wise / material, FP32: 1 = place E_0 and E_total and build the plan in ws, run no order
+       (the orders then run in sp_exchange_batch) */
+    int prepare_only;
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070
@@ -302,6 +305,44 @@ int sp_energy_totals(int precision, long long n_rows, int n_bins, int n_samples,
  * ws: sp_energy_budget_workspace bytes. */
 size_t sp_energy_budget_workspace(int n_patches, int n_dirs, int n_bins, long long n_dir_pairs);
 int sp_energy_budget(const sp_exchange_args* a, double* totals, void* ws, size_t ws_bytes, void* stream);
+
+/* ------------------------------------------------------------ batched rooms */
+
+/* The exchange orders of many rooms in one persistent launch (no counterpart
+ * in the reference, which solves one room per object).  Each room is an
+ * sp_exchange_args (FP32, structured / slot-wise / material, at least one
+ * pair inside the histogram) already prepared by sp_energy_exchange with
+ * prepare_only = 1 in its own workspace; all rooms share n_dirs, n_bins,
+ * n_samples (a multiple of 4) and max_order.  Blocks take work items (a
+ * room's scatter or mix piece of one order) from a device ticket counter and
+ * wait, bounded by wait_limit polls (0: 2^24), for the pieces they depend on;
+ * a wait that gives up makes the call return SP_ERR_TIMEOUT (the device stays
+ * usable).  On success every room's etc_total holds its E_total.
+ * window_bins (1024 or 512) and ctas_per_sm (blocks per SM of the persistent
+ * grid) are the tile choices an autotuner picks; force_timeout = 1 makes the
+ * first item wait for a count that is never reached (a test of the bounded
+ * wait).  Synchronises `stream`.  ws: sp_exchange_batch_workspace(n_rooms). */
+typedef struct sp_batch_room {
+    const sp_exchange_args* args;  /* HOST struct */
+    void* ws;                      /* the room's prepared exchange workspace */
+    size_t ws_bytes;
+} sp_batch_room;
+
+typedef struct sp_batch_args {
+    int n_rooms;
+    const sp_batch_room* rooms;  /* HOST array */
+    int window_bins;
+    int ctas_per_sm;
+    unsigned wait_limit;
+    int force_timeout;
+    float* exchange_ms;          /* HOST float or NULL: CUDA-event time of the launch */
+    long long* items;            /* HOST or NULL: work items of the launch */
+} sp_batch_args;
+
+size_t sp_exchange_batch_workspace(int n_rooms);
+int sp_exchange_batch(const sp_batch_args* args, void* ws, size_t ws_bytes, void* stream);
+/* sizeof(sp_batch_args), for bindings that mirror the struct. */
+size_t sp_batch_args_size(void);
 
 /* ------------------------------------------------------------------ adjoint */
 

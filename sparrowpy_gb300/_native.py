@@ -60,7 +60,7 @@ class ExchangeArgs(ctypes.Structure):
         ("state_in", P), ("state_order", I), ("states_out", P), ("states_every", I), ("skip_total", I),
         ("mat_alpha", P), ("mat_scattering", P), ("mat_mirror", P), ("mat_gain", P),
         ("plan_tag", LL), ("scatter_ms", ctypes.POINTER(ctypes.c_float)), ("plain_total", I),
-        ("class_table", P), ("no_tensor_cores", I),
+        ("class_table", P), ("no_tensor_cores", I), ("prepare_only", I),
     ]
 
 
@@ -79,12 +79,27 @@ class AdjointArgs(ctypes.Structure):
     ]
 
 
+class BatchRoom(ctypes.Structure):
+    """Mirror of `sp_batch_room` (host memory)."""
+    _fields_ = [("args", ctypes.POINTER(ExchangeArgs)), ("ws", P), ("ws_bytes", SZ)]
+
+
+class BatchArgs(ctypes.Structure):
+    """Mirror of `sp_batch_args` (host memory)."""
+    _fields_ = [("n_rooms", I), ("rooms", ctypes.POINTER(BatchRoom)), ("window_bins", I), ("ctas_per_sm", I),
+                ("wait_limit", ctypes.c_uint), ("force_timeout", I), ("exchange_ms", ctypes.POINTER(ctypes.c_float)),
+                ("items", ctypes.POINTER(ctypes.c_longlong))]
+
+
 # name: (restype, argtypes)
 _SIGS = {
     "sp_version": (ctypes.c_char_p, []),
     "sp_kernel_launches": (LL, []),
     "sp_exchange_args_size": (SZ, []),
     "sp_adjoint_args_size": (SZ, []),
+    "sp_batch_args_size": (SZ, []),
+    "sp_exchange_batch_workspace": (SZ, [I]),
+    "sp_exchange_batch": (I, [ctypes.POINTER(BatchArgs), P, SZ, P]),
     "sp_patch_geometry": (I, [I, I, P, P, P, P]),
     "sp_patch_visibility_workspace": (SZ, [I]),
     "sp_patch_visibility": (I, [I, I, P, P, P, P, P, SZ, P]),

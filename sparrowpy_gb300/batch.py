@@ -1,20 +1,32 @@
-"""Many independent rooms through the solver, one after another on one device.
+"""Many independent rooms on one device.
 
 A batch is a list of seeded shoebox rooms (dimensions, materials, source and
-receivers drawn per room).  `solve_rooms` runs the reference pipeline for
-each (bake_geometry, init_source_energy, calculate_energy_exchange,
-collect_energy_receiver_mono) and returns the receiver histograms with the
-device time per room.  Rooms are not co-resident: each room's histograms and
-workspace are released before the next room, so the batch needs only the
-memory of its largest room.
+receivers drawn per room).
+
+* `solve_rooms` runs the reference pipeline for each room in turn
+  (bake_geometry, init_source_energy, calculate_energy_exchange,
+  collect_energy_receiver_mono), releasing each room before the next.
+* `solve_rooms_batched` bakes the rooms of a memory-sized wave one by one,
+  prepares each room's exchange (source energy, E_total and the pair plan in
+  the room's workspace), then runs the exchange orders of the whole wave in
+  one persistent launch (sp_exchange_batch: blocks pull scatter and mix
+  pieces of every room from a device work queue, with bounded waits on the
+  pieces they depend on), and collects each room's receivers.  The
+  persistent launch's tile choices (scatter window of 1024 or 512 bins,
+  blocks per SM) come from `BatchTuner`, which times the candidates on a
+  short run of the first wave of each shape class and keeps the fastest.
 """
+import ctypes
+import itertools
+
 import numpy as np
 import torch
 
+from . import _native as nat
 from .brdf import create_from_scattering, hemisphere_directions
 from .coords import Coordinates, FrequencyData
 from .geometry import shoebox_room_stub
-from .radiosity import DirectionalRadiosityFast
+from .radiosity import DirectionalRadiosityFast, _ptr, _stream
 
 OCTAVES6 = np.array([125.0, 250.0, 500.0, 1000.0, 2000.0, 4000.0])
 
@@ -69,3 +81,185 @@ def solve_rooms(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, etc_durat
         del r
     torch.cuda.empty_cache()
     return out, ms, patches
+
+
+# ------------------------------------------------------------------ batched
+_TAGS = itertools.count(1 << 40)  # plan tags of prepared rooms (process-wide, never 0)
+
+
+class BatchTuner:
+    """Tile choices of the persistent batched exchange, timed per shape class and kept.
+
+    A shape class is (directions, bands, bins, size bucket of the wave's
+    largest room).  Candidates: scatter windows of 1024 and 512 bins, one and
+    two blocks per SM.  `choose` times each candidate's launch (CUDA events)
+    on `probe_orders` orders of the prepared wave, takes the fastest, and
+    returns the cached choice for later waves of the class.
+    """
+
+    CANDIDATES = ((1024, 1), (1024, 2), (512, 1), (512, 2))
+
+    def __init__(self, probe_orders=2):
+        self.cache = {}
+        self.timings = {}
+        self.probe_orders = probe_orders
+
+    @staticmethod
+    def shape_class(nd, nb, nt, n_max):
+        return (int(nd), int(nb), int(nt), int(np.ceil(np.log2(max(n_max, 1)))))
+
+    def choose(self, key, run_probe):
+        if key not in self.cache:
+            times = {}
+            for cand in self.CANDIDATES:
+                times[cand] = run_probe(cand, self.probe_orders)
+            self.timings[key] = times
+            self.cache[key] = min(times, key=times.get)
+        return self.cache[key]
+
+
+_TUNER = BatchTuner()
+
+
+def _room_bytes(n, nd, nb, nt, pairs, n_class):
+    """Device bytes one prepared room holds (its exchange workspace, E_total and bake state)."""
+    ws = nat.size("sp_energy_exchange_workspace", nat.SP_F32, nat.SP_EXCHANGE_STRUCTURED, n, nd, nb, nt, pairs, 1,
+                  nd, n_class)
+    return ws + n * nd * nb * nt * 4 + n * n * 9 + pairs * 60
+
+
+class PreparedWave:
+    """Rooms baked and prepared for one persistent batched exchange (all co-resident on the device)."""
+
+    def __init__(self, rooms, c, dt, nt, K):
+        dev = torch.device("cuda", torch.cuda.current_device())
+        self.c, self.dt, self.nt, self.K = c, dt, nt, K
+        self.objs, self.args, self.wss, self.etcs = [], [], [], []
+        for room in rooms:
+            r = build_room(room, "fp32")
+            r.bake_geometry()
+            r.init_source_energy(Coordinates(*room["source"]))
+            n, nd, nb = r._dev["e0dir"].shape
+            etc = torch.empty((n, nd, nb, nt), dtype=torch.float32, device=dev)
+            a = r._exchange_args(c, dt, nt, K, "auto", etc)
+            a.prepare_only = 1
+            a.plan_tag = next(_TAGS)
+            n_class = 1 + nd if a.algorithm == nat.SP_EXCHANGE_SLOTWISE else a.n_groups * a.n_in_dirs
+            wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, nt, a.n_dir_pairs,
+                           a.n_slots, a.n_in_dirs, n_class)
+            ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
+            nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())  # the plan
+            self.objs.append(r)
+            self.args.append(a)
+            self.wss.append((ws, wsz))
+            self.etcs.append(etc)
+        self.rooms = (nat.BatchRoom * len(rooms))()
+        for q, (a, (ws, wsz)) in enumerate(zip(self.args, self.wss)):
+            self.rooms[q].args = ctypes.pointer(a)
+            self.rooms[q].ws = ws.data_ptr()
+            self.rooms[q].ws_bytes = wsz
+        self.bsz = nat.size("sp_exchange_batch_workspace", len(rooms))
+        self.bws = torch.empty((self.bsz,), dtype=torch.uint8, device=dev)
+
+    def launch(self, choice, orders=None, wait_limit=0, force_timeout=False):
+        """Place E_0 and E_total again (plans reused), then run `orders` orders of every room in one launch.
+
+        Returns (status, launch ms, work items); status is the C-ABI's."""
+        orders = self.K if orders is None else orders
+        for a, (ws, wsz) in zip(self.args, self.wss):
+            a.max_order = orders
+            nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())
+        ms = ctypes.c_float(-1.0)
+        items = ctypes.c_longlong(0)
+        b = nat.BatchArgs()
+        b.n_rooms = len(self.args)
+        b.rooms = self.rooms
+        b.window_bins, b.ctas_per_sm = choice
+        b.wait_limit = wait_limit
+        b.force_timeout = 1 if force_timeout else 0
+        b.exchange_ms = ctypes.pointer(ms)
+        b.items = ctypes.pointer(items)
+        rc = nat.lib().sp_exchange_batch(ctypes.byref(b), _ptr(self.bws), self.bsz, _stream())
+        return rc, float(ms.value), int(items.value)
+
+    def results(self, rooms):
+        """Receiver histograms of each room after a full launch (collect_energy_receiver_mono)."""
+        out = []
+        for r, etc, room in zip(self.objs, self.etcs, rooms):
+            r._dev["etc"] = etc
+            r._etc_time_resolution, r._speed_of_sound, r._etc_duration = self.dt, self.c, self.nt * self.dt
+            r._max_order = self.K
+            rc = room["receivers"]
+            out.append(r.collect_energy_receiver_mono(Coordinates(rc[:, 0], rc[:, 1], rc[:, 2])).time)
+        return out
+
+
+def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, etc_duration=1.0,
+                        max_reflection_order=30, memory_fraction=0.6, tuner=None, force_choice=None):
+    """Solve every room, the exchange orders of each memory-sized wave in one persistent launch.
+
+    Returns (list of mono histograms (R, B, T) numpy in room order, stats):
+    stats holds per wave the rooms, their patch counts, the device ms of
+    bake + prepare, of the batched exchange launch and of exchange +
+    collection, the work items and the tile choice; plus the tuner's
+    timings.  FP32.
+    """
+    tuner = tuner or _TUNER
+    dev = torch.device("cuda", torch.cuda.current_device())
+    st = torch.cuda.current_stream()
+    c, dt = float(speed_of_sound), float(etc_time_resolution)
+    nt = int(etc_duration / etc_time_resolution)
+    K = int(max_reflection_order)
+    free, _ = torch.cuda.mem_get_info(dev)
+    budget = memory_fraction * (free + torch.cuda.memory_reserved(dev) - torch.cuda.memory_allocated(dev))
+    out = [None] * len(rooms)
+    waves = []
+    i = 0
+    while i < len(rooms):
+        wave, used = [], 0.0
+        while i < len(rooms):
+            room = rooms[i]
+            n_est = int(sum(2 * np.prod(np.round(np.delete(room["dims"], a) / room["patch_size"]))
+                            for a in range(3)))
+            need = _room_bytes(n_est, room["n_dirs"], room["n_bins"], nt, n_est * n_est, room["n_dirs"])
+            if wave and used + need > budget:
+                break
+            wave.append(i)
+            used += need
+            i += 1
+        waves.append(wave)
+    stats = {"waves": []}
+    for wave in waves:
+        sub = [rooms[idx] for idx in wave]
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(st)
+        pw = PreparedWave(sub, c, dt, nt, K)
+        e[1].record(st)
+
+        def probe(cand, k):
+            rc, ms, _ = pw.launch(cand, min(k, K))
+            if rc != nat.SP_OK:
+                raise nat.NativeError("sp_exchange_batch", rc)
+            return ms
+
+        n_max = max(r.n_patches for r in pw.objs)
+        nd, nb = pw.objs[0]._dev["e0dir"].shape[1:]
+        key = BatchTuner.shape_class(nd, nb, nt, n_max)
+        choice = force_choice or tuner.choose(key, probe)
+        e[2].record(st)
+        rc, ms_exchange, items = pw.launch(choice)
+        if rc != nat.SP_OK:
+            raise nat.NativeError("sp_exchange_batch", rc)
+        monos = pw.results(sub)
+        e[3].record(st)
+        e[3].synchronize()
+        for idx, mono in zip(wave, monos):
+            out[idx] = mono
+        stats["waves"].append({"rooms": len(wave), "patches": [int(r.n_patches) for r in pw.objs],
+                               "bake_prepare_ms": e[0].elapsed_time(e[1]), "exchange_ms": ms_exchange,
+                               "exchange_and_collect_ms": e[2].elapsed_time(e[3]), "items": items,
+                               "window_bins": choice[0], "ctas_per_sm": choice[1]})
+        del pw
+        torch.cuda.empty_cache()
+    stats["tuner"] = {str(k): {f"{w}x{c_}": v for (w, c_), v in t.items()} for k, t in tuner.timings.items()}
+    return out, stats

@@ -82,9 +82,9 @@ constexpr int kBarBytes = 128;                       // full[kStages], empty[kSt
 static_assert(2 * kStages * 8 <= kBarBytes, "barrier area too small");
 static_assert(kPackWarps == kConsumers, "one packed word per consumer warp");
 
-template <typename T>
+template <typename T, int kBinsPerLane = (sizeof(T) == 4 ? 32 : 8)>
 struct WsLayout {
-    static constexpr int kBins = sizeof(T) == 4 ? 32 : 8;   // bins per lane, strided by 32
+    static constexpr int kBins = kBinsPerLane;               // bins per lane, strided by 32
     static constexpr int kTW = 32 * kBins;                   // bins per window
     static constexpr int kAlign = 16 / (int)sizeof(T);       // elements per 16 bytes
     static constexpr int kStageF = kTW + kMaxSpan + kAlign - 1;  // staged elements per group
@@ -124,6 +124,15 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
     c = (t - s) - y;
     s = t;
 }
+// The compensation terms are kept between orders as bfloat16 (the top 16
+// bits of the FP32 term, rounded to nearest even): c is the rounding error
+// of s, at most half an FP32 ulp of s, so its 8-bit mantissa still carries
+// the sum to about 2^-33 of s, at half the memory traffic of FP32 terms.
+__device__ __forceinline__ float comp_get(uint16_t bits) { return __uint_as_float((uint32_t)bits << 16); }
+__device__ __forceinline__ uint16_t comp_put(float c) {
+    const uint32_t u = __float_as_uint(c);
+    return (uint16_t)((u + 0x7fffu + ((u >> 16) & 1u)) >> 16);  // finite values: round to nearest even
+}
 
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
@@ -144,15 +153,19 @@ __device__ __forceinline__ void slot_window(T (&acc)[kN], const T* win, T cf, in
 // no window starts before the buffer.  Every shared-memory read of a
 // consumer warp covers 32 consecutive elements (no bank conflict at any
 // offset).
-template <typename T>
+//
+// The work item is (seg_i: index into seg_order, win: window, b: band); the
+// kernels below take it from the block index, the batched exchange from its
+// work queue.
+template <typename T, int kB = WsLayout<T>::kBins>
 __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long long rs, int lead, long long cap,
                                            const int32_t* __restrict__ tile_recv,
                                            const int32_t* __restrict__ seg_order,
                                            const int64_t* __restrict__ seg_off, const Group* __restrict__ groups,
                                            const uint32_t* __restrict__ wpack, const T* __restrict__ coef,
                                            const T* __restrict__ eprev, T* __restrict__ gout,
-                                           int* __restrict__ err) {
-    using L = WsLayout<T>;
+                                           int* __restrict__ err, int seg_i, int win, int b) {
+    using L = WsLayout<T, kB>;
     using T2 = typename Vec2<T>::type;
     extern __shared__ __align__(128) unsigned char s_raw[];
     uint64_t* full = reinterpret_cast<uint64_t*>(s_raw);
@@ -161,9 +174,8 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
     __shared__ volatile int s_abort;
     __shared__ volatile int s_issued;  // stages issued
 
-    const long long seg = seg_order[blockIdx.x];
-    const int b = blockIdx.z;
-    const int t0 = blockIdx.y * L::kTW;
+    const long long seg = seg_order[seg_i];
+    const int t0 = win * L::kTW;
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
     const int n_grp = (int)(g_end - g_beg);  // groups of one segment (< 2^31)
     if (n_grp == 0) return;                   // the same for every thread of the block
@@ -306,11 +318,11 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
         const T *__restrict__ eprev, T *__restrict__ gout, int *__restrict__ err
 __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(SP_SCATTER_ARGS(float)) {
     scatter_ws<float>(n_class, nb, nt, rs, lead, cap, tile_recv, seg_order, seg_off, groups, wpack, coef, eprev, gout,
-                      err);
+                      err, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f64(SP_SCATTER_ARGS(double)) {
     scatter_ws<double>(n_class, nb, nt, rs, lead, cap, tile_recv, seg_order, seg_off, groups, wpack, coef, eprev, gout,
-                       err);
+                       err, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 #undef SP_SCATTER_ARGS
 

@@ -40,8 +40,8 @@ namespace {
 //
 // Late bins (t >= t_late) of an FP32 E_total are added with Kahan
 // compensation when comp is given: comp holds, per row, the compensation of
-// bins t_late .. nt - 1 (rows of nt - t_late values), zero before the first
-// order.  With x the order's addend (E_{k-1} + E_k, or E_k):
+// bins t_late .. nt - 1 (rows of nt - t_late bfloat16 values), zero before
+// the first order.  With x the order's addend (E_{k-1} + E_k, or E_k):
 //   y = x - c;  s' = s + y;  c' = (s' - s) - y
 // and the last update of a solve (fold) stores s' - c', the compensated sum.
 template <typename T>
@@ -49,7 +49,8 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                              const T* __restrict__ cdiff, const T* __restrict__ cspec,
                                              const T* __restrict__ g, T* __restrict__ ecur, T* __restrict__ etot,
-                                             const T* __restrict__ eadd, T* __restrict__ comp, int t_late, int fold) {
+                                             const T* __restrict__ eadd, uint16_t* __restrict__ comp, int t_late,
+                                             int fold) {
     extern __shared__ __align__(16) unsigned char s_mix[];
     const int stride = tile_tab_stride(n_class, nd);
     T* s_cd = reinterpret_cast<T*>(s_mix);  // [n_class] diffuse weight of band b
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
     T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;  // padded rows, stride rs
     T* et = etot ? etot + ((size_t)j * nd * nb + b) * nt : nullptr;  // nullptr: E_total not accumulated
     const T* ea = eadd ? eadd + ((size_t)j * nd * nb + b) * rs + lead : nullptr;  // deferred E_{k-1}, padded
-    T* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
+    uint16_t* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
         T diffuse = T(0);
         for (int q = 0; q < np; ++q) {
@@ -90,14 +91,14 @@ __global__ void __launch_bounds__(256) k_mix(int n_class, int nd, int nb, int nt
             if (et) {
                 T acc = et[o * cstride + t];
                 if (cj && t >= t_late) {
-                    T* cp = cj + (size_t)o * nb * nl + (t - t_late);
-                    T cc = *cp;
+                    uint16_t* cp = cj + (size_t)o * nb * nl + (t - t_late);
+                    T cc = (T)comp_get(*cp);
                     kahan_add(acc, cc, ea ? ea[(size_t)o * nb * rs + t] + v : v);
                     if (fold) {
                         et[o * cstride + t] = acc - cc;
                     } else {
                         et[o * cstride + t] = acc;
-                        *cp = cc;
+                        *cp = comp_put((float)cc);
                     }
                 } else {
                     if (ea) acc += ea[(size_t)o * nb * rs + t];
@@ -120,7 +121,7 @@ __global__ void __launch_bounds__(128) k_mix_general(int n_class, int nd, int nb
                                                      const int32_t* __restrict__ tab, const T* __restrict__ ctab,
                                                      const T* __restrict__ g, T* __restrict__ ecur,
                                                      T* __restrict__ etot, const T* __restrict__ eadd,
-                                                     T* __restrict__ comp, int t_late, int fold) {
+                                                     uint16_t* __restrict__ comp, int t_late, int fold) {
     extern __shared__ __align__(16) unsigned char s_mix[];
     const int stride = tile_tab_stride(n_class, nd);
     int* s_tab = reinterpret_cast<int*>(s_mix);
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(128) k_mix_general(int n_class, int nd, int nb
     T* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;
     T* et = etot ? etot + ((size_t)j * nd * nb + b) * nt : nullptr;
     const T* ea = eadd ? eadd + ((size_t)j * nd * nb + b) * rs + lead : nullptr;
-    T* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
+    uint16_t* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
         T v[kGeneralMaxDirs];
 #pragma unroll
@@ -154,25 +155,39 @@ __global__ void __launch_bounds__(128) k_mix_general(int n_class, int nd, int nb
             for (int o = 0; o < kGeneralMaxDirs; ++o)
                 if (o < nd) v[o] = fma(w[o], x, v[o]);
         }
+        const bool late = cj != nullptr && t >= t_late;
 #pragma unroll
-        for (int o = 0; o < kGeneralMaxDirs; ++o) {
-            if (o >= nd) break;
-            ek[(size_t)o * nb * rs + t] = v[o];
-            if (!et) continue;
-            T acc = et[o * cstride + t];
-            if (cj && t >= t_late) {
-                T* cp = cj + (size_t)o * nb * nl + (t - t_late);
-                T cc = *cp;
-                kahan_add(acc, cc, ea ? ea[(size_t)o * nb * rs + t] + v[o] : v[o]);
-                if (fold) {
-                    et[o * cstride + t] = acc - cc;
+        for (int o0 = 0; o0 < kGeneralMaxDirs; o0 += 8) {
+            if (o0 >= nd) break;
+            // eight directions' loads before their stores
+            T e8[8], a8[8];
+            uint16_t c8[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int o = o0 + q;
+                e8[q] = (o < nd && et) ? et[o * cstride + t] : T(0);
+                a8[q] = (o < nd && ea) ? ea[(size_t)o * nb * rs + t] : T(0);
+                c8[q] = (o < nd && late) ? cj[(size_t)o * nb * nl + (t - t_late)] : (uint16_t)0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int o = o0 + q;
+                if (o >= nd) break;
+                const T vo = v[o];  // o is a compile-time index (both loops unrolled)
+                ek[(size_t)o * nb * rs + t] = vo;
+                if (!et) continue;
+                if (late) {
+                    T acc = e8[q], cc = (T)comp_get(c8[q]);
+                    kahan_add(acc, cc, ea ? a8[q] + vo : vo);
+                    if (fold) {
+                        et[o * cstride + t] = acc - cc;
+                    } else {
+                        et[o * cstride + t] = acc;
+                        cj[(size_t)o * nb * nl + (t - t_late)] = comp_put((float)cc);
+                    }
                 } else {
-                    et[o * cstride + t] = acc;
-                    *cp = cc;
+                    et[o * cstride + t] = (ea ? e8[q] + a8[q] : e8[q]) + vo;
                 }
-            } else {
-                if (ea) acc += ea[(size_t)o * nb * rs + t];
-                et[o * cstride + t] = acc + v[o];
             }
         }
     }
@@ -203,18 +218,21 @@ __device__ __forceinline__ void kahan_add4(float4& s, float4& c, float4 x) {
     s = t;
 }
 
-__global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
-                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
-                                              const float* __restrict__ cdiff, const float* __restrict__ cspec,
-                                              const float* __restrict__ g, float* __restrict__ ecur,
-                                              float* __restrict__ etot, const float* __restrict__ eadd,
-                                              float* __restrict__ comp, int t_late, int fold) {
-    extern __shared__ __align__(16) unsigned char s_mix[];
+// The mix of one (band b, receiver j) by the whole block (any block size);
+// s_mix: 2 n_class floats + the tile table row.  kOG directions' loads are
+// issued together (8 in k_mix4; fewer where registers are short).
+template <int kOG = 8>
+__device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, long long rs, int lead,
+                                          const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
+                                          const float* __restrict__ cdiff, const float* __restrict__ cspec,
+                                          const float* __restrict__ g, float* __restrict__ ecur,
+                                          float* __restrict__ etot, const float* __restrict__ eadd,
+                                          uint16_t* __restrict__ comp, int t_late, int fold, int b, int j,
+                                          unsigned char* s_mix) {
     const int stride = tile_tab_stride(n_class, nd);
     float* s_cd = reinterpret_cast<float*>(s_mix);
     float* s_cs = s_cd + n_class;
     int* s_tab = reinterpret_cast<int*>(s_cs + n_class);
-    const int b = blockIdx.x, j = blockIdx.y;
     const int tile = tile_of[j];
     for (int k = threadIdx.x; k < stride; k += blockDim.x) s_tab[k] = tab[(size_t)tile * stride + k];
     for (int c = threadIdx.x; c < n_class; c += blockDim.x) {
@@ -235,7 +253,7 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
     float4* ek = reinterpret_cast<float4*>(ecur + ((size_t)j * nd * nb + b) * rs + lead);
     float4* et = etot ? reinterpret_cast<float4*>(etot + ((size_t)j * nd * nb + b) * nt) : nullptr;
     const float4* ea = eadd ? reinterpret_cast<const float4*>(eadd + ((size_t)j * nd * nb + b) * rs + lead) : nullptr;
-    float4* cj = (comp && et) ? reinterpret_cast<float4*>(comp + ((size_t)j * nd * nb + b) * (nt - t_late)) : nullptr;
+    ushort4* cj = (comp && et) ? reinterpret_cast<ushort4*>(comp + ((size_t)j * nd * nb + b) * (nt - t_late)) : nullptr;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int t = threadIdx.x; t < nt4; t += blockDim.x) {
         float4 d = zero;
@@ -244,18 +262,19 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
             if (s_cd[c] != 0.0f) d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);  // skip pure mirror classes
         }
         const bool late = cj != nullptr && t >= tl4;
-        for (int o0 = 0; o0 < nd; o0 += 8) {
-            const int no = min(8, nd - o0);
-            // every load of the 8 directions (E_total, deferred E_{k-1}, compensation) before any store
-            float4 e[8], x[8], c[8];
+        for (int o0 = 0; o0 < nd; o0 += kOG) {
+            const int no = min(kOG, nd - o0);
+            // every load of the kOG directions (E_total, deferred E_{k-1}, compensation) before any store
+            float4 e[kOG], x[kOG];
+            ushort4 c[kOG];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < kOG; ++k) {
                 e[k] = (k < no && et) ? et[(o0 + k) * cs4 + t] : zero;
                 x[k] = (k < no && ea) ? __ldg(ea + (o0 + k) * ers4 + t) : zero;
-                c[k] = (k < no && late) ? cj[(o0 + k) * cc4 + (t - tl4)] : zero;
+                c[k] = (k < no && late) ? cj[(o0 + k) * cc4 + (t - tl4)] : make_ushort4(0, 0, 0, 0);
             }
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < kOG; ++k) {
                 if (k < no) {
                     const int o = o0 + k;
                     float4 v = d;
@@ -266,13 +285,15 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
                     ek[o * ers4 + t] = v;
                     if (!et) continue;
                     if (late) {
-                        float4 s_ = e[k], cc = c[k];
+                        float4 s_ = e[k];
+                        float4 cc = make_float4(comp_get(c[k].x), comp_get(c[k].y), comp_get(c[k].z), comp_get(c[k].w));
                         kahan_add4(s_, cc, ea ? add4(x[k], v) : v);
                         if (fold) {
                             et[o * cs4 + t] = sub4(s_, cc);
                         } else {
                             et[o * cs4 + t] = s_;
-                            cj[o * cc4 + (t - tl4)] = cc;
+                            cj[o * cc4 + (t - tl4)] =
+                                make_ushort4(comp_put(cc.x), comp_put(cc.y), comp_put(cc.z), comp_put(cc.w));
                         }
                     } else {
                         et[o * cs4 + t] = add4(ea ? add4(e[k], x[k]) : e[k], v);
@@ -281,6 +302,17 @@ __global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int n
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
+                                              const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
+                                              const float* __restrict__ cdiff, const float* __restrict__ cspec,
+                                              const float* __restrict__ g, float* __restrict__ ecur,
+                                              float* __restrict__ etot, const float* __restrict__ eadd,
+                                              uint16_t* __restrict__ comp, int t_late, int fold) {
+    extern __shared__ __align__(16) unsigned char s_mix[];
+    mix4_item(n_class, nd, nb, nt, rs, lead, tile_of, tab, cdiff, cspec, g, ecur, etot, eadd, comp, t_late, fold,
+              blockIdx.x, blockIdx.y, s_mix);
 }
 
 template <typename T>
@@ -517,7 +549,7 @@ struct Plan {
     int64_t* info;  // [signature, n_active, n_groups, 0]
     int* err;
     int t_late;     // first compensated E_total bin (FP32): nt / 4, rounded down to a multiple of 4
-    void* comp;     // FP32: (N * D * B, nt - t_late) Kahan compensation of E_total's late bins
+    uint16_t* comp;  // FP32: (N * D * B, nt - t_late) Kahan compensation of E_total's late bins (bfloat16)
 };
 
 // First late bin of E_total: a quarter of the histogram, on a float4 boundary.
@@ -561,7 +593,7 @@ Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p
     L.info = (int64_t*)take(32);
     L.err = (int*)take(16);
     L.t_late = late_bin(nt);
-    L.comp = esz == 4 ? take(L.rows * (size_t)(nt - L.t_late) * 4) : nullptr;
+    L.comp = esz == 4 ? (uint16_t*)take(L.rows * (size_t)(nt - L.t_late) * 2) : nullptr;
     L.bytes = (size_t)(q - (char*)base);
     return L;
 }
@@ -618,7 +650,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     if (general && mix_general_smem(n_class, nd, sizeof(T)) > kMixGeneralMaxSmem) return SP_ERR_UNSUPPORTED;
     // the receiver-side contraction on tensor cores: FP32, 32 <= D <= 64 (a multiple of 16, the MMA's N)
     const bool tensor_mix = general && sizeof(T) == 4 && !a->no_tensor_cores && nd >= 32 && nd <= 64 &&
-                            nd % 16 == 0 && tc_smem_bytes(n_class, nd) <= kTcSmem;
+                            nd % 16 == 0 && tc_smem_bytes(n_class, nd) <= kTcSmemMax;
     Plan L = plan_layout(nullptr, sizeof(T), n, nd, nb, nt, p, n_class, material, general);
     if (ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
     L = plan_layout(ws, sizeof(T), n, nd, nb, nt, p, n_class, material, general);
@@ -631,9 +663,9 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     const int lead = L.R.lead;
     T* states = (T*)a->states_out;
     // Kahan compensation of E_total's late bins (FP32, unless switched off)
-    float* comp = (sizeof(T) == 4 && etot && !a->plain_total) ? (float*)L.comp : nullptr;
+    uint16_t* comp = (sizeof(T) == 4 && etot && !a->plain_total) ? L.comp : nullptr;
     cudaMemsetAsync(L.err, 0, sizeof(int), st);
-    if (comp) cudaMemsetAsync(comp, 0, L.rows * (size_t)(nt - L.t_late) * sizeof(float), st);
+    if (comp) cudaMemsetAsync(comp, 0, L.rows * (size_t)(nt - L.t_late) * sizeof(uint16_t), st);
     // ecur: only the leads need zeros (every bin is written each order);
     // eprev: the same when a starting state fills its bins, else all zero
     // before the starting energies are placed
@@ -732,12 +764,22 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     cudaMemcpyAsync(L.info, info, sizeof(info), cudaMemcpyHostToDevice, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;  // `info` is a host local
     }
+    if (a->prepare_only) {
+        // the batched exchange runs the orders: leave E_0, E_total and the plan (with n_active in info) in ws
+        if (reuse) {
+            const int64_t info[4] = {sig, (int64_t)n_active, (int64_t)n_groups, 0};
+            cudaMemcpyAsync(L.info, info, sizeof(info), cudaMemcpyHostToDevice, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+        }
+    }
     if (a->plan_stats) {
         a->plan_stats[0] = n_groups;
         a->plan_stats[1] = (long long)n_tiles * n_class;
         a->plan_stats[2] = pp;
         a->plan_stats[3] = n_tiles;
     }
+
+    if (a->prepare_only) return sp_check_launch();
 
     // ---- orders
     dim3 mgrid(nb, n);
@@ -771,9 +813,10 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         const int fold = k == a->max_order;  // the last E_total update folds the compensation in
         scatter_timer.stop(st);
         if (general && tensor_mix) {
+            const size_t tsmem = tc_smem_bytes(n_class, nd);
             if (k == k0 + 1)
-                cudaFuncSetAttribute(k_mix_general_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-            k_mix_general_tc<<<mgrid, kTcThreads, kTcSmem, sp_counted(st)>>>(
+                cudaFuncSetAttribute(k_mix_general_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
+            k_mix_general_tc<<<mgrid, kTcThreads, tsmem, sp_counted(st)>>>(
                 n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab, (const float*)L.ctab, (const float*)L.g,
                 (float*)ecur, (float*)et_k, (const float*)ea_k, comp, L.t_late, fold, L.err);
         } else if (general) {
@@ -782,7 +825,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
                 cudaFuncSetAttribute(k_mix_general<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
             k_mix_general<T><<<mgrid, 128, gsmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of,
                                                                     L.tile_tab, (const T*)L.ctab, (const T*)L.g, ecur,
-                                                                    et_k, ea_k, (T*)comp, L.t_late, fold);
+                                                                    et_k, ea_k, comp, L.t_late, fold);
         } else if (sizeof(T) == 4 && nt % 4 == 0)
             k_mix4<<<mgrid, 128, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                           (const float*)L.cdiff, (const float*)L.cspec,
@@ -791,7 +834,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         else
             k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
                                                             (const T*)L.cdiff, (const T*)L.cspec, (const T*)L.g, ecur,
-                                                            et_k, ea_k, (T*)comp, L.t_late, fold);
+                                                            et_k, ea_k, comp, L.t_late, fold);
         if (states && (k - k0) % a->states_every == 0)
             copy_rows(states + (size_t)((k - k0) / a->states_every) * e, (size_t)nt, ecur + lead, L.R.rs, nt, L.rows,
                       st);
@@ -810,7 +853,243 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     return herr ? SP_ERR_TIMEOUT : SP_OK;
 }
 
+// ------------------------------------------------------------ batched rooms
+// Many rooms' exchanges in one persistent launch.  Each room was prepared by
+// sp_energy_exchange with prepare_only (E_0, E_total, plan in its own
+// workspace); all rooms share D, B, T and the order count K.  The work items
+// of order k are every room's scatter items (segment, window, band) and then
+// every room's mix items (band, receiver); a block takes the next item from a
+// ticket counter, waits until the item's inputs are complete (a scatter item
+// of room r and order k: all mix items of (r, k - 1); a mix item: all scatter
+// items of (r, k) and all mix items of (r, k - 1)), runs it and counts it
+// done.  Tickets are taken in item order, so every item a block waits for
+// was taken earlier by a running block: the launch always progresses.  Waits
+// are bounded; a wait that gives up sets the error flag, after which blocks
+// only count the remaining items.
+struct BatchRoom {
+    int n, n_class, n_active, comp_on;
+    long long cap, n_scatter, n_mix;  // scatter / mix items per order
+    long long s_off, m_off;           // offsets of the room's items in an order's scatter / mix part
+    const int32_t* tile_recv;
+    const int32_t* seg_order;
+    const int64_t* seg_off;
+    const Group* groups;
+    const uint32_t* wpack;
+    const float* coef;
+    float* buf0;  // E_0 and the odd orders' inputs (padded rows)
+    float* buf1;
+    float* g;
+    const int32_t* tile_of;
+    const int32_t* tile_tab;
+    const float* cdiff;
+    const float* cspec;
+    float* etot;
+    uint16_t* comp;
+    unsigned long long* done;  // [0]: scatter items done, [1]: mix items done (over all orders)
+};
+
+struct BatchShape {
+    int nd, nb, nt, K, lead, t_late, windows, n_rooms;
+    long long rs, s_total, m_total, per_order, total;
+    unsigned wait_limit;
+    int force_timeout;
+};
+
+constexpr int kErrBatchWait = 5;  // error flag: a batched item's dependency wait gave up
+
+// Bounded wait until *ctr >= target (acquire); false when the limit is reached or another block failed.
+__device__ __forceinline__ bool batch_wait(const unsigned long long* ctr, unsigned long long target, unsigned limit,
+                                           const volatile int* err) {
+    for (unsigned it = 0;; ++it) {
+        unsigned long long v;
+        asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ctr) : "memory");
+        if (v >= target) return true;
+        if (it >= limit || *err) return false;
+        __nanosleep(128);
+    }
+}
+
+template <int kB>
+__global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoom* __restrict__ rooms, BatchShape S,
+                                                                  unsigned long long* __restrict__ ticket,
+                                                                  int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    __shared__ long long s_item;
+    __shared__ int s_go;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(ticket, 1ull);
+        __syncthreads();
+        const long long t = s_item;
+        if (t >= S.total) break;
+        const int k = (int)(t / S.per_order) + 1;
+        const long long rem = t % S.per_order;
+        const bool scatter = rem < S.s_total;
+        const long long pos = scatter ? rem : rem - S.s_total;
+        int lo = 0, hi = S.n_rooms - 1;  // the room whose part holds pos
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((scatter ? rooms[mid].s_off : rooms[mid].m_off) <= pos)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const BatchRoom& R = rooms[lo];
+        const long long local = pos - (scatter ? R.s_off : R.m_off);
+        if (threadIdx.x == 0) {
+            bool ok = *(volatile int*)err == 0;
+            const unsigned long long prev_mix = (unsigned long long)(k - 1) * (unsigned long long)R.n_mix;
+            if (ok && S.force_timeout && t == 0) ok = batch_wait(&R.done[1], ~0ull, S.wait_limit, err);  // test hook
+            if (ok) ok = batch_wait(&R.done[1], prev_mix, S.wait_limit, err);
+            if (ok && !scatter)
+                ok = batch_wait(&R.done[0], (unsigned long long)k * (unsigned long long)R.n_scatter, S.wait_limit,
+                                err);
+            if (!ok) atomicCAS(err, 0, kErrBatchWait);
+            __threadfence();
+            s_go = ok && *(volatile int*)err == 0;
+        }
+        __syncthreads();
+        if (s_go) {
+            float* eprev = (k & 1) ? R.buf0 : R.buf1;  // E_{k-1}
+            if (scatter) {
+                asm volatile("fence.proxy.async.global;" ::: "memory");  // E_{k-1} was written by generic stores
+                const int per_seg = S.windows * S.nb;
+                scatter_ws<float, kB>(R.n_class, S.nb, S.nt, S.rs, S.lead, R.cap, R.tile_recv, R.seg_order, R.seg_off,
+                                      R.groups, R.wpack, R.coef, eprev, R.g, err, (int)(local / per_seg),
+                                      (int)((local % per_seg) / S.nb), (int)(local % S.nb));
+            } else {
+                float* ecur = (k & 1) ? R.buf1 : R.buf0;
+                const bool first_of_pair = (k & 1) == 1;
+                float* et = (first_of_pair && k < S.K) ? nullptr : R.etot;
+                const float* ea = (R.etot && !first_of_pair) ? eprev : nullptr;
+                mix4_item<2>(R.n_class, S.nd, S.nb, S.nt, S.rs, S.lead, R.tile_of, R.tile_tab, R.cdiff, R.cspec, R.g,
+                          ecur, et, ea, R.comp_on ? R.comp : nullptr, S.t_late, k == S.K, (int)(local % S.nb),
+                          (int)(local / S.nb), s_dyn);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();  // the item's results before its count
+            atomicAdd(&R.done[scatter ? 0 : 1], 1ull);
+        }
+    }
+}
+
 }  // namespace
+
+extern "C" size_t sp_exchange_batch_workspace(int n_rooms) {
+    return sp_align((size_t)(n_rooms > 0 ? n_rooms : 1) * sizeof(BatchRoom)) +
+           sp_align((size_t)(n_rooms > 0 ? n_rooms : 1) * 2 * sizeof(unsigned long long)) + 256;
+}
+
+extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_bytes, void* stream) {
+    if (!b || !b->rooms || b->n_rooms < 1 || !ws) return SP_ERR_ARG;
+    if (b->window_bins != 1024 && b->window_bins != 512) return SP_ERR_ARG;
+    if (ws_bytes < sp_exchange_batch_workspace(b->n_rooms)) return SP_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    const sp_exchange_args* a0 = b->rooms[0].args;
+    if (!a0) return SP_ERR_ARG;
+    BatchShape S{};
+    S.nd = a0->n_dirs;
+    S.nb = a0->n_bins;
+    S.nt = a0->n_samples;
+    S.K = a0->max_order;
+    S.n_rooms = b->n_rooms;
+    S.wait_limit = b->wait_limit ? b->wait_limit : (1u << 24);
+    S.force_timeout = b->force_timeout;
+    if (S.nt % 4 != 0 || S.K < 1 || S.nt > 65535) return SP_ERR_UNSUPPORTED;
+    const Rows R0 = padded_rows(S.nt);
+    S.lead = R0.lead;
+    S.rs = (long long)R0.rs;
+    S.t_late = late_bin(S.nt);
+    const int kTWb = b->window_bins;
+    S.windows = (S.nt + kTWb - 1) / kTWb;
+    std::vector<BatchRoom> host((size_t)b->n_rooms);
+    size_t smem = b->window_bins == 1024 ? WsLayout<float, 32>::kSmem : WsLayout<float, 16>::kSmem;
+    long long s_tot = 0, m_tot = 0;
+    for (int r = 0; r < b->n_rooms; ++r) {
+        const sp_exchange_args* a = b->rooms[r].args;
+        if (!a || a->precision != SP_F32 || a->n_dirs != S.nd || a->n_bins != S.nb || a->n_samples != S.nt ||
+            a->max_order != S.K || a->state_in || a->states_out || !a->etc_total || a->skip_total ||
+            a->n_dir_pairs < 1 || (a->algorithm != SP_EXCHANGE_STRUCTURED && a->algorithm != SP_EXCHANGE_SLOTWISE &&
+                                   a->algorithm != SP_EXCHANGE_MATERIAL))
+            return SP_ERR_ARG;
+        const bool slotwise = a->algorithm == SP_EXCHANGE_SLOTWISE;
+        const bool material = a->algorithm == SP_EXCHANGE_MATERIAL || slotwise;
+        const int n_class = slotwise ? 1 + S.nd : material ? 1 + a->n_in_dirs : a->n_groups * a->n_in_dirs;
+        const Plan L = plan_layout(b->rooms[r].ws, 4, a->n_patches, S.nd, S.nb, S.nt, a->n_dir_pairs, n_class, material,
+                                   false);
+        if (b->rooms[r].ws_bytes < L.bytes) return SP_ERR_WORKSPACE;
+        int64_t info[4] = {0, 0, 0, 0};
+        cudaMemcpyAsync(info, L.info, sizeof(info), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+        BatchRoom& R = host[(size_t)r];
+        R.n = a->n_patches;
+        R.n_class = n_class;
+        R.n_active = (int)info[1];
+        R.comp_on = a->plain_total ? 0 : 1;
+        R.cap = material ? 2 * a->n_dir_pairs : a->n_dir_pairs;
+        R.n_scatter = (long long)R.n_active * S.windows * S.nb;
+        R.n_mix = (long long)S.nb * R.n;
+        if (R.n_scatter < 1) return SP_ERR_ARG;  // a room without pairs inside the histogram: solve it alone
+        R.s_off = s_tot;
+        R.m_off = m_tot;
+        s_tot += R.n_scatter;
+        m_tot += R.n_mix;
+        R.tile_recv = L.C.tile_recv;
+        R.seg_order = L.C.seg_order;
+        R.seg_off = L.C.seg_off;
+        R.groups = L.C.groups;
+        R.wpack = L.C.wpack;
+        R.coef = (const float*)L.C.coef;
+        R.buf0 = (float*)L.eprev;
+        R.buf1 = (float*)L.ecur;
+        R.g = (float*)L.g;
+        R.tile_of = L.C.tile_of;
+        R.tile_tab = L.tile_tab;
+        R.cdiff = (const float*)L.cdiff;
+        R.cspec = (const float*)L.cspec;
+        R.etot = (float*)a->etc_total;
+        R.comp = L.comp;
+        const size_t msmem = (size_t)2 * n_class * sizeof(float) + (size_t)tile_tab_stride(n_class, S.nd) * sizeof(int);
+        if (msmem > smem) smem = msmem;
+    }
+    S.s_total = s_tot;
+    S.m_total = m_tot;
+    S.per_order = s_tot + m_tot;
+    S.total = S.per_order * S.K;
+    char* q = (char*)ws;
+    BatchRoom* d_rooms = (BatchRoom*)q;
+    q += sp_align((size_t)b->n_rooms * sizeof(BatchRoom));
+    unsigned long long* done = (unsigned long long*)q;
+    q += sp_align((size_t)b->n_rooms * 2 * sizeof(unsigned long long));
+    unsigned long long* ticket = (unsigned long long*)q;
+    int* err = (int*)(q + 64);
+    for (int r = 0; r < b->n_rooms; ++r) host[(size_t)r].done = done + 2 * r;
+    cudaMemcpyAsync(d_rooms, host.data(), host.size() * sizeof(BatchRoom), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(done, 0, (size_t)b->n_rooms * 2 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(q, 0, 256, st);
+    int dev = 0, n_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = b->ctas_per_sm > 0 ? b->ctas_per_sm : 1;
+    SpEventTimer timer(b->exchange_ms != nullptr, st);
+    if (b->window_bins == 1024) {
+        cudaFuncSetAttribute(k_batch_exchange<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_batch_exchange<32><<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
+    } else {
+        cudaFuncSetAttribute(k_batch_exchange<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_batch_exchange<16><<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
+    }
+    timer.stop(st);
+    int rc = sp_check_launch();
+    if (rc != SP_OK) return rc;
+    int herr = 0;
+    cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
+    if (b->exchange_ms) *b->exchange_ms = timer.elapsed_ms();
+    if (b->items) *b->items = S.total;
+    return herr ? SP_ERR_TIMEOUT : SP_OK;
+}
 
 size_t sp_structured_workspace(int precision, int algorithm, int n_patches, int n_dirs, int n_bins, int n_samples,
                                long long n_dir_pairs, int n_class) {

@@ -36,8 +36,7 @@ constexpr int kTcM = 128;           // bins per chunk (MMA M)
 constexpr int kTcKc = 32;           // classes staged per A chunk (4 MMA k-steps)
 constexpr int kTcThreads = 128;     // 4 warps: one per tensor-memory lane quarter
 constexpr int kErrTcWait = 4;       // error flag: an MMA completion wait gave up
-constexpr uint32_t kTcCols = 512;   // tensor-memory columns held by a CTA (the kernel runs one CTA per SM)
-constexpr size_t kTcSmem = 200 * 1024;  // dynamic shared memory of a CTA (one per SM)
+constexpr size_t kTcSmemMax = 200 * 1024;  // dynamic shared memory limit of a CTA
 constexpr uint32_t kTcALbo = 128;                   // A: bytes between class groups of 4
 constexpr uint32_t kTcASbo = (kTcKc / 4) * 128;     // A: bytes between bin groups of 8 (1 KB)
 constexpr uint32_t kTcAPart = (kTcM / 8) * kTcASbo;  // one of A hi / A lo (16 KB)
@@ -103,7 +102,7 @@ __device__ __forceinline__ uint32_t tc_b_off(int o, int k, int kp) {
 __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
     int n_class, int nd, int nb, int nt, long long rs, int lead, const int32_t* __restrict__ tile_of,
     const int32_t* __restrict__ tab, const float* __restrict__ ctab, const float* __restrict__ g,
-    float* __restrict__ ecur, float* __restrict__ etot, const float* __restrict__ eadd, float* __restrict__ comp,
+    float* __restrict__ ecur, float* __restrict__ etot, const float* __restrict__ eadd, uint16_t* __restrict__ comp,
     int t_late, int fold, int* __restrict__ err) {
     extern __shared__ __align__(1024) unsigned char s_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(s_raw);            // MMA completion
@@ -126,7 +125,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
         *s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const uint32_t n_cols = kTcCols;
+    const uint32_t n_cols = nd <= 32 ? 32u : 64u;  // power of two >= N
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(s_tmem)),
                      "r"(n_cols)
@@ -155,22 +154,33 @@ __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
     float* ek = ecur + ((size_t)j * nd * nb + b) * rs + lead;
     float* et = etot ? etot + ((size_t)j * nd * nb + b) * nt : nullptr;
     const float* ea = eadd ? eadd + ((size_t)j * nd * nb + b) * rs + lead : nullptr;
-    float* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
+    uint16_t* cj = (comp && et) ? comp + ((size_t)j * nd * nb + b) * nl : nullptr;
     unsigned phase = 0;
     bool ok = true;
     for (int t0 = 0; t0 < nt && ok; t0 += kTcM) {
         for (int kc = 0; kc < kp && ok; kc += kTcKc) {
             // stage A = G[cls[kc + k], t0 + t] (hi / lo), transposed to classes-contiguous rows
+            // (all of a thread's loads are issued before its stores: 32 loads in flight per thread)
             const int kcn = min(kTcKc, kp - kc);
-            for (int q = threadIdx.x; q < kTcM * kTcKc; q += kTcThreads) {
+            constexpr int kPer = kTcM * kTcKc / kTcThreads;
+            float xs[kPer];
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int q = threadIdx.x + i * kTcThreads;
                 const int k = (q & 3) | (((q >> 5) & 7) << 2);  // class within the chunk (bits 0-1, 5-7)
                 const int t = ((q >> 2) & 7) | ((q >> 8) << 3);   // bin within the chunk (bits 2-4, 8-11)
-                float x = 0.0f;
-                if (k < kcn && kc + k < np && t0 + t < nt) x = __ldg(gj + (size_t)cls[kc + k] * cstride + t0 + t);
-                const float h = tf32_hi(x);
+                xs[i] = (k < kcn && kc + k < np && t0 + t < nt) ? __ldg(gj + (size_t)cls[kc + k] * cstride + t0 + t)
+                                                                : 0.0f;
+            }
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) {
+                const int q = threadIdx.x + i * kTcThreads;
+                const int k = (q & 3) | (((q >> 5) & 7) << 2);
+                const int t = ((q >> 2) & 7) | ((q >> 8) << 3);
+                const float h = tf32_hi(xs[i]);
                 const uint32_t off = tc_a_off(t, k);
                 a_hi[off] = h;
-                a_lo[off] = x - h;
+                a_lo[off] = xs[i] - h;
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
@@ -206,25 +216,33 @@ __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
             tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)o0, v);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (t >= nt) continue;
+            // the 16 columns' E_total, deferred E_{k-1} and compensation loads first, then the stores
+            const bool late = cj != nullptr && t >= t_late;
+            float e16[16], a16[16];
+            uint16_t c16[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int o = o0 + q;
+                e16[q] = et ? et[o * cstride + t] : 0.0f;
+                a16[q] = ea ? __ldg(ea + (size_t)o * nb * rs + t) : 0.0f;
+                c16[q] = late ? cj[(size_t)o * nb * nl + (t - t_late)] : (uint16_t)0;
+            }
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
                 const int o = o0 + q;
                 ek[(size_t)o * nb * rs + t] = v[q];
                 if (!et) continue;
-                float acc = et[o * cstride + t];
-                if (cj && t >= t_late) {
-                    float* cp = cj + (size_t)o * nb * nl + (t - t_late);
-                    float cc = *cp;
-                    kahan_add(acc, cc, ea ? ea[(size_t)o * nb * rs + t] + v[q] : v[q]);
+                if (late) {
+                    float acc = e16[q], cc = comp_get(c16[q]);
+                    kahan_add(acc, cc, ea ? a16[q] + v[q] : v[q]);
                     if (fold) {
                         et[o * cstride + t] = acc - cc;
                     } else {
                         et[o * cstride + t] = acc;
-                        *cp = cc;
+                        cj[(size_t)o * nb * nl + (t - t_late)] = comp_put(cc);
                     }
                 } else {
-                    if (ea) acc += ea[(size_t)o * nb * rs + t];
-                    et[o * cstride + t] = acc + v[q];
+                    et[o * cstride + t] = (ea ? e16[q] + a16[q] : e16[q]) + v[q];
                 }
             }
         }

@@ -13,3 +13,4 @@ extern "C" long long sp_kernel_launches(void) { return g_launches.load(std::memo
 
 extern "C" size_t sp_exchange_args_size(void) { return sizeof(sp_exchange_args); }
 extern "C" size_t sp_adjoint_args_size(void) { return sizeof(sp_adjoint_args); }
+extern "C" size_t sp_batch_args_size(void) { return sizeof(sp_batch_args); }

@@ -75,6 +75,7 @@ def test_struct_mirrors_match_the_library():
     lib = _native.lib()
     assert lib.sp_exchange_args_size() == ct.sizeof(_native.ExchangeArgs)
     assert lib.sp_adjoint_args_size() == ct.sizeof(_native.AdjointArgs)
+    assert lib.sp_batch_args_size() == ct.sizeof(_native.BatchArgs)
 
 
 def declared_prototypes():
