@@ -61,7 +61,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fwd-bwd", action="store_true", help="skip the gradient (forward + backward) leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the cfg1 / cfg2 legs")
-    ap.add_argument("--batch-rooms", type=int, default=8, help="seeded shoebox rooms for the batch leg (0: skip)")
+    ap.add_argument("--batch-rooms", type=int, default=256,
+                    help="seeded shoebox rooms for the batch leg (cfg5: 256; 0: skip)")
     ap.add_argument("--fwd-bwd-only", action="store_true",
                     help="print only the gradient leg (shoebox, 2016 patches) as one JSON line")
     return ap.parse_args()
@@ -481,6 +482,8 @@ def run_gpu(args):
         try:
             ms_cpu, cores, desc = cpu_baseline(cfg, rows_per_thread=2)
             cpu = {"value": ms_cpu, "unit": "ms/solve", "cores": cores, "kind": "port", "sample": desc}
+            if configs and "cfg1" in configs and "cpu_measured" in configs["cfg1"]:
+                cpu["measured_cfg1"] = configs["cfg1"]["cpu_measured"]
         except Exception as exc:  # the CPU leg must not hide the GPU result
             cpu = {"value": None, "unit": "ms/solve", "cores": None, "kind": "port", "sample": f"failed: {exc}"}
 
@@ -767,24 +770,53 @@ def fd_check_cfg1_geometry(n_params, seed=5, h=1e-4):
 
 
 # ------------------------------------------------------------------- batch
-def batch_rooms(n_rooms, seed=5, rank=0, world=1):
-    """Seeded shoebox rooms, dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, 1 s, order 30,
-    1 source + 4 receivers each.  Rank r of N solves rooms r, r + N, ... one after another; the job's
-    time is the slowest rank's sum of per-room device times."""
-    from sparrowpy_gb300.batch import shoebox_rooms, solve_rooms
+def batch_rooms(n_rooms, seed=5, rank=0, world=1, compare_rooms=16, fp64_sample=4):
+    """cfg5: seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, T = 1000, order 30,
+    1 source + 4 receivers each), each memory-sized wave's exchange orders in one persistent launch.
+
+    Rank r of N takes rooms r, r + N, ...; the job's time is the slowest
+    rank's sum of per-wave device times (bake and prepare, the persistent
+    exchange launch, the collection; the tuner's probe launches excluded).
+    Also, on rank 0: the first `compare_rooms` rooms solved one after
+    another and batched (rooms/s of both), and the FP32 batched receiver
+    histograms of the `fp64_sample` smallest rooms against their FP64 solves.
+    """
+    import torch
+    from sparrowpy_gb300.batch import BatchTuner, shoebox_rooms, solve_rooms, solve_rooms_batched
     from sparrowpy_gb300.replicas import gather_in_order, max_over_ranks, shard
     rooms = shoebox_rooms(n_rooms, seed=seed)
     idx, mine = shard(rooms, rank, world)
-    _, ms, patches = solve_rooms(mine) if mine else ([], [], [])
-    total = max_over_ranks(float(np.sum(ms)))
-    ms = gather_in_order(n_rooms, idx, [float(x) for x in ms])
-    patches = gather_in_order(n_rooms, idx, [int(x) for x in patches])
-    return {"workload": f"{n_rooms} seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, "
-                        f"T=1000, order 30, 4 receivers), dealt round-robin to {world} GPU(s), one after another "
-                        "on each",
-            "rooms": n_rooms, "patches_min": int(min(patches)), "patches_mean": float(np.mean(patches)),
-            "patches_max": int(max(patches)), "total_ms": total,
-            "rooms_per_s": float(n_rooms / (total * 1e-3)), "ms_per_room": ms}
+    tuner = BatchTuner()
+    monos, stats = solve_rooms_batched(mine, tuner=tuner) if mine else ([], {"waves": []})
+    wave_ms = [w["bake_prepare_ms"] + w["exchange_and_collect_ms"] for w in stats["waves"]]
+    total = max_over_ranks(float(np.sum(wave_ms)))
+    patches = gather_in_order(n_rooms, idx, [p for w in stats["waves"] for p in w["patches"]])
+    out = {"workload": f"{n_rooms} seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, "
+                       f"T=1000, order 30, 4 receivers), dealt round-robin to {world} GPU(s); per GPU, waves of rooms "
+                       "that fit in memory, each wave's exchange orders in one persistent launch",
+           "rooms": n_rooms, "patches_min": int(min(patches)), "patches_mean": float(np.mean(patches)),
+           "patches_max": int(max(patches)), "total_ms": total, "rooms_per_s": float(n_rooms / (total * 1e-3)),
+           "waves": [{k: w[k] for k in ("rooms", "bake_prepare_ms", "exchange_ms", "exchange_and_collect_ms",
+                                        "items", "window_bins", "ctas_per_sm")} for w in stats["waves"]],
+           "tuner_ms": stats.get("tuner")}
+    if rank == 0 and compare_rooms > 0:
+        sub = rooms[:compare_rooms]
+        _, ms_seq, _ = solve_rooms(sub)
+        _, st2 = solve_rooms_batched(sub, tuner=tuner)
+        ms_b = sum(w["bake_prepare_ms"] + w["exchange_and_collect_ms"] for w in st2["waves"])
+        out["compare"] = {"rooms": compare_rooms, "one_by_one_ms": float(np.sum(ms_seq)), "batched_ms": float(ms_b),
+                          "speedup": float(np.sum(ms_seq) / ms_b)}
+    if rank == 0 and fp64_sample > 0 and mine:
+        sizes = [p for w in stats["waves"] for p in w["patches"]]
+        pick = list(np.argsort(sizes)[:fp64_sample])
+        errs = []
+        for q in pick:
+            m64, _, _ = solve_rooms([mine[q]], precision="fp64")
+            errs.append(float(np.linalg.norm(monos[q] - m64[0]) / np.linalg.norm(m64[0])))
+        out["fp64_sample"] = {"rooms": [int(i) for i in pick], "patches": [int(sizes[i]) for i in pick],
+                              "receiver_rel_l2_fp32_vs_fp64": errs}
+    torch.cuda.empty_cache()
+    return out
 
 
 # ----------------------------------------------------------- reference arm
@@ -800,16 +832,18 @@ def run_reference(args):
         cfg["max_order"] = args.max_order
     times, desc, cores = [], "", orc.num_threads()
     for k in range(args.warmup + args.steps):
-        ms, cores, desc = cpu_baseline(cfg, rows_per_thread=1)
+        ms, cores, desc = cpu_baseline(cfg, rows_per_thread=1, exchange_rows=4)
         if k >= args.warmup:
             times.append(ms)
     v = float(np.mean(times))
+    cfg1_ms, cfg1_cores, cfg1_desc, _ = cpu_full_solve_cfg1()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms/solve", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded street-canyon geometry and materials (no dataset)",
             "config": workload_config(args.config, cfg, world),
-            "cpu_baseline": {"value": v, "unit": "ms/solve", "cores": cores, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": v, "unit": "ms/solve", "cores": cores, "kind": "port", "sample": desc,
+                             "measured_cfg1": {"ms": cfg1_ms, "cores": cfg1_cores, "sample": cfg1_desc}},
             "e2e": {"value": v, "unit": "ms/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
