@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--no-configs", action="store_true", help="skip the cfg1 / cfg2 legs")
     ap.add_argument("--batch-rooms", type=int, default=256,
                     help="seeded shoebox rooms for the batch leg (cfg5: 256; 0: skip)")
+    ap.add_argument("--leg", default=None, choices=["general", "batch"],
+                    help="print only one leg as one JSON line (profiling runs)")
+    ap.add_argument("--general-patch", type=float, default=0.25,
+                    help="patch size of the general-BRDF leg's room (1.0: 126 patches, a small profiling case)")
     ap.add_argument("--fwd-bwd-only", action="store_true",
                     help="print only the gradient leg (shoebox, 2016 patches) as one JSON line")
     return ap.parse_args()
@@ -128,6 +132,11 @@ class ClockSampler:
             out = {"sm_mhz": statistics.median(busy), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
                    "samples": len(sm)}
         return out
+
+
+def nt_late(cfg):
+    """First Kahan-compensated bin of E_total: a quarter of the histogram, on a multiple of 4."""
+    return (int(round(cfg["duration"] / cfg["dt"])) // 4) & ~3
 
 
 def algorithmic_bytes_per_order(n, d, b, t, pairs, n_slots, n_in, elem=4):
@@ -405,6 +414,24 @@ def run_gpu(args):
         del r2, mono
     e2e_ms = max_over_ranks(float(np.mean(e2e_times)) if e2e_times else None)
 
+    # the time the Kahan compensation of E_total's late bins costs: the same solve with plain FP32 sums
+    r.compensated_total = False
+    plain = []
+    for k in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        solve(r, cfg, as_coords)
+        e1.record(st)
+        e1.synchronize()
+        plain.append((e0.elapsed_time(e1), r.exchange_stats["order_ms"]))
+    r.compensated_total = True
+    kahan = {"ms_per_solve_plain_sums": float(np.mean([p[0] for p in plain])),
+             "ms_per_solve_compensated": ms_step,
+             "exchange_ms_plain_sums": float(np.mean([p[1] for p in plain])),
+             "exchange_ms_compensated": float(np.mean(order_ms)),
+             "late_bins_from": int(nt_late(cfg)),
+             "compensation_storage": "bfloat16 per late bin"}
+
     # roofline of one exchange order (scatter + mix launches of that order)
     stats = r.exchange_stats
     n, nd, nb, nt = r._dev["etc"].shape
@@ -505,6 +532,7 @@ def run_gpu(args):
             "roofline_smem": smem,
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
+            "kahan": kahan,
             "fwd_bwd": fwd_bwd,
             "configs": configs,
             "general_brdf": general,
@@ -581,7 +609,7 @@ def config_legs(cpu_cfg1=None):
 
 
 # ------------------------------------------------------------ general BRDF
-def general_brdf_leg(orders=50, dense_orders=5):
+def general_brdf_leg(orders=50, dense_orders=5, patch_size=0.25):
     """A table without diffuse-plus-mirror structure on every wall: cfg2's geometry and histogram.
 
     5 x 6 x 3 m shoebox at 0.25 m (2016 patches), one seeded random positive
@@ -598,15 +626,15 @@ def general_brdf_leg(orders=50, dense_orders=5):
     from sparrowpy_gb300.coords import FrequencyData
 
     def room():
-        r = scenes.shoebox(0.25, n_dirs=64, n_bins=6, scattering=0.3, absorption=0.1, precision="fp32")
+        r = scenes.shoebox(patch_size, n_dirs=64, n_bins=6, scattering=0.3, absorption=0.1, precision="fp32")
         rng = np.random.default_rng(9)
         dirs = hemisphere_directions(64)
         tab = rng.uniform(0.05, 0.25, size=(64, 64, 6)) / 8.0
         r.set_wall_brdf(np.arange(r.n_walls), FrequencyData(tab, np.asarray(r._frequencies, float)), dirs, dirs)
         return r
 
-    out = {"workload": "cfg2 geometry (2016 patches), a seeded random positive 64 x 64 x 6 BRDF table on every wall, "
-                       "6 bands, T=2000, FP32"}
+    out = {"workload": f"cfg2's 5 x 6 x 3 m shoebox at {patch_size} m patches, a seeded random positive 64 x 64 x 6 "
+                       "BRDF table on every wall, 6 bands, T=2000, FP32"}
     monos = {}
     for name, algo, tc, k in (("general_tensor_cores", "general", True, orders),
                               ("general_cuda_cores", "general", False, orders),
@@ -850,7 +878,16 @@ def run_reference(args):
 
 if __name__ == "__main__":
     a = parse()
-    if a.fwd_bwd_only:
+    if a.leg is not None:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        if a.leg == "general":
+            k = a.max_order or 50
+            leg = general_brdf_leg(orders=k, dense_orders=min(k, 5), patch_size=a.general_patch)
+        else:
+            leg = batch_rooms(a.batch_rooms, compare_rooms=0, fp64_sample=0)
+        print(json.dumps({"metric": f"{a.leg} leg", a.leg: leg}), flush=True)
+    elif a.fwd_bwd_only:
         import torch
         torch.cuda.set_device(dist_env()[2])
         print(json.dumps({"metric": "fwd+bwd ms", "fwd_bwd": fwd_bwd_config4(steps=a.steps)}), flush=True)

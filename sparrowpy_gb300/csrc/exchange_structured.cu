@@ -304,7 +304,7 @@ __device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, l
     }
 }
 
-__global__ void __launch_bounds__(128) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
+__global__ void __launch_bounds__(128, 4) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                               const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                               const float* __restrict__ cdiff, const float* __restrict__ cspec,
                                               const float* __restrict__ g, float* __restrict__ ecur,
