@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fwd-bwd", action="store_true", help="skip the gradient (forward + backward) leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the cfg1 / cfg2 legs")
+    ap.add_argument("--no-kahan", action="store_true", help="skip the plain-sum solves that time the Kahan cost")
     ap.add_argument("--batch-rooms", type=int, default=256,
                     help="seeded shoebox rooms for the batch leg (cfg5: 256; 0: skip)")
     ap.add_argument("--leg", default=None, choices=["general", "batch"],
@@ -135,8 +136,8 @@ class ClockSampler:
 
 
 def nt_late(cfg):
-    """First Kahan-compensated bin of E_total: a quarter of the histogram, on a multiple of 4."""
-    return (int(round(cfg["duration"] / cfg["dt"])) // 4) & ~3
+    """First Kahan-compensated bin of E_total: half the histogram, on a multiple of 4."""
+    return (int(round(cfg["duration"] / cfg["dt"])) // 2) & ~3
 
 
 def algorithmic_bytes_per_order(n, d, b, t, pairs, n_slots, n_in, elem=4):
@@ -417,7 +418,7 @@ def run_gpu(args):
     # the time the Kahan compensation of E_total's late bins costs: the same solve with plain FP32 sums
     r.compensated_total = False
     plain = []
-    for k in range(2):
+    for k in range(0 if args.no_kahan else 2):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         solve(r, cfg, as_coords)
@@ -425,7 +426,7 @@ def run_gpu(args):
         e1.synchronize()
         plain.append((e0.elapsed_time(e1), r.exchange_stats["order_ms"]))
     r.compensated_total = True
-    kahan = {"ms_per_solve_plain_sums": float(np.mean([p[0] for p in plain])),
+    kahan = None if not plain else {"ms_per_solve_plain_sums": float(np.mean([p[0] for p in plain])),
              "ms_per_solve_compensated": ms_step,
              "exchange_ms_plain_sums": float(np.mean([p[1] for p in plain])),
              "exchange_ms_compensated": float(np.mean(order_ms)),

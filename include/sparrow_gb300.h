@@ -248,7 +248,7 @@ typedef struct sp_exchange_args {
        previous call with this tag (and these sizes) is then reused */
     long long plan_tag;
     float* scatter_ms;      /* HOST float or NULL: CUDA-event time of the scatter launches alone (all orders) */
-    /* structured / material, FP32: E_total's late bins (t >= n_samples / 4, rounded down to a multiple of 4)
+    /* structured / material, FP32: E_total's late bins (t >= n_samples / 2, rounded down to a multiple of 4)
        are accumulated over the orders with Kahan compensation; 1 = plain FP32 sums instead */
     int plain_total;
     /* SP_EXCHANGE_GENERAL only: (n_groups * n_in_dirs, D, B) normalised table rows of the classes, with

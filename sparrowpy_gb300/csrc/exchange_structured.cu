@@ -221,25 +221,93 @@ __device__ __forceinline__ void kahan_add4(float4& s, float4& c, float4 x) {
 // The mix of one (band b, receiver j) by the whole block (any block size);
 // s_mix: 2 n_class floats + the tile table row.  kOG directions' loads are
 // issued together (8 in k_mix4; fewer where registers are short).
-template <int kOG = 8>
+// One float4 of bins (index t) of one (band, receiver) row of the mix: the
+// class sums, E_k and the E_total update (see k_mix).  s_cd / s_cs: the
+// band's class weights; the row pointers are those of the (band, receiver).
+template <int kOG>
+__device__ __forceinline__ void mix4_bin(int t, int np, const int* cls, const int* inv_off, const int* inv,
+                                         const float* s_cd, const float* s_cs, int nd, size_t cs4, size_t ers4,
+                                         size_t cc4, int tl4, const float4* __restrict__ gj, float4* __restrict__ ek,
+                                         float4* __restrict__ et, const float4* __restrict__ ea,
+                                         ushort4* __restrict__ cj, int fold) {
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d = zero;
+    for (int q = 0; q < np; ++q) {
+        const int c = cls[q];
+        if (s_cd[c] != 0.0f) d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);  // skip pure mirror classes
+    }
+    const bool late = cj != nullptr && t >= tl4;
+    for (int o0 = 0; o0 < nd; o0 += kOG) {
+        const int no = min(kOG, nd - o0);
+        // every load of the kOG directions (E_total, deferred E_{k-1}, compensation) before any store
+        float4 e[kOG], x[kOG];
+        ushort4 c[kOG];
+#pragma unroll
+        for (int k = 0; k < kOG; ++k) {
+            e[k] = (k < no && et) ? et[(o0 + k) * cs4 + t] : zero;
+            x[k] = (k < no && ea) ? __ldg(ea + (o0 + k) * ers4 + t) : zero;
+            c[k] = (k < no && late) ? cj[(o0 + k) * cc4 + (t - tl4)] : make_ushort4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int k = 0; k < kOG; ++k) {
+            if (k < no) {
+                const int o = o0 + k;
+                float4 v = d;
+                for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
+                    const int cl = inv[q];
+                    v = fma4(s_cs[cl], __ldg(gj + cl * cs4 + t), v);
+                }
+                ek[o * ers4 + t] = v;
+                if (!et) continue;
+                if (late) {
+                    float4 s_ = e[k];
+                    float4 cc = make_float4(comp_get(c[k].x), comp_get(c[k].y), comp_get(c[k].z), comp_get(c[k].w));
+                    kahan_add4(s_, cc, ea ? add4(x[k], v) : v);
+                    if (fold) {
+                        et[o * cs4 + t] = sub4(s_, cc);
+                    } else {
+                        et[o * cs4 + t] = s_;
+                        cj[o * cc4 + (t - tl4)] =
+                            make_ushort4(comp_put(cc.x), comp_put(cc.y), comp_put(cc.z), comp_put(cc.w));
+                    }
+                } else {
+                    et[o * cs4 + t] = add4(ea ? add4(e[k], x[k]) : e[k], v);
+                }
+            }
+        }
+    }
+}
+
+// The mix of receiver j for the bands [b0, b0 + n_bands) by the whole block
+// (any block size): the tile table and the bands' class weights in s_mix
+// (n_bands x 2 n_class floats, then the tile table row), then the threads
+// split evenly over the bands, each walking its band's bins (float4).
+template <int kOG = 8, bool kSplitBands = false>
 __device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                           const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                           const float* __restrict__ cdiff, const float* __restrict__ cspec,
                                           const float* __restrict__ g, float* __restrict__ ecur,
                                           float* __restrict__ etot, const float* __restrict__ eadd,
-                                          uint16_t* __restrict__ comp, int t_late, int fold, int b, int j,
-                                          unsigned char* s_mix) {
+                                          uint16_t* __restrict__ comp, int t_late, int fold, int b0, int j,
+                                          unsigned char* s_mix, int n_bands = 1) {
     const int stride = tile_tab_stride(n_class, nd);
-    float* s_cd = reinterpret_cast<float*>(s_mix);
-    float* s_cs = s_cd + n_class;
-    int* s_tab = reinterpret_cast<int*>(s_cs + n_class);
+    float* s_w = reinterpret_cast<float*>(s_mix);  // [n_bands][2][n_class]
+    int* s_tab = reinterpret_cast<int*>(s_w + (size_t)2 * n_bands * n_class);
     const int tile = tile_of[j];
     for (int k = threadIdx.x; k < stride; k += blockDim.x) s_tab[k] = tab[(size_t)tile * stride + k];
-    for (int c = threadIdx.x; c < n_class; c += blockDim.x) {
-        s_cd[c] = cdiff[(size_t)c * nb + b];
-        s_cs[c] = cspec[(size_t)c * nb + b];
+    for (int q = threadIdx.x; q < n_bands * n_class; q += blockDim.x) {
+        const int bb = q / n_class, c = q % n_class;
+        s_w[(size_t)2 * bb * n_class + c] = cdiff[(size_t)c * nb + b0 + bb];
+        s_w[(size_t)(2 * bb + 1) * n_class + c] = cspec[(size_t)c * nb + b0 + bb];
     }
     __syncthreads();
+    const int per = kSplitBands ? (int)blockDim.x / n_bands : (int)blockDim.x;  // threads per band
+    const int bb = kSplitBands ? (int)threadIdx.x / per : 0;
+    const int lt = kSplitBands ? (int)threadIdx.x % per : (int)threadIdx.x;
+    if (kSplitBands && bb >= n_bands) return;  // the remainder threads have no band
+    const int b = b0 + bb;
+    const float* s_cd = s_w + (size_t)2 * bb * n_class;
+    const float* s_cs = s_cd + n_class;
     const int np = s_tab[0];
     const int* cls = s_tab + 1;
     const int* inv_off = cls + n_class;
@@ -254,54 +322,8 @@ __device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, l
     float4* et = etot ? reinterpret_cast<float4*>(etot + ((size_t)j * nd * nb + b) * nt) : nullptr;
     const float4* ea = eadd ? reinterpret_cast<const float4*>(eadd + ((size_t)j * nd * nb + b) * rs + lead) : nullptr;
     ushort4* cj = (comp && et) ? reinterpret_cast<ushort4*>(comp + ((size_t)j * nd * nb + b) * (nt - t_late)) : nullptr;
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int t = threadIdx.x; t < nt4; t += blockDim.x) {
-        float4 d = zero;
-        for (int q = 0; q < np; ++q) {
-            const int c = cls[q];
-            if (s_cd[c] != 0.0f) d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);  // skip pure mirror classes
-        }
-        const bool late = cj != nullptr && t >= tl4;
-        for (int o0 = 0; o0 < nd; o0 += kOG) {
-            const int no = min(kOG, nd - o0);
-            // every load of the kOG directions (E_total, deferred E_{k-1}, compensation) before any store
-            float4 e[kOG], x[kOG];
-            ushort4 c[kOG];
-#pragma unroll
-            for (int k = 0; k < kOG; ++k) {
-                e[k] = (k < no && et) ? et[(o0 + k) * cs4 + t] : zero;
-                x[k] = (k < no && ea) ? __ldg(ea + (o0 + k) * ers4 + t) : zero;
-                c[k] = (k < no && late) ? cj[(o0 + k) * cc4 + (t - tl4)] : make_ushort4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int k = 0; k < kOG; ++k) {
-                if (k < no) {
-                    const int o = o0 + k;
-                    float4 v = d;
-                    for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
-                        const int cl = inv[q];
-                        v = fma4(s_cs[cl], __ldg(gj + cl * cs4 + t), v);
-                    }
-                    ek[o * ers4 + t] = v;
-                    if (!et) continue;
-                    if (late) {
-                        float4 s_ = e[k];
-                        float4 cc = make_float4(comp_get(c[k].x), comp_get(c[k].y), comp_get(c[k].z), comp_get(c[k].w));
-                        kahan_add4(s_, cc, ea ? add4(x[k], v) : v);
-                        if (fold) {
-                            et[o * cs4 + t] = sub4(s_, cc);
-                        } else {
-                            et[o * cs4 + t] = s_;
-                            cj[o * cc4 + (t - tl4)] =
-                                make_ushort4(comp_put(cc.x), comp_put(cc.y), comp_put(cc.z), comp_put(cc.w));
-                        }
-                    } else {
-                        et[o * cs4 + t] = add4(ea ? add4(e[k], x[k]) : e[k], v);
-                    }
-                }
-            }
-        }
-    }
+    for (int t = lt; t < nt4; t += per)
+        mix4_bin<kOG>(t, np, cls, inv_off, inv, s_cd, s_cs, nd, cs4, ers4, cc4, tl4, gj, ek, et, ea, cj, fold);
 }
 
 __global__ void __launch_bounds__(128, 4) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
@@ -548,12 +570,12 @@ struct Plan {
     int32_t *x_src, *x_dst, *x_row, *x_cls, *x_delay, *x_fwd;
     int64_t* info;  // [signature, n_active, n_groups, 0]
     int* err;
-    int t_late;     // first compensated E_total bin (FP32): nt / 4, rounded down to a multiple of 4
+    int t_late;     // first compensated E_total bin (FP32): nt / 2, rounded down to a multiple of 4
     uint16_t* comp;  // FP32: (N * D * B, nt - t_late) Kahan compensation of E_total's late bins (bfloat16)
 };
 
-// First late bin of E_total: a quarter of the histogram, on a float4 boundary.
-inline int late_bin(int nt) { return (nt / 4) & ~3; }
+// First late bin of E_total: half the histogram, on a float4 boundary.
+inline int late_bin(int nt) { return (nt / 2) & ~3; }
 
 Plan plan_layout(void* base, int esz, int n, int nd, int nb, int nt, long long p, int n_class, bool material,
                  bool general) {
@@ -857,8 +879,8 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
 // Many rooms' exchanges in one persistent launch.  Each room was prepared by
 // sp_energy_exchange with prepare_only (E_0, E_total, plan in its own
 // workspace); all rooms share D, B, T and the order count K.  The work items
-// of order k are every room's scatter items (segment, window, band) and then
-// every room's mix items (band, receiver); a block takes the next item from a
+// of order k are every room's scatter items (segment, window; all bands) and
+// then every room's mix items (receiver; all bands); a block takes the next item from a
 // ticket counter, waits until the item's inputs are complete (a scatter item
 // of room r and order k: all mix items of (r, k - 1); a mix item: all scatter
 // items of (r, k) and all mix items of (r, k - 1)), runs it and counts it
@@ -915,7 +937,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoo
                                                                   int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char s_dyn[];
     __shared__ long long s_item;
-    __shared__ int s_go;
+    __shared__ int s_go, s_room;
+    int room_hint = 0;  // thread 0: the last item's room (consecutive items mostly share it)
     for (;;) {
         if (threadIdx.x == 0) s_item = (long long)atomicAdd(ticket, 1ull);
         __syncthreads();
@@ -925,17 +948,25 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoo
         const long long rem = t % S.per_order;
         const bool scatter = rem < S.s_total;
         const long long pos = scatter ? rem : rem - S.s_total;
-        int lo = 0, hi = S.n_rooms - 1;  // the room whose part holds pos
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((scatter ? rooms[mid].s_off : rooms[mid].m_off) <= pos)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        const BatchRoom& R = rooms[lo];
-        const long long local = pos - (scatter ? R.s_off : R.m_off);
         if (threadIdx.x == 0) {
+            // the room whose part holds pos: the last one if it still does, else a binary search
+            const BatchRoom& H = rooms[room_hint];
+            const long long h0 = scatter ? H.s_off : H.m_off, hn = scatter ? H.n_scatter : H.n_mix;
+            int lo = room_hint;
+            if (pos < h0 || pos >= h0 + hn) {
+                lo = 0;
+                int hi = S.n_rooms - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if ((scatter ? rooms[mid].s_off : rooms[mid].m_off) <= pos)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+            }
+            room_hint = lo;
+            s_room = lo;
+            const BatchRoom& R = rooms[lo];
             bool ok = *(volatile int*)err == 0;
             const unsigned long long prev_mix = (unsigned long long)(k - 1) * (unsigned long long)R.n_mix;
             if (ok && S.force_timeout && t == 0) ok = batch_wait(&R.done[1], ~0ull, S.wait_limit, err);  // test hook
@@ -948,22 +979,28 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoo
             s_go = ok && *(volatile int*)err == 0;
         }
         __syncthreads();
+        const BatchRoom& R = rooms[s_room];
+        const long long local = pos - (scatter ? R.s_off : R.m_off);
         if (s_go) {
             float* eprev = (k & 1) ? R.buf0 : R.buf1;  // E_{k-1}
             if (scatter) {
+                // one (segment, window) item covers every band
                 asm volatile("fence.proxy.async.global;" ::: "memory");  // E_{k-1} was written by generic stores
-                const int per_seg = S.windows * S.nb;
-                scatter_ws<float, kB>(R.n_class, S.nb, S.nt, S.rs, S.lead, R.cap, R.tile_recv, R.seg_order, R.seg_off,
-                                      R.groups, R.wpack, R.coef, eprev, R.g, err, (int)(local / per_seg),
-                                      (int)((local % per_seg) / S.nb), (int)(local % S.nb));
+                for (int b = 0; b < S.nb; ++b) {
+                    if (b > 0) __syncthreads();  // the previous band's stages and barriers are free
+                    scatter_ws<float, kB>(R.n_class, S.nb, S.nt, S.rs, S.lead, R.cap, R.tile_recv, R.seg_order,
+                                          R.seg_off, R.groups, R.wpack, R.coef, eprev, R.g, err,
+                                          (int)(local / S.windows), (int)(local % S.windows), b);
+                }
             } else {
+                // one receiver item covers every band, the block's threads split over the bands
                 float* ecur = (k & 1) ? R.buf1 : R.buf0;
                 const bool first_of_pair = (k & 1) == 1;
                 float* et = (first_of_pair && k < S.K) ? nullptr : R.etot;
                 const float* ea = (R.etot && !first_of_pair) ? eprev : nullptr;
-                mix4_item<2>(R.n_class, S.nd, S.nb, S.nt, S.rs, S.lead, R.tile_of, R.tile_tab, R.cdiff, R.cspec, R.g,
-                          ecur, et, ea, R.comp_on ? R.comp : nullptr, S.t_late, k == S.K, (int)(local % S.nb),
-                          (int)(local / S.nb), s_dyn);
+                mix4_item<2, true>(R.n_class, S.nd, S.nb, S.nt, S.rs, S.lead, R.tile_of, R.tile_tab, R.cdiff, R.cspec,
+                             R.g, ecur, et, ea, R.comp_on ? R.comp : nullptr, S.t_late, k == S.K, 0, (int)local,
+                             s_dyn, S.nb);
             }
         }
         __syncthreads();
@@ -1028,8 +1065,8 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
         R.n_active = (int)info[1];
         R.comp_on = a->plain_total ? 0 : 1;
         R.cap = material ? 2 * a->n_dir_pairs : a->n_dir_pairs;
-        R.n_scatter = (long long)R.n_active * S.windows * S.nb;
-        R.n_mix = (long long)S.nb * R.n;
+        R.n_scatter = (long long)R.n_active * S.windows;  // (segment, window) items, all bands each
+        R.n_mix = (long long)R.n;                          // receiver items, all bands each
         if (R.n_scatter < 1) return SP_ERR_ARG;  // a room without pairs inside the histogram: solve it alone
         R.s_off = s_tot;
         R.m_off = m_tot;
@@ -1050,7 +1087,8 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
         R.cspec = (const float*)L.cspec;
         R.etot = (float*)a->etc_total;
         R.comp = L.comp;
-        const size_t msmem = (size_t)2 * n_class * sizeof(float) + (size_t)tile_tab_stride(n_class, S.nd) * sizeof(int);
+        const size_t msmem =
+            (size_t)2 * S.nb * n_class * sizeof(float) + (size_t)tile_tab_stride(n_class, S.nd) * sizeof(int);
         if (msmem > smem) smem = msmem;
     }
     S.s_total = s_tot;

@@ -313,7 +313,7 @@ class DirectionalRadiosityFast:
         self._bake = None   # device state of the last bake
         self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
         self._dirs_xyz = None         # rotated direction sets as arrays (set_wall_brdf)
-        # FP32 exchange: E_total's late bins (the last three quarters of the
+        # FP32 exchange: E_total's late bins (the second half of the
         # histogram) are summed over the orders with Kahan compensation
         self.compensated_total = True
         # general BRDF tables, FP32, 32 <= directions <= 64: the receiver-side
