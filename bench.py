@@ -34,7 +34,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 # the FP32 and FP64 solves each hold tens of GB of histograms and workspace;
 # growable segments let the second reuse what the first released
-os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "expandable_segments:True")
+if "PYTORCH_CUDA_ALLOC_CONF" not in os.environ:
+    os.environ.setdefault("PYTORCH_ALLOC_CONF", "expandable_segments:True")
 
 import numpy as np  # noqa: E402
 

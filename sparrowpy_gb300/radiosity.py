@@ -187,11 +187,22 @@ def _unique_rows(key):
     return first_h[order], rank[inv_h]
 
 
-def group_brdf_rows(diff, spec, target, scale):
+def _fold_unused(key, used):
+    """Rows of slots no wall uses take the first used slot's row, so that they form no group of their own."""
+    if used is None or not np.any(used) or np.all(used):
+        return key
+    key = key.copy()
+    key[~used] = key[np.argmax(used)]
+    return key
+
+
+def group_brdf_rows(diff, spec, target, scale, used=None):
     """Group slots whose normalised rows agree: BRDF = scale[slot, b] * (diff + spec [o == m]).
 
     Returns slot_group (S,), slot_scale (S, B), n_groups, class_diff /
     class_spec (G * n_in, B), class_target (G * n_in,) (-1 = no mirror term).
+    used: optional (S,) mask of the slots some wall uses; the others join
+    the first used slot's group.
     """
     diff, spec, target = np.asarray(diff, float), np.asarray(spec, float), np.asarray(target)
     S, Din, B = diff.shape
@@ -201,7 +212,7 @@ def group_brdf_rows(diff, spec, target, scale):
     ns = spec / scale[:, None, :]
     key = np.concatenate([np.round(nd.reshape(S, -1), 12), np.round(ns.reshape(S, -1), 12),
                           target.reshape(S, -1).astype(float)], axis=1)
-    first, inverse = _unique_rows(key)
+    first, inverse = _unique_rows(_fold_unused(key, used))
     G = first.size
     reps = first
     class_diff = nd[reps].reshape(G * Din, B)
@@ -212,7 +223,7 @@ def group_brdf_rows(diff, spec, target, scale):
                 class_target=class_target.astype(np.int32))
 
 
-def group_brdf_tables(brdf):
+def group_brdf_tables(brdf, used=None):
     """Group slots whose whole tables agree up to a per-slot, per-band scale: BRDF[slot] = scale[slot, b] T_g.
 
     brdf: (n_slots, n_in, n_out, n_bins), any values.  Returns slot_group
@@ -226,7 +237,7 @@ def group_brdf_tables(brdf):
     scale = np.max(np.abs(brdf), axis=(1, 2)) if brdf.size else np.zeros((S, B))
     scale = np.where(scale > 0, scale, 1.0)
     norm = brdf / scale[:, None, None, :]
-    first, inverse = _unique_rows(np.round(norm.reshape(S, -1), 12))
+    first, inverse = _unique_rows(_fold_unused(np.round(norm.reshape(S, -1), 12), used))
     G = first.size
     return dict(slot_group=inverse.astype(np.int32), slot_scale=scale, n_groups=int(G),
                 class_table=np.ascontiguousarray(norm[first].reshape(G * Din, Dout, B)))
@@ -492,6 +503,14 @@ class DirectionalRadiosityFast:
                 v.record_stream(main)
         return bs
 
+    def _used_slots(self, n_slots):
+        """(n_slots,) mask of the BRDF slots some wall refers to (tables replaced later stay in the list)."""
+        used = np.zeros(n_slots, dtype=bool)
+        if self._brdf_index is not None:
+            idx = np.asarray(self._brdf_index)
+            used[idx[(idx >= 0) & (idx < n_slots)]] = True
+        return used
+
     def _brdf_structure(self, bs):
         """Diffuse-plus-mirror structure of the current BRDF tables (None if absent), kept with them.
 
@@ -515,7 +534,8 @@ class DirectionalRadiosityFast:
         if int(n_irr.item()) > 0:
             st = None
         else:
-            st = group_brdf_rows(diff.cpu().numpy(), spec.cpu().numpy(), target.cpu().numpy(), scale.cpu().numpy())
+            st = group_brdf_rows(diff.cpu().numpy(), spec.cpu().numpy(), target.cpu().numpy(), scale.cpu().numpy(),
+                                 used=self._used_slots(S))
         bs["structure"] = st
         return st
 
@@ -723,7 +743,7 @@ class DirectionalRadiosityFast:
         if mode is None:
             # any other tables: per (group of proportional tables, incoming
             # direction) class, contracted with the full table rows
-            general = group_brdf_tables(plan["host"])
+            general = group_brdf_tables(plan["host"], used=self._used_slots(plan["n_slots"]))
             n_class = general["n_groups"] * plan["n_in"]
             # the contraction keeps a tile's table rows in shared memory (at most 200 KB) and a bin's
             # outgoing directions in registers (at most 64)
