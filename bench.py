@@ -41,11 +41,11 @@ import numpy as np  # noqa: E402
 
 METRIC = "ms/solve (bake+exchange) ~5.5k patches FP32 vs FP64 GPU; fwd+bwd ms; HBM GB/s"
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
-# DRAM bytes moved per algorithmic byte by one exchange order (scatter + mix,
-# averaged over a deferred and a pairing order), from a single-pass ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 1759-patch
-# canyon
-TRAFFIC_PER_ALGO_BYTE = 1.20
+# DRAM bytes moved per algorithmic byte by one exchange order (scatter, mix
+# and source add of the partial sums, which read and write no E_total), from
+# a single-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
+# of the 1759-patch canyon
+TRAFFIC_PER_ALGO_BYTE = 0.81
 
 
 def parse():
@@ -142,11 +142,13 @@ def nt_late(cfg):
 
 
 def algorithmic_bytes_per_order(n, d, b, t, pairs, n_slots, n_in, elem=4):
-    """Bytes one exchange order must move at least.
+    """Algorithmic bytes of one exchange order in the reference's order-by-order form.
 
     4 x N D B T histogram elements (read E_{k-1}, write E_k, read and write
     E_total) + 16 bytes per directed pair (F', delay, directions) + one read
-    of the BRDF tables (S Din D B, FP32).
+    of the BRDF tables (S Din D B, FP32).  The partial sums (the default)
+    need only the first two of the four histogram terms; the figure keeps the
+    reference form's count, so `roofline.traffic` falls below it.
     """
     return 4.0 * elem * n * d * b * t + 16.0 * pairs + 4.0 * n_slots * n_in * d * b
 
@@ -416,23 +418,28 @@ def run_gpu(args):
         del r2, mono
     e2e_ms = max_over_ranks(float(np.mean(e2e_times)) if e2e_times else None)
 
-    # the time the Kahan compensation of E_total's late bins costs: the same solve with plain FP32 sums
-    r.compensated_total = False
-    plain = []
-    for k in range(0 if args.no_kahan else 2):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        solve(r, cfg, as_coords)
-        e1.record(st)
-        e1.synchronize()
-        plain.append((e0.elapsed_time(e1), r.exchange_stats["order_ms"]))
-    r.compensated_total = True
-    kahan = None if not plain else {"ms_per_solve_plain_sums": float(np.mean([p[0] for p in plain])),
-             "ms_per_solve_compensated": ms_step,
-             "exchange_ms_plain_sums": float(np.mean([p[1] for p in plain])),
-             "exchange_ms_compensated": float(np.mean(order_ms)),
-             "late_bins_from": int(nt_late(cfg)),
-             "compensation_storage": "bfloat16 per late bin"}
+    # E_total as the last partial sum (the default, timed above) against the reference's order-by-order
+    # sums, with the late bins Kahan-compensated and with plain FP32 sums: time and receivers of each
+    monos = {"partial_sums": r.collect_energy_receiver_mono(as_coords(cfg["receivers"])).time}
+    forms = {}
+    for name, comp in ([] if args.no_kahan else [("order_sums_compensated", True), ("order_sums_plain", False)]):
+        r.partial_sums, r.compensated_total = False, comp
+        t = []
+        for k in range(2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            solve(r, cfg, as_coords)
+            e1.record(st)
+            e1.synchronize()
+            t.append((e0.elapsed_time(e1), r.exchange_stats["order_ms"]))
+        forms[name] = {"ms_per_solve": float(np.mean([p[0] for p in t])),
+                       "exchange_ms": float(np.mean([p[1] for p in t]))}
+        monos[name] = r.collect_energy_receiver_mono(as_coords(cfg["receivers"])).time
+    r.partial_sums, r.compensated_total = True, True
+    sum_forms = None if not forms else {
+        "default": "partial sums: S_k = E_0 + M(S_{k-1}), E_total = S_K",
+        "partial_sums": {"ms_per_solve": ms_step, "exchange_ms": float(np.mean(order_ms))},
+        **forms, "late_bins_from": int(nt_late(cfg)), "compensation_storage": "bfloat16 per late bin"}
 
     # roofline of one exchange order (scatter + mix launches of that order)
     stats = r.exchange_stats
@@ -462,11 +469,11 @@ def run_gpu(args):
             e1.synchronize()
             t64.append(e0.elapsed_time(e1))
         m64 = r64.collect_energy_receiver_mono(as_coords(cfg["receivers"])).time
-        m32 = r.collect_energy_receiver_mono(as_coords(cfg["receivers"])).time
-        err = float(np.linalg.norm(m32 - m64) / np.linalg.norm(m64))
+        rel = lambda m: float(np.linalg.norm(m - m64) / np.linalg.norm(m64))
         fp64 = {"ms_per_solve": float(np.mean(t64)), "fp64_over_fp32": float(np.mean(t64)) / ms_step,
                 "exchange_ms_per_order": r64.exchange_stats["order_ms"] / max(stats["orders"], 1),
-                "receiver_rel_l2_fp32_vs_fp64": err}
+                "receiver_rel_l2_fp32_vs_fp64": rel(monos["partial_sums"]),
+                "receiver_rel_l2_fp32_vs_fp64_by_sum_form": {k: rel(m) for k, m in monos.items()}}
         del r64, c64
         torch.cuda.empty_cache()
 
@@ -527,14 +534,14 @@ def run_gpu(args):
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": TRAFFIC_PER_ALGO_BYTE * bytes_order,
-                         "kernel": "one exchange order: k_scatter_f32 + k_mix launches", "peak_of": peak_kind,
+                         "kernel": "one exchange order: k_scatter_f32 + k_mix4 + k_add_e0_t launches", "peak_of": peak_kind,
                          "algorithmic_bytes": bytes_order, "ms_per_launch": ms_order,
                          "binding": "shared-memory bandwidth of k_scatter_f32 (roofline_smem); the order's HBM "
                                     "traffic is a byproduct"},
             "roofline_smem": smem,
             "cpu_baseline": cpu,
             "fp64_gpu": fp64,
-            "kahan": kahan,
+            "sum_forms": sum_forms,
             "fwd_bwd": fwd_bwd,
             "configs": configs,
             "general_brdf": general,

@@ -260,6 +260,12 @@ typedef struct sp_exchange_args {
     /* structured / slot-wise / material, FP32: 1 = place E_0 and E_total and build the plan in ws, run no order
        (the orders then run in sp_exchange_batch) */
     int prepare_only;
+    /* structured / slot-wise / general / material: 1 = E_total is computed as the last of the partial sums
+       S_0 = E_0, S_k = E_0 + M(S_{k-1}) (M: one order's exchange, linear, with the histogram's truncation),
+       S_K = E_0 + E_1 + ... + E_K; every order then writes S_k and updates no separate E_total (half the
+       order's memory traffic of the mix; no compensation terms).  Needs etc_total and excludes states_out,
+       state_in and prepare_only (SP_ERR_ARG).  0 = the reference's order: E_k per order, added to E_total */
+    int partial_sums;
 } sp_exchange_args;
 
 /* Replaces RadiosityFast.py:1073-1145 `_energy_exchange` and :1037-1070

@@ -60,7 +60,7 @@ class ExchangeArgs(ctypes.Structure):
         ("state_in", P), ("state_order", I), ("states_out", P), ("states_every", I), ("skip_total", I),
         ("mat_alpha", P), ("mat_scattering", P), ("mat_mirror", P), ("mat_gain", P),
         ("plan_tag", LL), ("scatter_ms", ctypes.POINTER(ctypes.c_float)), ("plain_total", I),
-        ("class_table", P), ("no_tensor_cores", I), ("prepare_only", I),
+        ("class_table", P), ("no_tensor_cores", I), ("prepare_only", I), ("partial_sums", I),
     ]
 
 

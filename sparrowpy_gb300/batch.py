@@ -143,6 +143,7 @@ class PreparedWave:
             etc = torch.empty((n, nd, nb, nt), dtype=torch.float32, device=dev)
             a = r._exchange_args(c, dt, nt, K, "auto", etc)
             a.prepare_only = 1
+            a.partial_sums = 0  # the batched launch updates E_total order by order
             a.plan_tag = next(_TAGS)
             n_class = 1 + nd if a.algorithm == nat.SP_EXCHANGE_SLOTWISE else a.n_groups * a.n_in_dirs
             wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, nt, a.n_dir_pairs,

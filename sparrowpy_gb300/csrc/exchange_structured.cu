@@ -224,7 +224,9 @@ __device__ __forceinline__ void kahan_add4(float4& s, float4& c, float4 x) {
 // One float4 of bins (index t) of one (band, receiver) row of the mix: the
 // class sums, E_k and the E_total update (see k_mix).  s_cd / s_cs: the
 // band's class weights; the row pointers are those of the (band, receiver).
-template <int kOG>
+// kTotal = false: no E_total update at all (et, ea and cj are not read),
+// a separate instantiation with far fewer live registers.
+template <int kOG, bool kTotal = true>
 __device__ __forceinline__ void mix4_bin(int t, int np, const int* cls, const int* inv_off, const int* inv,
                                          const float* s_cd, const float* s_cs, int nd, size_t cs4, size_t ers4,
                                          size_t cc4, int tl4, const float4* __restrict__ gj, float4* __restrict__ ek,
@@ -235,6 +237,17 @@ __device__ __forceinline__ void mix4_bin(int t, int np, const int* cls, const in
     for (int q = 0; q < np; ++q) {
         const int c = cls[q];
         if (s_cd[c] != 0.0f) d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);  // skip pure mirror classes
+    }
+    if constexpr (!kTotal) {
+        for (int o = 0; o < nd; ++o) {
+            float4 v = d;
+            for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
+                const int cl = inv[q];
+                v = fma4(s_cs[cl], __ldg(gj + cl * cs4 + t), v);
+            }
+            ek[o * ers4 + t] = v;
+        }
+        return;
     }
     const bool late = cj != nullptr && t >= tl4;
     for (int o0 = 0; o0 < nd; o0 += kOG) {
@@ -282,7 +295,7 @@ __device__ __forceinline__ void mix4_bin(int t, int np, const int* cls, const in
 // (any block size): the tile table and the bands' class weights in s_mix
 // (n_bands x 2 n_class floats, then the tile table row), then the threads
 // split evenly over the bands, each walking its band's bins (float4).
-template <int kOG = 8, bool kSplitBands = false>
+template <int kOG = 8, bool kSplitBands = false, bool kTotal = true>
 __device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                           const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                           const float* __restrict__ cdiff, const float* __restrict__ cspec,
@@ -323,9 +336,13 @@ __device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, l
     const float4* ea = eadd ? reinterpret_cast<const float4*>(eadd + ((size_t)j * nd * nb + b) * rs + lead) : nullptr;
     ushort4* cj = (comp && et) ? reinterpret_cast<ushort4*>(comp + ((size_t)j * nd * nb + b) * (nt - t_late)) : nullptr;
     for (int t = lt; t < nt4; t += per)
-        mix4_bin<kOG>(t, np, cls, inv_off, inv, s_cd, s_cs, nd, cs4, ers4, cc4, tl4, gj, ek, et, ea, cj, fold);
+        mix4_bin<kOG, kTotal>(t, np, cls, inv_off, inv, s_cd, s_cs, nd, cs4, ers4, cc4, tl4, gj, ek, et, ea, cj,
+                              fold);
 }
 
+// kTotal: with the E_total update (etot non-null); without it (the first
+// order of a pair, and every order of the partial sums) only E_k is written.
+template <bool kTotal>
 __global__ void __launch_bounds__(128, 4) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                               const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                               const float* __restrict__ cdiff, const float* __restrict__ cspec,
@@ -333,8 +350,8 @@ __global__ void __launch_bounds__(128, 4) k_mix4(int n_class, int nd, int nb, in
                                               float* __restrict__ etot, const float* __restrict__ eadd,
                                               uint16_t* __restrict__ comp, int t_late, int fold) {
     extern __shared__ __align__(16) unsigned char s_mix[];
-    mix4_item(n_class, nd, nb, nt, rs, lead, tile_of, tab, cdiff, cspec, g, ecur, etot, eadd, comp, t_late, fold,
-              blockIdx.x, blockIdx.y, s_mix);
+    mix4_item<8, false, kTotal>(n_class, nd, nb, nt, rs, lead, tile_of, tab, cdiff, cspec, g, ecur, etot, eadd,
+                                comp, t_late, fold, blockIdx.x, blockIdx.y, s_mix);
 }
 
 template <typename T>
@@ -353,6 +370,21 @@ __global__ void k_init_energy_t(int n, int nd, int nb, int nt, long long rs, int
     T v = (T)e0dir[e];
     if (etot) etot[(size_t)e * nt + dly] = v;
     eprev[(size_t)e * rs + lead + dly] = v;
+}
+
+// Partial sums (sp_exchange_args.partial_sums): S_k = E_0 + M(S_{k-1}).
+// After the mix has written M(S_{k-1}) into `dst` (rows of pitch rs, bin 0
+// at lead), add the source energies at the bins k_init_energy_t placed them
+// in (one bin per row; the delays were range-checked there).
+template <typename T>
+__global__ void k_add_e0_t(int n, int nd, int nb, int nt, long long rs, int lead, const double* __restrict__ e0dir,
+                           const double* __restrict__ d0, double c, double dt, T* __restrict__ dst) {
+    long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)n * nd * nb) return;
+    int i = (int)(e / ((long long)nd * nb));
+    long long dly = (long long)xdiv(xdiv(d0[i], c), dt);
+    if (dly < 0 || dly >= nt) return;
+    dst[(size_t)e * rs + lead + dly] += (T)e0dir[e];
 }
 
 template <typename T>
@@ -684,8 +716,11 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     const long long rs = (long long)L.R.rs;
     const int lead = L.R.lead;
     T* states = (T*)a->states_out;
+    // partial sums S_k = E_0 + M(S_{k-1}): E_total is S_K, no per-order E_total update
+    const bool partial = a->partial_sums != 0;
+    if (partial && (!etot || states || a->state_in || a->prepare_only)) return SP_ERR_ARG;
     // Kahan compensation of E_total's late bins (FP32, unless switched off)
-    uint16_t* comp = (sizeof(T) == 4 && etot && !a->plain_total) ? L.comp : nullptr;
+    uint16_t* comp = (sizeof(T) == 4 && etot && !a->plain_total && !partial) ? L.comp : nullptr;
     cudaMemsetAsync(L.err, 0, sizeof(int), st);
     if (comp) cudaMemsetAsync(comp, 0, L.rows * (size_t)(nt - L.t_late) * sizeof(uint16_t), st);
     // ecur: only the leads need zeros (every bin is written each order);
@@ -833,30 +868,49 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
         T* et_k = (first_of_pair && k < a->max_order) ? nullptr : etot;
         const T* ea_k = (etot && !first_of_pair) ? eprev : nullptr;
         const int fold = k == a->max_order;  // the last E_total update folds the compensation in
+        // the mix's destination rows: the padded ecur, or (partial sums, last order) E_total itself
+        T* ek_k = ecur;
+        long long rs_k = rs;
+        int lead_k = lead;
+        if (partial) {
+            et_k = nullptr;
+            ea_k = nullptr;
+            if (k == a->max_order) {
+                ek_k = etot;
+                rs_k = nt;
+                lead_k = 0;
+            }
+        }
         scatter_timer.stop(st);
         if (general && tensor_mix) {
             const size_t tsmem = tc_smem_bytes(n_class, nd);
             if (k == k0 + 1)
                 cudaFuncSetAttribute(k_mix_general_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
             k_mix_general_tc<<<mgrid, kTcThreads, tsmem, sp_counted(st)>>>(
-                n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab, (const float*)L.ctab, (const float*)L.g,
-                (float*)ecur, (float*)et_k, (const float*)ea_k, comp, L.t_late, fold, L.err);
+                n_class, nd, nb, nt, rs_k, lead_k, L.C.tile_of, L.tile_tab, (const float*)L.ctab, (const float*)L.g,
+                (float*)ek_k, (float*)et_k, (const float*)ea_k, comp, L.t_late, fold, L.err);
         } else if (general) {
             const size_t gsmem = mix_general_smem(n_class, nd, sizeof(T));
             if (k == k0 + 1)
                 cudaFuncSetAttribute(k_mix_general<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem);
-            k_mix_general<T><<<mgrid, 128, gsmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of,
-                                                                    L.tile_tab, (const T*)L.ctab, (const T*)L.g, ecur,
+            k_mix_general<T><<<mgrid, 128, gsmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs_k, lead_k, L.C.tile_of,
+                                                                    L.tile_tab, (const T*)L.ctab, (const T*)L.g, ek_k,
                                                                     et_k, ea_k, comp, L.t_late, fold);
         } else if (sizeof(T) == 4 && nt % 4 == 0)
-            k_mix4<<<mgrid, 128, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
-                                                          (const float*)L.cdiff, (const float*)L.cspec,
-                                                          (const float*)L.g, (float*)ecur, (float*)et_k,
-                                                          (const float*)ea_k, comp, L.t_late, fold);
+            (et_k ? k_mix4<true> : k_mix4<false>)<<<mgrid, 128, msmem, sp_counted(st)>>>(
+                n_class, nd, nb, nt, rs_k, lead_k, L.C.tile_of, L.tile_tab, (const float*)L.cdiff,
+                (const float*)L.cspec, (const float*)L.g, (float*)ek_k, (float*)et_k, (const float*)ea_k, comp,
+                L.t_late, fold);
         else
-            k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs, lead, L.C.tile_of, L.tile_tab,
-                                                            (const T*)L.cdiff, (const T*)L.cspec, (const T*)L.g, ecur,
-                                                            et_k, ea_k, comp, L.t_late, fold);
+            k_mix<T><<<mgrid, 256, msmem, sp_counted(st)>>>(n_class, nd, nb, nt, rs_k, lead_k, L.C.tile_of,
+                                                            L.tile_tab, (const T*)L.cdiff, (const T*)L.cspec,
+                                                            (const T*)L.g, ek_k, et_k, ea_k, comp, L.t_late, fold);
+        if (partial) {
+            const long long ne = (long long)n * nd * nb;
+            k_add_e0_t<T><<<sp_blocks(ne, 256), 256, 0, sp_counted(st)>>>(
+                n, nd, nb, nt, rs_k, lead_k, a->energy_0_dir, a->distance_0, a->speed_of_sound, a->time_resolution,
+                ek_k);
+        }
         if (states && (k - k0) % a->states_every == 0)
             copy_rows(states + (size_t)((k - k0) / a->states_every) * e, (size_t)nt, ecur + lead, L.R.rs, nt, L.rows,
                       st);

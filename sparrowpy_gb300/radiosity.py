@@ -324,8 +324,12 @@ class DirectionalRadiosityFast:
         self._bake = None   # device state of the last bake
         self.host_bytes_uploaded = 0  # host -> device bytes copied by this object
         self._dirs_xyz = None         # rotated direction sets as arrays (set_wall_brdf)
-        # FP32 exchange: E_total's late bins (the second half of the
-        # histogram) are summed over the orders with Kahan compensation
+        # E_total as the last partial sum S_K of S_k = E_0 + M(S_{k-1}) (the
+        # tiled exchanges): no per-order E_total update
+        self.partial_sums = True
+        # order-by-order E_total (partial_sums False, or exchange states
+        # saved), FP32: the late bins (the second half of the histogram) are
+        # summed over the orders with Kahan compensation
         self.compensated_total = True
         # general BRDF tables, FP32, 32 <= directions <= 64: the receiver-side
         # contraction on the tensor cores (False: on the CUDA cores)
@@ -860,6 +864,7 @@ class DirectionalRadiosityFast:
         a.etc_total = etc.data_ptr()
         a.plain_total = 0 if self.compensated_total else 1
         a.no_tensor_cores = 0 if self.tensor_cores else 1
+        a.partial_sums = 1 if (self.partial_sums and use_struct) else 0
         if use_struct:
             s = plan["structured"]
             a.slot_group = s["slot_group"].data_ptr()
@@ -890,6 +895,7 @@ class DirectionalRadiosityFast:
                 raise ValueError("saving exchange states needs the structured exchange")
             a.states_out = states.data_ptr()
             a.states_every = int(states_every)
+            a.partial_sums = 0  # the states are the per-order energies E_k
         stats = (ctypes.c_int64 * 4)()
         a.plan_stats = stats
         order_ms = ctypes.c_float(-1.0)
@@ -911,7 +917,7 @@ class DirectionalRadiosityFast:
         self.exchange_stats = dict(algorithm=names.get(a.algorithm, "dense"),
                                    source_groups=int(stats[0]), segments=int(stats[1]), pairs=int(stats[2]),
                                    tiles=int(stats[3]), order_ms=float(order_ms.value), orders=int(max_order),
-                                   scatter_ms=float(scatter_ms.value))
+                                   scatter_ms=float(scatter_ms.value), partial_sums=bool(a.partial_sums))
 
     def energy_balance(self):
         """FP64 per-band energy check of the last exchange (no counterpart in the reference).

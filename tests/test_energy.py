@@ -4,6 +4,8 @@
   late bins (the second half) are compensated.  Against the exact
   (FP64) sum of the very E_k the GPU computed, the compensated late bins
   must be closer than plain FP32 sums (and within 1e-7 rel L2).
+* Partial sums: E_total computed as the last of S_k = E_0 + M(S_{k-1})
+  against the order-by-order sums, all against the FP64 solve.
 * Energy check (DirectionalRadiosityFast.energy_balance): per band, the
   FP64 totals of the histograms against the time-free energy budget of the
   orders.  In a closed room whose histogram outlasts the orders nothing is
@@ -51,6 +53,32 @@ def test_kahan_late_bins_beat_plain_sums():
     print(f"late-bin rel L2 against the exact sum: compensated {out[True]:.2e}, plain {out[False]:.2e}")
     assert out[True] < out[False]
     assert out[True] < 1e-7
+
+
+def test_partial_sums_match_order_sums():
+    """E_total as the last partial sum against the order-by-order sums (compensated and plain), all against
+    the FP64 solve: the same sum, so FP64 agrees to 1e-12 and FP32 stays as close to FP64 as the
+    compensated order-by-order sum (within a factor 2, and below 1e-6)."""
+    from sparrowpy_gb300.coords import Coordinates
+    c, dt, dur, K = 343.0, 1e-3, 1.0, 50
+    res = {}
+    for precision, partial, comp in (("fp64", True, True), ("fp64", False, True), ("fp32", True, True),
+                                     ("fp32", False, True), ("fp32", False, False)):
+        r = _room(precision)
+        r.partial_sums, r.compensated_total = partial, comp
+        r.bake_geometry()
+        r.init_source_energy(Coordinates(*SRC))
+        r.calculate_energy_exchange(c, dt, dur, K)
+        assert r.exchange_stats["partial_sums"] == partial
+        res[(precision, partial, comp)] = r._dev["etc"].double().cpu().numpy()
+    ref = res[("fp64", False, True)]
+    err = lambda x: float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+    assert err(res[("fp64", True, True)]) < 1e-12
+    e_part, e_comp, e_plain = (err(res[k]) for k in (("fp32", True, True), ("fp32", False, True),
+                                                      ("fp32", False, False)))
+    print(f"E_total rel L2 against FP64: partial sums {e_part:.2e}, order sums compensated {e_comp:.2e}, "
+          f"plain {e_plain:.2e}")
+    assert e_part < 1e-6 and e_part < 2 * e_comp
 
 
 @pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("fp64", 1e-12)])

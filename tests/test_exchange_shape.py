@@ -10,9 +10,10 @@ tests put exactly those code paths against the oracle
 
 * a per-patch-material shoebox solved end to end with histograms of 2200 and
   2500 bins, delays up to 43 and 215 bins, 50 and 49 orders (the pairing
-  order of the benchmark, and an unpaired last order): receiver histograms,
-  E_total, and the bins past 2048 (third window) within rel L2 1e-4 (FP32)
-  and 1e-10 (FP64);
+  order of the benchmark, and an unpaired last order), with E_total as the
+  last partial sum (S_k = E_0 + M(S_{k-1})) and order by order: receiver
+  histograms, E_total, and the bins past 2048 (third window) within rel L2
+  1e-4 (FP32) and 1e-10 (FP64);
 * the 5939-patch street canyon itself, two orders: 16 sampled destination
   rows of E_1 and E_2 recomputed by the oracle from the GPU's own previous
   state and pair data (p2o, incoming BRDF row, F', delays), within rel L2
@@ -34,12 +35,14 @@ def _room(precision):
                           air_attenuation=[0.0012, 0.0031], precision=precision)
 
 
+@pytest.mark.parametrize("partial_sums", [True, False])
 @pytest.mark.parametrize("dt,duration,k", [(5e-4, 1.1, 50), (1e-4, 0.25, 49)])
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_long_histograms_match_oracle(precision, dt, duration, k):
+def test_long_histograms_match_oracle(precision, dt, duration, k, partial_sums):
     from oracle.scene import scene_from_radiosity
     from sparrowpy_gb300.coords import Coordinates
     r = _room(precision)
+    r.partial_sums = partial_sums
     src, rcv = np.array([2.0, 2.0, 1.5]), np.array([[3.0, 4.0, 1.5], [4.1, 1.2, 2.3]])
     c = 343.0
     r.bake_geometry()
@@ -47,7 +50,7 @@ def test_long_histograms_match_oracle(precision, dt, duration, k):
     r.calculate_energy_exchange(c, dt, duration, k)
     st = r.exchange_stats
     nt = int(duration / dt)
-    assert st["algorithm"] == "structured" and nt >= 2048
+    assert st["algorithm"] == "structured" and nt >= 2048 and st["partial_sums"] == partial_sums
     assert st["tiles"] > 1 and st["segments"] > st["tiles"]
     delays = (r._bake["dist"].cpu().numpy()[: r._bake["n_dir"]] / c / dt).astype(np.int64)
     assert delays.max() >= (200 if dt < 2e-4 else 40)  # up to 4.7 times the 45-bin group spread
