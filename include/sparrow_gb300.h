@@ -263,8 +263,9 @@ typedef struct sp_exchange_args {
     /* structured / slot-wise / general / material: 1 = E_total is computed as the last of the partial sums
        S_0 = E_0, S_k = E_0 + M(S_{k-1}) (M: one order's exchange, linear, with the histogram's truncation),
        S_K = E_0 + E_1 + ... + E_K; every order then writes S_k and updates no separate E_total (half the
-       order's memory traffic of the mix; no compensation terms).  Needs etc_total and excludes states_out,
-       state_in and prepare_only (SP_ERR_ARG).  0 = the reference's order: E_k per order, added to E_total */
+       order's memory traffic of the mix; no compensation terms).  Needs etc_total and excludes states_out
+       and state_in (SP_ERR_ARG); with prepare_only, sp_exchange_batch runs the partial sums.  0 = the
+       reference's order: E_k per order, added to E_total */
     int partial_sums;
 } sp_exchange_args;
 
@@ -319,7 +320,7 @@ int sp_energy_budget(const sp_exchange_args* a, double* totals, void* ws, size_t
  * sp_exchange_args (FP32, structured / slot-wise / material, at least one
  * pair inside the histogram) already prepared by sp_energy_exchange with
  * prepare_only = 1 in its own workspace; all rooms share n_dirs, n_bins,
- * n_samples (a multiple of 4) and max_order.  Blocks take work items (a
+ * n_samples (a multiple of 4), max_order and partial_sums.  Blocks take work items (a
  * room's scatter or mix piece of one order) from a device ticket counter and
  * wait, bounded by wait_limit polls (0: 2^24), for the pieces they depend on;
  * a wait that gives up makes the call return SP_ERR_TIMEOUT (the device stays

@@ -60,12 +60,15 @@ def build_room(room, precision="fp32"):
 
 
 def solve_rooms(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, etc_duration=1.0, max_reflection_order=30,
-                precision="fp32"):
-    """Solve every room; returns (list of mono histograms (R, B, T) numpy, per-room device ms, patches)."""
+                precision="fp32", partial_sums=True):
+    """Solve every room; returns (list of mono histograms (R, B, T) numpy, per-room device ms, patches).
+
+    partial_sums: E_total as the last partial sum (DirectionalRadiosityFast.partial_sums)."""
     out, ms, patches = [], [], []
     st = torch.cuda.current_stream()
     for room in rooms:
         r = build_room(room, precision)
+        r.partial_sums = partial_sums
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         r.bake_geometry()
@@ -131,19 +134,19 @@ def _room_bytes(n, nd, nb, nt, pairs, n_class):
 class PreparedWave:
     """Rooms baked and prepared for one persistent batched exchange (all co-resident on the device)."""
 
-    def __init__(self, rooms, c, dt, nt, K):
+    def __init__(self, rooms, c, dt, nt, K, partial_sums=True):
         dev = torch.device("cuda", torch.cuda.current_device())
         self.c, self.dt, self.nt, self.K = c, dt, nt, K
         self.objs, self.args, self.wss, self.etcs = [], [], [], []
         for room in rooms:
             r = build_room(room, "fp32")
+            r.partial_sums = partial_sums
             r.bake_geometry()
             r.init_source_energy(Coordinates(*room["source"]))
             n, nd, nb = r._dev["e0dir"].shape
             etc = torch.empty((n, nd, nb, nt), dtype=torch.float32, device=dev)
             a = r._exchange_args(c, dt, nt, K, "auto", etc)
             a.prepare_only = 1
-            a.partial_sums = 0  # the batched launch updates E_total order by order
             a.plan_tag = next(_TAGS)
             n_class = 1 + nd if a.algorithm == nat.SP_EXCHANGE_SLOTWISE else a.n_groups * a.n_in_dirs
             wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, nt, a.n_dir_pairs,
@@ -196,14 +199,15 @@ class PreparedWave:
 
 
 def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, etc_duration=1.0,
-                        max_reflection_order=30, memory_fraction=0.6, tuner=None, force_choice=None):
+                        max_reflection_order=30, memory_fraction=0.6, tuner=None, force_choice=None,
+                        partial_sums=True):
     """Solve every room, the exchange orders of each memory-sized wave in one persistent launch.
 
     Returns (list of mono histograms (R, B, T) numpy in room order, stats):
     stats holds per wave the rooms, their patch counts, the device ms of
     bake + prepare, of the batched exchange launch and of exchange +
     collection, the work items and the tile choice; plus the tuner's
-    timings.  FP32.
+    timings.  FP32; partial_sums as in solve_rooms.
     """
     tuner = tuner or _TUNER
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -234,7 +238,7 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
         sub = [rooms[idx] for idx in wave]
         e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         e[0].record(st)
-        pw = PreparedWave(sub, c, dt, nt, K)
+        pw = PreparedWave(sub, c, dt, nt, K, partial_sums)
         e[1].record(st)
 
         def probe(cand, k):

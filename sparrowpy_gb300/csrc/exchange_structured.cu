@@ -718,7 +718,7 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
     T* states = (T*)a->states_out;
     // partial sums S_k = E_0 + M(S_{k-1}): E_total is S_K, no per-order E_total update
     const bool partial = a->partial_sums != 0;
-    if (partial && (!etot || states || a->state_in || a->prepare_only)) return SP_ERR_ARG;
+    if (partial && (!etot || states || a->state_in)) return SP_ERR_ARG;
     // Kahan compensation of E_total's late bins (FP32, unless switched off)
     uint16_t* comp = (sizeof(T) == 4 && etot && !a->plain_total && !partial) ? L.comp : nullptr;
     cudaMemsetAsync(L.err, 0, sizeof(int), st);
@@ -938,12 +938,17 @@ int run_tiled(const sp_exchange_args* a, void* ws, size_t ws_bytes, cudaStream_t
 // ticket counter, waits until the item's inputs are complete (a scatter item
 // of room r and order k: all mix items of (r, k - 1); a mix item: all scatter
 // items of (r, k) and all mix items of (r, k - 1)), runs it and counts it
-// done.  Tickets are taken in item order, so every item a block waits for
+// done.  With partial sums (every room's partial_sums) a mix item writes
+// S_k = M(S_{k-1}) + E_0 (the last order straight into E_total) instead of
+// E_k and an E_total update.  Tickets are taken in item order, so every item a block waits for
 // was taken earlier by a running block: the launch always progresses.  Waits
 // are bounded; a wait that gives up sets the error flag, after which blocks
 // only count the remaining items.
 struct BatchRoom {
     int n, n_class, n_active, comp_on;
+    double c, dt;          // speed of sound, bin width (the source delays of the partial sums)
+    const double* e0dir;   // (N, D, B) source energies
+    const double* d0;      // (N) source distances
     long long cap, n_scatter, n_mix;  // scatter / mix items per order
     long long s_off, m_off;           // offsets of the room's items in an order's scatter / mix part
     const int32_t* tile_recv;
@@ -985,7 +990,7 @@ __device__ __forceinline__ bool batch_wait(const unsigned long long* ctr, unsign
     }
 }
 
-template <int kB>
+template <int kB, bool kPartial>
 __global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoom* __restrict__ rooms, BatchShape S,
                                                                   unsigned long long* __restrict__ ticket,
                                                                   int* __restrict__ err) {
@@ -1046,6 +1051,22 @@ __global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoo
                                           R.seg_off, R.groups, R.wpack, R.coef, eprev, R.g, err,
                                           (int)(local / S.windows), (int)(local % S.windows), b);
                 }
+            } else if constexpr (kPartial) {
+                // S_k of one receiver, every band: the mix, then E_0 at the source delay of each row
+                const bool last = k == S.K;
+                float* dst = last ? R.etot : ((k & 1) ? R.buf1 : R.buf0);
+                const long long rs = last ? (long long)S.nt : S.rs;
+                const int lead = last ? 0 : S.lead;
+                mix4_item<8, true, false>(R.n_class, S.nd, S.nb, S.nt, rs, lead, R.tile_of, R.tile_tab, R.cdiff,
+                                          R.cspec, R.g, dst, nullptr, nullptr, nullptr, S.t_late, 0, 0, (int)local,
+                                          s_dyn, S.nb);
+                __syncthreads();  // the rows are written before the source energies are added to them
+                const long long dly = (long long)xdiv(xdiv(R.d0[local], R.c), R.dt);
+                if (dly >= 0 && dly < S.nt)
+                    for (int q = threadIdx.x; q < S.nd * S.nb; q += blockDim.x) {
+                        const size_t e = (size_t)local * S.nd * S.nb + q;
+                        dst[e * rs + lead + dly] += (float)R.e0dir[e];
+                    }
             } else {
                 // one receiver item covers every band, the block's threads split over the bands
                 float* ecur = (k & 1) ? R.buf1 : R.buf0;
@@ -1118,6 +1139,11 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
         R.n_class = n_class;
         R.n_active = (int)info[1];
         R.comp_on = a->plain_total ? 0 : 1;
+        R.c = a->speed_of_sound;
+        R.dt = a->time_resolution;
+        R.e0dir = a->energy_0_dir;
+        R.d0 = a->distance_0;
+        if ((a->partial_sums != 0) != (a0->partial_sums != 0)) return SP_ERR_ARG;  // one form for the launch
         R.cap = material ? 2 * a->n_dir_pairs : a->n_dir_pairs;
         R.n_scatter = (long long)R.n_active * S.windows;  // (segment, window) items, all bands each
         R.n_mix = (long long)R.n;                          // receiver items, all bands each
@@ -1165,13 +1191,11 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
     const int per_sm = b->ctas_per_sm > 0 ? b->ctas_per_sm : 1;
     SpEventTimer timer(b->exchange_ms != nullptr, st);
-    if (b->window_bins == 1024) {
-        cudaFuncSetAttribute(k_batch_exchange<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_batch_exchange<32><<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
-    } else {
-        cudaFuncSetAttribute(k_batch_exchange<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_batch_exchange<16><<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
-    }
+    const bool partial = a0->partial_sums != 0;
+    auto kern = b->window_bins == 1024 ? (partial ? k_batch_exchange<32, true> : k_batch_exchange<32, false>)
+                                       : (partial ? k_batch_exchange<16, true> : k_batch_exchange<16, false>);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
     timer.stop(st);
     int rc = sp_check_launch();
     if (rc != SP_OK) return rc;

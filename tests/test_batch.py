@@ -29,15 +29,18 @@ def _rooms(n=3, seed=11):
     return shoebox_rooms(n, seed=seed, patch_size=0.5, dims_range=(1.5, 3.0), n_dirs=8, n_bins=2, n_receivers=2)
 
 
-def test_persistent_batch_matches_rooms_one_by_one():
-    """All orders of three rooms in one persistent launch, for every tile choice the tuner can pick: the same
-    receiver histograms as the rooms solved one after another (rel L2 <= 1e-6), and the oracle's (1e-4)."""
+@pytest.mark.parametrize("partial_sums", [True, False])
+def test_persistent_batch_matches_rooms_one_by_one(partial_sums):
+    """All orders of three rooms in one persistent launch, for every tile choice the tuner can pick, with E_total
+    as the last partial sum and order by order: the same receiver histograms as the rooms solved one after
+    another in the same form (rel L2 <= 1e-6), and the oracle's (1e-4)."""
     from oracle.scene import scene_from_radiosity
     from sparrowpy_gb300.batch import BatchTuner, build_room, solve_rooms, solve_rooms_batched
     rooms = _rooms()
-    ref, _, _ = solve_rooms(rooms, etc_duration=0.06, max_reflection_order=6)
+    ref, _, _ = solve_rooms(rooms, etc_duration=0.06, max_reflection_order=6, partial_sums=partial_sums)
     for choice in BatchTuner.CANDIDATES:
-        got, stats = solve_rooms_batched(rooms, etc_duration=0.06, max_reflection_order=6, force_choice=choice)
+        got, stats = solve_rooms_batched(rooms, etc_duration=0.06, max_reflection_order=6, force_choice=choice,
+                                         partial_sums=partial_sums)
         assert stats["waves"][0]["rooms"] == 3
         for a, b in zip(got, ref):
             assert rel_l2(a, b) < 1e-6, choice
