@@ -162,8 +162,13 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
 
 /* Universal patch-to-patch form factor for each listed pair (i = source).
  * Replaces universal.py:12-52 `patch2patch_ff_universal` (+ :54-96,
- * integration.py:38-114 Stokes, :116-289 Nusselt).  Quadrilateral patches.
- * precision SP_F64: FP64 throughout.  SP_F32: Stokes re-centred on the patch
+ * integration.py:38-114 Stokes, :116-289 Nusselt).  pts (n_patches, nv, 3):
+ * convex planar polygons of nv vertices, 3 <= nv <= 8.  nv != 4: FP64
+ * throughout whatever the precision (the Nusselt surface samples of a
+ * triangle follow integration.py:533-605's triangle branch; other polygons
+ * are sampled as the parallelogram of their first and last sides, as there);
+ * method gets 1 or 2 and ws is not used.
+ * nv == 4, precision SP_F64: FP64 throughout.  SP_F32: Stokes re-centred on the patch
  * centres, the second-order terms from FP64 moments and the remainder sum in
  * FP32; FP64 for vertex-sharing pairs (Nusselt), near pairs and pairs whose
  * FP32 error indicator exceeds 5e-6 of the sum.  ff (n_pairs) FP64; method
@@ -172,26 +177,27 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
  * bytes) and synchronises `stream` once; SP_F64, or SP_F32 with method ==
  * NULL, computes FP64 throughout and uses no ws. */
 size_t sp_form_factors_workspace(int n_patches, long long n_pairs);
-int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
+int sp_form_factors(int precision, int n_patches, int nv, long long n_pairs, const int32_t* pairs, const double* pts,
                     const double* normals, const double* areas, double* ff, uint8_t* method, void* ws,
                     size_t ws_bytes, void* stream);
 
 /* Source -> patch energy and directional initial energy.
  * Replaces universal.py:98-147 `_source2patch_energy_universal` and
- * RadiosityFast.py:988-1034 `_add_directional`.  src (3); vis (n) from
- * sp_point_visibility; brdf (n_slots, n_in, n_out, nb); outputs e0 (n, nb),
- * d0 (n), e0dir (n, n_out, nb). */
-int sp_source_energy(const double* src, int n, const double* centers, const double* pts, const uint8_t* vis, int nb,
-                     const double* att, const int32_t* wall_of, const int32_t* brdf_index, int n_in,
+ * RadiosityFast.py:988-1034 `_add_directional`.  src (3); pts (n, nv, 3),
+ * 3 <= nv <= 8; vis (n) from sp_point_visibility; brdf (n_slots, n_in,
+ * n_out, nb); outputs e0 (n, nb), d0 (n), e0dir (n, n_out, nb). */
+int sp_source_energy(const double* src, int n, const double* centers, const double* pts, int nv, const uint8_t* vis,
+                     int nb, const double* att, const int32_t* wall_of, const int32_t* brdf_index, int n_in,
                      const double* dirs_in, int n_out, const double* brdf, double* e0, double* d0, double* e0dir,
                      void* stream);
 
 /* Patch -> receiver factors: point factor (universal.py:149-160), outgoing
  * direction toward the receiver (RadiosityFast.py:728-730) and distance
- * (:712, :745).  rcv (3) -> rfac (n), ridx (n), dist (n). */
-int sp_receiver_factors(const double* rcv, int n, const double* centers, const double* pts, const uint8_t* vis,
-                        const int32_t* wall_of, int n_out, const double* dirs_out, double* rfac, int32_t* ridx,
-                        double* dist, void* stream);
+ * (:712, :745).  rcv (3), pts (n, nv, 3) with 3 <= nv <= 8 -> rfac (n),
+ * ridx (n), dist (n). */
+int sp_receiver_factors(const double* rcv, int n, const double* centers, const double* pts, int nv,
+                        const uint8_t* vis, const int32_t* wall_of, int n_out, const double* dirs_out, double* rfac,
+                        int32_t* ridx, double* dist, void* stream);
 
 /* ---------------------------------------------------------- energy exchange */
 

@@ -25,6 +25,7 @@
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
+constexpr int kMaxPoly = 8;  // patch polygon vertices the form factors accept
 
 inline double dot3(const double* a, const double* b) {
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
@@ -199,37 +200,38 @@ inline double newton_cotes_4th(const double* x, const double* y) {
     return 2 * h / 45 * (7 * y[0] + 32 * y[1] + 12 * y[2] + 32 * y[3] + 7 * y[4]);
 }
 
-// integration.py:38-114 `stokes_integration` with load_stokes_entries :12-36.
-double stokes_integration(const double* pi, const double* pj, double area_i) {
-    double ib[16 * 3], jb[16 * 3];
-    sample_boundary(pi, 4, 5, ib);
-    sample_boundary(pj, 4, 5, jb);
-    double form[16][16];
-    for (int a = 0; a < 16; ++a)
-        for (int b = 0; b < 16; ++b) {
-            double d[3] = {ib[3 * a] - jb[3 * b], ib[3 * a + 1] - jb[3 * b + 1],
-                           ib[3 * a + 2] - jb[3 * b + 2]};
-            form[a][b] = std::log(norm3(d));
+// integration.py:38-114 `stokes_integration` with load_stokes_entries :12-36,
+// for convex polygons of nvi and nvj vertices (4 nv boundary points each,
+// nv segments of 5 points).
+double stokes_integration(const double* pi, int nvi, const double* pj, int nvj, double area_i) {
+    const int na = 4 * nvi, nb = 4 * nvj;
+    std::vector<double> ib((size_t)na * 3), jb((size_t)nb * 3);
+    sample_boundary(pi, nvi, 5, ib.data());
+    sample_boundary(pj, nvj, 5, jb.data());
+    std::vector<double> form((size_t)na * nb);
+    for (int a = 0; a < na; ++a)
+        for (int b = 0; b < nb; ++b) {
+            double d[3] = {ib[3 * a] - jb[3 * b], ib[3 * a + 1] - jb[3 * b + 1], ib[3 * a + 2] - jb[3 * b + 2]};
+            form[(size_t)a * nb + b] = std::log(norm3(d));
         }
     double outer = 0.0;
-    double inner[16][3];
-    std::memset(inner, 0, sizeof(inner));
+    std::vector<double> inner((size_t)na * 3, 0.0);
     for (int dim = 0; dim < 3; ++dim) {
-        for (int a = 0; a < 16; ++a) {
-            for (int s = 0; s < 4; ++s) {
+        for (int a = 0; a < na; ++a) {
+            for (int s = 0; s < nvj; ++s) {
                 double xj[5], sub[5];
-                for (int k = 0; k < 5; ++k) xj[k] = jb[3 * ((4 * s + k) % 16) + dim];
+                for (int k = 0; k < 5; ++k) xj[k] = jb[3 * ((4 * s + k) % nb) + dim];
                 if (std::fabs(xj[4] - xj[0]) > 1e-3) {
-                    for (int k = 0; k < 5; ++k) sub[k] = form[a][(4 * s + k) % 16];
-                    inner[a][dim] += newton_cotes_4th(xj, sub);
+                    for (int k = 0; k < 5; ++k) sub[k] = form[(size_t)a * nb + (4 * s + k) % nb];
+                    inner[3 * a + dim] += newton_cotes_4th(xj, sub);
                 }
             }
         }
-        for (int s = 0; s < 4; ++s) {
+        for (int s = 0; s < nvi; ++s) {
             double xi[5], sub[5];
-            for (int k = 0; k < 5; ++k) xi[k] = ib[3 * ((4 * s + k) % 16) + dim];
+            for (int k = 0; k < 5; ++k) xi[k] = ib[3 * ((4 * s + k) % na) + dim];
             if (std::fabs(xi[4] - xi[0]) > 1e-3) {
-                for (int k = 0; k < 5; ++k) sub[k] = inner[(4 * s + k) % 16][dim];
+                for (int k = 0; k < 5; ++k) sub[k] = inner[3 * ((4 * s + k) % na) + dim];
                 outer += newton_cotes_4th(xi, sub);
             }
         }
@@ -300,37 +302,39 @@ double area_under_curve(const double ps[3][2]) {
 
 inline double sign(double v) { return (v > 0) ? 1.0 : ((v < 0) ? -1.0 : 0.0); }
 
-// integration.py:116-230 `nusselt_analog` for a quadrilateral receiver.
-double nusselt_analog(const double* origin, const double* surf_normal, const double* pp,
+// integration.py:116-230 `nusselt_analog` for a receiver polygon of nvp
+// vertices (2 nvp boundary points, nvp segments of 3).
+double nusselt_analog(const double* origin, const double* surf_normal, const double* pp, int nvp,
                       const double* patch_normal) {
-    double bp[8 * 3];
-    sample_boundary(pp, 4, 3, bp);
+    const int nbp = 2 * nvp;
+    double bp[2 * kMaxPoly * 3];
+    sample_boundary(pp, nvp, 3, bp);
     double e1[3] = {pp[3] - pp[0], pp[4] - pp[1], pp[5] - pp[2]};
     double e2[3] = {pp[6] - pp[3], pp[7] - pp[4], pp[8] - pp[5]};
     double cr[3];
     cross3(e1, e2, cr);
     double hand = sign(dot3(cr, patch_normal));
-    double sph[8][3], pln[8][2], proj[8][3];
-    for (int ii = 0; ii < 8; ++ii) {
+    double sph[2 * kMaxPoly][3], pln[2 * kMaxPoly][2], proj[2 * kMaxPoly][3];
+    for (int ii = 0; ii < nbp; ++ii) {
         double d[3] = {bp[3 * ii] - origin[0], bp[3 * ii + 1] - origin[1], bp[3 * ii + 2] - origin[2]};
         double nd = norm3(d);
         for (int k = 0; k < 3; ++k) sph[ii][k] = d[k] / nd;
     }
     double rot[9];
     rotation_matrix(surf_normal, rot);
-    for (int ii = 0; ii < 8; ++ii) {
+    for (int ii = 0; ii < nbp; ++ii) {
         rot_xy(rot, sph[ii], pln[ii]);
         proj[ii][0] = pln[ii][0];
         proj[ii][1] = pln[ii][1];
         proj[ii][2] = 0.0;
     }
-    double corners[4][3];
-    for (int c = 0; c < 4; ++c)
+    double corners[kMaxPoly][3];
+    for (int c = 0; c < nvp; ++c)
         for (int k = 0; k < 3; ++k) corners[c][k] = proj[2 * c][k];
-    double big_poly = polygon_area(&corners[0][0], 4, 3);
+    double big_poly = polygon_area(&corners[0][0], nvp, 3);
     double curved = 0.0;
-    for (int jj = 0; jj < 4; ++jj) {
-        int s0 = (2 * jj) % 8, s1 = (2 * jj + 1) % 8, s2 = (2 * jj + 2) % 8;
+    for (int jj = 0; jj < nvp; ++jj) {
+        int s0 = (2 * jj) % nbp, s1 = (2 * jj + 1) % nbp, s2 = (2 * jj + 2) % nbp;
         double cr2[3];
         cross3(proj[s2], proj[s0], cr2);
         if (norm3(cr2) > 1e-6) {
@@ -371,23 +375,29 @@ double nusselt_analog(const double* origin, const double* surf_normal, const dou
 // Python's round() on a float64: round half to even.
 inline long round_half_even(double v) { return (long)std::nearbyint(v); }
 
-// integration.py:533-605 `_surf_sample_regulargrid` for a quadrilateral.
-int surf_sample_regulargrid(const double* el, int npoints, std::vector<double>& out) {
+// integration.py:533-605 `_surf_sample_regulargrid`: a parallelogram
+// spanned by el[1] - el[0] and el[nv - 1] - el[0], or (nv == 3) the
+// triangle half of it, whose columns shorten along the first edge and whose
+// points beyond the hypotenuse (s + t > 1 - thres) are left out.
+int surf_sample_regulargrid(const double* el, int nv, int npoints, std::vector<double>& out) {
+    const double* last = el + 3 * (nv - 1);
     double u[3] = {el[3] - el[0], el[4] - el[1], el[5] - el[2]};
-    double v[3] = {el[9] - el[0], el[10] - el[1], el[11] - el[2]};
+    double v[3] = {last[0] - el[0], last[1] - el[1], last[2] - el[2]};
+    const bool tri = nv == 3;
+    const double a = tri ? 2.0 : 1.0;
     double nu = norm3(u), nvv = norm3(v);
-    long npx = round_half_even(nu / nvv * std::sqrt(1.0 * npoints));
-    long npz = round_half_even(nvv / nu * std::sqrt(1.0 * npoints));
+    long npx = round_half_even(nu / nvv * std::sqrt(a * npoints));
+    long npz = round_half_even(nvv / nu * std::sqrt(a * npoints));
     if (npz == 0) npz = 1;
     if (npx == 0) npx = 1;
     std::vector<double> tt(npx), tz(npz);
     // numpy.linspace(0, stop, num): k*step, last element exactly stop.
+    double sstep = 1.0 / (npx * 2), sstepz = 1.0 / (npz * 2);
     {
         double stop = 1 - 1.0 / npx;
         double step = (npx > 1) ? (stop - 0.0) / (npx - 1) : 0.0;
         for (long k = 0; k < npx; ++k) tt[k] = k * step + 0.0;
         if (npx > 1) tt[npx - 1] = stop;
-        double sstep = 1.0 / (npx * 2);
         for (long k = 0; k < npx; ++k) tt[k] += sstep;
     }
     {
@@ -395,43 +405,51 @@ int surf_sample_regulargrid(const double* el, int npoints, std::vector<double>& 
         double step = (npz > 1) ? (stop - 0.0) / (npz - 1) : 0.0;
         for (long k = 0; k < npz; ++k) tz[k] = k * step + 0.0;
         if (npz > 1) tz[npz - 1] = stop;
-        double sstep = 1.0 / (npz * 2);
-        for (long k = 0; k < npz; ++k) tz[k] += sstep;
+        for (long k = 0; k < npz; ++k) tz[k] += sstepz;
     }
+    const double thres = std::sqrt(sstepz * sstepz + sstep * sstep) / 2;
     out.clear();
-    for (long i = 0; i < npx; ++i)
-        for (long k = 0; k < npz; ++k)
+    for (long i = 0; i < npx; ++i) {
+        const long jj = tri ? i : 0;
+        // tz[0 : len(tz) - round(npz / npx * jj)] (never a negative stop for these sizes)
+        long stop = npz - round_half_even((double)npz / (double)npx * (double)jj);
+        if (stop < 0) stop = std::max(0L, npz + stop);
+        for (long k = 0; k < stop; ++k) {
+            const bool inside = tt[i] + tz[k] <= 1 - thres;
+            if (tri && !inside) continue;
             for (int d = 0; d < 3; ++d) out.push_back(tt[i] * u[d] + tz[k] * v[d] + el[d]);
-    return (int)(npx * npz);
+        }
+    }
+    return (int)(out.size() / 3);
 }
 
 // integration.py:232-289 `nusselt_integration` (regular grid, nsamples).
-double nusselt_integration(const double* pi, const double* pj, const double* ni, const double* nj,
+double nusselt_integration(const double* pi, int nvi, const double* pj, int nvj, const double* ni, const double* nj,
                            int nsamples) {
     std::vector<double> p0;
-    int n = surf_sample_regulargrid(pi, nsamples, p0);
+    int n = surf_sample_regulargrid(pi, nvi, nsamples, p0);
     double out = 0.0;
-    for (int i = 0; i < n; ++i) out += nusselt_analog(&p0[3 * i], ni, pj, nj);
+    for (int i = 0; i < n; ++i) out += nusselt_analog(&p0[3 * i], ni, pj, nvj, nj);
     out *= 1 / (kPi * n);
     return out;
 }
 
 // geometry.py:719-748 `_coincidence_check`.
-bool coincidence_check(const double* p0, const double* p1, int nv) {
-    for (int i = 0; i < nv; ++i)
-        for (int j = 0; j < nv; ++j) {
+bool coincidence_check(const double* p0, int nv0, const double* p1, int nv1) {
+    for (int i = 0; i < nv0; ++i)
+        for (int j = 0; j < nv1; ++j) {
             double d[3] = {p0[3 * i] - p1[3 * j], p0[3 * i + 1] - p1[3 * j + 1], p0[3 * i + 2] - p1[3 * j + 2]};
             if (norm3(d) < 1e-6) return true;
         }
     return false;
 }
 
-// universal.py:54-96 `universal_form_factor`.
+// universal.py:54-96 `universal_form_factor` (patches of nv vertices each).
 double universal_form_factor(const double* src_pts, const double* src_n, double src_area,
-                             const double* rcv_pts, const double* rcv_n) {
-    if (coincidence_check(rcv_pts, src_pts, 4))
-        return nusselt_integration(src_pts, rcv_pts, src_n, rcv_n, 64);
-    return stokes_integration(src_pts, rcv_pts, src_area);
+                             const double* rcv_pts, const double* rcv_n, int nv) {
+    if (coincidence_check(rcv_pts, nv, src_pts, nv))
+        return nusselt_integration(src_pts, nv, rcv_pts, nv, src_n, rcv_n, 64);
+    return stokes_integration(src_pts, nv, rcv_pts, nv, src_area);
 }
 
 // geometry.py:688-715 `_sphere_tangent_vector`.
@@ -538,28 +556,32 @@ int orc_point_visibility(const double* point, int n, const double* centers, int 
     return 0;
 }
 
-// universal.py:12-52 `patch2patch_ff_universal`: one value per listed pair.
-int orc_form_factors(int n_pairs, const int32_t* pairs, const double* points, const double* normals,
+// universal.py:12-52 `patch2patch_ff_universal`: one value per listed pair
+// (all patches with nv vertices, as the reference's arrays have).
+int orc_form_factors(int n_pairs, const int32_t* pairs, const double* points, int nv, const double* normals,
                      const double* areas, double* out) {
+    if (nv < 3 || nv > kMaxPoly) return -1;
 #pragma omp parallel for schedule(dynamic, 64)
     for (int p = 0; p < n_pairs; ++p) {
         int i = pairs[2 * p], j = pairs[2 * p + 1];
-        out[p] = universal_form_factor(points + 12 * (size_t)i, normals + 3 * i, areas[i],
-                                       points + 12 * (size_t)j, normals + 3 * j);
+        out[p] = universal_form_factor(points + 3 * (size_t)nv * i, normals + 3 * i, areas[i],
+                                       points + 3 * (size_t)nv * j, normals + 3 * j, nv);
     }
     return 0;
 }
 
-double orc_stokes(const double* pi, const double* pj, double area_i) {
-    return stokes_integration(pi, pj, area_i);
+double orc_stokes(const double* pi, int nvi, const double* pj, int nvj, double area_i) {
+    return stokes_integration(pi, nvi, pj, nvj, area_i);
 }
-double orc_nusselt(const double* pi, const double* pj, const double* ni, const double* nj, int ns) {
-    return nusselt_integration(pi, pj, ni, nj, ns);
+double orc_nusselt(const double* pi, int nvi, const double* pj, int nvj, const double* ni, const double* nj, int ns) {
+    return nusselt_integration(pi, nvi, pj, nvj, ni, nj, ns);
 }
 double orc_pt_solution(const double* point, const double* patch, int nv, int mode) {
     return pt_solution(point, patch, nv, mode);
 }
-int orc_coincident(const double* p0, const double* p1) { return coincidence_check(p0, p1, 4) ? 1 : 0; }
+int orc_coincident(const double* p0, int nv0, const double* p1, int nv1) {
+    return coincidence_check(p0, nv0, p1, nv1) ? 1 : 0;
+}
 
 // Per directed pair (i -> j): nearest direction index among `dirs[wall[i]]`
 // toward unit(c_to - c_from).  Covers RadiosityFast.py:402-414 (outgoing map,

@@ -7,7 +7,7 @@ the smoke check and the CPU-baseline leg of the benchmark, as the checker;
 the product (sparrowpy_gb300) never imports it.
 
 A scene is a dict of numpy arrays:
-  patches_points (N, 4, 3), patch_to_wall_ids (N,), walls_points (W, 4, 3),
+  patches_points (N, nv, 3) with 3 <= nv <= 8, patch_to_wall_ids (N,), walls_points (W, nw, 3),
   walls_normal (W, 3), dirs_in (W, Din, 3), dirs_out (W, Dout, 3),
   brdf (S, Din, Dout, B) (already times pi), brdf_index (W,),
   air_attenuation (B,) or None.
@@ -98,16 +98,22 @@ def form_factors(points, normals, area, pairs):
     pairs = _c(pairs, np.int32)
     out = np.zeros(pairs.shape[0])
     points, normals, area = _c(points, float), _c(normals, float), _c(area, float)
-    lib().orc_form_factors(pairs.shape[0], _p(pairs), _p(points), _p(normals), _p(area), _p(out))
+    rc = lib().orc_form_factors(pairs.shape[0], _p(pairs), _p(points), points.shape[1], _p(normals), _p(area),
+                                _p(out))
+    if rc != 0:
+        raise ValueError("patches need 3 to 8 vertices")
     return out
 
 
 def stokes(pi, pj, area_i):
-    return lib().orc_stokes(_p(_c(pi, float)), _p(_c(pj, float)), ctypes.c_double(area_i))
+    pi, pj = _c(pi, float), _c(pj, float)
+    return lib().orc_stokes(_p(pi), pi.shape[0], _p(pj), pj.shape[0], ctypes.c_double(area_i))
 
 
 def nusselt(pi, pj, ni, nj, nsamples=64):
-    return lib().orc_nusselt(_p(_c(pi, float)), _p(_c(pj, float)), _p(_c(ni, float)), _p(_c(nj, float)), nsamples)
+    pi, pj = _c(pi, float), _c(pj, float)
+    return lib().orc_nusselt(_p(pi), pi.shape[0], _p(pj), pj.shape[0], _p(_c(ni, float)), _p(_c(nj, float)),
+                             nsamples)
 
 
 def pt_solution(point, patch, mode="source"):

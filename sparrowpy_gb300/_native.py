@@ -113,11 +113,11 @@ _SIGS = {
     "sp_pair_setup": (I, [LL, I, P, P, P, P, P, P, P, I, P, I, P, P, P, P, P, P, P]),
     "sp_outgoing_index_map": (I, [LL, I, P, P, P, ctypes.c_int64, P, P]),
     "sp_form_factors_workspace": (SZ, [I, LL]),
-    "sp_form_factors": (I, [I, I, LL, P, P, P, P, P, P, P, SZ, P]),
+    "sp_form_factors": (I, [I, I, I, LL, P, P, P, P, P, P, P, SZ, P]),
     "sp_dense_form_factors": (I, [LL, I, P, P, P, P]),
     "sp_form_factors_tilde": (I, [LL, I, I, I, I, P, P, P, P, P, P, P, P, P, P, P]),
-    "sp_source_energy": (I, [P, I, P, P, P, I, P, P, P, I, P, I, P, P, P, P, P]),
-    "sp_receiver_factors": (I, [P, I, P, P, P, P, I, P, P, P, P, P]),
+    "sp_source_energy": (I, [P, I, P, P, I, P, I, P, P, P, I, P, I, P, P, P, P, P]),
+    "sp_receiver_factors": (I, [P, I, P, P, I, P, P, I, P, P, P, P, P]),
     "sp_energy_exchange_workspace": (SZ, [I, I, I, I, I, I, LL, I, I, I]),
     "sp_energy_exchange": (I, [ctypes.POINTER(ExchangeArgs), P, SZ, P]),
     "sp_energy_totals_workspace": (SZ, [I]),

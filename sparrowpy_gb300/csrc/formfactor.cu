@@ -376,6 +376,238 @@ __global__ void __launch_bounds__(256) k_form_factors(long long n_pairs, const i
 }
 
 // ---------------------------------------------------------------------------
+// Patches of nv != 4 vertices (3 <= nv <= kMaxPolyVerts): the same universal
+// form factor, FP64, one warp per pair, written for any convex polygon.
+constexpr int kMaxPolyVerts = 8;
+
+// Boundary sample point a of a polygon of nv vertices, n_div points per side
+// (integration.py:639-649 with npoints = n_div + 1): side a / n_div,
+// position a % n_div.
+__device__ __forceinline__ void boundary_point_n(const double* el, int nv, int n_div, int a, double* out) {
+    const int s = a / n_div, k = a % n_div;
+    const double* p = el + 3 * s;
+    const double* q = el + 3 * ((s + 1) % nv);
+    for (int d = 0; d < 3; ++d) out[d] = p[d] + (k * (q[d] - p[d])) / n_div;
+}
+
+// Boole weight vector of boundary point a (0 .. 4 nv - 1); see boole_weight.
+__device__ void boole_weight_n(const double* el, int nv, int a, double* w) {
+    const int s = a >> 2, k = a & 3, nb = 4 * nv;
+    for (int d = 0; d < 3; ++d) w[d] = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+        int seg, pos;
+        if (pass == 0) {
+            seg = s;
+            pos = k;
+        } else {
+            if (k != 0) break;
+            seg = (s + nv - 1) % nv;
+            pos = 4;
+        }
+        double x0[3], x1[3], x4[3];
+        boundary_point_n(el, nv, 4, 4 * seg, x0);
+        boundary_point_n(el, nv, 4, 4 * seg + 1, x1);
+        boundary_point_n(el, nv, 4, (4 * seg + 4) % nb, x4);
+        for (int d = 0; d < 3; ++d) {
+            if (fabs(x4[d] - x0[d]) > 1e-3) {
+                double h = x1[d] - x0[d];
+                w[d] += 2 * h / 45 * boole_coef(pos);
+            }
+        }
+    }
+}
+
+// integration.py:38-114 `stokes_integration` for polygons of nvi and nvj
+// vertices (4 nv <= 32 sample points each), one warp, FP64 logarithms: lane
+// l owns point l of both boundaries, patch j's points reach every lane by
+// shuffles.  Returns the same value on all lanes.
+__device__ double stokes_pair_n(const double* pi, int nvi, const double* pj, int nvj, double area_i) {
+    const int lane = threadIdx.x & 31;
+    const int na = 4 * nvi, nb = 4 * nvj;
+    double P[3] = {0, 0, 0}, u[3] = {0, 0, 0}, Q[3] = {0, 0, 0}, v[3] = {0, 0, 0};
+    if (lane < na) {
+        boundary_point_n(pi, nvi, 4, lane, P);
+        boole_weight_n(pi, nvi, lane, u);
+    }
+    if (lane < nb) {
+        boundary_point_n(pj, nvj, 4, lane, Q);
+        boole_weight_n(pj, nvj, lane, v);
+    }
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        double Qb[3], vb[3];
+        for (int d = 0; d < 3; ++d) {
+            Qb[d] = __shfl_sync(0xffffffffu, Q[d], b);
+            vb[d] = __shfl_sync(0xffffffffu, v[d], b);
+        }
+        if (lane < na) {
+            double dd[3] = {P[0] - Qb[0], P[1] - Qb[1], P[2] - Qb[2]};
+            double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+            s += (u[0] * vb[0] + u[1] * vb[1] + u[2] * vb[2]) * log(r);
+        }
+    }
+    s = warp_sum(s);
+    return fabs(s / (2 * SP_PI * area_i));
+}
+
+// integration.py:116-230 `nusselt_analog` for a receiver polygon of nvp
+// vertices (2 nvp boundary points, nvp sides of 3 points).
+__device__ double nusselt_analog_n(const double* origin, const double* rot, const double* pp, int nvp, double hand) {
+    const int nbp = 2 * nvp;
+    double sph[2 * kMaxPolyVerts][3], pln[2 * kMaxPolyVerts][2];
+    for (int ii = 0; ii < nbp; ++ii) {
+        double bp[3], d[3];
+        boundary_point_n(pp, nvp, 2, ii, bp);
+        for (int dd = 0; dd < 3; ++dd) d[dd] = bp[dd] - origin[dd];
+        double nd = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int dd = 0; dd < 3; ++dd) sph[ii][dd] = d[dd] / nd;
+        pln[ii][0] = rot[0] * sph[ii][0] + rot[1] * sph[ii][1] + rot[2] * sph[ii][2];
+        pln[ii][1] = rot[3] * sph[ii][0] + rot[4] * sph[ii][1] + rot[5] * sph[ii][2];
+    }
+    // geometry.py:420-440 `_polygon_area` of the nvp projected corners (z = 0)
+    double big = 0.0;
+    for (int t = 0; t < nvp - 2; ++t) {
+        double a0 = pln[2 * (t + 1)][0] - pln[0][0], a1 = pln[2 * (t + 1)][1] - pln[0][1];
+        double b0 = pln[2 * (t + 2)][0] - pln[0][0], b1 = pln[2 * (t + 2)][1] - pln[0][1];
+        big += 0.5 * fabs(a0 * b1 - a1 * b0);
+    }
+    double curved = 0.0;
+    for (int jj = 0; jj < nvp; ++jj) {
+        int s0 = 2 * jj, s1 = 2 * jj + 1, s2 = (2 * jj + 2) % nbp;
+        double crz = pln[s2][0] * pln[s0][1] - pln[s2][1] * pln[s0][0];
+        if (fabs(crz) > 1e-6) {
+            if (pln[s2][0] * pln[s0][0] + pln[s2][1] * pln[s0][1] >= 1e-6) {
+                double seg[3][2] = {{pln[s0][0], pln[s0][1]}, {pln[s1][0], pln[s1][1]}, {pln[s2][0], pln[s2][1]}};
+                curved += area_under_curve(seg);
+            } else {
+                double mp[3], marc[3], a[3], b[3];
+                for (int k = 0; k < 3; ++k) mp[k] = sph[s0][k] + (sph[s2][k] - sph[s0][k]) / 2;
+                double nm = sqrt(mp[0] * mp[0] + mp[1] * mp[1] + mp[2] * mp[2]);
+                for (int k = 0; k < 3; ++k) marc[k] = mp[k] / nm;
+                for (int k = 0; k < 3; ++k) a[k] = sph[s0][k] + (marc[k] - sph[s0][k]) / 2;
+                for (int k = 0; k < 3; ++k) b[k] = marc[k] + (sph[s2][k] - marc[k]) / 2;
+                double na = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+                double nb = sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+                for (int k = 0; k < 3; ++k) {
+                    a[k] /= na;
+                    b[k] /= nb;
+                }
+                double mp2[2] = {rot[0] * mp[0] + rot[1] * mp[1] + rot[2] * mp[2],
+                                 rot[3] * mp[0] + rot[4] * mp[1] + rot[5] * mp[2]};
+                double marc2[2] = {rot[0] * marc[0] + rot[1] * marc[1] + rot[2] * marc[2],
+                                   rot[3] * marc[0] + rot[4] * marc[1] + rot[5] * marc[2]};
+                double a2[2] = {rot[0] * a[0] + rot[1] * a[1] + rot[2] * a[2],
+                                rot[3] * a[0] + rot[4] * a[1] + rot[5] * a[2]};
+                double b2[2] = {rot[0] * b[0] + rot[1] * b[1] + rot[2] * b[2],
+                                rot[3] * b[0] + rot[4] * b[1] + rot[5] * b[2]};
+                double d1[2] = {pln[s2][0] - pln[s0][0], pln[s2][1] - pln[s0][1]};
+                double d2[2] = {mp2[0] - marc2[0], mp2[1] - marc2[1]};
+                double lin = sqrt(d1[0] * d1[0] + d1[1] * d1[1]) * sqrt(d2[0] * d2[0] + d2[1] * d2[1]) / 2;
+                double left_seg[3][2] = {{pln[s0][0], pln[s0][1]}, {a2[0], a2[1]}, {marc2[0], marc2[1]}};
+                double right_seg[3][2] = {{marc2[0], marc2[1]}, {b2[0], b2[1]}, {pln[s2][0], pln[s2][1]}};
+                double left = area_under_curve(left_seg);
+                double right = area_under_curve(right_seg);
+                curved += (lin * dsign(left) + left + right);
+            }
+        }
+    }
+    return big + hand * curved;
+}
+
+// integration.py:232-289 `nusselt_integration` with the regular grid of
+// integration.py:533-605 (64 requested samples): the parallelogram spanned
+// by el[1] - el[0] and el[nv - 1] - el[0], or for a triangle (twice the
+// requested density) the columns shortened along the first side and the
+// points past the hypotenuse (s + t > 1 - thres) left out.  One warp.
+__device__ double nusselt_pair_n(const double* pi, int nvi, const double* pj, int nvj, const double* ni,
+                                 const double* nj) {
+    const int lane = threadIdx.x & 31;
+    const double* last = pi + 3 * (nvi - 1);
+    double u[3] = {pi[3] - pi[0], pi[4] - pi[1], pi[5] - pi[2]};
+    double v[3] = {last[0] - pi[0], last[1] - pi[1], last[2] - pi[2]};
+    const bool tri = nvi == 3;
+    const double dens = tri ? 2.0 * 64.0 : 64.0;
+    double nu = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    double nvv = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    long npx = (long)rint(nu / nvv * sqrt(dens));
+    long npz = (long)rint(nvv / nu * sqrt(dens));
+    if (npz == 0) npz = 1;
+    if (npx == 0) npx = 1;
+    const double sstep = 1.0 / (npx * 2), sstepz = 1.0 / (npz * 2);
+    const double thres = sqrt(sstepz * sstepz + sstep * sstep) / 2;
+    double e1[3] = {pj[3] - pj[0], pj[4] - pj[1], pj[5] - pj[2]};
+    double e2[3] = {pj[6] - pj[3], pj[7] - pj[4], pj[8] - pj[5]};
+    double cr[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    double hand = dsign(cr[0] * nj[0] + cr[1] * nj[1] + cr[2] * nj[2]);
+    double rot[9];
+    rotation_matrix_ff(ni, rot);
+    const long total = npx * npz;
+    double s = 0.0;
+    int cnt = 0;
+    for (long idx = lane; idx < total; idx += 32) {
+        long ix = idx / npz, iz = idx % npz;
+        // tz[0 : npz - round(npz / npx * ix)] for a triangle (a stop below 0 counts from the end)
+        long stop = tri ? npz - (long)rint((double)npz / (double)npx * (double)ix) : npz;
+        if (stop < 0) stop = npz + stop > 0 ? npz + stop : 0;
+        if (iz >= stop) continue;
+        double stopx = 1 - 1.0 / npx, stopz = 1 - 1.0 / npz;
+        double tx = (npx > 1) ? ((ix == npx - 1) ? stopx : ix * (stopx / (npx - 1))) : 0.0;
+        double tz = (npz > 1) ? ((iz == npz - 1) ? stopz : iz * (stopz / (npz - 1))) : 0.0;
+        tx += sstep;
+        tz += sstepz;
+        if (tri && !(tx + tz <= 1 - thres)) continue;
+        double o[3];
+        for (int d = 0; d < 3; ++d) o[d] = tx * u[d] + tz * v[d] + pi[d];
+        s += nusselt_analog_n(o, rot, pj, nvj, hand);
+        ++cnt;
+    }
+    s = warp_sum(s);
+    cnt = warp_sum(cnt);
+    return s * (1 / (SP_PI * cnt));
+}
+
+__device__ __forceinline__ bool coincident_n(const double* p0, int nv0, const double* p1, int nv1) {
+    for (int i = 0; i < nv0; ++i)
+        for (int j = 0; j < nv1; ++j) {
+            double d[3] = {p0[3 * i] - p1[3 * j], p0[3 * i + 1] - p1[3 * j + 1], p0[3 * i + 2] - p1[3 * j + 2]};
+            if (sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) < 1e-6) return true;
+        }
+    return false;
+}
+
+// universal.py:54-96 for patches of nv vertices, one warp per pair.
+__global__ void __launch_bounds__(256) k_form_factors_poly(long long n_pairs, int nv, const int32_t* __restrict__ pairs,
+                                                           const double* __restrict__ pts,
+                                                           const double* __restrict__ normals,
+                                                           const double* __restrict__ areas, double* __restrict__ ff,
+                                                           uint8_t* __restrict__ method) {
+    long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= n_pairs) return;
+    int lane = threadIdx.x & 31;
+    int i = pairs[2 * q], j = pairs[2 * q + 1];
+    double pi[3 * kMaxPolyVerts], pj[3 * kMaxPolyVerts];
+    for (int k = 0; k < 3 * nv; ++k) {
+        pi[k] = pts[(size_t)i * 3 * nv + k];
+        pj[k] = pts[(size_t)j * 3 * nv + k];
+    }
+    double result;
+    int m;
+    if (coincident_n(pj, nv, pi, nv)) {
+        double ni[3] = {normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]};
+        double nj[3] = {normals[3 * j], normals[3 * j + 1], normals[3 * j + 2]};
+        result = nusselt_pair_n(pi, nv, pj, nv, ni, nj);
+        m = kNusselt;
+    } else {
+        result = stokes_pair_n(pi, nv, pj, nv, areas[i]);
+        m = kStokes64;
+    }
+    if (lane == 0) {
+        ff[q] = result;
+        if (method) method[q] = (uint8_t)m;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // FP32 Stokes in three passes (the FP64 pipe carries only per-patch sums and
 // one short base term per pair):
 //   k_ff_patch_data: per patch, the 16 boundary points relative to the centre
@@ -695,7 +927,7 @@ namespace {
 // universal.py:98-147 `_source2patch_energy_universal` fused with
 // RadiosityFast.py:988-1034 `_add_directional`.
 __global__ void k_source_energy(const double* __restrict__ src, int n, const double* __restrict__ centers,
-                                const double* __restrict__ pts, const uint8_t* __restrict__ vis, int nb,
+                                const double* __restrict__ pts, int nv, const uint8_t* __restrict__ vis, int nb,
                                 const double* __restrict__ att, const int32_t* __restrict__ wall_of,
                                 const int32_t* __restrict__ brdf_index, int n_in, const double* __restrict__ dirs_in,
                                 int n_out, const double* __restrict__ brdf, double* __restrict__ e0,
@@ -709,7 +941,7 @@ __global__ void k_source_energy(const double* __restrict__ src, int n, const dou
     if (v) {
         double dv[3] = {xsub(s[0], c[0]), xsub(s[1], c[1]), xsub(s[2], c[2])};
         dist = xnorm3(dv);
-        g = sp_pt_solution(s, pts + (size_t)j * 12, 4, 0);
+        g = sp_pt_solution(s, pts + (size_t)j * 3 * nv, nv, 0);
     }
     d0[j] = dist;
     int w = wall_of[j];
@@ -729,14 +961,14 @@ __global__ void k_source_energy(const double* __restrict__ src, int n, const dou
 // (get_scattering_data_receiver_index with pos_j = receiver) and the
 // patch-receiver distance (:712, :745).
 __global__ void k_receiver_factors(const double* __restrict__ rcv, int n, const double* __restrict__ centers,
-                                   const double* __restrict__ pts, const uint8_t* __restrict__ vis,
+                                   const double* __restrict__ pts, int nv, const uint8_t* __restrict__ vis,
                                    const int32_t* __restrict__ wall_of, int n_out, const double* __restrict__ dirs_out,
                                    double* __restrict__ rfac, int32_t* __restrict__ ridx, double* __restrict__ dist) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     double r[3] = {rcv[0], rcv[1], rcv[2]};
     double c[3] = {centers[3 * k], centers[3 * k + 1], centers[3 * k + 2]};
-    rfac[k] = vis[k] ? sp_pt_solution(r, pts + (size_t)k * 12, 4, 1) : 0.0;
+    rfac[k] = vis[k] ? sp_pt_solution(r, pts + (size_t)k * 3 * nv, nv, 1) : 0.0;
     ridx[k] = sp_nearest_dir(c, r, dirs_out + (size_t)wall_of[k] * n_out * 3, n_out);
     double dv[3] = {xsub(c[0], r[0]), xsub(c[1], r[1]), xsub(c[2], r[2])};
     dist[k] = xnorm3(dv);
@@ -746,28 +978,27 @@ __global__ void k_receiver_factors(const double* __restrict__ rcv, int n, const 
 
 extern "C" {
 
-int sp_source_energy(const double* src, int n, const double* centers, const double* pts, const uint8_t* vis, int nb,
-                     const double* att, const int32_t* wall_of, const int32_t* brdf_index, int n_in,
+int sp_source_energy(const double* src, int n, const double* centers, const double* pts, int nv, const uint8_t* vis,
+                     int nb, const double* att, const int32_t* wall_of, const int32_t* brdf_index, int n_in,
                      const double* dirs_in, int n_out, const double* brdf, double* e0, double* d0, double* e0dir,
                      void* stream) {
-    if (n < 0 || nb < 1 || n_in < 1 || n_out < 1) return SP_ERR_ARG;
+    if (n < 0 || nb < 1 || n_in < 1 || n_out < 1 || nv < 3 || nv > kMaxPolyVerts) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
     if (!src || !centers || !pts || !vis || !att || !wall_of || !brdf_index || !dirs_in || !brdf || !e0 || !d0 || !e0dir)
         return SP_ERR_ARG;
-    k_source_energy<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(src, n, centers, pts, vis, nb, att, wall_of,
-                                                                         brdf_index, n_in, dirs_in, n_out, brdf, e0, d0,
-                                                                         e0dir);
+    k_source_energy<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        src, n, centers, pts, nv, vis, nb, att, wall_of, brdf_index, n_in, dirs_in, n_out, brdf, e0, d0, e0dir);
     return sp_check_launch();
 }
 
-int sp_receiver_factors(const double* rcv, int n, const double* centers, const double* pts, const uint8_t* vis,
-                        const int32_t* wall_of, int n_out, const double* dirs_out, double* rfac, int32_t* ridx,
-                        double* dist, void* stream) {
-    if (n < 0 || n_out < 1) return SP_ERR_ARG;
+int sp_receiver_factors(const double* rcv, int n, const double* centers, const double* pts, int nv,
+                        const uint8_t* vis, const int32_t* wall_of, int n_out, const double* dirs_out, double* rfac,
+                        int32_t* ridx, double* dist, void* stream) {
+    if (n < 0 || n_out < 1 || nv < 3 || nv > kMaxPolyVerts) return SP_ERR_ARG;
     if (n == 0) return SP_OK;
     if (!rcv || !centers || !pts || !vis || !wall_of || !dirs_out || !rfac || !ridx || !dist) return SP_ERR_ARG;
-    k_receiver_factors<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(rcv, n, centers, pts, vis, wall_of, n_out,
-                                                                            dirs_out, rfac, ridx, dist);
+    k_receiver_factors<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        rcv, n, centers, pts, nv, vis, wall_of, n_out, dirs_out, rfac, ridx, dist);
     return sp_check_launch();
 }
 
@@ -777,13 +1008,19 @@ size_t sp_form_factors_workspace(int n_patches, long long n_pairs) {
            sp_align((size_t)n_pairs * sizeof(float2)) + 256;
 }
 
-int sp_form_factors(int precision, int n_patches, long long n_pairs, const int32_t* pairs, const double* pts,
+int sp_form_factors(int precision, int n_patches, int nv, long long n_pairs, const int32_t* pairs, const double* pts,
                     const double* normals, const double* areas, double* ff, uint8_t* method, void* ws,
                     size_t ws_bytes, void* stream) {
     if (n_pairs < 0 || n_patches < 0 || (precision != SP_F32 && precision != SP_F64)) return SP_ERR_ARG;
+    if (nv < 3 || nv > kMaxPolyVerts) return SP_ERR_ARG;
     if (n_pairs == 0) return SP_OK;
     if (!pairs || !pts || !normals || !areas || !ff) return SP_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    if (nv != 4) {  // polygons other than quadrilaterals: FP64, one warp per pair
+        k_form_factors_poly<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, nv, pairs, pts,
+                                                                                      normals, areas, ff, method);
+        return sp_check_launch();
+    }
     if (precision == SP_F64 || !method) {
         long long threads = n_pairs * 32;
         k_form_factors<<<sp_blocks(threads, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, pts, normals, areas, ff,

@@ -174,18 +174,57 @@ def create_patches_general(polygon_points, max_size):
     return out
 
 
+def create_patches_triangles(polygon_points, max_size):
+    """Triangular patches of a planar convex polygon wall of 3 or more vertices (no counterpart in the reference).
+
+    The wall is cut into the fan (p0, p_k, p_k+1), k = 1 .. nv - 2; each
+    triangle (a, b, c) into n x n similar triangles, n = max(1, int(longest
+    side / max_size)), with corners a + (i/n)(b - a) + (j/n)(c - a).  Every
+    patch keeps the wall's vertex order, so its normal is the wall's.  The
+    form factors, visibility and point factors take triangles as the
+    reference's universal method defines them (universal.py:12-96,
+    integration.py:533-605 with its triangle branch).
+    """
+    p = np.asarray(polygon_points, dtype=float)
+    if p.ndim != 2 or p.shape[0] < 3 or p.shape[1] != 3:
+        raise ValueError("a wall needs at least 3 vertices")
+    out = []
+    for k in range(1, p.shape[0] - 1):
+        a, b, c = p[0], p[k], p[k + 1]
+        longest = max(np.sqrt(np.sum((b - a) ** 2)), np.sqrt(np.sum((c - b) ** 2)), np.sqrt(np.sum((a - c) ** 2)))
+        n = max(1, int(longest / max_size + 1e-6))
+
+        def at(i, j):
+            return a + (i / n) * (b - a) + (j / n) * (c - a)
+
+        for i in range(n):
+            for j in range(n - i):
+                out.append((at(i, j), at(i + 1, j), at(i, j + 1)))
+                if i + j < n - 1:
+                    out.append((at(i + 1, j), at(i + 1, j + 1), at(i, j + 1)))
+    return np.array(out, dtype=float).reshape(-1, 3, 3)
+
+
 def process_patches(walls_points, walls_normal, patch_size):
     """sparrowpy/geometry.py:290-339 `_process_patches`.
 
-    Axis-aligned walls are patched as the reference does, with its
-    arithmetic; any other wall (where the reference fails) by
-    create_patches_general.  Returns patches_points (n, 4, 3), patches_normal
-    (n, 3), n_patches and patch_to_wall_ids (n,).
+    Quadrilateral walls: axis-aligned ones are patched as the reference
+    does, with its arithmetic; any other (where the reference fails) by
+    create_patches_general; the patches are quadrilaterals.  Walls of any
+    other vertex count (all walls share one, as the arrays demand):
+    triangular patches (create_patches_triangles).  Returns patches_points
+    (n, 4 or 3, 3), patches_normal (n, 3), n_patches and patch_to_wall_ids
+    (n,).
     """
     walls_points = np.asarray(walls_points, dtype=float)
-    parts = [create_patches(w, patch_size) if axis_patchable(w, patch_size) else create_patches_general(w, patch_size)
-             for w in walls_points]
-    patches_points = np.concatenate(parts, axis=0) if parts else np.zeros((0, 4, 3))
+    if walls_points.ndim == 3 and walls_points.shape[1] != 4:
+        parts = [create_patches_triangles(w, patch_size) for w in walls_points]
+        nv = 3
+    else:
+        parts = [create_patches(w, patch_size) if axis_patchable(w, patch_size)
+                 else create_patches_general(w, patch_size) for w in walls_points]
+        nv = 4
+    patches_points = np.concatenate(parts, axis=0) if parts else np.zeros((0, nv, 3))
     patch_to_wall_ids = np.concatenate(
         [np.full(p.shape[0], i, dtype=np.int64) for i, p in enumerate(parts)]) if parts else np.zeros(0, np.int64)
     patches_normal = np.asarray(walls_normal, dtype=float)[patch_to_wall_ids, :]

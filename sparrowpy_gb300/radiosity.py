@@ -546,8 +546,8 @@ class DirectionalRadiosityFast:
     # ------------------------------------------------------------------ bake
     def bake_geometry(self):
         """Bake the geometry by calculating all the form factors (RadiosityFast.py:369-433)."""
-        if self._patches_points.shape[1] != 4:
-            raise NotImplementedError("the form factor kernels support quadrilateral patches only")
+        if not 3 <= self._patches_points.shape[1] <= 8:
+            raise NotImplementedError("the form factor kernels support patches of 3 to 8 vertices")
         d = self._geometry()
         n = self.n_patches
         nv = self._patches_points.shape[1]
@@ -577,8 +577,8 @@ class DirectionalRadiosityFast:
         method = torch.zeros((max(n_vis, 1),), dtype=torch.uint8, device=dev)
         fsz = nat.size("sp_form_factors_workspace", n, n_vis)
         fws = torch.empty((max(fsz, 1),), dtype=torch.uint8, device=dev)
-        nat.call("sp_form_factors", _PREC[self.precision], n, n_vis, _ptr(pairs), _ptr(d["pts"]), _ptr(d["normals"]),
-                 _ptr(d["areas"]), _ptr(ff), _ptr(method), _ptr(fws), fsz, st)
+        nat.call("sp_form_factors", _PREC[self.precision], n, nv, n_vis, _ptr(pairs), _ptr(d["pts"]),
+                 _ptr(d["normals"]), _ptr(d["areas"]), _ptr(ff), _ptr(method), _ptr(fws), fsz, st)
         del fws
         self._bake_pairs(vis, pairs, pair_index, n_vis, ff, method, brdf_job.result)
         for k in ("visibility_matrix", "visible_patches", "form_factors", "form_factors_tilde",
@@ -689,7 +689,8 @@ class DirectionalRadiosityFast:
         e0 = torch.empty((n, nb), dtype=torch.float64, device=dev)
         d0 = torch.empty((n,), dtype=torch.float64, device=dev)
         e0dir = torch.empty((n, bs["n_out"], nb), dtype=torch.float64, device=dev)
-        nat.call("sp_source_energy", _ptr(src), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(svis), nb, _ptr(att),
+        nat.call("sp_source_energy", _ptr(src), n, _ptr(d["centers"]), _ptr(d["pts"]), self._patches_points.shape[1],
+                 _ptr(svis), nb, _ptr(att),
                  _ptr(d["wall_of"]), _ptr(bs["brdf_index"]), bs["n_in"], _ptr(bs["dirs_in"]), bs["n_out"],
                  _ptr(bs["brdf"]), _ptr(e0), _ptr(d0), _ptr(e0dir), st)
         directivity = getattr(source, "directivity", None)
@@ -1084,7 +1085,8 @@ class DirectionalRadiosityFast:
         rdev = self._t(rc, torch.float64)
         rvis = self._point_visibility(rdev)  # every receiver in one launch
         for r in range(n_r):
-            nat.call("sp_receiver_factors", _ptr(rdev[r]), n, _ptr(d["centers"]), _ptr(d["pts"]), _ptr(rvis[r]),
+            nat.call("sp_receiver_factors", _ptr(rdev[r]), n, _ptr(d["centers"]), _ptr(d["pts"]),
+                     self._patches_points.shape[1], _ptr(rvis[r]),
                      _ptr(d["wall_of"]), bs["n_out"], _ptr(bs["dirs_out"]), _ptr(rfac[r]), _ptr(ridx[r]),
                      _ptr(dist[r]), st)
         return ridx, rfac, dist

@@ -7,7 +7,7 @@ missing packages (pyfar's Coordinates / FrequencyData / TimeData are
 replaced by the light classes of sparrowpy_gb300.coords), imports the
 reference module functions from the read-only source tree and calls them in
 the order of DirectionalRadiosityFast's methods (RadiosityFast.py:369-752)
-on three small scenes.  Inputs (built with sparrowpy_gb300's host code) and
+on four small scenes (the last with triangular patches).  Inputs (built with sparrowpy_gb300's host code) and
 outputs are written to tests/golden/<scene>.npz.
 
 Usage:  python tests/golden/make_golden.py [--ref /path/to/sparrowpy] [scene ...]
@@ -59,11 +59,34 @@ def import_reference(path):
 
 
 def cube_scene():
-    from sparrowpy_gb300 import DirectionalRadiosityFast, shoebox_room_stub, FrequencyData
+    from sparrowpy_gb300 import DirectionalRadiosityFast, shoebox_room_stub
     r = DirectionalRadiosityFast.from_polygon(shoebox_room_stub(1, 1, 1), 0.5)
-    g = sph_gaussian(sh_order=1)
-    keep = g.z > 0
-    dirs = coords.Coordinates.from_cartesian(g.cartesian[keep], weights=g.weights[keep])
+    return _cube_materials(r)
+
+
+def tri_scene():
+    """The cube's room with every 0.5 m patch cut into two triangles (48 patches), the cube's materials on 6
+    seeded random directions (the symmetric cube with a symmetric direction set has exact ties in the
+    outgoing-direction argmin, which rounding alone decides)."""
+    from sparrowpy_gb300 import DirectionalRadiosityFast, shoebox_room_stub
+    q = DirectionalRadiosityFast.from_polygon(shoebox_room_stub(1, 1, 1), 0.5)
+    quads = np.asarray(q._patches_points)
+    tris = np.stack([quads[:, [0, 1, 2]], quads[:, [0, 2, 3]]], axis=1).reshape(-1, 3, 3)
+    ids = np.repeat(np.asarray(q._patch_to_wall_ids), 2)
+    r = DirectionalRadiosityFast(q._walls_points, q._walls_normal, q._walls_up_vector, tris, tris.shape[0], ids)
+    rng = np.random.default_rng(31)
+    v = rng.normal(size=(6, 3))
+    v[:, 2] = np.abs(v[:, 2]) + 0.2
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return _cube_materials(r, coords.Coordinates.from_cartesian(v, weights=np.full(6, 2 * np.pi / 6)))
+
+
+def _cube_materials(r, dirs=None):
+    from sparrowpy_gb300 import FrequencyData
+    if dirs is None:
+        g = sph_gaussian(sh_order=1)
+        keep = g.z > 0
+        dirs = coords.Coordinates.from_cartesian(g.cartesian[keep], weights=g.weights[keep])
     freqs = np.array([125., 250., 500., 1000.])
     brdf = create_from_scattering(dirs, dirs, FrequencyData(np.full(4, 0.5), freqs),
                                   FrequencyData(np.array([0.1, 0.15, 0.2, 0.3]), freqs))
@@ -86,7 +109,7 @@ def rot_scene():
     return r, dict(source=src, receivers=rcv, c=343.0, dt=1e-3, duration=0.15, max_order=4), None
 
 
-SCENES = {'cube': cube_scene, 'cfg1': cfg1_scene, 'rot': rot_scene}
+SCENES = {'cube': cube_scene, 'cfg1': cfg1_scene, 'rot': rot_scene, 'tri': tri_scene}
 
 
 def run_reference(mods, sc, setup, brdf_inputs):

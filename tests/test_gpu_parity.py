@@ -13,7 +13,7 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-SCENES = ["cube", "cfg1", "rot"]
+SCENES = ["cube", "cfg1", "rot", "tri"]
 
 
 def _solve(g, precision, algorithm="auto"):

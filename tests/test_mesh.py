@@ -4,7 +4,9 @@ The reference reads STL through Blender and checks, for a cube, that the
 rough mesh keeps the fine mesh's vertices and has half as many faces.  The
 same checks run here on cubes written as binary and ASCII STL (the
 reference's cube.stl is a binary STL of the cube [-1, 1]^3 with 12
-triangles), and the meshes feed DirectionalRadiosityFast.from_polygon.
+triangles), and the meshes feed DirectionalRadiosityFast.from_polygon: the
+rough mesh as quadrilateral walls, the fine mesh as triangular walls cut
+into triangular patches.
 """
 import struct
 
@@ -141,3 +143,46 @@ def test_inconsistent_winding_stays_a_face_of_its_own(tmp_path):
     _, rough = read_geometry_file(path)
     sizes = sorted(len(c) for c in rough["conn"])
     assert sizes[0] == 3 and len(sizes) == 2
+
+
+def test_stl_fine_mesh_room_patches(tmp_path):
+    """The fine mesh (the file's own triangles) as walls: triangular patches tiling each triangle."""
+    path = tmp_path / "room.stl"
+    write_binary_stl(path, cube_triangles())
+    fine, _ = read_geometry_file(path)
+    walls = polygons_from_mesh(fine, flip=True)
+    assert all(p.pts.shape == (3, 3) for p in walls)
+    r = DirectionalRadiosityFast.from_polygon(walls, 0.5)
+    assert r._patches_points.shape[1:] == (3, 3)
+    assert r.n_patches == 12 * 25  # each half-face triangle: longest side 2.83 m, cut 5 x 5 at 0.5 m
+    areas = np.array([0.5 * np.linalg.norm(np.cross(p[1] - p[0], p[2] - p[0])) for p in r._patches_points])
+    npt.assert_allclose(areas.sum(), 24.0, rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_stl_fine_mesh_room_matches_oracle(tmp_path):
+    """The STL cube's fine mesh (12 triangles) as a room of triangular patches, FP64 on the GPU against the
+    oracle."""
+    from oracle import oracle as orc
+    from oracle.scene import scene_from_radiosity
+    from sparrowpy_gb300.brdf import create_from_scattering, hemisphere_directions
+    from sparrowpy_gb300.coords import Coordinates, FrequencyData
+    path = tmp_path / "room.stl"
+    write_binary_stl(path, cube_triangles())
+    fine, _ = read_geometry_file(path)
+    r = DirectionalRadiosityFast.from_polygon(polygons_from_mesh(fine, flip=True), 1.0, precision="fp64")
+    f = np.array([1000.0])
+    dirs = hemisphere_directions(8)
+    brdf = create_from_scattering(dirs, dirs, FrequencyData([0.5], f), FrequencyData([0.2], f))
+    r.set_wall_brdf(np.arange(12), brdf, dirs, dirs)
+    r.set_air_attenuation(FrequencyData([0.0], f))
+    src, rcv = np.array([0.2, -0.3, 0.1]), np.array([[-0.4, 0.5, -0.2]])
+    c, dt, dur, k = 343.0, 1e-3, 0.05, 5
+    r.bake_geometry()
+    r.init_source_energy(Coordinates(*src))
+    r.calculate_energy_exchange(c, dt, dur, k)
+    mono = r.collect_energy_receiver_mono(Coordinates(rcv[:, 0], rcv[:, 1], rcv[:, 2])).time
+    ref = orc.solve(scene_from_radiosity(r), src, rcv, c, dt, dur, k)
+    np.testing.assert_array_equal(r._visibility_matrix, ref["bake"]["vis"])
+    assert np.sum(ref["mono"]) > 0
+    assert np.linalg.norm(mono - ref["mono"]) / np.linalg.norm(ref["mono"]) < 1e-10

@@ -1,7 +1,7 @@
 """Pin the FP64 CPU oracle to golden vectors produced by the sparrowpy reference.
 
 The fixtures (tests/golden/*.npz, made by tests/golden/make_golden.py)
-hold the reference's own outputs for three scenes: a 1 m cube at 0.5 m
+hold the reference's own outputs for four scenes: a 1 m cube at 0.5 m
 patches, the 5 x 6 x 3 m shoebox at 1 m (126 patches) and a rotated room with
 an occluder in generic position.
 """
@@ -11,7 +11,7 @@ import pytest
 from conftest import acoustics, load_golden, rel_l2, scene_from_golden
 from oracle import oracle as orc
 
-SCENES = ["cube", "cfg1", "rot"]
+SCENES = ["cube", "cfg1", "rot", "tri"]
 
 
 @pytest.fixture(scope="module", params=SCENES)

@@ -151,7 +151,8 @@ def gpu_form_factors(pts, normals, areas, pairs, precision):
     ws = torch.empty((max(wsz, 1),), dtype=torch.uint8, device="cuda")
     p, nr, ar, pr = (_dev(pts, torch.float64), _dev(normals, torch.float64), _dev(areas, torch.float64),
                      _dev(pairs, torch.int32))
-    nat.call("sp_form_factors", nat.SP_F32 if precision == "fp32" else nat.SP_F64, n, m, pr.data_ptr(),
+    nat.call("sp_form_factors", nat.SP_F32 if precision == "fp32" else nat.SP_F64, n, np.asarray(pts).shape[1], m,
+             pr.data_ptr(),
              p.data_ptr(), nr.data_ptr(), ar.data_ptr(), ff.data_ptr(), method.data_ptr(), ws.data_ptr(), wsz,
              _stream())
     return ff.cpu().numpy()
@@ -384,14 +385,14 @@ def test_reciprocity_source_patch_receiver(src, rec):
         d0 = torch.empty((1,), dtype=torch.float64, device="cuda")
         e0dir = torch.empty((1, 1, 1), dtype=torch.float64, device="cuda")
         sa = _dev(np.asarray(a, float), torch.float64)
-        nat.call("sp_source_energy", sa.data_ptr(), 1, c.data_ptr(), p.data_ptr(), ones["vis"].data_ptr(), 1,
+        nat.call("sp_source_energy", sa.data_ptr(), 1, c.data_ptr(), p.data_ptr(), 4, ones["vis"].data_ptr(), 1,
                  ones["att"].data_ptr(), ones["wall"].data_ptr(), ones["slot"].data_ptr(), 1, ones["dirs"].data_ptr(),
                  1, ones["brdf"].data_ptr(), e0.data_ptr(), d0.data_ptr(), e0dir.data_ptr(), _stream())
         rb = _dev(np.asarray(b, float), torch.float64)
         rfac = torch.empty((1,), dtype=torch.float64, device="cuda")
         ridx = torch.empty((1,), dtype=torch.int32, device="cuda")
         dist = torch.empty((1,), dtype=torch.float64, device="cuda")
-        nat.call("sp_receiver_factors", rb.data_ptr(), 1, c.data_ptr(), p.data_ptr(), ones["vis"].data_ptr(),
+        nat.call("sp_receiver_factors", rb.data_ptr(), 1, c.data_ptr(), p.data_ptr(), 4, ones["vis"].data_ptr(),
                  ones["wall"].data_ptr(), 1, ones["dirs"].data_ptr(), rfac.data_ptr(), ridx.data_ptr(),
                  dist.data_ptr(), _stream())
         energy.append(e0.cpu().numpy()[:, 0] * rfac.cpu().numpy())
