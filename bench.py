@@ -334,6 +334,9 @@ def workload_config(name, cfg, world):
             "name": name, "patches": r.n_patches, "bands": nb, "directions": nd, "bins": nt,
             "max_order": cfg["max_order"], "receivers": int(np.atleast_2d(cfg["receivers"]).shape[0]),
             "l2_policy": "inputs larger than L2 (each histogram array >= 1 GB), no flush",
+            "value_state": "each timed solve re-runs bake, source and exchange on one object; it reuses that "
+                           "object's uploaded BRDF tables, their grouping and the receiver tile order (e2e builds "
+                           "a fresh object per step and includes them)",
             "parallelism": f"replicas x{world}"}
 
 

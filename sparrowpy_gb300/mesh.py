@@ -15,7 +15,9 @@ here, so this module reads STL (binary or ASCII) directly:
 
 polygons_from_mesh turns a mesh into Polygon objects (vertices projected
 onto each polygon's plane) for DirectionalRadiosityFast.from_polygon, which
-patches quadrilateral walls in any orientation.  .blend files raise NotImplementedError.
+patches quadrilateral walls in any orientation and cuts the walls of other
+vertex counts (the fine mesh's triangles) into triangular patches.  .blend
+files raise NotImplementedError.
 """
 import os
 import struct
