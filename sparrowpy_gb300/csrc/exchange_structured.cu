@@ -224,9 +224,53 @@ __device__ __forceinline__ void kahan_add4(float4& s, float4& c, float4 x) {
 // One float4 of bins (index t) of one (band, receiver) row of the mix: the
 // class sums, E_k and the E_total update (see k_mix).  s_cd / s_cs: the
 // band's class weights; the row pointers are those of the (band, receiver).
-// kTotal = false: no E_total update at all (et, ea and cj are not read),
-// a separate instantiation with far fewer live registers.
-template <int kOG, bool kTotal = true>
+// The mix of float4 bins t, t + step, ..., t + (kU - 1) step (those below
+// nt4) without an E_total update: the class sums and E_k only.  The kU bins'
+// loads of one class are issued together, so that a thread keeps kU loads in
+// flight (the persistent batch runs few threads per SM).
+template <int kU>
+__device__ __forceinline__ void mix4_store_bins(int t, int step, int nt4, int np, const int* cls, const int* inv_off,
+                                                const int* inv, const float* s_cd, const float* s_cs, int nd,
+                                                size_t cs4, size_t ers4, const float4* __restrict__ gj,
+                                                float4* __restrict__ ek) {
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 d[kU];
+    bool on[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+        on[u] = t + u * step < nt4;
+        d[u] = zero;
+    }
+    for (int q = 0; q < np; ++q) {
+        const int c = cls[q];
+        const float w = s_cd[c];
+        if (w == 0.0f) continue;  // pure mirror classes
+        float4 g[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) g[u] = on[u] ? __ldg(gj + c * cs4 + t + u * step) : zero;
+#pragma unroll
+        for (int u = 0; u < kU; ++u) d[u] = fma4(w, g[u], d[u]);
+    }
+    for (int o = 0; o < nd; ++o) {
+        float4 v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) v[u] = d[u];
+        for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
+            const int cl = inv[q];
+            const float w = s_cs[cl];
+            float4 g[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) g[u] = on[u] ? __ldg(gj + cl * cs4 + t + u * step) : zero;
+#pragma unroll
+            for (int u = 0; u < kU; ++u) v[u] = fma4(w, g[u], v[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+            if (on[u]) ek[o * ers4 + t + u * step] = v[u];
+    }
+}
+
+template <int kOG>
 __device__ __forceinline__ void mix4_bin(int t, int np, const int* cls, const int* inv_off, const int* inv,
                                          const float* s_cd, const float* s_cs, int nd, size_t cs4, size_t ers4,
                                          size_t cc4, int tl4, const float4* __restrict__ gj, float4* __restrict__ ek,
@@ -237,17 +281,6 @@ __device__ __forceinline__ void mix4_bin(int t, int np, const int* cls, const in
     for (int q = 0; q < np; ++q) {
         const int c = cls[q];
         if (s_cd[c] != 0.0f) d = fma4(s_cd[c], __ldg(gj + c * cs4 + t), d);  // skip pure mirror classes
-    }
-    if constexpr (!kTotal) {
-        for (int o = 0; o < nd; ++o) {
-            float4 v = d;
-            for (int q = inv_off[o]; q < inv_off[o + 1]; ++q) {
-                const int cl = inv[q];
-                v = fma4(s_cs[cl], __ldg(gj + cl * cs4 + t), v);
-            }
-            ek[o * ers4 + t] = v;
-        }
-        return;
     }
     const bool late = cj != nullptr && t >= tl4;
     for (int o0 = 0; o0 < nd; o0 += kOG) {
@@ -335,15 +368,20 @@ __device__ __forceinline__ void mix4_item(int n_class, int nd, int nb, int nt, l
     float4* et = etot ? reinterpret_cast<float4*>(etot + ((size_t)j * nd * nb + b) * nt) : nullptr;
     const float4* ea = eadd ? reinterpret_cast<const float4*>(eadd + ((size_t)j * nd * nb + b) * rs + lead) : nullptr;
     ushort4* cj = (comp && et) ? reinterpret_cast<ushort4*>(comp + ((size_t)j * nd * nb + b) * (nt - t_late)) : nullptr;
-    for (int t = lt; t < nt4; t += per)
-        mix4_bin<kOG, kTotal>(t, np, cls, inv_off, inv, s_cd, s_cs, nd, cs4, ers4, cc4, tl4, gj, ek, et, ea, cj,
-                              fold);
+    if constexpr (kTotal) {
+        for (int t = lt; t < nt4; t += per)
+            mix4_bin<kOG>(t, np, cls, inv_off, inv, s_cd, s_cs, nd, cs4, ers4, cc4, tl4, gj, ek, et, ea, cj, fold);
+    } else {
+        constexpr int kU = 4;
+        for (int t = lt; t < nt4; t += per * kU)
+            mix4_store_bins<kU>(t, per, nt4, np, cls, inv_off, inv, s_cd, s_cs, nd, cs4, ers4, gj, ek);
+    }
 }
 
 // kTotal: with the E_total update (etot non-null); without it (the first
 // order of a pair, and every order of the partial sums) only E_k is written.
 template <bool kTotal>
-__global__ void __launch_bounds__(128, 4) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
+__global__ void __launch_bounds__(128, kTotal ? 4 : 8) k_mix4(int n_class, int nd, int nb, int nt, long long rs, int lead,
                                               const int32_t* __restrict__ tile_of, const int32_t* __restrict__ tab,
                                               const float* __restrict__ cdiff, const float* __restrict__ cspec,
                                               const float* __restrict__ g, float* __restrict__ ecur,
