@@ -100,7 +100,7 @@ class BatchTuner:
     returns the cached choice for later waves of the class.
     """
 
-    CANDIDATES = ((1024, 1), (1024, 2), (512, 1), (512, 2))
+    CANDIDATES = ((1024, 1), (1024, 2), (512, 1), (512, 2), (512, 3))
 
     def __init__(self, probe_orders=2):
         self.cache = {}

@@ -10,6 +10,11 @@ __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
+// An mbarrier's shared memory may serve another purpose (the next work item
+// of a persistent block) only after the barrier is invalidated.
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
@@ -292,11 +297,25 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
         // last kStages stages can still have copies in flight
         if (threadIdx.x == 0) {
             const int issued = s_issued;
+            bool landed = true;
             for (int si = issued - 1; si >= 0 && si >= issued - kStages; --si)
-                if (!mbar_drain(&full[si % kStages], (unsigned)((si / kStages) & 1))) atomicCAS(err, 0, kErrDrain);
+                if (!mbar_drain(&full[si % kStages], (unsigned)((si / kStages) & 1))) {
+                    atomicCAS(err, 0, kErrDrain);
+                    landed = false;
+                }
+            if (landed)
+                for (int s = 0; s < kStages; ++s) {
+                    mbar_inval(&full[s]);
+                    mbar_inval(&empty[s]);
+                }
         }
         return;
     }
+    if (threadIdx.x == 0)  // every stage is consumed: the barriers are done with
+        for (int s = 0; s < kStages; ++s) {
+            mbar_inval(&full[s]);
+            mbar_inval(&empty[s]);
+        }
     if (warp < kConsumers) {
         const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
 #pragma unroll

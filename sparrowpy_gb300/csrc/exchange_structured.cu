@@ -1028,8 +1028,8 @@ __device__ __forceinline__ bool batch_wait(const unsigned long long* ctr, unsign
     }
 }
 
-template <int kB, bool kPartial>
-__global__ void __launch_bounds__(kWsThreads, 2) k_batch_exchange(const BatchRoom* __restrict__ rooms, BatchShape S,
+template <int kB, bool kPartial, int kMinBlocks = 2>
+__global__ void __launch_bounds__(kWsThreads, kMinBlocks) k_batch_exchange(const BatchRoom* __restrict__ rooms, BatchShape S,
                                                                   unsigned long long* __restrict__ ticket,
                                                                   int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char s_dyn[];
@@ -1230,8 +1230,10 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
     const int per_sm = b->ctas_per_sm > 0 ? b->ctas_per_sm : 1;
     SpEventTimer timer(b->exchange_ms != nullptr, st);
     const bool partial = a0->partial_sums != 0;
+    // three blocks per SM (512-bin windows only): an instantiation compiled for that register budget
     auto kern = b->window_bins == 1024 ? (partial ? k_batch_exchange<32, true> : k_batch_exchange<32, false>)
-                                       : (partial ? k_batch_exchange<16, true> : k_batch_exchange<16, false>);
+                : per_sm >= 3 ? (partial ? k_batch_exchange<16, true, 3> : k_batch_exchange<16, false, 3>)
+                              : (partial ? k_batch_exchange<16, true> : k_batch_exchange<16, false>);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kern<<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
     timer.stop(st);
