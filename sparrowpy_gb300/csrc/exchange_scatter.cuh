@@ -151,25 +151,29 @@ __device__ __forceinline__ void slot_window(T (&acc)[kN], const T* win, T cf, in
     for (int r = 0; r < kN; ++r) acc[r] = fma_t(cf, p[32 * r], acc[r]);
 }
 
-// One order, one band, one window: G[j, c, b, window] for the 16 receivers
-// of a segment.  Histogram rows of eprev are padded: row r starts at r * rs
-// with bin 0 at offset `lead` (>= nt + kMaxSpan + 4 zeros before it), so a
-// staged window reaching before bin 0 reads zeros and needs no masking, and
-// no window starts before the buffer.  Every shared-memory read of a
-// consumer warp covers 32 consecutive elements (no bank conflict at any
-// offset).
+// One order, one window, bands b_lo .. b_hi - 1: G[j, c, b, window] for the
+// 16 receivers of a segment.  Histogram rows of eprev are padded: row r
+// starts at r * rs with bin 0 at offset `lead` (>= nt + kMaxSpan + 4 zeros
+// before it), so a staged window reaching before bin 0 reads zeros and needs
+// no masking, and no window starts before the buffer.  Every shared-memory
+// read of a consumer warp covers 32 consecutive elements (no bank conflict
+// at any offset).  The bands run through one pipeline: the producer streams
+// band after band (the groups are the same, their rows and coefficients
+// differ), and a consumer warp writes a band's rows out as soon as it has
+// consumed that band's last stage.
 //
-// The work item is (seg_i: index into seg_order, win: window, b: band); the
-// kernels below take it from the block index, the batched exchange from its
-// work queue.
-template <typename T, int kB = WsLayout<T>::kBins>
+// The work item is (seg_i: index into seg_order, win: window, bands); the
+// kernels below take one band from the block index (kBands false: the band
+// loop and the write-out compile to the single-band form), the batched
+// exchange every band from its work queue (kBands true).
+template <typename T, int kB = WsLayout<T>::kBins, bool kBands = false>
 __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long long rs, int lead, long long cap,
                                            const int32_t* __restrict__ tile_recv,
                                            const int32_t* __restrict__ seg_order,
                                            const int64_t* __restrict__ seg_off, const Group* __restrict__ groups,
                                            const uint32_t* __restrict__ wpack, const T* __restrict__ coef,
                                            const T* __restrict__ eprev, T* __restrict__ gout,
-                                           int* __restrict__ err, int seg_i, int win, int b) {
+                                           int* __restrict__ err, int seg_i, int win, int b_lo, int b_hi) {
     using L = WsLayout<T, kB>;
     using T2 = typename Vec2<T>::type;
     extern __shared__ __align__(128) unsigned char s_raw[];
@@ -183,8 +187,9 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
     const int t0 = win * L::kTW;
     const long long g_beg = seg_off[seg], g_end = seg_off[seg + 1];
     const int n_grp = (int)(g_end - g_beg);  // groups of one segment (< 2^31)
-    if (n_grp == 0) return;                   // the same for every thread of the block
-    const int n_stage = (n_grp + kGps - 1) / kGps;
+    if (n_grp == 0 || b_hi <= b_lo) return;   // the same for every thread of the block
+    const int n_stage = (n_grp + kGps - 1) / kGps;  // stages per band
+    const int n_band = kBands ? b_hi - b_lo : 1;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -210,85 +215,117 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
         // producer: lane q computes the window address of group base + q and,
         // once lane 0 has claimed the stage, issues that group's copy itself
         bool stop = false;
-        for (int base = 0; base < n_grp && !stop; base += 32) {
-            long long a0 = 0;
-            if (base + lane < n_grp) {
-                const int2 h = __ldg(reinterpret_cast<const int2*>(groups + g_beg + base + lane));
-                const long long row = ((long long)h.x * nb + b) * rs + lead;
-                a0 = (row + t0 - h.y - kMaxSpan) & ~(long long)(L::kAlign - 1);  // 16-byte aligned start
-            }
-            const int cnt = min(32, n_grp - base);
-            for (int k0 = 0; k0 < cnt; k0 += kGps) {
-                const int si = (base + k0) / kGps;  // stage index (base is a multiple of kGps)
-                const int st = si % kStages;
-                const int ng = min(kGps, cnt - k0);
-                int halt = 0;
-                if (lane == 0) {
-                    if (s_abort) {
-                        halt = 1;
-                    } else if (si >= kStages && !mbar_wait(&empty[st], (unsigned)((si / kStages - 1) & 1), err)) {
-                        atomicCAS(err, 0, kErrProducerWait);
-                        s_abort = 1;
-                        halt = 1;
-                    } else {
-                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                        mbar_expect_tx(&full[st],
-                                       (unsigned)(ng * (L::kWinBytes + kPackWarps * 4 + kTile * (int)sizeof(T))));
+        for (int bi = 0; bi < n_band && !stop; ++bi) {
+            const int b = b_lo + bi;
+            for (int base = 0; base < n_grp && !stop; base += 32) {
+                long long a0 = 0;
+                if (base + lane < n_grp) {
+                    const int2 h = __ldg(reinterpret_cast<const int2*>(groups + g_beg + base + lane));
+                    const long long row = ((long long)h.x * nb + b) * rs + lead;
+                    a0 = (row + t0 - h.y - kMaxSpan) & ~(long long)(L::kAlign - 1);  // 16-byte aligned start
+                }
+                const int cnt = min(32, n_grp - base);
+                for (int k0 = 0; k0 < cnt; k0 += kGps) {
+                    // stage index over all bands (base is a multiple of kGps)
+                    const int si = bi * n_stage + (base + k0) / kGps;
+                    const int st = si % kStages;
+                    const int ng = min(kGps, cnt - k0);
+                    int halt = 0;
+                    if (lane == 0) {
+                        if (s_abort) {
+                            halt = 1;
+                        } else if (si >= kStages && !mbar_wait(&empty[st], (unsigned)((si / kStages - 1) & 1), err)) {
+                            atomicCAS(err, 0, kErrProducerWait);
+                            s_abort = 1;
+                            halt = 1;
+                        } else {
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            mbar_expect_tx(&full[st], (unsigned)(ng * (L::kWinBytes + kPackWarps * 4 +
+                                                                       kTile * (int)sizeof(T))));
+                        }
                     }
-                }
-                halt = __shfl_sync(0xffffffffu, halt, 0);
-                if (halt) {
-                    stop = true;
-                    break;
-                }
-                unsigned char* sp = stages + (size_t)st * L::kStageBytes;
-                const int q = lane - k0;  // this lane's group within the stage
-                if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * L::kWinBytes, eprev + a0, L::kWinBytes, &full[st]);
-                if (lane == 0) {
-                    const long long g0 = g_beg + base + k0;
-                    bulk_copy_g2s(sp + L::kPackOff, wpack + g0 * kPackWarps, (unsigned)(ng * kPackWarps * 4), &full[st]);
-                    bulk_copy_g2s(sp + L::kCoefOff, coef + ((size_t)b * cap + g0) * kTile,
-                                  (unsigned)(ng * kTile * (int)sizeof(T)), &full[st]);
-                    s_issued = si + 1;
+                    halt = __shfl_sync(0xffffffffu, halt, 0);
+                    if (halt) {
+                        stop = true;
+                        break;
+                    }
+                    unsigned char* sp = stages + (size_t)st * L::kStageBytes;
+                    const int q = lane - k0;  // this lane's group within the stage
+                    if (q >= 0 && q < ng) bulk_copy_g2s(sp + q * L::kWinBytes, eprev + a0, L::kWinBytes, &full[st]);
+                    if (lane == 0) {
+                        const long long g0 = g_beg + base + k0;
+                        bulk_copy_g2s(sp + L::kPackOff, wpack + g0 * kPackWarps, (unsigned)(ng * kPackWarps * 4),
+                                      &full[st]);
+                        bulk_copy_g2s(sp + L::kCoefOff, coef + ((size_t)b * cap + g0) * kTile,
+                                      (unsigned)(ng * kTile * (int)sizeof(T)), &full[st]);
+                        s_issued = si + 1;
+                    }
                 }
             }
         }
     } else {
         // consumer: receiver slots 2 warp and 2 warp + 1 of the tile
         const int sh = kSlotsPerWarp * warp;
-        for (int si = 0; si < n_stage; ++si) {
-            const int st = si % kStages;
-            const bool ok = mbar_wait(&full[st], (unsigned)((si / kStages) & 1), err);
-            if (!__all_sync(0xffffffffu, ok)) {  // the whole warp leaves together
-                if (lane == 0) {
-                    atomicCAS(err, 0, kErrConsumerWait);
-                    s_abort = 1;
+        const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+        bool failed = false;
+        for (int bi = 0; bi < n_band && !failed; ++bi) {
+            if (kBands && bi > 0) {
+#pragma unroll
+                for (int r = 0; r < L::kBins; ++r) {
+                    acc0[r] = T(0);
+                    acc1[r] = T(0);
                 }
-                break;
             }
-            const unsigned char* sp = stages + (size_t)st * L::kStageBytes;
-            const int ng = min(kGps, n_grp - si * kGps);
-            const uint32_t* packs = reinterpret_cast<const uint32_t*>(sp + L::kPackOff) + warp;
-            const T* coefs = reinterpret_cast<const T*>(sp + L::kCoefOff) + sh;
-            // the stage's words first (independent loads), then the windows
-            uint32_t pk[kGps];
-            T2 cf[kGps];
+            for (int sb = 0; sb < n_stage; ++sb) {
+                const int si = bi * n_stage + sb;
+                const int st = si % kStages;
+                const bool ok = mbar_wait(&full[st], (unsigned)((si / kStages) & 1), err);
+                if (!__all_sync(0xffffffffu, ok)) {  // the whole warp leaves together
+                    if (lane == 0) {
+                        atomicCAS(err, 0, kErrConsumerWait);
+                        s_abort = 1;
+                    }
+                    failed = true;
+                    break;
+                }
+                const unsigned char* sp = stages + (size_t)st * L::kStageBytes;
+                const int ng = min(kGps, n_grp - sb * kGps);
+                const uint32_t* packs = reinterpret_cast<const uint32_t*>(sp + L::kPackOff) + warp;
+                const T* coefs = reinterpret_cast<const T*>(sp + L::kCoefOff) + sh;
+                // the stage's words first (independent loads), then the windows
+                uint32_t pk[kGps];
+                T2 cf[kGps];
 #pragma unroll
-            for (int q = 0; q < kGps; ++q) {
-                pk[q] = q < ng ? packs[q * kPackWarps] : 0u;  // 0: no member of this warp
-                cf[q] = *reinterpret_cast<const T2*>(coefs + q * kTile);
-            }
+                for (int q = 0; q < kGps; ++q) {
+                    pk[q] = q < ng ? packs[q * kPackWarps] : 0u;  // 0: no member of this warp
+                    cf[q] = *reinterpret_cast<const T2*>(coefs + q * kTile);
+                }
 #pragma unroll
-            for (int q = 0; q < kGps; ++q) {
-                const unsigned bits = (pk[q] >> 12) & 3u;
-                // the word's alignment field holds (-n_base - kMaxSpan) mod 4
-                const int base_off = kMaxSpan + (int)((pk[q] >> 14) & (unsigned)(L::kAlign - 1));
-                const T* win = reinterpret_cast<const T*>(sp + q * L::kWinBytes);
-                if (bits & 1u) slot_window(acc0, win, cf[q].x, (int)(pk[q] & 63u), base_off, lane);
-                if (bits & 2u) slot_window(acc1, win, cf[q].y, (int)((pk[q] >> 6) & 63u), base_off, lane);
+                for (int q = 0; q < kGps; ++q) {
+                    const unsigned bits = (pk[q] >> 12) & 3u;
+                    // the word's alignment field holds (-n_base - kMaxSpan) mod 4
+                    const int base_off = kMaxSpan + (int)((pk[q] >> 14) & (unsigned)(L::kAlign - 1));
+                    const T* w = reinterpret_cast<const T*>(sp + q * L::kWinBytes);
+                    if (bits & 1u) slot_window(acc0, w, cf[q].x, (int)(pk[q] & 63u), base_off, lane);
+                    if (bits & 2u) slot_window(acc1, w, cf[q].y, (int)((pk[q] >> 6) & 63u), base_off, lane);
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&empty[st]);
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[st]);
+            if (failed) break;
+            if constexpr (kBands) {
+                // this band's rows of the warp's two slots
+                const int b = b_lo + bi;
+#pragma unroll
+                for (int h = 0; h < kSlotsPerWarp; ++h) {
+                    const int j = tile_recv[tile * kTile + sh + h];
+                    if (j < 0) continue;
+                    T* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + lane;
+#pragma unroll
+                    for (int r = 0; r < L::kBins; ++r)
+                        if (t0 + lane + 32 * r < nt) out[32 * r] = h == 0 ? acc0[r] : acc1[r];
+                }
+            }
         }
     }
     __syncthreads();
@@ -316,16 +353,18 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
             mbar_inval(&full[s]);
             mbar_inval(&empty[s]);
         }
-    if (warp < kConsumers) {
-        const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
+    if constexpr (!kBands) {
+        if (warp < kConsumers) {
+            const int tile = (int)(seg / n_class), c = (int)(seg % n_class);
 #pragma unroll
-        for (int h = 0; h < kSlotsPerWarp; ++h) {
-            const int j = tile_recv[tile * kTile + kSlotsPerWarp * warp + h];
-            if (j < 0) continue;
-            T* out = gout + (((size_t)j * n_class + c) * nb + b) * nt + t0 + lane;
+            for (int h = 0; h < kSlotsPerWarp; ++h) {
+                const int j = tile_recv[tile * kTile + kSlotsPerWarp * warp + h];
+                if (j < 0) continue;
+                T* out = gout + (((size_t)j * n_class + c) * nb + b_lo) * nt + t0 + lane;
 #pragma unroll
-            for (int r = 0; r < L::kBins; ++r)
-                if (t0 + lane + 32 * r < nt) out[32 * r] = h == 0 ? acc0[r] : acc1[r];
+                for (int r = 0; r < L::kBins; ++r)
+                    if (t0 + lane + 32 * r < nt) out[32 * r] = h == 0 ? acc0[r] : acc1[r];
+            }
         }
     }
 }
@@ -337,11 +376,11 @@ __device__ __forceinline__ void scatter_ws(int n_class, int nb, int nt, long lon
         const T *__restrict__ eprev, T *__restrict__ gout, int *__restrict__ err
 __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f32(SP_SCATTER_ARGS(float)) {
     scatter_ws<float>(n_class, nb, nt, rs, lead, cap, tile_recv, seg_order, seg_off, groups, wpack, coef, eprev, gout,
-                      err, blockIdx.x, blockIdx.y, blockIdx.z);
+                      err, blockIdx.x, blockIdx.y, blockIdx.z, blockIdx.z + 1);
 }
 __global__ void __launch_bounds__(kWsThreads, 2) k_scatter_f64(SP_SCATTER_ARGS(double)) {
     scatter_ws<double>(n_class, nb, nt, rs, lead, cap, tile_recv, seg_order, seg_off, groups, wpack, coef, eprev, gout,
-                       err, blockIdx.x, blockIdx.y, blockIdx.z);
+                       err, blockIdx.x, blockIdx.y, blockIdx.z, blockIdx.z + 1);
 }
 #undef SP_SCATTER_ARGS
 

@@ -1081,14 +1081,11 @@ __global__ void __launch_bounds__(kWsThreads, kMinBlocks) k_batch_exchange(const
         if (s_go) {
             float* eprev = (k & 1) ? R.buf0 : R.buf1;  // E_{k-1}
             if (scatter) {
-                // one (segment, window) item covers every band
+                // one (segment, window) item covers every band, in one pipeline
                 asm volatile("fence.proxy.async.global;" ::: "memory");  // E_{k-1} was written by generic stores
-                for (int b = 0; b < S.nb; ++b) {
-                    if (b > 0) __syncthreads();  // the previous band's stages and barriers are free
-                    scatter_ws<float, kB>(R.n_class, S.nb, S.nt, S.rs, S.lead, R.cap, R.tile_recv, R.seg_order,
-                                          R.seg_off, R.groups, R.wpack, R.coef, eprev, R.g, err,
-                                          (int)(local / S.windows), (int)(local % S.windows), b);
-                }
+                scatter_ws<float, kB, true>(R.n_class, S.nb, S.nt, S.rs, S.lead, R.cap, R.tile_recv, R.seg_order,
+                                      R.seg_off, R.groups, R.wpack, R.coef, eprev, R.g, err,
+                                      (int)(local / S.windows), (int)(local % S.windows), 0, S.nb);
             } else if constexpr (kPartial) {
                 // S_k of one receiver, every band: the mix, then E_0 at the source delay of each row
                 const bool last = k == S.K;
