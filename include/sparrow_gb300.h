@@ -350,6 +350,7 @@ typedef struct sp_batch_args {
     int force_timeout;
     float* exchange_ms;          /* HOST float or NULL: CUDA-event time of the launch */
     long long* items;            /* HOST or NULL: work items of the launch */
+    long long* wait_polls;       /* HOST or NULL: polls the dependency waits of all items took (0: no item waited) */
 } sp_batch_args;
 
 size_t sp_exchange_batch_workspace(int n_rooms);

@@ -88,7 +88,7 @@ class BatchArgs(ctypes.Structure):
     """Mirror of `sp_batch_args` (host memory)."""
     _fields_ = [("n_rooms", I), ("rooms", ctypes.POINTER(BatchRoom)), ("window_bins", I), ("ctas_per_sm", I),
                 ("wait_limit", ctypes.c_uint), ("force_timeout", I), ("exchange_ms", ctypes.POINTER(ctypes.c_float)),
-                ("items", ctypes.POINTER(ctypes.c_longlong))]
+                ("items", ctypes.POINTER(ctypes.c_longlong)), ("wait_polls", ctypes.POINTER(ctypes.c_longlong))]
 
 
 # name: (restype, argtypes)

@@ -132,14 +132,22 @@ def _room_bytes(n, nd, nb, nt, pairs, n_class):
 
 
 class PreparedWave:
-    """Rooms baked and prepared for one persistent batched exchange (all co-resident on the device)."""
+    """Rooms baked and prepared for one persistent batched exchange (all co-resident on the device).
+
+    The room objects are built on the host first; `bake_prepare_ms` is the
+    device time of the bakes, source energies and exchange preparations
+    that follow (CUDA events), the part a one-by-one solve also spends.
+    """
 
     def __init__(self, rooms, c, dt, nt, K, partial_sums=True):
         dev = torch.device("cuda", torch.cuda.current_device())
+        st = torch.cuda.current_stream()
         self.c, self.dt, self.nt, self.K = c, dt, nt, K
         self.objs, self.args, self.wss, self.etcs = [], [], [], []
-        for room in rooms:
-            r = build_room(room, "fp32")
+        built = [build_room(room, "fp32") for room in rooms]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for room, r in zip(rooms, built):
             r.partial_sums = partial_sums
             r.bake_geometry()
             r.init_source_energy(Coordinates(*room["source"]))
@@ -157,6 +165,10 @@ class PreparedWave:
             self.args.append(a)
             self.wss.append((ws, wsz))
             self.etcs.append(etc)
+        e1.record(st)
+        e1.synchronize()
+        self.bake_prepare_ms = e0.elapsed_time(e1)
+        self.fresh = True  # E_0, E_total and the plans are in place for a launch
         self.rooms = (nat.BatchRoom * len(rooms))()
         for q, (a, (ws, wsz)) in enumerate(zip(self.args, self.wss)):
             self.rooms[q].args = ctypes.pointer(a)
@@ -166,13 +178,17 @@ class PreparedWave:
         self.bws = torch.empty((self.bsz,), dtype=torch.uint8, device=dev)
 
     def launch(self, choice, orders=None, wait_limit=0, force_timeout=False):
-        """Place E_0 and E_total again (plans reused), then run `orders` orders of every room in one launch.
+        """Run `orders` orders of every room in one launch (placing E_0 and E_total again, plans reused, unless
+        the state prepared by the constructor is still unused).
 
-        Returns (status, launch ms, work items); status is the C-ABI's."""
+        Returns (status, launch ms, work items); status is the C-ABI's.  The polls the items' dependency
+        waits took are kept in `last_wait_polls`."""
         orders = self.K if orders is None else orders
-        for a, (ws, wsz) in zip(self.args, self.wss):
-            a.max_order = orders
-            nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())
+        if not self.fresh or orders != self.K:  # a launch consumed the prepared state: place it again
+            for a, (ws, wsz) in zip(self.args, self.wss):
+                a.max_order = orders
+                nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())
+        self.fresh = False
         ms = ctypes.c_float(-1.0)
         items = ctypes.c_longlong(0)
         b = nat.BatchArgs()
@@ -183,7 +199,10 @@ class PreparedWave:
         b.force_timeout = 1 if force_timeout else 0
         b.exchange_ms = ctypes.pointer(ms)
         b.items = ctypes.pointer(items)
+        polls = ctypes.c_longlong(0)
+        b.wait_polls = ctypes.pointer(polls)
         rc = nat.lib().sp_exchange_batch(ctypes.byref(b), _ptr(self.bws), self.bsz, _stream())
+        self.last_wait_polls = int(polls.value)
         return rc, float(ms.value), int(items.value)
 
     def results(self, rooms):
@@ -205,9 +224,11 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
 
     Returns (list of mono histograms (R, B, T) numpy in room order, stats):
     stats holds per wave the rooms, their patch counts, the device ms of
-    bake + prepare, of the batched exchange launch and of exchange +
-    collection, the work items and the tile choice; plus the tuner's
-    timings.  FP32; partial_sums as in solve_rooms.
+    bake + prepare (after the room objects are built on the host, as
+    solve_rooms times its rooms), of the batched exchange launch and of
+    exchange + collection (a launch after the tuner's probes places E_0
+    again first), the work items, the dependency-wait polls and the tile
+    choice; plus the tuner's timings.  FP32; partial_sums as in solve_rooms.
     """
     tuner = tuner or _TUNER
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -236,10 +257,8 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
     stats = {"waves": []}
     for wave in waves:
         sub = [rooms[idx] for idx in wave]
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        e[0].record(st)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
         pw = PreparedWave(sub, c, dt, nt, K, partial_sums)
-        e[1].record(st)
 
         def probe(cand, k):
             rc, ms, _ = pw.launch(cand, min(k, K))
@@ -251,18 +270,19 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
         nd, nb = pw.objs[0]._dev["e0dir"].shape[1:]
         key = BatchTuner.shape_class(nd, nb, nt, n_max)
         choice = force_choice or tuner.choose(key, probe)
-        e[2].record(st)
+        e[0].record(st)
         rc, ms_exchange, items = pw.launch(choice)
         if rc != nat.SP_OK:
             raise nat.NativeError("sp_exchange_batch", rc)
         monos = pw.results(sub)
-        e[3].record(st)
-        e[3].synchronize()
+        e[1].record(st)
+        e[1].synchronize()
         for idx, mono in zip(wave, monos):
             out[idx] = mono
         stats["waves"].append({"rooms": len(wave), "patches": [int(r.n_patches) for r in pw.objs],
-                               "bake_prepare_ms": e[0].elapsed_time(e[1]), "exchange_ms": ms_exchange,
-                               "exchange_and_collect_ms": e[2].elapsed_time(e[3]), "items": items,
+                               "bake_prepare_ms": pw.bake_prepare_ms, "exchange_ms": ms_exchange,
+                               "exchange_and_collect_ms": e[0].elapsed_time(e[1]), "items": items,
+                               "wait_polls": pw.last_wait_polls,
                                "window_bins": choice[0], "ctas_per_sm": choice[1]})
         del pw
         torch.cuda.empty_cache()

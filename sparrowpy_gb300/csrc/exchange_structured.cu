@@ -1017,12 +1017,14 @@ struct BatchShape {
 constexpr int kErrBatchWait = 5;  // error flag: a batched item's dependency wait gave up
 
 // Bounded wait until *ctr >= target (acquire); false when the limit is reached or another block failed.
+// *polls counts the polls that found the count short.
 __device__ __forceinline__ bool batch_wait(const unsigned long long* ctr, unsigned long long target, unsigned limit,
-                                           const volatile int* err) {
+                                           const volatile int* err, unsigned long long* polls) {
     for (unsigned it = 0;; ++it) {
         unsigned long long v;
         asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(ctr) : "memory");
         if (v >= target) return true;
+        ++*polls;
         if (it >= limit || *err) return false;
         __nanosleep(128);
     }
@@ -1031,7 +1033,8 @@ __device__ __forceinline__ bool batch_wait(const unsigned long long* ctr, unsign
 template <int kB, bool kPartial, int kMinBlocks = 2>
 __global__ void __launch_bounds__(kWsThreads, kMinBlocks) k_batch_exchange(const BatchRoom* __restrict__ rooms, BatchShape S,
                                                                   unsigned long long* __restrict__ ticket,
-                                                                  int* __restrict__ err) {
+                                                                  int* __restrict__ err,
+                                                                  unsigned long long* __restrict__ wait_polls) {
     extern __shared__ __align__(128) unsigned char s_dyn[];
     __shared__ long long s_item;
     __shared__ int s_go, s_room;
@@ -1066,11 +1069,14 @@ __global__ void __launch_bounds__(kWsThreads, kMinBlocks) k_batch_exchange(const
             const BatchRoom& R = rooms[lo];
             bool ok = *(volatile int*)err == 0;
             const unsigned long long prev_mix = (unsigned long long)(k - 1) * (unsigned long long)R.n_mix;
-            if (ok && S.force_timeout && t == 0) ok = batch_wait(&R.done[1], ~0ull, S.wait_limit, err);  // test hook
-            if (ok) ok = batch_wait(&R.done[1], prev_mix, S.wait_limit, err);
+            unsigned long long polls = 0;
+            if (ok && S.force_timeout && t == 0)
+                ok = batch_wait(&R.done[1], ~0ull, S.wait_limit, err, &polls);  // test hook
+            if (ok) ok = batch_wait(&R.done[1], prev_mix, S.wait_limit, err, &polls);
             if (ok && !scatter)
                 ok = batch_wait(&R.done[0], (unsigned long long)k * (unsigned long long)R.n_scatter, S.wait_limit,
-                                err);
+                                err, &polls);
+            if (polls) atomicAdd(wait_polls, polls);
             if (!ok) atomicCAS(err, 0, kErrBatchWait);
             __threadfence();
             s_go = ok && *(volatile int*)err == 0;
@@ -1217,6 +1223,7 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
     q += sp_align((size_t)b->n_rooms * 2 * sizeof(unsigned long long));
     unsigned long long* ticket = (unsigned long long*)q;
     int* err = (int*)(q + 64);
+    unsigned long long* wait_polls = (unsigned long long*)(q + 128);
     for (int r = 0; r < b->n_rooms; ++r) host[(size_t)r].done = done + 2 * r;
     cudaMemcpyAsync(d_rooms, host.data(), host.size() * sizeof(BatchRoom), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(done, 0, (size_t)b->n_rooms * 2 * sizeof(unsigned long long), st);
@@ -1232,15 +1239,18 @@ extern "C" int sp_exchange_batch(const sp_batch_args* b, void* ws, size_t ws_byt
                 : per_sm >= 3 ? (partial ? k_batch_exchange<16, true, 3> : k_batch_exchange<16, false, 3>)
                               : (partial ? k_batch_exchange<16, true> : k_batch_exchange<16, false>);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err);
+    kern<<<n_sm * per_sm, kWsThreads, smem, sp_counted(st)>>>(d_rooms, S, ticket, err, wait_polls);
     timer.stop(st);
     int rc = sp_check_launch();
     if (rc != SP_OK) return rc;
     int herr = 0;
+    unsigned long long polls = 0;
     cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&polls, wait_polls, sizeof(polls), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return SP_ERR_CUDA;
     if (b->exchange_ms) *b->exchange_ms = timer.elapsed_ms();
     if (b->items) *b->items = S.total;
+    if (b->wait_polls) *b->wait_polls = (long long)polls;
     return herr ? SP_ERR_TIMEOUT : SP_OK;
 }
 
