@@ -837,7 +837,7 @@ def batch_rooms(n_rooms, seed=5, rank=0, world=1, compare_rooms=16, fp64_sample=
            "rooms": n_rooms, "patches_min": int(min(patches)), "patches_mean": float(np.mean(patches)),
            "patches_max": int(max(patches)), "total_ms": total, "rooms_per_s": float(n_rooms / (total * 1e-3)),
            "waves": [{k: w[k] for k in ("rooms", "bake_prepare_ms", "exchange_ms", "exchange_and_collect_ms",
-                                        "items", "window_bins", "ctas_per_sm")} for w in stats["waves"]],
+                                        "items", "mode", "window_bins", "ctas_per_sm")} for w in stats["waves"]],
            "tuner_ms": stats.get("tuner")}
     if rank == 0 and compare_rooms > 0:
         sub = rooms[:compare_rooms]

@@ -16,8 +16,10 @@ receivers drawn per room).
   blocks per SM) come from `BatchTuner`, which times the candidates on a
   short run of the first wave of each shape class and keeps the fastest.
 """
+import concurrent.futures as cf
 import ctypes
 import itertools
+import threading
 
 import numpy as np
 import torch
@@ -94,13 +96,20 @@ class BatchTuner:
     """Tile choices of the persistent batched exchange, timed per shape class and kept.
 
     A shape class is (directions, bands, bins, size bucket of the wave's
-    largest room).  Candidates: scatter windows of 1024 and 512 bins, one and
-    two blocks per SM.  `choose` times each candidate's launch (CUDA events)
-    on `probe_orders` orders of the prepared wave, takes the fastest, and
-    returns the cached choice for later waves of the class.
+    largest room).  Candidates: the persistent launch with scatter windows
+    of 1024 and 512 bins and one to three blocks per SM, and ROOMS, the
+    rooms' orders launched room after room on their prepared plans (the
+    persistent launch's alternative where one room already fills the GPU).
+    `choose` times each candidate (CUDA events) on `probe_orders` and on
+    2 * probe_orders orders of the prepared wave, extrapolates each to the
+    wave's order count (fixed cost plus cost per order: a short probe alone
+    would favour the candidate with the smaller fixed cost), takes the
+    fastest, and returns the cached choice for later waves of the class.
     """
 
-    CANDIDATES = ((1024, 1), (1024, 2), (512, 1), (512, 2), (512, 3))
+    ROOMS = (0, 0)
+    PERSISTENT = ((1024, 1), (1024, 2), (512, 1), (512, 2), (512, 3))
+    CANDIDATES = PERSISTENT + (ROOMS,)
 
     def __init__(self, probe_orders=2):
         self.cache = {}
@@ -111,11 +120,17 @@ class BatchTuner:
     def shape_class(nd, nb, nt, n_max):
         return (int(nd), int(nb), int(nt), int(np.ceil(np.log2(max(n_max, 1)))))
 
-    def choose(self, key, run_probe):
+    def choose(self, key, run_probe, orders=None):
+        """The cached choice of the shape class `key`, or the fastest candidate for `orders` orders (default:
+        2 * probe_orders) by run_probe(candidate, k) -> ms."""
         if key not in self.cache:
+            a = self.probe_orders
+            b = 2 * a
+            k = b if orders is None else max(int(orders), 1)
             times = {}
             for cand in self.CANDIDATES:
-                times[cand] = run_probe(cand, self.probe_orders)
+                ta, tb = run_probe(cand, a), run_probe(cand, b)
+                times[cand] = ta + (k - a) * (tb - ta) / (b - a)
             self.timings[key] = times
             self.cache[key] = min(times, key=times.get)
         return self.cache[key]
@@ -137,34 +152,57 @@ class PreparedWave:
     The room objects are built on the host first; `bake_prepare_ms` is the
     device time of the bakes, source energies and exchange preparations
     that follow (CUDA events), the part a one-by-one solve also spends.
+    bake_threads rooms are baked at a time, each thread on its own stream.
     """
 
-    def __init__(self, rooms, c, dt, nt, K, partial_sums=True):
+    def __init__(self, rooms, c, dt, nt, K, partial_sums=True, bake_threads=4):
         dev = torch.device("cuda", torch.cuda.current_device())
         st = torch.cuda.current_stream()
         self.c, self.dt, self.nt, self.K = c, dt, nt, K
-        self.objs, self.args, self.wss, self.etcs = [], [], [], []
         built = [build_room(room, "fp32") for room in rooms]
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        for room, r in zip(rooms, built):
-            r.partial_sums = partial_sums
-            r.bake_geometry()
-            r.init_source_energy(Coordinates(*room["source"]))
-            n, nd, nb = r._dev["e0dir"].shape
-            etc = torch.empty((n, nd, nb, nt), dtype=torch.float32, device=dev)
-            a = r._exchange_args(c, dt, nt, K, "auto", etc)
-            a.prepare_only = 1
-            a.plan_tag = next(_TAGS)
-            n_class = 1 + nd if a.algorithm == nat.SP_EXCHANGE_SLOTWISE else a.n_groups * a.n_in_dirs
-            wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, nt, a.n_dir_pairs,
-                           a.n_slots, a.n_in_dirs, n_class)
-            ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
-            nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())  # the plan
-            self.objs.append(r)
-            self.args.append(a)
-            self.wss.append((ws, wsz))
-            self.etcs.append(etc)
+        # the rooms are baked and prepared by bake_threads host threads, each
+        # on its own stream: a small room's bake is bound by launch latency
+        # and host round trips, which the others' kernels then fill
+        local = threading.local()
+        streams = []
+        lock = threading.Lock()
+
+        def prepare(room, r):
+            if not hasattr(local, "stream"):
+                torch.cuda.set_device(dev)
+                local.stream = torch.cuda.Stream(device=dev)
+                local.stream.wait_event(start)
+                with lock:
+                    streams.append(local.stream)
+            with torch.cuda.device(dev), torch.cuda.stream(local.stream):
+                r.partial_sums = partial_sums
+                r.bake_geometry()
+                r.init_source_energy(Coordinates(*room["source"]))
+                n, nd, nb = r._dev["e0dir"].shape
+                etc = torch.empty((n, nd, nb, nt), dtype=torch.float32, device=dev)
+                a = r._exchange_args(c, dt, nt, K, "auto", etc)
+                a.prepare_only = 1
+                a.plan_tag = next(_TAGS)
+                n_class = 1 + nd if a.algorithm == nat.SP_EXCHANGE_SLOTWISE else a.n_groups * a.n_in_dirs
+                wsz = nat.size("sp_energy_exchange_workspace", a.precision, a.algorithm, n, nd, nb, nt,
+                               a.n_dir_pairs, a.n_slots, a.n_in_dirs, n_class)
+                ws = torch.empty((wsz,), dtype=torch.uint8, device=dev)
+                nat.call("sp_energy_exchange", ctypes.byref(a), _ptr(ws), wsz, _stream())  # the plan
+            return r, a, (ws, wsz), etc
+
+        start = torch.cuda.Event()
+        start.record(st)
+        workers = max(1, min(int(bake_threads), len(rooms)))
+        with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+            done = list(ex.map(prepare, rooms, built))
+        for s_ in streams:
+            st.wait_stream(s_)
+        self.objs = [d[0] for d in done]
+        self.args = [d[1] for d in done]
+        self.wss = [d[2] for d in done]
+        self.etcs = [d[3] for d in done]
         e1.record(st)
         e1.synchronize()
         self.bake_prepare_ms = e0.elapsed_time(e1)
@@ -184,6 +222,8 @@ class PreparedWave:
         Returns (status, launch ms, work items); status is the C-ABI's.  The polls the items' dependency
         waits took are kept in `last_wait_polls`."""
         orders = self.K if orders is None else orders
+        if tuple(choice) == BatchTuner.ROOMS:
+            return self._launch_rooms(orders)
         if not self.fresh or orders != self.K:  # a launch consumed the prepared state: place it again
             for a, (ws, wsz) in zip(self.args, self.wss):
                 a.max_order = orders
@@ -204,6 +244,28 @@ class PreparedWave:
         rc = nat.lib().sp_exchange_batch(ctypes.byref(b), _ptr(self.bws), self.bsz, _stream())
         self.last_wait_polls = int(polls.value)
         return rc, float(ms.value), int(items.value)
+
+    def _launch_rooms(self, orders):
+        """The orders of each room by its own launches (sp_energy_exchange on the prepared plan, which places
+        E_0 and E_total itself).  Returns (status, ms, 0) as launch does."""
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        rc = nat.SP_OK
+        for a, (ws, wsz) in zip(self.args, self.wss):
+            a.max_order = orders
+            a.prepare_only = 0
+            try:
+                rc = nat.lib().sp_energy_exchange(ctypes.byref(a), _ptr(ws), wsz, _stream())
+            finally:
+                a.prepare_only = 1
+            if rc != nat.SP_OK:
+                break
+        e1.record(st)
+        e1.synchronize()
+        self.fresh = False
+        self.last_wait_polls = 0
+        return rc, e0.elapsed_time(e1), 0
 
     def results(self, rooms):
         """Receiver histograms of each room after a full launch (collect_energy_receiver_mono)."""
@@ -269,7 +331,7 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
         n_max = max(r.n_patches for r in pw.objs)
         nd, nb = pw.objs[0]._dev["e0dir"].shape[1:]
         key = BatchTuner.shape_class(nd, nb, nt, n_max)
-        choice = force_choice or tuner.choose(key, probe)
+        choice = force_choice or tuner.choose(key, probe, K)
         e[0].record(st)
         rc, ms_exchange, items = pw.launch(choice)
         if rc != nat.SP_OK:
@@ -283,6 +345,7 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
                                "bake_prepare_ms": pw.bake_prepare_ms, "exchange_ms": ms_exchange,
                                "exchange_and_collect_ms": e[0].elapsed_time(e[1]), "items": items,
                                "wait_polls": pw.last_wait_polls,
+                               "mode": "rooms" if tuple(choice) == BatchTuner.ROOMS else "persistent",
                                "window_bins": choice[0], "ctas_per_sm": choice[1]})
         del pw
         torch.cuda.empty_cache()

@@ -31,9 +31,10 @@ def _rooms(n=3, seed=11):
 
 @pytest.mark.parametrize("partial_sums", [True, False])
 def test_persistent_batch_matches_rooms_one_by_one(partial_sums):
-    """All orders of three rooms in one persistent launch, for every tile choice the tuner can pick, with E_total
-    as the last partial sum and order by order: the same receiver histograms as the rooms solved one after
-    another in the same form (rel L2 <= 1e-6), and the oracle's (1e-4)."""
+    """All orders of three rooms in one persistent launch, for every tile choice the tuner can pick (and its
+    room-after-room alternative on the prepared plans), with E_total as the last partial sum and order by
+    order: the same receiver histograms as the rooms solved one after another in the same form
+    (rel L2 <= 1e-6), and the oracle's (1e-4)."""
     from oracle.scene import scene_from_radiosity
     from sparrowpy_gb300.batch import BatchTuner, build_room, solve_rooms, solve_rooms_batched
     rooms = _rooms()
