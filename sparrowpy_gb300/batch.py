@@ -6,15 +6,17 @@ receivers drawn per room).
 * `solve_rooms` runs the reference pipeline for each room in turn
   (bake_geometry, init_source_energy, calculate_energy_exchange,
   collect_energy_receiver_mono), releasing each room before the next.
-* `solve_rooms_batched` bakes the rooms of a memory-sized wave one by one,
-  prepares each room's exchange (source energy, E_total and the pair plan in
-  the room's workspace), then runs the exchange orders of the whole wave in
-  one persistent launch (sp_exchange_batch: blocks pull scatter and mix
-  pieces of every room from a device work queue, with bounded waits on the
-  pieces they depend on), and collects each room's receivers.  The
-  persistent launch's tile choices (scatter window of 1024 or 512 bins,
-  blocks per SM) come from `BatchTuner`, which times the candidates on a
-  short run of the first wave of each shape class and keeps the fastest.
+* `solve_rooms_batched` bakes the rooms of a memory-sized wave (four host
+  threads, one stream each), prepares each room's exchange (source energy,
+  E_total and the pair plan in the room's workspace), then runs the
+  exchange orders of the whole wave in one persistent launch
+  (sp_exchange_batch: blocks pull scatter and mix pieces of every room from
+  a device work queue, with bounded waits on the pieces they depend on), or
+  in the rooms' own launches on their prepared plans, and collects each
+  room's receivers.  The choice and the persistent launch's tile shape
+  (scatter window of 1024 or 512 bins, blocks per SM) come from
+  `BatchTuner`, which times the candidates on short runs of the first wave
+  of each shape class and keeps the fastest.
 """
 import concurrent.futures as cf
 import ctypes
