@@ -96,3 +96,33 @@ def test_binding_argument_counts_match_header():
            if name in protos and len(args) != protos[name]}
     assert not bad, bad
     assert len(protos) >= 30
+
+
+def test_argument_checks_before_any_device_work():
+    """Calls whose arguments the library refuses return SP_ERR_ARG before any CUDA call (so they run here):
+    polygons of 2 or 9 vertices; partial sums together with saved per-order states."""
+    import ctypes
+    from sparrowpy_gb300 import _native as nat
+    if not os.path.exists(nat.LIB_PATH):
+        pytest.skip("library not built")
+    lib = nat.lib()
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: the checks come first
+    for nv in (2, 9):
+        assert lib.sp_form_factors(nat.SP_F64, 4, nv, 1, fake, fake, fake, fake, fake, None, None, 0,
+                                   None) == nat.SP_ERR_ARG
+        assert lib.sp_source_energy(fake, 1, fake, fake, nv, fake, 1, fake, fake, fake, 1, fake, 1, fake, fake,
+                                    fake, fake, None) == nat.SP_ERR_ARG
+        assert lib.sp_receiver_factors(fake, 1, fake, fake, nv, fake, fake, 1, fake, fake, fake, fake,
+                                       None) == nat.SP_ERR_ARG
+    a = nat.ExchangeArgs()
+    a.precision, a.algorithm = nat.SP_F32, nat.SP_EXCHANGE_STRUCTURED
+    a.n_patches, a.n_dirs, a.n_bins, a.n_samples, a.max_order = 4, 2, 1, 100, 3
+    a.n_dir_pairs, a.n_slots, a.n_in_dirs, a.n_groups = 4, 1, 2, 1
+    a.speed_of_sound, a.time_resolution = 343.0, 1e-3
+    for name in ("energy_0_dir", "distance_0", "etc_total", "wall_of", "brdf_index", "brdf", "dst_offset",
+                 "pair_src", "pair_out_dir", "pair_in_dir", "pair_distance", "pair_fprime", "pair_unit_len",
+                 "pair_dst", "slot_group", "slot_scale", "class_diff", "class_spec", "class_target"):
+        setattr(a, name, 0x1000)
+    a.states_out, a.states_every, a.partial_sums = 0x1000, 1, 1
+    huge = 1 << 40  # the workspace check passes; nothing is touched before the argument checks
+    assert lib.sp_energy_exchange(ctypes.byref(a), fake, huge, None) == nat.SP_ERR_ARG
