@@ -90,17 +90,19 @@ def _copy_pool():
     return _COPY_POOL
 
 
-def _stack_tables(arrays):
+def _stack_tables(arrays, out=None):
     """np.stack of equally shaped float64 tables, joined in C (np.concatenate along the first axis).
 
     A scene with one wall per patch has thousands of BRDF slots; np.stack's
-    per-array Python work would dominate its copy.
+    per-array Python work would dominate its copy.  out: an optional
+    destination of the stacked shape (e.g. pinned host memory).
     """
     first = arrays[0]
     if first.ndim == 0 or any(a.shape != first.shape for a in arrays):
         raise ValueError("all BRDF tables must have the same shape")
     n = len(arrays)
-    out = np.empty((n,) + first.shape)
+    if out is None:
+        out = np.empty((n,) + first.shape)
     flat = out.reshape((n * first.shape[0],) + first.shape[1:])
     if n < 256:
         np.concatenate(arrays, axis=0, out=flat)
@@ -473,10 +475,21 @@ class DirectionalRadiosityFast:
             if b.ndim == 1:  # default BRDF: one value per band (RadiosityFast.py:459-467)
                 b = b.reshape(1, 1, -1)
             slots.append(b)
-        brdf = _stack_tables(slots)
+        shape = (len(slots),) + slots[0].shape
+        if int(np.prod(shape)) >= (1 << 20):
+            # large tables (one per wall of a per-patch material): stacked straight into pinned host memory
+            # (the caching host allocator keeps it for the next object) and copied without a staging pass
+            pinned = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+            brdf = _stack_tables(slots, out=pinned.numpy())
+            dev_brdf = pinned.to(self.device, non_blocking=True)
+            self.host_bytes_uploaded += pinned.numel() * pinned.element_size()
+            torch.cuda.current_stream(self.device).synchronize()  # brdf_host may outlive this call
+        else:
+            brdf = _stack_tables(slots)
+            dev_brdf = self._t(brdf, torch.float64)
         state = dict(key=key, n_in=din.shape[1], n_out=dout.shape[1], n_slots=brdf.shape[0], brdf_host=brdf,
                      dirs_in=self._t(din, torch.float64), dirs_out=self._t(dout, torch.float64),
-                     brdf=self._t(brdf, torch.float64), brdf_index=self._t(self._brdf_index, torch.int32))
+                     brdf=dev_brdf, brdf_index=self._t(self._brdf_index, torch.int32))
         self._dev["brdf_state"] = state
         return state
 
