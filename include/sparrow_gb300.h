@@ -163,12 +163,12 @@ int sp_form_factors_tilde(long long n_dir, int n, int nd, int nb, int n_in, cons
 /* Universal patch-to-patch form factor for each listed pair (i = source).
  * Replaces universal.py:12-52 `patch2patch_ff_universal` (+ :54-96,
  * integration.py:38-114 Stokes, :116-289 Nusselt).  pts (n_patches, nv, 3):
- * convex planar polygons of nv vertices, 3 <= nv <= 8.  nv != 4: FP64
- * throughout whatever the precision (the Nusselt surface samples of a
- * triangle follow integration.py:533-605's triangle branch; other polygons
- * are sampled as the parallelogram of their first and last sides, as there);
- * method gets 1 or 2 and ws is not used.
- * nv == 4, precision SP_F64: FP64 throughout.  SP_F32: Stokes re-centred on the patch
+ * convex planar polygons of nv vertices, 3 <= nv <= 8 (the Nusselt surface
+ * samples of a triangle follow integration.py:533-605's triangle branch;
+ * polygons of 5 or more vertices are sampled as the parallelogram of their
+ * first and last sides, as there).  nv >= 5: FP64 throughout whatever the
+ * precision, one warp per pair; method gets 1 or 2 and ws is not used.
+ * nv = 3 or 4, precision SP_F64: FP64 throughout.  SP_F32: Stokes re-centred on the patch
  * centres, the second-order terms from FP64 moments and the remainder sum in
  * FP32; FP64 for vertex-sharing pairs (Nusselt), near pairs and pairs whose
  * FP32 error indicator exceeds 5e-6 of the sum.  ff (n_pairs) FP64; method

@@ -645,8 +645,9 @@ __device__ __forceinline__ int sym_slot(int e, int f) {
 }
 
 // Two patches per warp: lanes 0-15 patch 2w, lanes 16-31 patch 2w + 1 (the
-// half-warp reduction order of stokes_pair).
-__global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStokes* __restrict__ out,
+// half-warp reduction order of stokes_pair).  nv = 4 (16 sample points) or
+// 3 (12 sample points; the last four slots carry weight 0 at the centre).
+__global__ void k_ff_patch_data(int n, int nv, const double* __restrict__ pts, PatchStokes* __restrict__ out,
                                 float* __restrict__ outf) {
     const int warp = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -654,11 +655,24 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
     const bool on = k < n;
     const int a = lane & 15;
     double el[12];
-    for (int q = 0; q < 12; ++q) el[q] = on ? pts[(size_t)k * 12 + q] : 0.0;
+    for (int q = 0; q < 12; ++q) el[q] = (on && q < 3 * nv) ? pts[(size_t)k * 3 * nv + q] : 0.0;
     double P[3], w[3], c[3];
-    boundary_point5(el, a, P);
-    boole_weight(el, a, w);
-    for (int d = 0; d < 3; ++d) c[d] = (((el[d] + el[3 + d]) + el[6 + d]) + el[9 + d]) / 4;
+    if (nv == 4) {
+        boundary_point5(el, a, P);
+        boole_weight(el, a, w);
+        for (int d = 0; d < 3; ++d) c[d] = (((el[d] + el[3 + d]) + el[6 + d]) + el[9 + d]) / 4;
+    } else {
+        for (int d = 0; d < 3; ++d) c[d] = ((el[d] + el[3 + d]) + el[6 + d]) / 3;
+        if (a < 4 * nv) {
+            boundary_point_n(el, nv, 4, a, P);
+            boole_weight_n(el, nv, a, w);
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                P[d] = c[d];
+                w[d] = 0.0;
+            }
+        }
+    }
     double loc[3] = {P[0] - c[0], P[1] - c[1], P[2] - c[2]};
     double l2 = loc[0] * loc[0] + loc[1] * loc[1] + loc[2] * loc[2];
     constexpr int kMom = 42;  // W 3, Q 3, M 9, T 18, R 9
@@ -700,7 +714,7 @@ __global__ void k_ff_patch_data(int n, const double* __restrict__ pts, PatchStok
         }
         for (int q = 0; q < 18; ++q) r.T[q] = mom[15 + q];
         double rad2 = 0.0;
-        for (int v = 0; v < 4; ++v) {
+        for (int v = 0; v < nv; ++v) {
             const double dv[3] = {el[3 * v] - c[0], el[3 * v + 1] - c[1], el[3 * v + 2] - c[2]};
             rad2 = fmax(rad2, dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
         }
@@ -730,7 +744,7 @@ __device__ __forceinline__ void d_moments(const PatchStokes& P, const double* D,
 
 // One pair per thread.  method: kNusselt for shared-vertex pairs (handled in
 // k_ff_rework), else kStokes32 with ff = base (completed by k_ff_finish).
-__global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, const double* __restrict__ pts,
+__global__ void k_ff_base(long long n_pairs, int nv, const int32_t* __restrict__ pairs, const double* __restrict__ pts,
                           const PatchStokes* __restrict__ pd, double* __restrict__ ff, uint8_t* __restrict__ method,
                           float4* __restrict__ geo, unsigned long long* __restrict__ n_rework,
                           int64_t* __restrict__ rework) {
@@ -747,11 +761,11 @@ __global__ void k_ff_base(long long n_pairs, const int32_t* __restrict__ pairs, 
     const double reach = A.rad + B.rad + 1e-5;
     if (D2 <= reach * reach) {
         double pi[12], pj[12];
-        for (int k = 0; k < 12; ++k) {
-            pi[k] = pts[(size_t)i * 12 + k];
-            pj[k] = pts[(size_t)j * 12 + k];
+        for (int k = 0; k < 3 * nv; ++k) {
+            pi[k] = pts[(size_t)i * 3 * nv + k];
+            pj[k] = pts[(size_t)j * 3 * nv + k];
         }
-        if (coincident(pj, pi)) {
+        if (coincident_n(pj, nv, pi, nv)) {
             method[q] = kNusselt;
             rework[atomicAdd(n_rework, 1ull)] = q;
             return;
@@ -850,7 +864,7 @@ __global__ void k_ff_finish(long long n_pairs, const int32_t* __restrict__ pairs
 }
 
 // Set-aside pairs, one warp each: FP64 Stokes or the Nusselt analogue.
-__global__ void __launch_bounds__(256) k_ff_rework(long long count, const int64_t* __restrict__ rework,
+__global__ void __launch_bounds__(256) k_ff_rework(long long count, int nv, const int64_t* __restrict__ rework,
                                                    const int32_t* __restrict__ pairs, const double* __restrict__ pts,
                                                    const double* __restrict__ normals, const double* __restrict__ areas,
                                                    double* __restrict__ ff, const uint8_t* __restrict__ method) {
@@ -860,17 +874,17 @@ __global__ void __launch_bounds__(256) k_ff_rework(long long count, const int64_
     const long long q = rework[w];
     const int i = pairs[2 * q], j = pairs[2 * q + 1];
     double pi[12], pj[12];
-    for (int k = 0; k < 12; ++k) {
-        pi[k] = pts[(size_t)i * 12 + k];
-        pj[k] = pts[(size_t)j * 12 + k];
+    for (int k = 0; k < 3 * nv; ++k) {
+        pi[k] = pts[(size_t)i * 3 * nv + k];
+        pj[k] = pts[(size_t)j * 3 * nv + k];
     }
     double result;
     if (method[q] == kNusselt) {
         double ni[3] = {normals[3 * i], normals[3 * i + 1], normals[3 * i + 2]};
         double nj[3] = {normals[3 * j], normals[3 * j + 1], normals[3 * j + 2]};
-        result = nusselt_pair(pi, pj, ni, nj);
+        result = nv == 4 ? nusselt_pair(pi, pj, ni, nj) : nusselt_pair_n(pi, nv, pj, nv, ni, nj);
     } else {
-        result = stokes_pair(pi, pj, areas[i]);
+        result = nv == 4 ? stokes_pair(pi, pj, areas[i]) : stokes_pair_n(pi, nv, pj, nv, areas[i]);
     }
     if (lane == 0) ff[q] = result;
 }
@@ -1016,7 +1030,7 @@ int sp_form_factors(int precision, int n_patches, int nv, long long n_pairs, con
     if (n_pairs == 0) return SP_OK;
     if (!pairs || !pts || !normals || !areas || !ff) return SP_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    if (nv != 4) {  // polygons other than quadrilaterals: FP64, one warp per pair
+    if (nv > 4 || (nv == 3 && (precision == SP_F64 || !method))) {  // FP64, one warp per pair
         k_form_factors_poly<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, nv, pairs, pts,
                                                                                       normals, areas, ff, method);
         return sp_check_launch();
@@ -1042,8 +1056,8 @@ int sp_form_factors(int precision, int n_patches, int nv, long long n_pairs, con
     unsigned long long* n_rework = (unsigned long long*)q;
     cudaMemsetAsync(n_rework, 0, sizeof(unsigned long long), st);
     const long long warps = ((long long)n_patches + 1) / 2;
-    k_ff_patch_data<<<sp_blocks(warps * 32, 256), 256, 0, sp_counted(st)>>>(n_patches, pts, pd, pf);
-    k_ff_base<<<sp_blocks(n_pairs, 128), 128, 0, sp_counted(st)>>>(n_pairs, pairs, pts, pd, ff, method, geo,
+    k_ff_patch_data<<<sp_blocks(warps * 32, 256), 256, 0, sp_counted(st)>>>(n_patches, nv, pts, pd, pf);
+    k_ff_base<<<sp_blocks(n_pairs, 128), 128, 0, sp_counted(st)>>>(n_pairs, nv, pairs, pts, pd, ff, method, geo,
                                                                   n_rework, rework);
     k_ff_phi<<<sp_blocks(n_pairs * 32, 256), 256, 0, sp_counted(st)>>>(n_pairs, pairs, geo, pf, acc, method,
                                                                       n_rework, rework);
@@ -1055,7 +1069,7 @@ int sp_form_factors(int precision, int n_patches, int nv, long long n_pairs, con
     if (count > (unsigned long long)n_pairs) return SP_ERR_CUDA;
     if (count > 0)
         k_ff_rework<<<sp_blocks((long long)count * 32, 256), 256, 0, sp_counted(st)>>>(
-            (long long)count, rework, pairs, pts, normals, areas, ff, method);
+            (long long)count, nv, rework, pairs, pts, normals, areas, ff, method);
     return sp_check_launch();
 }
 

@@ -151,7 +151,8 @@ def test_triangle_patches_tile_the_wall():
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_triangle_room_matches_oracle(precision):
     """A tetrahedron room in a general orientation, triangular walls cut into triangular patches by
-    from_polygon, through the GPU path (FP64 form factors for triangles) against the oracle."""
+    from_polygon, through the GPU path against the oracle (form factors: FP32 Stokes pairs within 1e-5, the
+    FP64 ones within 1e-10)."""
     from oracle import oracle as orc
     from oracle.scene import scene_from_radiosity
     from sparrowpy_gb300 import DirectionalRadiosityFast
@@ -175,7 +176,11 @@ def test_triangle_room_matches_oracle(precision):
     ref = orc.solve(scene_from_radiosity(r), src, rcv, c, dt, dur, k)
     np.testing.assert_array_equal(r._visibility_matrix, ref["bake"]["vis"])
     ff = r._form_factors[ref["bake"]["pairs"][:, 0], ref["bake"]["pairs"][:, 1]]
-    np.testing.assert_allclose(ff, ref["bake"]["ff"], rtol=1e-10)
+    method = r._bake["ff_method"].cpu().numpy()[: ff.size]
+    rel = np.abs(ff - ref["bake"]["ff"]) / np.abs(ref["bake"]["ff"])
+    assert rel[method != 0].max(initial=0) < 1e-10  # FP64 Stokes and Nusselt pairs
+    assert rel[method == 0].max(initial=0) < 1e-5   # FP32 Stokes pairs (precision "fp32")
+    assert precision == "fp32" or (method != 0).all()
     assert np.sum(ref["mono"]) > 0
     tol = 1e-10 if precision == "fp64" else 1e-4
     rel = np.linalg.norm(mono - ref["mono"]) / np.linalg.norm(ref["mono"])

@@ -9,8 +9,9 @@ against quadrilaterals) and point factors of triangles and pentagons are in
 tests/golden/polygons.npz (tests/golden/make_polygon_golden.py):
 
 * the oracle against them, relative 1e-12 (CPU);
-* sp_form_factors on patches of 3, 5 and 6 vertices (FP64, one warp per
-  pair, whatever the precision) against them, relative 1e-10;
+* sp_form_factors on patches of 3, 5 and 6 vertices against them: FP64
+  results within 1e-10 (pentagons and hexagons always FP64, one warp per
+  pair), FP32 Stokes results of triangles within 1e-5;
 * the point factors of sp_source_energy and sp_receiver_factors against
   them, relative 1e-12.
 
@@ -88,10 +89,15 @@ def test_gpu_polygon_form_factors(golden, precision):
         nat.call("sp_form_factors", nat.SP_F32 if precision == "fp32" else nat.SP_F64, pts.shape[0], nv, m,
                  pr.data_ptr(), p.data_ptr(), nr.data_ptr(), ar.data_ptr(), ff.data_ptr(), method.data_ptr(),
                  ws.data_ptr(), wsz, torch.cuda.current_stream().cuda_stream)
-        got = ff.cpu().numpy()
-        np.testing.assert_allclose(got, g["value"][sel], rtol=1e-10, err_msg=f"nv={nv}")
-        # Nusselt for the pairs sharing a vertex, FP64 Stokes for the others
-        np.testing.assert_array_equal(method.cpu().numpy(), np.where(g["nusselt"][sel], 2, 1))
+        got, meth = ff.cpu().numpy(), method.cpu().numpy()
+        rel = np.abs(got - g["value"][sel]) / np.abs(g["value"][sel])
+        # Nusselt for the pairs sharing a vertex; Stokes for the others: FP32 (method 0, triangles in FP32)
+        # within 1e-5, FP64 (method 1) within 1e-10
+        np.testing.assert_array_equal(meth == 2, g["nusselt"][sel])
+        assert rel[meth != 0].max(initial=0) < 1e-10, nv
+        assert rel[meth == 0].max(initial=0) < 1e-5, nv
+        if precision == "fp64" or nv > 3:
+            assert (meth != 0).all()
 
 
 @pytest.mark.gpu
