@@ -15,9 +15,16 @@ members:
   (n_walls, n, 3) and `<name>/weights/$ndarray`;
 * the list of BRDF tables: `<name>/<i>/$ndarray`, one per slot.
 
-The JSON object names them under "sparrowpy_gb300.encoding". Files with
-other pyfar object members, such as the reference's own Coordinates
-encoding, are refused with the member's name.
+The JSON object names them under "sparrowpy_gb300.encoding".
+
+Files the reference writes (pyfar.io.write of RadiosityFast.to_dict, whose
+arrays are nested lists) are read through pyfar's codec, restated: a value
+['$<type>', payload] is a type hint, '$ndarray' naming the npy member that
+holds the array (as `signal/_data` in the reference's test data files),
+'$Coordinates' the object's attribute dict (its cartesian points `_data`
+and `_weights`), '$tuple' and '$dtype' and numpy scalar types their
+values; a top-level object member is `<name>/$<type>`.  Other pyfar types
+are refused with their name.
 """
 import io
 import json
@@ -68,17 +75,58 @@ def write(filename, values, compress=True):
         z.writestr(_BUILTINS, json.dumps(builtins))
 
 
+def _coordinates_from_pyfar(d):
+    """Coordinates from a pyfar Coordinates attribute dict (cartesian `_data`, or `_x`, `_y`, `_z`)."""
+    if "_data" in d:
+        xyz = np.asarray(d["_data"], dtype=float)
+    elif all(k in d for k in ("_x", "_y", "_z")):
+        xyz = np.stack([np.asarray(d[k], dtype=float) for k in ("_x", "_y", "_z")], axis=-1)
+    else:
+        raise NotImplementedError(f"a Coordinates object with members {sorted(d)} cannot be read here")
+    w = d.get("_weights")
+    w = None if w is None or (isinstance(w, str) and w == "None") else np.asarray(w, dtype=float)
+    return Coordinates.from_cartesian(xyz, weights=w)
+
+
+def _pyfar_decode(obj, z):
+    """A value of the pyfar codec with its type hints resolved (arrays loaded from their zip members)."""
+    if isinstance(obj, list):
+        if len(obj) == 2 and isinstance(obj[0], str) and obj[0].startswith("$"):
+            hint, payload = obj[0][1:], obj[1]
+            if hint == "ndarray":
+                return _npy_load(z.read(payload))
+            if hint == "Coordinates":
+                return _coordinates_from_pyfar(_pyfar_decode(payload, z))
+            if hint == "tuple":
+                return tuple(_pyfar_decode(payload, z))
+            if hint == "dtype":
+                return np.dtype(payload)
+            scalar = getattr(np, hint, None)
+            if isinstance(scalar, type) and issubclass(scalar, np.generic):
+                return scalar(payload)
+            raise NotImplementedError(f"pyfar type '{hint}' cannot be read here")
+        return [_pyfar_decode(x, z) for x in obj]
+    if isinstance(obj, dict):
+        return {k: _pyfar_decode(v, z) for k, v in obj.items()}
+    return obj
+
+
 def read(filename):
-    """Read a file written by write(), or a pyfar file holding only ndarray and builtin members."""
+    """Read a file written by write(), or a pyfar file (the reference's write()) of arrays, builtins and
+    Coordinates."""
     values, arrays = {}, {}
     with zipfile.ZipFile(filename, "r") as z:
         for m in z.namelist():
+            head, _, last = m.rpartition("/")
             if m == _BUILTINS:
-                values.update(json.loads(z.read(m).decode("utf-8")))
-            elif m.endswith("/$ndarray"):
-                arrays[m[:-len("/$ndarray")]] = _npy_load(z.read(m))
-            else:
-                raise NotImplementedError(f"member '{m}': only ndarray and builtin members can be read here")
+                values.update(_pyfar_decode(json.loads(z.read(m).decode("utf-8")), z))
+            elif last == "$ndarray":
+                arrays[head] = _npy_load(z.read(m))
+            elif last == "$Coordinates" and "/" not in head:
+                values[head] = _pyfar_decode(["$Coordinates", json.loads(z.read(m).decode("utf-8"))], z)
+            elif last.startswith("$"):
+                raise NotImplementedError(f"member '{m}': pyfar type '{last[1:]}' cannot be read here")
+            # any other member is the payload of a type hint, read where it is named
     encoding = values.pop("sparrowpy_gb300.encoding", {})
     values.pop("sparrowpy_gb300.format", None)
     values.pop("pyfar.__version__", None)

@@ -115,6 +115,17 @@ def _stack_tables(arrays, out=None):
     return out
 
 
+def _object_array(values):
+    """A per-wall list (e.g. of Coordinates, as RadiosityFast.to_dict writes an object array) as a 1-D object
+    array; arrays and None pass through."""
+    if values is None or isinstance(values, np.ndarray):
+        return values
+    out = np.empty(len(values), dtype=object)
+    for k, v in enumerate(values):
+        out[k] = v
+    return out
+
+
 def _side_stream(device):
     """One side stream per device for host-bound preparation that overlaps the bake kernels."""
     key = torch.device(device).index
@@ -306,8 +317,8 @@ class DirectionalRadiosityFast:
         self._frequencies = None if frequencies is None else np.array(frequencies)
         self._brdf = None if brdf is None else [np.array(b) for b in brdf]
         self._brdf_index = None if brdf_index is None else np.array(brdf_index, dtype=np.int64)
-        self._brdf_incoming_directions = brdf_incoming_directions
-        self._brdf_outgoing_directions = brdf_outgoing_directions
+        self._brdf_incoming_directions = _object_array(brdf_incoming_directions)
+        self._brdf_outgoing_directions = _object_array(brdf_outgoing_directions)
         self._air_attenuation = None if air_attenuation is None else np.array(air_attenuation, dtype=float)
         self._speed_of_sound = None if speed_of_sound is None else float(speed_of_sound)
         self._etc_time_resolution = None if etc_time_resolution is None else float(etc_time_resolution)
