@@ -660,6 +660,9 @@ def general_brdf_leg(orders=50, dense_orders=5, patch_size=0.25):
             r.calculate_energy_exchange(343.0, 1e-3, 2.0, k, recalculate=True, algorithm=algo)
         st = r.exchange_stats
         out[name] = {"orders": k, "ms_per_order": st["order_ms"] / k, "algorithm": st["algorithm"]}
+        if st.get("scatter_ms", -1.0) >= 0 and st["algorithm"] != "dense":
+            out[name]["scatter_ms_per_order"] = st["scatter_ms"] / k
+            out[name]["contraction_ms_per_order"] = (st["order_ms"] - st["scatter_ms"]) / k
         if k == orders:
             monos[name] = r.collect_energy_receiver_mono(as_coords(np.array([[3.0, 4.0, 1.5]]))).time
         del r
