@@ -3,7 +3,7 @@
 Restates the reference pipeline of sparrowpy 1.0.1
 (sparrowpy/classes/RadiosityFast.py:369-752) on plain arrays, calling the
 C++ restatement of its numba loops in oracle.cpp.  Used only by the tests,
-the smoke check and the CPU-baseline leg of the benchmark, as the checker;
+the smoke check and the CPU-baseline leg of the benchmark, to check against;
 the product (sparrowpy_gb300) never imports it.
 
 A scene is a dict of numpy arrays:
