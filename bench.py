@@ -836,7 +836,8 @@ def batch_rooms(n_rooms, seed=5, rank=0, world=1, compare_rooms=16, fp64_sample=
     patches = gather_in_order(n_rooms, idx, [p for w in stats["waves"] for p in w["patches"]])
     out = {"workload": f"{n_rooms} seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, "
                        f"T=1000, order 30, 4 receivers), dealt round-robin to {world} GPU(s); per GPU, waves of rooms "
-                       "that fit in memory, each wave's exchange orders in one persistent launch",
+                       "that fit in memory, each wave's exchange orders in one persistent launch or in the rooms' "
+                       "own launches, whichever the autotuner measures faster (the mode is per wave)",
            "rooms": n_rooms, "patches_min": int(min(patches)), "patches_mean": float(np.mean(patches)),
            "patches_max": int(max(patches)), "total_ms": total, "rooms_per_s": float(n_rooms / (total * 1e-3)),
            "waves": [{k: w[k] for k in ("rooms", "bake_prepare_ms", "exchange_ms", "exchange_and_collect_ms",
