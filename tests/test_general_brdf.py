@@ -100,3 +100,21 @@ def test_tensor_core_contraction_matches_cuda_cores():
         out[tc] = _solve(r)[0]
         assert r.exchange_stats["algorithm"] == "general"
     assert rel_l2(out[True], out[False]) < 1e-6
+
+
+@pytest.mark.parametrize("partial_sums", [True, False])
+@pytest.mark.parametrize("room,algorithm", [("random", "general"), ("per_patch", "slotwise")])
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("fp64", 1e-10)])
+def test_long_histograms_general_and_slotwise(precision, tol, room, algorithm, partial_sums):
+    """The benchmarked histogram shape (2200 bins: two full 1024-bin scatter windows and a partial third,
+    17 contraction chunks of 128 bins with a partial last one) through the general (tensor cores at 64
+    directions) and slot-wise exchanges, E_total as the last partial sum and order by order, 12 orders."""
+    from oracle.scene import scene_from_radiosity
+    r = random_table_room(precision, 64) if room == "random" else per_patch_scattering_room(precision, n_dirs=64)
+    r.partial_sums = partial_sums
+    mono, (c, dt, dur, k) = _solve(r, dt=5e-4, dur=1.1, k=12)
+    st = r.exchange_stats
+    assert st["algorithm"] == algorithm and st["partial_sums"] == partial_sums
+    ref = orc.solve(scene_from_radiosity(r), SRC, RCV, c, dt, dur, k)
+    assert rel_l2(mono, ref["mono"]) < tol
+    assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
