@@ -107,7 +107,6 @@ __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
     extern __shared__ __align__(1024) unsigned char s_raw[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(s_raw);            // MMA completion
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_raw + 16);    // tensor-memory address
-    volatile int* s_abort = reinterpret_cast<volatile int*>(s_raw + 32);
     const int kp_max = tc_kpad(n_class);
     float* a_hi = reinterpret_cast<float*>(s_raw + 256);
     float* a_lo = a_hi + kTcAPart / 4;
@@ -122,7 +121,6 @@ __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
     for (int k = threadIdx.x; k < stride; k += kTcThreads) s_tab[k] = tab[(size_t)tile * stride + k];
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
-        *s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     const uint32_t n_cols = nd <= 32 ? 32u : 64u;  // power of two >= N
@@ -198,14 +196,11 @@ __global__ void __launch_bounds__(kTcThreads) k_mix_general_tc(
                 }
                 tc_commit(bar);
             }
-            // every thread waits for the chain (the A buffers are reused by the next chunk)
-            if (!mbar_wait(bar, phase, err)) {
-                ok = false;
-                if (lane == 0) *s_abort = 1;
-            }
+            // every thread waits for the chain (the A buffers are reused by the next chunk); the block agrees
+            // on the outcome, so that every thread leaves the loops together
+            const bool waited = mbar_wait(bar, phase, err);
             phase ^= 1u;
-            __syncthreads();
-            if (*s_abort) ok = false;
+            if (__syncthreads_or(waited ? 0 : 1)) ok = false;
         }
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
