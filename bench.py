@@ -581,6 +581,44 @@ def _gpu_solve_timed(cfg, precision, repeats=2):
     return float(np.mean(ms)), mono, r
 
 
+def _triangle_leg(cfg):
+    """The config's room with every patch cut into two triangles (FP32): ms per solve through the public API,
+    against the quadrilateral room, and how the form factors were computed (triangles take the FP32 moment
+    path; shared-vertex pairs the FP64 Nusselt analogue)."""
+    import torch
+    from sparrowpy_gb300 import DirectionalRadiosityFast, scenes
+    c = scenes.config(cfg, precision="fp32")
+    r = c["radiosity"]
+    q = np.asarray(r._patches_points)
+    tris = np.stack([q[:, [0, 1, 2]], q[:, [0, 2, 3]]], axis=1).reshape(-1, 3, 3)
+    t = DirectionalRadiosityFast(r._walls_points, r._walls_normal, r._walls_up_vector, tris, tris.shape[0],
+                                 np.repeat(np.asarray(r._patch_to_wall_ids), 2), frequencies=r._frequencies,
+                                 air_attenuation=r._air_attenuation, precision="fp32")
+    t._brdf = [np.array(b) for b in r._brdf]
+    t._brdf_index = r._brdf_index.copy()
+    t._brdf_incoming_directions = r._brdf_incoming_directions.copy()
+    t._brdf_outgoing_directions = r._brdf_outgoing_directions.copy()
+    del r
+    st = torch.cuda.current_stream()
+    ms = []
+    for k in range(3):  # the first solve warms up
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        solve(t, c, as_coords)
+        e1.record(st)
+        e1.synchronize()
+        if k > 0:
+            ms.append(e0.elapsed_time(e1))
+    method = t._bake["ff_method"].cpu().numpy()[: int(t._bake["n_vis"])]
+    out = {"patches": int(t.n_patches), "fp32_ms_per_solve": float(np.mean(ms)),
+           "exchange_ms": float(t.exchange_stats["order_ms"]),
+           "form_factor_pairs": {"fp32_stokes": int((method == 0).sum()), "fp64_stokes": int((method == 1).sum()),
+                                 "nusselt": int((method == 2).sum())}}
+    del t
+    torch.cuda.empty_cache()
+    return out
+
+
 def config_legs(cpu_cfg1=None):
     """cfg1 and cfg2 at FP32 and FP64 on the GPU, with their errors and the FP64 energy check.
 
@@ -610,6 +648,8 @@ def config_legs(cpu_cfg1=None):
                                  "check_ms": eb32["ms"],
                                  "meaning": "per-band FP64 sum of E_total against the time-free energy budget of "
                                             "the orders; nothing is delayed past this histogram"})
+        if name == "cfg2":
+            leg["triangles"] = _triangle_leg(name)
         if name == "cfg1" and cpu_cfg1 is not None:
             cpu_ms, cores, desc, mono_ref = cpu_cfg1
             leg.update(receiver_rel_l2_fp32_vs_oracle=float(np.linalg.norm(m32 - mono_ref) / np.linalg.norm(mono_ref)),
