@@ -6,6 +6,8 @@
   must be closer than plain FP32 sums (and within 1e-7 rel L2).
 * Partial sums: E_total computed as the last of S_k = E_0 + M(S_{k-1})
   against the order-by-order sums, all against the FP64 solve.
+* The energy check of general-table and slot-wise rooms (the budget reads
+  the dense tables, so it checks those factorisations too).
 * Energy check (DirectionalRadiosityFast.energy_balance): per band, the
   FP64 totals of the histograms against the time-free energy budget of the
   orders.  In a closed room whose histogram outlasts the orders nothing is
@@ -107,3 +109,18 @@ def test_energy_past_short_histogram_shows_in_the_check():
     r.calculate_energy_exchange(343.0, 1e-3, 0.1, 20)  # 100 ms: later orders fall past the end
     eb = r.energy_balance()
     assert np.all(eb["histogram"] < eb["budget"]) and np.all(eb["rel_dev"] > 1e-3)
+
+
+@pytest.mark.parametrize("room", ["general", "slotwise"])
+def test_energy_conserved_with_general_and_slotwise_tables(room):
+    """The energy check reads the dense tables, so it also checks the factorised exchanges: a random table
+    (general exchange) and per-wall scattering (slot-wise exchange) in a closed room, FP64 to 1e-12."""
+    from test_general_brdf import per_patch_scattering_room, random_table_room
+    from sparrowpy_gb300.coords import Coordinates
+    r = random_table_room("fp64", 16) if room == "general" else per_patch_scattering_room("fp64", n_dirs=16)
+    r.bake_geometry()
+    r.init_source_energy(Coordinates(2.0, 1.0, 1.0))
+    r.calculate_energy_exchange(343.0, 1e-3, 1.0, 20)
+    assert r.exchange_stats["algorithm"] == room
+    eb = r.energy_balance()
+    assert np.all(eb["rel_dev"] < 1e-12), eb["rel_dev"]
