@@ -160,3 +160,24 @@ def test_brdf_structure_matches_host():
         if not irregular:
             np.testing.assert_array_equal(out["target"].cpu().numpy(), target)
             np.testing.assert_array_equal(out["spec"].cpu().numpy(), spec)
+
+
+@pytest.mark.parametrize("max_order", [0, 1, 2])
+@pytest.mark.parametrize("partial_sums", [True, False])
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-5), ("fp64", 1e-12)])
+def test_lowest_orders(precision, tol, partial_sums, max_order):
+    """Orders 0 (E_total = E_0, the initial energies alone), 1 and 2 on the cube, against the reference-run
+    golden scene's oracle solve at the same order, in both sum forms."""
+    from sparrowpy_gb300.coords import Coordinates
+    g = load_golden("cube")
+    c, dt, duration, _ = acoustics(g)
+    r = radiosity_from_golden(g, precision)
+    r.partial_sums = partial_sums
+    r.bake_geometry()
+    r.init_source_energy(Coordinates(*g["source"]))
+    r.calculate_energy_exchange(c, dt, duration, max_order)
+    rc = g["receivers"]
+    mono = r.collect_energy_receiver_mono(Coordinates(rc[:, 0], rc[:, 1], rc[:, 2])).time
+    ref = orc.solve(scene_from_golden(g), g["source"], rc, c, dt, duration, max_order)
+    assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
+    assert rel_l2(mono, ref["mono"]) < tol
