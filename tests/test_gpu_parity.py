@@ -181,3 +181,36 @@ def test_lowest_orders(precision, tol, partial_sums, max_order):
     ref = orc.solve(scene_from_golden(g), g["source"], rc, c, dt, duration, max_order)
     assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
     assert rel_l2(mono, ref["mono"]) < tol
+
+
+@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("fp64", 1e-10)])
+def test_seeded_rooms_of_varied_shapes(precision, tol, seed):
+    """Seeded shoeboxes of varied sizes, patch sizes, direction counts, bands, bin widths and orders, with
+    histogram lengths that are not multiples of 4 on odd seeds (the mix for any length), against the oracle."""
+    from oracle.scene import scene_from_radiosity
+    from sparrowpy_gb300 import scenes
+    from sparrowpy_gb300.coords import Coordinates
+    rng = np.random.default_rng(100 + seed)
+    dims = tuple(float(x) for x in np.round(rng.uniform(2.0, 4.0, 3) * 2) / 2)
+    patch = float(rng.choice([0.5, 1.0]))
+    n_dirs, n_bins = int(rng.choice([8, 16])), int(rng.choice([1, 3]))
+    r = scenes.shoebox(patch, n_dirs=n_dirs, n_bins=n_bins, scattering=float(rng.uniform(0.2, 0.9)),
+                       per_patch=bool(seed % 3 == 0), seed=seed, dims=dims, alpha_range=(0.05, 0.4),
+                       air_attenuation=list(rng.uniform(0.0, 0.005, n_bins)), precision=precision)
+    dt = float(rng.choice([1e-3, 7e-4]))
+    nt = int(rng.integers(150, 320)) | (1 if seed % 2 else 0)
+    nt += (4 - nt % 4) % 4 if seed % 2 == 0 else 0
+    k = int(rng.integers(2, 8))
+    src = np.array(dims) * rng.uniform(0.2, 0.8, 3)
+    rcv = np.array(dims) * rng.uniform(0.2, 0.8, (2, 3))
+    c = 343.0
+    duration = nt * dt
+    r.bake_geometry()
+    r.init_source_energy(Coordinates(*src))
+    r.calculate_energy_exchange(c, dt, duration, k)
+    assert r._energy_exchange_etc.shape[-1] == int(duration / dt)
+    mono = r.collect_energy_receiver_mono(Coordinates(rcv[:, 0], rcv[:, 1], rcv[:, 2])).time
+    ref = orc.solve(scene_from_radiosity(r), src, rcv, c, dt, duration, k)
+    assert rel_l2(mono, ref["mono"]) < tol, (dims, patch, n_dirs, n_bins, dt, nt, k)
+    assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
