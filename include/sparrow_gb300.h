@@ -479,6 +479,44 @@ int sp_kang_receiver(int n, const double* centers, const double* normal, int nb,
                      const double* E, int max_order, const double* receiver, const double* attenuation,
                      double speed_of_sound, double sampling_rate, double* out, int* err, void* stream);
 
+/* The directional Kang variant (RadiosityKang.py:500-810,
+ * PatchesDirectionalKang).  A wall's histograms are E (nb, n_orders, n,
+ * n_dirs, nt): one row per patch and outgoing direction of the wall's
+ * directional data (the reference's E_matrix is (nb, n_orders, n, nt,
+ * n_dirs)).  scat (n_src_dirs, n_dirs, nb) is the receiving wall's
+ * directional data (|data| * pi, the reference's directivity_data.freq);
+ * scat_idx picks its source-direction row: per patch for the init, per
+ * (receiver patch, source patch) pair, row-major, for the exchange.  Both
+ * walls of an exchange have the same n_dirs. */
+
+/* Replaces RadiosityKang.py:629-671 `init_energy_exchange`: the plain
+ * init's energy at each patch's delay, times |scat[scat_idx[i], d, b]| for
+ * every direction d. */
+int sp_kang_directional_init_energy(int n, const double* centers, const double* sizes, const double* normal,
+                                    const double* src, double sound_power, int nb, const double* absorption,
+                                    const double* attenuation, double speed_of_sound, double sampling_rate,
+                                    int n_orders, int nt, int n_dirs, const double* scat, const int32_t* scat_idx,
+                                    double* E, int* err, void* stream);
+
+/* Replaces RadiosityKang.py:673-745 `calculate_energy_exchange` for one
+ * (receiver wall, source wall) pair: as sp_kang_exchange per direction row
+ * (scattering is the wall's, all ones in the reference), each term times
+ * scat[scat_idx[r * n_src + s], d, b].  ws as sp_kang_exchange. */
+int sp_kang_directional_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const double* rcv_centers,
+                                 double* E_rcv, const double* scattering, const double* absorption,
+                                 const double* attenuation, int n_src, const double* src_centers, const double* E_src,
+                                 const double* ff_src, long long ff_stride, long long ff_col0, double speed_of_sound,
+                                 double sampling_rate, int n_dirs, const double* scat, const int32_t* scat_idx,
+                                 void* ws, size_t ws_bytes, int* err, void* stream);
+
+/* Replaces RadiosityKang.py:747-810 `energy_at_receiver`: as
+ * sp_kang_receiver, patch s contributing its row of direction dir_idx[s]
+ * (the outgoing direction nearest to the receiver). */
+int sp_kang_directional_receiver(int n, const double* centers, const double* normal, int nb, int n_orders, int nt,
+                                 const double* E, int max_order, const double* receiver, const double* attenuation,
+                                 double speed_of_sound, double sampling_rate, int n_dirs, const int32_t* dir_idx,
+                                 double* out, int* err, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

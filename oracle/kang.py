@@ -228,3 +228,143 @@ def make_walls(polygons, max_size, scattering, absorption, attenuation):
                         attenuation=np.atleast_1d(np.asarray(attenuation, float)),
                         patches=kang_patches(pts, max_size)))
     return out
+
+
+# ------------------------------------------------------------- directional variant
+# A directional wall adds: dir_data (n_src_dirs, n_dirs, n_bins) (already |data| * pi),
+# dir_sources (n_src_dirs, 3) and dir_receivers (n_dirs, 3), both in the wall's frame
+# (reference_frame_directions).
+
+def wall_frame_directions(xyz, normal, up):
+    """RadiosityKang.py:558-567: directions of the data frame (normal +z, up +x) in the wall's frame, radius 1.
+
+    Restated with the rotation matrix whose columns are (up, normal x up, normal), not through Euler angles."""
+    n = np.asarray(normal, float) / np.linalg.norm(normal)
+    u = np.asarray(up, float) / np.linalg.norm(up)
+    rot = np.stack([u, np.cross(n, u), n], axis=1)
+    out = np.asarray(xyz, float).reshape(-1, 3) @ rot.T
+    return out / np.linalg.norm(out, axis=1)[:, None]
+
+
+def reference_frame_directions(xyz, normal, up):
+    """RadiosityKang.py:558-567 step by step, with scipy's Rotation (pyfar's Orientations extend it).
+
+    o1 = from_view_up(normal, up) and o2 = from_view_up(+z, +x) are the rotations whose matrix rows are
+    (view, up, view x up); the directions are rotated by the 'xyz' Euler angles (degrees) of o1^-1 o2 and
+    moved to radius 1 through spherical coordinates (azimuth = atan2(y, x) mod 2 pi, colatitude =
+    arccos(z / r); back with x = (r sin col) cos az, y = (r sin col) sin az, z = r cos col, components
+    below the FP64 epsilon set to 0), as pyfar's Coordinates.rotate and radius assignment do.  Ties of
+    the nearest-direction search depend on these roundings."""
+    import warnings
+    from scipy.spatial.transform import Rotation
+
+    def orientation(view, upv):
+        view = np.asarray(view, float) / np.linalg.norm(view)
+        upv = np.asarray(upv, float) / np.linalg.norm(upv)
+        return Rotation.from_matrix(np.stack([view, upv, np.cross(view, upv)])[None])
+
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", UserWarning)
+        euler = (orientation(normal, up).inv() * orientation([0, 0, 1], [1, 0, 0])).as_euler('xyz', True).flatten()
+    p = Rotation.from_euler('xyz', euler, degrees=True).apply(np.asarray(xyz, float).reshape(-1, 3))
+    return unit_sphere(p)
+
+
+def unit_sphere(p):
+    """Points moved to radius 1 through spherical coordinates, as pyfar's `radius = 1` does."""
+    p = np.asarray(p, float).reshape(-1, 3)
+    r = np.sqrt(p[:, 0] ** 2 + p[:, 1] ** 2 + p[:, 2] ** 2)
+    az = np.mod(np.arctan2(p[:, 1], p[:, 0]), 2 * np.pi)
+    col = np.arccos(np.divide(p[:, 2], r, out=np.zeros_like(r), where=r != 0))
+    rs = 1.0 * np.sin(col)
+    out = np.stack([rs * np.cos(az), rs * np.sin(az), 1.0 * np.cos(col)], axis=1)
+    out[np.abs(out) < np.finfo(float).eps] = 0
+    return out
+
+
+def nearest(points, q):
+    """Index of the nearest point of every query: a k-d tree on the Euclidean distance, as pyfar's
+    Coordinates.find_nearest (scipy's cKDTree), so that exact ties resolve as in the reference."""
+    from scipy.spatial import cKDTree
+    return cKDTree(np.asarray(points, float).reshape(-1, 3)).query(np.asarray(q, float).reshape(-1, 3))[1]
+
+
+def dkang_init(wall, max_order, ir_length_s, src, power, fs, c):
+    """RadiosityKang.py:629-671: the plain init tiled over the outgoing directions, times |data| of the
+    source direction nearest to (source - patch centre)."""
+    E = kang_init(wall, max_order, ir_length_s, src, power, fs, c)
+    nd = wall["dir_data"].shape[1]
+    E = np.repeat(E[..., None], nd, axis=-1)
+    ctr = centers(wall["patches"])
+    idx = nearest(wall["dir_sources"], np.asarray(src, float)[None, :] - ctr)
+    for b in range(E.shape[0]):
+        for i in range(ctr.shape[0]):
+            E[b, 0, i, :, :] *= np.abs(wall["dir_data"][idx[i], :, b])
+    return E
+
+
+def dkang_exchange(walls, E, FF, w, k, c, fs):
+    """RadiosityKang.py:673-745 for wall w, order k: per (receiver, source) the delayed source histograms
+    (every outgoing direction) times ff (1 - alpha) exp(-m d), times the receiver wall's data row of the
+    source direction nearest to (source centre - receiver centre)."""
+    me = walls[w]
+    rc = centers(me["patches"])
+    for r in range(rc.shape[0]):
+        for o in me["other"]:
+            sw = walls[o]
+            col = sum(walls[x]["patches"].shape[0] for x in sw["other"][:list(sw["other"]).index(w)])
+            sc = centers(sw["patches"])
+            for s in range(sc.shape[0]):
+                dist = np.linalg.norm(rc[r] - sc[s])
+                delay = int(dist / c * fs)
+                ff = FF[o][s, col + r]
+                for b in range(len(me["absorption"])):
+                    a_prev = E[o][b, k - 1, s, :, :]
+                    if delay > a_prev.shape[0]:
+                        raise ValueError("delay longer than the histogram")
+                    energy = np.roll(a_prev, delay, axis=0) * ff * (1 - me["absorption"][b]) * np.exp(
+                        -me["attenuation"][b] * dist)
+                    idx = nearest(me["dir_sources"], sc[s] - rc[r])[0]
+                    energy *= me["dir_data"][idx, :, b]
+                    E[w][b, k, r, :, :] += energy
+
+
+def dkang_receiver(wall, E_w, max_order, rcv, c, fs):
+    """RadiosityKang.py:747-810: each patch's histogram of the outgoing direction nearest to the receiver."""
+    nb, _, n, nt, _ = E_w.shape
+    out = np.zeros((nb, nt))
+    rcv = np.asarray(rcv, float)
+    nrm = np.asarray(wall["normal"], float)
+    for s, sp in enumerate(wall["patches"]):
+        spos = centers(sp)
+        cos_xi = np.abs(np.sum(nrm * np.abs(rcv - spos))) / np.linalg.norm(spos - rcv)
+        i_dir = nearest(wall["dir_receivers"], unit_sphere(rcv - spos))[0]
+        R = np.linalg.norm(rcv - spos)
+        delay = int(R / c * fs)
+        for k in range(max_order + 1):
+            for b in range(nb):
+                factor = cos_xi * (np.exp(-wall["attenuation"][b] * R)) / (np.pi * R ** 2)
+                out[b] += np.roll(E_w[b, k, s, :, i_dir], delay) * factor
+    return out
+
+
+def dkang_run(walls, max_order, ir_length_s, src, c, fs, power=1.0):
+    """RadiosityKang.py:1163-1184 over directional walls: per wall E (n_bins, K + 1, n, T, n_dirs)."""
+    E = [dkang_init(w, max_order, ir_length_s, src, power, fs, c) for w in walls]
+    FF = [kang_ff(walls, i) for i in range(len(walls))] if len(walls) > 1 else [None]
+    if len(walls) > 1:
+        for k in range(1, max_order + 1):
+            for i in range(len(walls)):
+                dkang_exchange(walls, E, FF, i, k, c, fs)
+    return E, FF
+
+
+def dkang_energy_at_receiver(walls, E, max_order, rcv, src, c, fs):
+    """RadiosityKang.py:1186-1202: the walls' responses plus the direct sound."""
+    ir = 0
+    for i, w in enumerate(walls):
+        ir = ir + dkang_receiver(w, E[i], max_order, rcv, c, fs)
+    m = np.asarray(walls[0]["attenuation"], float)
+    r = np.sqrt(np.sum((np.asarray(rcv, float) - np.asarray(src, float)) ** 2))
+    ir[:, int(r / c * fs)] += (1 / (4 * np.pi * np.square(r))) * np.exp(-m * r)
+    return ir

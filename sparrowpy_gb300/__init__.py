@@ -2,15 +2,16 @@
 
 Drop-in for ``sparrowpy.DirectionalRadiosityFast``; see radiosity.py.
 """
-from . import brdf, geometry, kang, mesh, sound_object
+from . import brdf, geometry, kang, mesh, sofa, sound_object
 from .coords import Coordinates, FrequencyData, TimeData
 from .geometry import Polygon, shoebox_room_stub
-from .kang import PatchesKang, RadiosityKang
+from .kang import DirectionalRadiosityKang, PatchesDirectionalKang, PatchesKang, RadiosityKang
 from .radiosity import DirectionalRadiosityFast, analyse_brdf
 
 __version__ = "0.1.0"
 
 __all__ = [
     "DirectionalRadiosityFast", "Polygon", "shoebox_room_stub", "Coordinates", "FrequencyData", "TimeData",
-    "brdf", "geometry", "sound_object", "analyse_brdf", "kang", "mesh", "PatchesKang", "RadiosityKang",
+    "brdf", "geometry", "sound_object", "analyse_brdf", "kang", "mesh", "sofa", "PatchesKang", "RadiosityKang",
+    "PatchesDirectionalKang", "DirectionalRadiosityKang",
 ]

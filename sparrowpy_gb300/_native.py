@@ -137,6 +137,10 @@ _SIGS = {
     "sp_kang_exchange_workspace": (SZ, [I, I, I]),
     "sp_kang_exchange": (I, [I, I, I, I, I, P, P, P, P, P, I, P, P, P, LL, LL, D, D, P, SZ, P, P]),
     "sp_kang_receiver": (I, [I, P, P, I, I, I, P, I, P, P, D, D, P, P, P]),
+    "sp_kang_directional_init_energy": (I, [I, P, P, P, P, D, I, P, P, D, D, I, I, I, P, P, P, P, P]),
+    "sp_kang_directional_exchange": (I, [I, I, I, I, I, P, P, P, P, P, I, P, P, P, LL, LL, D, D, I, P, P, P, SZ, P,
+                                         P]),
+    "sp_kang_directional_receiver": (I, [I, P, P, I, I, I, P, I, P, P, D, D, I, P, P, P, P]),
 }
 
 

@@ -42,6 +42,12 @@ class Coordinates:
         z = radius * np.cos(colatitude)
         return cls(x, y, z, weights=weights)
 
+    @classmethod
+    def from_spherical_elevation(cls, azimuth, elevation, radius=1.0, weights=None):
+        """Points from azimuth, elevation (radians) and radius, as pyfar computes them (see sph2cart)."""
+        x, y, z = sph2cart(azimuth, np.pi / 2 - np.asarray(elevation, float), radius)
+        return cls(x, y, z, weights=weights)
+
     @property
     def cartesian(self):
         return self._pts
@@ -137,11 +143,41 @@ class Coordinates:
         return (np.argmin(d, axis=1),), np.sqrt(np.min(d, axis=1))
 
 
+def sph2cart(azimuth, colatitude, radius):
+    """Spherical to cartesian as pyfar's `sph2cart`: x = (r sin col) cos az, y = (r sin col) sin az,
+    z = r cos col, with components below the FP64 epsilon in magnitude set to 0."""
+    azimuth, colatitude, radius = (np.atleast_1d(np.asarray(v, float)) for v in (azimuth, colatitude, radius))
+    r_sin_col = radius * np.sin(colatitude)
+    x = r_sin_col * np.cos(azimuth)
+    y = r_sin_col * np.sin(azimuth)
+    z = radius * np.cos(colatitude)
+    eps = np.finfo(float).eps
+    for v in (x, y, z):
+        v[np.abs(v) < eps] = 0
+    return x, y, z
+
+
+def cart2sph(x, y, z):
+    """Cartesian to (azimuth in [0, 2 pi), colatitude, radius) as pyfar's `cart2sph`."""
+    radius = np.sqrt(x ** 2 + y ** 2 + z ** 2)
+    z_div_r = np.divide(z, radius, out=np.zeros_like(radius, dtype=float), where=radius != 0)
+    return np.mod(np.arctan2(y, x), 2 * np.pi), np.arccos(z_div_r), radius
+
+
+def unit_radius(xyz):
+    """Points moved to radius 1 through spherical coordinates, as assigning pyfar's `radius = 1` does."""
+    xyz = np.asarray(xyz, float)
+    az, col, _ = cart2sph(xyz[..., 0], xyz[..., 1], xyz[..., 2])
+    x, y, z = sph2cart(az, col, np.ones_like(az))
+    return np.stack([x, y, z], axis=-1).reshape(xyz.shape)
+
+
 class FrequencyData:
-    """Frequency-domain data ``freq`` (..., n_bins) at ``frequencies``."""
+    """Frequency-domain data ``freq`` (..., n_bins) at ``frequencies`` (real or complex, as given)."""
 
     def __init__(self, data, frequencies):
-        self.freq = np.atleast_1d(np.asarray(data, dtype=float))
+        data = np.asarray(data)
+        self.freq = np.atleast_1d(data.astype(complex if np.iscomplexobj(data) else float))
         self.frequencies = np.atleast_1d(np.asarray(frequencies, dtype=float))
         if self.freq.shape[-1] != self.frequencies.size:
             raise ValueError("last dimension of data must match the number of frequencies")

@@ -5,6 +5,15 @@
 // unfused operations (x* helpers), so results agree with it up to the last
 // bit of exp / atan / pow.  Histograms are E (n_bins, n_orders, n, nt) per
 // wall, as the reference's E_matrix.
+//
+// The directional variant (RadiosityKang.py:500-810) keeps one histogram per
+// outgoing direction: E (n_bins, n_orders, n, n_dirs, nt) on the device (the
+// reference's E_matrix is (n_bins, n_orders, n, nt, n_dirs); the host
+// transposes).  Every kernel is templated on kDir; with kDir false, n_dirs is
+// 1 and the arithmetic is the plain solver's.  The directional factors come
+// from the receiving wall's table scat (n_src_dirs, n_dirs, n_bins), indexed
+// per patch (init) or per (receiver, source) pair (exchange) by the nearest
+// source direction, which the host finds as the reference does.
 #include "common.cuh"
 #include "exchange_common.cuh"
 
@@ -40,10 +49,14 @@ __device__ void kang_init_geom(double dl, double dm, double dn, double dd_l, dou
 
 // RadiosityKang.py:141-207 `init_energy_exchange`, one patch per thread:
 // E[b, 0, i, delay] += energy_b.
+// Directional (RadiosityKang.py:629-671): E[b, 0, i, d, delay] = energy_b *
+// |scat[idx_i, d, b]|, the tiled histogram times the directional factors.
+template <bool kDir>
 __global__ void k_kang_init(int n, const double* __restrict__ centers, const double* __restrict__ sizes,
                             const double* __restrict__ normal, const double* __restrict__ src, double power, int nb,
                             const double* __restrict__ absorption, const double* __restrict__ attenuation, double c,
-                            double fs, int n_orders, int nt, double* __restrict__ E, int* __restrict__ err) {
+                            double fs, int n_orders, int nt, int n_dirs, const double* __restrict__ scat,
+                            const int32_t* __restrict__ scat_idx, double* __restrict__ E, int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s[3] = {src[0], src[1], src[2]};
@@ -72,8 +85,15 @@ __global__ void k_kang_init(int n, const double* __restrict__ centers, const dou
     for (int b = 0; b < nb; ++b) {
         const double cst = xmul(xmul(power, xsub(1.0, absorption[b])), exp(xmul(-attenuation[b], distance)));
         const double e = xdiv(xmul(xmul(cst, dphi), beta), 4 * SP_PI);
-        double* p = E + (((size_t)b * n_orders) * n + i) * nt + delay;
-        *p = xadd(*p, e);
+        if (!kDir) {
+            double* p = E + (((size_t)b * n_orders) * n + i) * nt + delay;
+            *p = xadd(*p, e);
+        } else {
+            for (int d = 0; d < n_dirs; ++d) {
+                double* p = E + ((((size_t)b * n_orders) * n + i) * n_dirs + d) * nt + delay;
+                *p = xmul(xadd(*p, e), fabs(scat[((size_t)scat_idx[i] * n_dirs + d) * nb + b]));
+            }
+        }
     }
 }
 
@@ -149,26 +169,36 @@ __global__ void k_kang_pair(int n_rcv, const double* __restrict__ rcv_c, int n_s
 
 // RadiosityKang.py:209-267 for one source wall: E_rcv[b, k, r, t] +=
 // sum_s (((roll(E_src[b, k-1, s], delay)[t] * ff) * scattering_b) * (1 - alpha_b)) * expo,
-// sources in order, one (band, receiver patch, bin) per thread.
-__global__ void k_kang_exchange(int k, int nb, int n_orders, int nt, int n_rcv, int r0, double* __restrict__ E_rcv,
-                                const double* __restrict__ scattering, const double* __restrict__ absorption,
-                                int n_src, const double* __restrict__ E_src, const double* __restrict__ ff,
-                                long long ff_stride, long long ff_col0, const int32_t* __restrict__ delay,
-                                const double* __restrict__ expo) {
+// sources in order, one (band, receiver row, bin) per thread.  A row is a
+// receiver patch r and an outgoing direction d (row = r * n_dirs + d).
+// Directional (RadiosityKang.py:673-745): the source's direction-d row, the
+// term times scat[idx(r, s), d, b]; the wall's scattering is 1 there, so
+// ((v * ff) * 1) * (1 - alpha) equals the reference's (v * ff) * (1 - alpha).
+template <bool kDir>
+__global__ void k_kang_exchange(int k, int nb, int n_orders, int nt, int n_rcv, int n_dirs, long long row0,
+                                double* __restrict__ E_rcv, const double* __restrict__ scattering,
+                                const double* __restrict__ absorption, int n_src, const double* __restrict__ E_src,
+                                const double* __restrict__ ff, long long ff_stride, long long ff_col0,
+                                const int32_t* __restrict__ delay, const double* __restrict__ expo,
+                                const double* __restrict__ scat, const int32_t* __restrict__ scat_idx) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r = r0 + (int)blockIdx.y, b = blockIdx.z;
-    if (t >= nt || r >= n_rcv) return;
-    const double scat = scattering[b], om = xsub(1.0, absorption[b]);
-    const double* prev = E_src + (((size_t)b * n_orders + (k - 1)) * n_src) * nt;
-    double* out = E_rcv + (((size_t)b * n_orders + k) * n_rcv + r) * nt + t;
+    const long long row = row0 + (long long)blockIdx.y;
+    const int b = blockIdx.z;
+    if (t >= nt || row >= (long long)n_rcv * n_dirs) return;
+    const int r = (int)(row / n_dirs), d = (int)(row % n_dirs);
+    const double sc = scattering[b], om = xsub(1.0, absorption[b]);
+    const double* prev = E_src + (((size_t)b * n_orders + (k - 1)) * n_src) * n_dirs * nt;
+    double* out = E_rcv + ((((size_t)b * n_orders + k) * n_rcv + r) * n_dirs + d) * nt + t;
     double acc = *out;
     for (int s = 0; s < n_src; ++s) {
         const long long q = (long long)r * n_src + s;
         int src_t = t - delay[q];
         if (src_t < 0) src_t += nt;
-        const double v = prev[(size_t)s * nt + src_t];
+        const double v = prev[((size_t)s * n_dirs + d) * nt + src_t];
         const double f = ff[(size_t)s * ff_stride + ff_col0 + r];
-        acc = xadd(acc, xmul(xmul(xmul(xmul(v, f), scat), om), expo[(size_t)b * n_rcv * n_src + q]));
+        double e = xmul(xmul(xmul(xmul(v, f), sc), om), expo[(size_t)b * n_rcv * n_src + q]);
+        if (kDir) e = xmul(e, scat[((size_t)scat_idx[q] * n_dirs + d) * nb + b]);
+        acc = xadd(acc, e);
     }
     *out = acc;
 }
@@ -176,10 +206,14 @@ __global__ void k_kang_exchange(int k, int nb, int n_orders, int nt, int n_rcv, 
 // RadiosityKang.py:443-498 `energy_at_receiver` of one wall, added to out
 // (n_bins, nt): out[b, t] += sum_s sum_k roll(E[b, k, s], delay_s)[t] * factor_sb,
 // one (band, bin) per thread.
+// Directional (RadiosityKang.py:747-810): patch s contributes its row of
+// the outgoing direction dir_idx[s] nearest to the receiver.
+template <bool kDir>
 __global__ void k_kang_receiver(int n, const double* __restrict__ centers, const double* __restrict__ normal, int nb,
                                 int n_orders, int nt, const double* __restrict__ E, int max_order,
                                 const double* __restrict__ rcv, const double* __restrict__ attenuation, double c,
-                                double fs, double* __restrict__ out, int* __restrict__ err) {
+                                double fs, int n_dirs, const int32_t* __restrict__ dir_idx, double* __restrict__ out,
+                                int* __restrict__ err) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;
     if (t >= nt) return;
@@ -199,11 +233,79 @@ __global__ void k_kang_receiver(int n, const double* __restrict__ centers, const
         const double factor = xdiv(xmul(cos_xi, exp(xmul(-attenuation[b], R))), xmul(SP_PI, xmul(R, R)));
         int src_t = t - delay;
         if (src_t < 0) src_t += nt;
+        const int d = kDir ? dir_idx[s] : 0;
         for (int k = 0; k <= max_order; ++k)
-            resp = xadd(resp, xmul(E[(((size_t)b * n_orders + k) * n + s) * nt + src_t], factor));
+            resp = xadd(resp, xmul(E[((((size_t)b * n_orders + k) * n + s) * n_dirs + d) * nt + src_t], factor));
     }
     double* o = out + (size_t)b * nt + t;
     *o = xadd(*o, resp);
+}
+
+// Launchers shared by the plain and the directional entry points.
+template <bool kDir>
+int kang_init(int n, const double* centers, const double* sizes, const double* normal, const double* src,
+              double sound_power, int nb, const double* absorption, const double* attenuation,
+              double speed_of_sound, double sampling_rate, int n_orders, int nt, int n_dirs, const double* scat,
+              const int32_t* scat_idx, double* E, int* err, void* stream) {
+    if (n < 0 || nb < 1 || n_orders < 1 || nt < 1 || n_dirs < 1 || !(speed_of_sound > 0) || !(sampling_rate > 0))
+        return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!centers || !sizes || !normal || !src || !absorption || !attenuation || !E || !err) return SP_ERR_ARG;
+    if (kDir && (!scat || !scat_idx)) return SP_ERR_ARG;
+    k_kang_init<kDir><<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        n, centers, sizes, normal, src, sound_power, nb, absorption, attenuation, speed_of_sound, sampling_rate,
+        n_orders, nt, n_dirs, scat, scat_idx, E, err);
+    return sp_check_launch();
+}
+
+template <bool kDir>
+int kang_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const double* rcv_centers, double* E_rcv,
+                  const double* scattering, const double* absorption, const double* attenuation, int n_src,
+                  const double* src_centers, const double* E_src, const double* ff_src, long long ff_stride,
+                  long long ff_col0, double speed_of_sound, double sampling_rate, int n_dirs, const double* scat,
+                  const int32_t* scat_idx, void* ws, size_t ws_bytes, int* err, void* stream) {
+    if (order < 1 || order >= n_orders || nb < 1 || nt < 1 || n_rcv < 0 || n_src < 0 || n_dirs < 1 ||
+        ff_stride < 0 || ff_col0 < 0 || !(speed_of_sound > 0) || !(sampling_rate > 0))
+        return SP_ERR_ARG;
+    if (n_rcv == 0 || n_src == 0) return SP_OK;
+    if (ff_col0 + n_rcv > ff_stride) return SP_ERR_ARG;
+    if (!rcv_centers || !E_rcv || !scattering || !absorption || !attenuation || !src_centers || !E_src || !ff_src ||
+        !err)
+        return SP_ERR_ARG;
+    if (kDir && (!scat || !scat_idx)) return SP_ERR_ARG;
+    if (!ws || ws_bytes < sp_kang_exchange_workspace(n_rcv, n_src, nb)) return SP_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t pairs = (size_t)n_rcv * n_src;
+    int32_t* delay = (int32_t*)ws;
+    double* expo = (double*)((char*)ws + sp_align(pairs * 4));
+    k_kang_pair<<<sp_blocks((long long)pairs, 128), 128, 0, sp_counted(st)>>>(
+        n_rcv, rcv_centers, n_src, src_centers, nb, attenuation, speed_of_sound, sampling_rate, nt, delay, expo, err);
+    constexpr long long kMaxGridY = 65535;  // receiver rows per launch (grid y limit)
+    const long long rows = (long long)n_rcv * n_dirs;
+    for (long long r0 = 0; r0 < rows; r0 += kMaxGridY) {
+        dim3 grid((nt + 127) / 128, (unsigned)(rows - r0 < kMaxGridY ? rows - r0 : kMaxGridY), nb);
+        k_kang_exchange<kDir><<<grid, 128, 0, sp_counted(st)>>>(order, nb, n_orders, nt, n_rcv, n_dirs, r0, E_rcv,
+                                                                scattering, absorption, n_src, E_src, ff_src,
+                                                                ff_stride, ff_col0, delay, expo, scat, scat_idx);
+    }
+    return sp_check_launch();
+}
+
+template <bool kDir>
+int kang_receiver(int n, const double* centers, const double* normal, int nb, int n_orders, int nt, const double* E,
+                  int max_order, const double* receiver, const double* attenuation, double speed_of_sound,
+                  double sampling_rate, int n_dirs, const int32_t* dir_idx, double* out, int* err, void* stream) {
+    if (n < 0 || nb < 1 || n_orders < 1 || nt < 1 || n_dirs < 1 || max_order < 0 || max_order >= n_orders ||
+        !(speed_of_sound > 0) || !(sampling_rate > 0))
+        return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!centers || !normal || !E || !receiver || !attenuation || !out || !err) return SP_ERR_ARG;
+    if (kDir && !dir_idx) return SP_ERR_ARG;
+    dim3 grid((nt + 127) / 128, nb);
+    k_kang_receiver<kDir><<<grid, 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        n, centers, normal, nb, n_orders, nt, E, max_order, receiver, attenuation, speed_of_sound, sampling_rate,
+        n_dirs, dir_idx, out, err);
+    return sp_check_launch();
 }
 
 }  // namespace
@@ -214,13 +316,17 @@ int sp_kang_init_energy(int n, const double* centers, const double* sizes, const
                         double sound_power, int nb, const double* absorption, const double* attenuation,
                         double speed_of_sound, double sampling_rate, int n_orders, int nt, double* E, int* err,
                         void* stream) {
-    if (n < 0 || nb < 1 || n_orders < 1 || nt < 1 || !(speed_of_sound > 0) || !(sampling_rate > 0)) return SP_ERR_ARG;
-    if (n == 0) return SP_OK;
-    if (!centers || !sizes || !normal || !src || !absorption || !attenuation || !E || !err) return SP_ERR_ARG;
-    k_kang_init<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
-        n, centers, sizes, normal, src, sound_power, nb, absorption, attenuation, speed_of_sound, sampling_rate,
-        n_orders, nt, E, err);
-    return sp_check_launch();
+    return kang_init<false>(n, centers, sizes, normal, src, sound_power, nb, absorption, attenuation, speed_of_sound,
+                            sampling_rate, n_orders, nt, 1, nullptr, nullptr, E, err, stream);
+}
+
+int sp_kang_directional_init_energy(int n, const double* centers, const double* sizes, const double* normal,
+                                    const double* src, double sound_power, int nb, const double* absorption,
+                                    const double* attenuation, double speed_of_sound, double sampling_rate,
+                                    int n_orders, int nt, int n_dirs, const double* scat, const int32_t* scat_idx,
+                                    double* E, int* err, void* stream) {
+    return kang_init<true>(n, centers, sizes, normal, src, sound_power, nb, absorption, attenuation, speed_of_sound,
+                           sampling_rate, n_orders, nt, n_dirs, scat, scat_idx, E, err, stream);
 }
 
 int sp_kang_form_factors(int n_src, const double* src_centers, const double* src_normal, const double* src_wall_center,
@@ -247,44 +353,35 @@ int sp_kang_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const d
                      const double* src_centers, const double* E_src, const double* ff_src, long long ff_stride,
                      long long ff_col0, double speed_of_sound, double sampling_rate, void* ws, size_t ws_bytes,
                      int* err, void* stream) {
-    if (order < 1 || order >= n_orders || nb < 1 || nt < 1 || n_rcv < 0 || n_src < 0 || ff_stride < 0 ||
-        ff_col0 < 0 || !(speed_of_sound > 0) || !(sampling_rate > 0))
-        return SP_ERR_ARG;
-    if (n_rcv == 0 || n_src == 0) return SP_OK;
-    if (ff_col0 + n_rcv > ff_stride) return SP_ERR_ARG;
-    if (!rcv_centers || !E_rcv || !scattering || !absorption || !attenuation || !src_centers || !E_src || !ff_src ||
-        !err)
-        return SP_ERR_ARG;
-    if (!ws || ws_bytes < sp_kang_exchange_workspace(n_rcv, n_src, nb)) return SP_ERR_WORKSPACE;
-    cudaStream_t st = (cudaStream_t)stream;
-    const size_t pairs = (size_t)n_rcv * n_src;
-    int32_t* delay = (int32_t*)ws;
-    double* expo = (double*)((char*)ws + sp_align(pairs * 4));
-    k_kang_pair<<<sp_blocks((long long)pairs, 128), 128, 0, sp_counted(st)>>>(
-        n_rcv, rcv_centers, n_src, src_centers, nb, attenuation, speed_of_sound, sampling_rate, nt, delay, expo, err);
-    constexpr int kMaxGridY = 65535;  // receiver patches per launch (grid y limit)
-    for (int r0 = 0; r0 < n_rcv; r0 += kMaxGridY) {
-        dim3 grid((nt + 127) / 128, (unsigned)(n_rcv - r0 < kMaxGridY ? n_rcv - r0 : kMaxGridY), nb);
-        k_kang_exchange<<<grid, 128, 0, sp_counted(st)>>>(order, nb, n_orders, nt, n_rcv, r0, E_rcv, scattering,
-                                                          absorption, n_src, E_src, ff_src, ff_stride, ff_col0,
-                                                          delay, expo);
-    }
-    return sp_check_launch();
+    return kang_exchange<false>(order, nb, n_orders, nt, n_rcv, rcv_centers, E_rcv, scattering, absorption,
+                                attenuation, n_src, src_centers, E_src, ff_src, ff_stride, ff_col0, speed_of_sound,
+                                sampling_rate, 1, nullptr, nullptr, ws, ws_bytes, err, stream);
+}
+
+int sp_kang_directional_exchange(int order, int nb, int n_orders, int nt, int n_rcv, const double* rcv_centers,
+                                 double* E_rcv, const double* scattering, const double* absorption,
+                                 const double* attenuation, int n_src, const double* src_centers, const double* E_src,
+                                 const double* ff_src, long long ff_stride, long long ff_col0, double speed_of_sound,
+                                 double sampling_rate, int n_dirs, const double* scat, const int32_t* scat_idx,
+                                 void* ws, size_t ws_bytes, int* err, void* stream) {
+    return kang_exchange<true>(order, nb, n_orders, nt, n_rcv, rcv_centers, E_rcv, scattering, absorption,
+                               attenuation, n_src, src_centers, E_src, ff_src, ff_stride, ff_col0, speed_of_sound,
+                               sampling_rate, n_dirs, scat, scat_idx, ws, ws_bytes, err, stream);
 }
 
 int sp_kang_receiver(int n, const double* centers, const double* normal, int nb, int n_orders, int nt,
                      const double* E, int max_order, const double* receiver, const double* attenuation,
                      double speed_of_sound, double sampling_rate, double* out, int* err, void* stream) {
-    if (n < 0 || nb < 1 || n_orders < 1 || nt < 1 || max_order < 0 || max_order >= n_orders ||
-        !(speed_of_sound > 0) || !(sampling_rate > 0))
-        return SP_ERR_ARG;
-    if (n == 0) return SP_OK;
-    if (!centers || !normal || !E || !receiver || !attenuation || !out || !err) return SP_ERR_ARG;
-    dim3 grid((nt + 127) / 128, nb);
-    k_kang_receiver<<<grid, 128, 0, sp_counted((cudaStream_t)stream)>>>(n, centers, normal, nb, n_orders, nt, E,
-                                                                        max_order, receiver, attenuation,
-                                                                        speed_of_sound, sampling_rate, out, err);
-    return sp_check_launch();
+    return kang_receiver<false>(n, centers, normal, nb, n_orders, nt, E, max_order, receiver, attenuation,
+                                speed_of_sound, sampling_rate, 1, nullptr, out, err, stream);
+}
+
+int sp_kang_directional_receiver(int n, const double* centers, const double* normal, int nb, int n_orders, int nt,
+                                 const double* E, int max_order, const double* receiver, const double* attenuation,
+                                 double speed_of_sound, double sampling_rate, int n_dirs, const int32_t* dir_idx,
+                                 double* out, int* err, void* stream) {
+    return kang_receiver<true>(n, centers, normal, nb, n_orders, nt, E, max_order, receiver, attenuation,
+                               speed_of_sound, sampling_rate, n_dirs, dir_idx, out, err, stream);
 }
 
 }  // extern "C"

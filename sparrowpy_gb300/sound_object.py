@@ -5,10 +5,11 @@ directivity, the source energy of every patch and band is multiplied by the
 directivity value towards the patch centre (RadiosityFast.py:500-519).
 
 DirectivityMS holds a directivity as data (n_points, n_frequencies) over
-sampled directions (Coordinates) in the source's frame. The reference reads
-it from a SOFA file (FreeFieldDirectivityTF) with sofar, which is not
-installed here, so it is built from arrays (DirectivityMS.from_arrays); a
-file path raises NotImplementedError.
+sampled directions (Coordinates) in the source's frame. As in the
+reference it is read from a SOFA file (FreeFieldDirectivityTF): the
+emitter `source_index` of Data_Real + 1j Data_Imag at the frequencies N,
+over the receiver positions (sofa.py reads the file without sofar).
+DirectivityMS.from_arrays builds one from data.
 """
 import numpy as np
 
@@ -39,8 +40,18 @@ class DirectivityMS:
 
     def __init__(self, file_path=None, source_index=0, *, data=None, receivers=None):
         if file_path is not None:
-            raise NotImplementedError("reading SOFA files needs sofar, which is not installed; "
-                                      "use DirectivityMS.from_arrays")
+            # sound_object.py:26-40
+            from .sofa import read_sofa, sofa_pos
+            sofa = read_sofa(file_path)
+            data = FrequencyData(np.asarray(sofa.Data_Real)[source_index, :] +
+                                 1j * np.asarray(sofa.Data_Imag)[source_index, :], sofa.N)
+            positions = np.asarray(sofa.ReceiverPosition)
+            if positions.ndim > 2:
+                positions = np.squeeze(positions)
+            receivers = sofa_pos(sofa.ReceiverPosition_Type, positions)
+            if receivers.cdim != 1:
+                raise ValueError("DirectivityMS only supports 1D coordinates, "
+                                 f"got {receivers.cdim}D coordinates. Squeezing did not work.")
         if data is None or receivers is None:
             raise ValueError("a directivity needs data (FrequencyData) and receivers (Coordinates)")
         if np.asarray(data.freq).shape[0] != receivers.csize:

@@ -1,8 +1,9 @@
 """Sound objects and source directivity (sparrowpy/sound_object.py; tests/test_radiosity_sound_object.py).
 
-The CPU tests restate the reference's sound-object tests that need no SOFA
-file: construction and normalisation, errors, defaults, and the
-azimuth/elevation convention of _get_metrics, whose known answer is exact.
+The CPU tests restate the reference's sound-object tests: construction and
+normalisation, errors, defaults, and the azimuth/elevation convention of
+_get_metrics, whose known answer is exact; the directivity read from the
+reference's SOFA file and its known answer are in test_sofa.py.
 The GPU test checks the directivity path of init_source_energy
 (RadiosityFast.py:500-519): E0dir of a directive source equals the
 omnidirectional E0dir times the directivity towards each patch centre,
@@ -41,8 +42,10 @@ def test_sound_source_defaults_and_errors():
         so.SoundSource([0, 0, 0], [2, 0, 0], [0, 0, 2], "a", 1)
     with pytest.raises((ValueError, AssertionError)):
         so.SoundSource([0, 0, 0], [2, 0, 0], [0, 0, 2], None, "a")
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(FileNotFoundError):
         so.DirectivityMS("directivity.sofa")
+    with pytest.raises(ValueError):
+        so.DirectivityMS()
 
 
 def test_get_metrics_known_answer():
