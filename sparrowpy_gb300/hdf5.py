@@ -15,6 +15,13 @@ fixed-array chunk indexes) with the deflate, shuffle and Fletcher-32
 filters.  Anything else raises ``NotImplementedError`` naming the
 feature, so an unsupported file fails loudly instead of decoding wrongly.
 
+Checked against real files (sparrowpy's SOFA test data): superblocks of
+versions 0 and 2, version-2 object headers, dense link and attribute
+storage, chunked data under version-1 B-trees with shuffle and deflate,
+fixed-length string attributes.  Version-1 object headers, symbol-table
+groups, variable-length strings, compact layouts and the version-4 chunk
+indexes follow the specification with no such file at hand to check them.
+
 Only what the radiosity path needs is exposed: ``File(path)`` with
 ``datasets()`` (name -> numpy array, read on demand) and ``attrs`` of the
 root group and of each dataset.
