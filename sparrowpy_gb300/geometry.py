@@ -51,8 +51,55 @@ class Polygon:
         return np.sum(self.pts, axis=0) / self.pts.shape[0]
 
     @property
+    def size(self):
+        """Extent (l, m, n) as the reference computes it: |(p0 - p1) - (p1 - p2)| (geometry.py:84-89)."""
+        return np.abs((self.pts[0] - self.pts[1]) - (self.pts[1] - self.pts[2]))
+
+    @property
     def area(self):
-        return float(calculate_area(self.pts[None])[0])
+        """Area in m^2 (geometry.py:91-121): one triangle, two triangles (0, 1, 2) and (2, 3, 0), or for more
+        points the fan of triangles (p_i, p_i+1, centre)."""
+        pts = self.pts
+        if len(pts) == 3:
+            tris = np.array([pts])
+        elif len(pts) == 4:
+            tris = np.array([pts[0:3], [pts[2], pts[3], pts[0]]])
+        else:
+            c = self.center
+            tris = np.array([[pts[i % len(pts)], pts[(i + 1) % len(pts)], c] for i in range(len(pts))])
+        area = 0
+        for tri in tris:
+            area += .5 * np.linalg.norm(np.cross(tri[1] - tri[0], tri[2] - tri[0]))
+        return area
+
+    def on_surface(self, point):
+        """True if the point lies on the polygon: the angles its vertices subtend sum to 2 pi, or it is a
+        vertex (geometry.py:132-153, absolute tolerance 1e-12)."""
+        n = self.pts.shape[0]
+        p = np.asarray(point, dtype=float)
+        sum_angle = 0
+        for i in range(n):
+            v1 = self.pts[i] - p
+            v2 = self.pts[(i + 1) % n] - p
+            m1, m2 = np.sqrt(np.dot(v1, v1)), np.sqrt(np.dot(v2, v2))
+            if abs(m1 * m2) < 1e-12:
+                return True
+            sum_angle = sum_angle + np.arccos(np.dot(v1, v2) / (m1 * m2))
+        return abs(sum_angle - 2 * np.pi) < 1e-12
+
+    def intersection(self, origin, direction):
+        """Intersection of the ray origin + t direction (t > 0) with the polygon, or None
+        (geometry.py:155-193)."""
+        origin = np.asarray(origin, dtype=float)
+        direction = np.asarray(direction, dtype=float)
+        n = self.normal
+        if abs(np.dot(direction, n)) < 1e-12:
+            return None
+        t = 1 / (np.dot(direction, n)) * (np.dot(n, self.pts[0]) - np.dot(n, origin))
+        if t <= 0.0:
+            return None
+        point = origin + t * direction
+        return point if self.on_surface(point) else None
 
     def to_dict(self):
         return {'up_vector': self.up_vector.tolist(), 'pts': self.pts.tolist(), 'normal': self._normal.tolist()}
@@ -60,6 +107,16 @@ class Polygon:
     @classmethod
     def from_dict(cls, d):
         return cls(d['pts'], d['up_vector'], d['normal'])
+
+
+class _Environment:
+    """Walls, a source, a receiver and the speed of sound (geometry.py:232-273, without plotting)."""
+
+    def __init__(self, polygons, source, receiver, speed_of_sound):
+        self.speed_of_sound = speed_of_sound
+        self.polygons = polygons
+        self.source = source
+        self.receiver = receiver
 
 
 def shoebox_room_stub(length_x, length_y, length_z):
