@@ -1,7 +1,8 @@
 """Direction samplings and BRDF construction (host-side inputs).
 
-`create_from_scattering` restates sparrowpy/brdf.py:8-130 (SOFA output is
-not provided).  `sph_gaussian` restates the Gauss-Legendre sphere sampling
+`create_from_scattering` and `create_from_directional_scattering` restate
+sparrowpy/brdf.py:8-225 and return the tables; writing them to a SOFA file
+(`file_path`) is not provided and raises NotImplementedError.  `sph_gaussian` restates the Gauss-Legendre sphere sampling
 the reference tests draw their BRDF directions from (pyfar.samplings).
 """
 import numpy as np
@@ -50,8 +51,13 @@ def hemisphere_directions(n_directions):
     return out
 
 
+def _no_sofa_output(file_path):
+    if file_path is not None:
+        raise NotImplementedError("writing SOFA files is not provided; the BRDF is returned as FrequencyData")
+
+
 def create_from_scattering(source_directions, receiver_directions, scattering_coefficient,
-                           absorption_coefficient=None):
+                           absorption_coefficient=None, file_path=None):
     """Diffuse-plus-mirror BRDF (sparrowpy/brdf.py:8-130).
 
     rho(i, o) = s(1-a)/pi + (1-s)(1-a)/(cos(theta) w) [o == mirror(i)],
@@ -64,6 +70,7 @@ def create_from_scattering(source_directions, receiver_directions, scattering_co
         raise TypeError('source_directions must be a pf.Coordinates object')
     if not hasattr(receiver_directions, "cartesian"):
         raise TypeError('receiver_directions must be a pf.Coordinates object')
+    _no_sofa_output(file_path)
     freqs = np.asarray(scattering_coefficient.frequencies)
     if absorption_coefficient is None:
         absorption_coefficient = FrequencyData(np.zeros_like(freqs), freqs)
@@ -88,3 +95,36 @@ def create_from_scattering(source_directions, receiver_directions, scattering_co
     brdf[i_sources, i_receiver, :] += scattering_factor / cos_factor[i_sources, i_receiver, np.newaxis]
     brdf *= (1 - np.asarray(absorption_coefficient.freq).flatten())
     return FrequencyData(brdf, freqs)
+
+
+def create_from_directional_scattering(source_directions, receiver_directions, directional_scattering,
+                                       absorption_coefficient=None, file_path=None):
+    """BRDF from a directional scattering coefficient s_d (sparrowpy/brdf.py:133-225).
+
+    rho(i, o) = (1 - a) s_d(i, o) / (cos(theta_o) w_o), with the receiver
+    weights scaled to sum to 2 pi; directional_scattering is FrequencyData
+    of cshape (n_sources, n_receivers).  Returned as FrequencyData
+    (n_sources, n_receivers, n_bins) at the absorption's frequencies.
+    """
+    if not hasattr(source_directions, "cartesian"):
+        raise TypeError('source_directions must be a pf.Coordinates object')
+    if not hasattr(receiver_directions, "cartesian"):
+        raise TypeError('receiver_directions must be a pf.Coordinates object')
+    n_src = int(np.prod(np.shape(_cart(source_directions))[:-1]))
+    n_rcv = int(np.prod(np.shape(_cart(receiver_directions))[:-1]))
+    if not is_frequency_data(directional_scattering) or \
+            tuple(np.shape(directional_scattering.freq)[:-1]) != (n_src, n_rcv):
+        raise TypeError('directional_scattering must be a pf.FrequencyData object with'
+                        f' cshape ({n_src, n_rcv})')
+    _no_sofa_output(file_path)
+    freqs = np.asarray(directional_scattering.frequencies)
+    if absorption_coefficient is None:
+        absorption_coefficient = FrequencyData(np.zeros_like(freqs), freqs)
+    rcv = _cart(receiver_directions).reshape(-1, 3)
+    colat = np.arccos(np.clip(rcv[:, 2] / np.sqrt(np.sum(rcv ** 2, axis=-1)), -1, 1))
+    cos_receiver = np.cos(colat)[np.newaxis, :, np.newaxis]
+    w = np.asarray(receiver_directions.weights, dtype=float).reshape(-1).copy()
+    w *= 2 * np.pi / np.sum(w)
+    brdf = np.asarray(directional_scattering.freq) / w[..., np.newaxis] / cos_receiver
+    brdf = brdf * (1 - np.asarray(absorption_coefficient.freq).flatten())
+    return FrequencyData(brdf, np.asarray(absorption_coefficient.frequencies))

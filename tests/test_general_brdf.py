@@ -6,7 +6,7 @@
   classes exceed 256 and the slot-wise exchange runs (a diffuse class and
   one class per mirror direction).
 * A seeded random positive table (no diffuse-plus-mirror structure) on some
-  walls.
+  walls, and tables of create_from_directional_scattering.
 
 Tolerances: receiver histograms and E_total rel L2 <= 1e-4 (FP32) and
 <= 1e-10 (FP64) against the FP64 oracle.
@@ -115,6 +115,32 @@ def test_long_histograms_general_and_slotwise(precision, tol, room, algorithm, p
     mono, (c, dt, dur, k) = _solve(r, dt=5e-4, dur=1.1, k=12)
     st = r.exchange_stats
     assert st["algorithm"] == algorithm and st["partial_sums"] == partial_sums
+    ref = orc.solve(scene_from_radiosity(r), SRC, RCV, c, dt, dur, k)
+    assert rel_l2(mono, ref["mono"]) < tol
+    assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
+
+
+@pytest.mark.parametrize("n_dirs", [16, 32])
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("fp64", 1e-10)])
+def test_directional_scattering_tables(precision, tol, n_dirs):
+    """Floor and ceiling with create_from_directional_scattering tables (brdf.py:133-225): seeded random
+    directional scattering coefficients normalised per incoming direction, absorption 0.2; the general
+    exchange (tensor cores at 32 directions) against the oracle."""
+    from oracle.scene import scene_from_radiosity
+    from sparrowpy_gb300 import scenes
+    from sparrowpy_gb300.brdf import create_from_directional_scattering, hemisphere_directions
+    from sparrowpy_gb300.coords import FrequencyData
+    r = scenes.shoebox(1.0, n_dirs=n_dirs, n_bins=2, scattering=0.4, absorption=0.15, seed=9,
+                       dims=(3.0, 2.0, 2.0), air_attenuation=[0.001, 0.002], precision=precision)
+    freqs = np.asarray(r._frequencies, float)
+    dirs = hemisphere_directions(n_dirs)
+    sd = np.random.default_rng(9).random((n_dirs, n_dirs, 2))
+    sd /= np.sum(sd, axis=1, keepdims=True)
+    tab = create_from_directional_scattering(dirs, dirs, FrequencyData(sd, freqs),
+                                             FrequencyData(np.full(2, 0.2), freqs))
+    r.set_wall_brdf([0, 1], tab, dirs, dirs)
+    mono, (c, dt, dur, k) = _solve(r)
+    assert r.exchange_stats["algorithm"] == "general"
     ref = orc.solve(scene_from_radiosity(r), SRC, RCV, c, dt, dur, k)
     assert rel_l2(mono, ref["mono"]) < tol
     assert rel_l2(r._energy_exchange_etc, ref["etot"]) < tol
