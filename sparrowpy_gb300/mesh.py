@@ -1,13 +1,15 @@
-"""Room geometry from STL files (sparrowpy/utils/blender.py:22-142, without Blender).
+"""Room geometry from STL and .blend files (sparrowpy/utils/blender.py:22-142, without Blender).
 
 The reference reads .blend and .stl files through Blender's Python modules
 (bpy, bmesh) and returns two meshes: the file's own faces ("fine") and the
 faces merged across edges whose normals differ by less than an angular
 tolerance ("rough", bmesh.ops.dissolve_limit).  Blender is not available
-here, so this module reads STL (binary or ASCII) directly:
+here, so this module reads the files directly:
 
-* fine: the triangles, with identical vertices welded;
-* rough: edge-connected triangles whose normals differ by less than
+* fine: an STL file's triangles with identical vertices welded, or the
+  mesh of a .blend file's object "Geometry" as stored (blend.py), its
+  vertices and faces in the file's order;
+* rough: edge-connected faces whose normals differ by less than
   angular_tolerance merged into polygons, each traced as its boundary loop.
   A loop vertex where the boundary runs straight on (turn below the
   tolerance) is left out of that polygon.  `verts` keeps every vertex, so
@@ -16,8 +18,7 @@ here, so this module reads STL (binary or ASCII) directly:
 polygons_from_mesh turns a mesh into Polygon objects (vertices projected
 onto each polygon's plane) for DirectionalRadiosityFast.from_polygon, which
 patches quadrilateral walls in any orientation and cuts the walls of other
-vertex counts (the fine mesh's triangles) into triangular patches.  .blend
-files raise NotImplementedError.
+vertex counts (the fine mesh's triangles) into triangular patches.
 """
 import os
 import struct
@@ -80,8 +81,8 @@ def _merge_coplanar(verts, faces, angular_tolerance):
 
     edge_faces = {}
     for fi, f in enumerate(faces):
-        for k in range(3):
-            e = (min(f[k], f[(k + 1) % 3]), max(f[k], f[(k + 1) % 3]))
+        for k in range(len(f)):
+            e = (min(f[k], f[(k + 1) % len(f)]), max(f[k], f[(k + 1) % len(f)]))
             edge_faces.setdefault(e, []).append(fi)
     for fs in edge_faces.values():
         if len(fs) == 2 and normals[fs[0]] @ normals[fs[1]] >= cos_tol:
@@ -100,8 +101,8 @@ def _merge_coplanar(verts, faces, angular_tolerance):
         uses = {}
         for fi in members:
             f = faces[fi]
-            for k in range(3):
-                a, b = int(f[k]), int(f[(k + 1) % 3])
+            for k in range(len(f)):
+                a, b = int(f[k]), int(f[(k + 1) % len(f)])
                 uses.setdefault((min(a, b), max(a, b)), []).append((a, b))
         nxt = {}
         for used in uses.values():
@@ -139,12 +140,17 @@ def read_geometry_file(path, angular_tolerance=3.):
     """Fine and rough meshes of a geometry file (sparrowpy/utils/blender.py:22-97).
 
     Returns two dicts {"verts": (n, 3) array, "conn": list of vertex index
-    lists}: the file's triangles and the polygons of faces merged within
+    lists}: the file's faces and the polygons of faces merged within
     angular_tolerance degrees.
     """
     ext = os.path.splitext(str(path))[-1].lower()
     if ext == ".blend":
-        raise NotImplementedError(".blend files need Blender (bpy), which is not installed; export the model as STL")
+        from .blend import read_mesh
+        verts, faces = read_mesh(path)
+        fine = {"verts": verts, "conn": [list(map(int, f)) for f in faces]}
+        rough = {"verts": verts,
+                 "conn": [list(map(int, p)) for p in _merge_coplanar(verts, faces, angular_tolerance)]}
+        return fine, rough
     if ext != ".stl":
         raise NotImplementedError("Only .stl and .blend files are supported.")
     verts, faces = _weld(_read_stl(path))

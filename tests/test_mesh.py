@@ -1,4 +1,5 @@
-"""STL geometry import (sparrowpy/utils/blender.py; tests/test_blender_import.py).
+"""STL geometry import (sparrowpy/utils/blender.py; tests/test_blender_import.py); .blend files in
+test_blend.py.
 
 The reference reads STL through Blender and checks, for a cube, that the
 rough mesh keeps the fine mesh's vertices and has half as many faces.  The
@@ -103,11 +104,13 @@ def test_stl_room_patches(tmp_path, rotate):
     assert r.n_patches == 6 * 16
 
 
-def test_blend_files_need_blender(tmp_path):
-    with pytest.raises(NotImplementedError):
-        read_geometry_file(tmp_path / "room.blend")
+def test_other_formats_and_bad_blend_files(tmp_path):
     with pytest.raises(NotImplementedError):
         read_geometry_file(tmp_path / "room.obj")
+    bad = tmp_path / "room.blend"
+    bad.write_bytes(b"not a blend file")
+    with pytest.raises(ValueError):
+        read_geometry_file(bad)
 
 
 def _grid_triangles(cells, flip=()):
