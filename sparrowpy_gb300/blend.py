@@ -46,6 +46,8 @@ class BlendFile:
             length, = np.frombuffer(b, self.end + "i4", 1, p + 4)
             old = int(np.frombuffer(b, self.end + ("u8" if self.ptr == 8 else "u4"), 1, p + 8)[0])
             sdna, count = np.frombuffer(b, self.end + "i4", 2, p + 8 + self.ptr)
+            if length < 0 or p + head + int(length) > len(b):
+                raise ValueError(f"{path}: block at {p} runs past the end of the file")
             self.blocks.append((code, int(length), old, int(sdna), int(count), p + head))
             if code == b"ENDB":
                 break

@@ -250,6 +250,7 @@ def _messages(r, addr):
         size = r.uint(p, width)
         p += width
         blocks = [(p, p + size)]
+        seen_blocks = set()
         hdr = 6 if flags & 0x04 else 4
         while blocks:
             p, end = blocks.pop(0)
@@ -258,6 +259,9 @@ def _messages(r, addr):
                 d = p + hdr
                 if mtype == 0x10:
                     c, n = r.off(d), r.length(d + r.so)
+                    if c in seen_blocks or c + n > len(r.b):
+                        raise ValueError(f"HDF5: bad continuation block at {c:#x}")
+                    seen_blocks.add(c)
                     r.sig(c, b"OCHK")
                     blocks.append((c + 4, c + n - 4))
                 elif mtype:
@@ -268,7 +272,7 @@ def _messages(r, addr):
         raise NotImplementedError(f"HDF5: object header version {r.b[addr]}")
     nmsg, size = r.uint(addr + 2, 2), r.uint(addr + 8, 4)
     blocks = [(addr + 16, addr + 16 + size)]
-    seen = 0
+    seen, seen_blocks = 0, set()
     while blocks and seen < nmsg:
         p, end = blocks.pop(0)
         while p + 8 <= end and seen < nmsg:
@@ -276,7 +280,11 @@ def _messages(r, addr):
             d = p + 8
             seen += 1
             if mtype == 0x10:
-                blocks.append((r.off(d), r.off(d) + r.length(d + r.so)))
+                c, n = r.off(d), r.length(d + r.so)
+                if c in seen_blocks or c + n > len(r.b):
+                    raise ValueError(f"HDF5: bad continuation block at {c:#x}")
+                seen_blocks.add(c)
+                blocks.append((c, c + n))
             elif mtype:
                 out.append((mtype, d, msize, mflags))
             p = d + msize
@@ -442,10 +450,12 @@ class Dataset:
             out[dst] = block[src]
         return out.tobytes()
 
-    def _btree1_chunks(self, addr, nd, chunks):
+    def _btree1_chunks(self, addr, nd, chunks, parent_level=None):
         r = self._f.r
         r.sig(addr, b"TREE")
         level, used = r.b[addr + 5], r.uint(addr + 6, 2)
+        if parent_level is not None and level >= parent_level:
+            raise ValueError("HDF5: chunk B-tree levels do not decrease")
         p = addr + 8 + 2 * r.so
         ksize = 8 + 8 * nd
         for i in range(used):
@@ -455,7 +465,7 @@ class Dataset:
             if level == 0:
                 chunks.append((offs, child, size, mask))
             else:
-                self._btree1_chunks(child, nd, chunks)
+                self._btree1_chunks(child, nd, chunks, level)
             p += ksize + r.so
 
     def _fixed_array_chunks(self, addr, shape, cdims, chunks):
@@ -600,15 +610,17 @@ class File:
                 self._symbol_table(r.off(d), _local_heap_data(r, r.off(d + r.so)), links)
         return links
 
-    def _symbol_table(self, addr, heap_data, links):
+    def _symbol_table(self, addr, heap_data, links, parent_level=None):
         r = self.r
         r.sig(addr, b"TREE")
         level, used = r.b[addr + 5], r.uint(addr + 6, 2)
+        if parent_level is not None and level >= parent_level:
+            raise ValueError("HDF5: group B-tree levels do not decrease")
         p = addr + 8 + 2 * r.so + r.sl
         for _ in range(used):
             child = r.off(p)
             if level > 0:
-                self._symbol_table(child, heap_data, links)
+                self._symbol_table(child, heap_data, links, level)
             else:
                 r.sig(child, b"SNOD")
                 n = r.uint(child + 6, 2)
