@@ -2,7 +2,7 @@
 
 Drop-in for ``sparrowpy.DirectionalRadiosityFast``; see radiosity.py.
 """
-from . import brdf, geometry, kang, mesh, sofa, sound_object
+from . import brdf, form_factor, geometry, kang, mesh, sofa, sound_object, testing, utils
 from .coords import Coordinates, FrequencyData, TimeData
 from .geometry import Polygon, shoebox_room_stub
 from .kang import DirectionalRadiosityKang, PatchesDirectionalKang, PatchesKang, RadiosityKang
@@ -13,5 +13,5 @@ __version__ = "0.1.0"
 __all__ = [
     "DirectionalRadiosityFast", "Polygon", "shoebox_room_stub", "Coordinates", "FrequencyData", "TimeData",
     "brdf", "geometry", "sound_object", "analyse_brdf", "kang", "mesh", "sofa", "PatchesKang", "RadiosityKang",
-    "PatchesDirectionalKang", "DirectionalRadiosityKang",
+    "PatchesDirectionalKang", "DirectionalRadiosityKang", "form_factor", "testing", "utils",
 ]
