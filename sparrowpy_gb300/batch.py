@@ -216,6 +216,14 @@ class PreparedWave:
             self.rooms[q].ws_bytes = wsz
         self.bsz = nat.size("sp_exchange_batch_workspace", len(rooms))
         self.bws = torch.empty((self.bsz,), dtype=torch.uint8, device=dev)
+        # what sp_exchange_batch takes: FP32 rooms of one shape (directions, bands, bins) whose histogram
+        # length is a multiple of 4 below 65536, in the structured, slot-wise or material exchange; other
+        # waves run the rooms' own launches
+        a0 = self.args[0]
+        self.persistent_ok = nt % 4 == 0 and nt <= 65535 and all(
+            a.precision == nat.SP_F32 and a.n_dir_pairs > 0 and
+            a.algorithm in (nat.SP_EXCHANGE_STRUCTURED, nat.SP_EXCHANGE_SLOTWISE, nat.SP_EXCHANGE_MATERIAL) and
+            (a.n_dirs, a.n_bins) == (a0.n_dirs, a0.n_bins) for a in self.args)
 
     def launch(self, choice, orders=None, wait_limit=0, force_timeout=False):
         """Run `orders` orders of every room in one launch (placing E_0 and E_total again, plans reused, unless
@@ -333,7 +341,12 @@ def solve_rooms_batched(rooms, speed_of_sound=343.0, etc_time_resolution=1e-3, e
         n_max = max(r.n_patches for r in pw.objs)
         nd, nb = pw.objs[0]._dev["e0dir"].shape[1:]
         key = BatchTuner.shape_class(nd, nb, nt, n_max)
-        choice = force_choice or tuner.choose(key, probe, K)
+        if force_choice:
+            choice = force_choice
+        elif not pw.persistent_ok:
+            choice = BatchTuner.ROOMS
+        else:
+            choice = tuner.choose(key, probe, K)
         e[0].record(st)
         rc, ms_exchange, items = pw.launch(choice)
         if rc != nat.SP_OK:

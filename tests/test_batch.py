@@ -77,3 +77,19 @@ def test_persistent_batch_bounded_wait_reports_timeout():
     ref, _, _ = solve_rooms(rooms, etc_duration=0.06, max_reflection_order=6)
     for a, b in zip(pw.results(rooms), ref):
         assert rel_l2(a, b) < 1e-6
+
+
+def test_batch_of_mixed_shapes_runs_room_by_room():
+    """Rooms of different direction counts in one wave, and a histogram length that is not a multiple of 4:
+    the persistent launch does not take them, so the wave runs the rooms' own launches; the histograms equal
+    the rooms solved one after another (rel L2 <= 1e-6)."""
+    from sparrowpy_gb300.batch import BatchTuner, shoebox_rooms, solve_rooms, solve_rooms_batched
+    rooms = _rooms(2) + shoebox_rooms(1, seed=5, patch_size=0.5, dims_range=(1.5, 3.0), n_dirs=16, n_bins=2,
+                                      n_receivers=2)
+    for dur, sub in ((0.06, rooms), (0.061, rooms[:2])):
+        ref, _, _ = solve_rooms(sub, etc_duration=dur, max_reflection_order=5)
+        tuner = BatchTuner()
+        got, stats = solve_rooms_batched(sub, etc_duration=dur, max_reflection_order=5, tuner=tuner)
+        assert [w["mode"] for w in stats["waves"]] == ["rooms"] and not tuner.timings
+        for a, b in zip(got, ref):
+            assert rel_l2(a, b) < 1e-6
