@@ -415,6 +415,11 @@ class DirectionalRadiosityFast:
     @classmethod
     def from_polygon(cls, polygon_list, patch_size, *, precision="fp32", device=None):
         """Create the object from wall polygons (RadiosityFast.py:340-367)."""
+        counts = sorted({p.pts.shape[0] for p in polygon_list})
+        if len(counts) > 1:
+            raise ValueError(f"walls of different vertex counts {counts}: the wall arrays hold one count (as the "
+                             "reference's); split the walls into polygons of one count, e.g. the triangles of a "
+                             "mesh's fine version")
         walls_points = np.array([p.pts for p in polygon_list])
         walls_normal = np.array([p.normal for p in polygon_list])
         walls_up_vector = np.array([p.up_vector for p in polygon_list])

@@ -142,3 +142,12 @@ def test_bake_rejects_unsupported_vertex_counts():
     r = DirectionalRadiosityFast(walls, np.array([[0, 0, 1.0]]), np.array([[1.0, 0, 0]]), nine[None], 1, [0])
     with pytest.raises(NotImplementedError):
         r.bake_geometry()
+
+
+def test_walls_of_mixed_vertex_counts_are_refused():
+    from sparrowpy_gb300 import DirectionalRadiosityFast
+    from sparrowpy_gb300.geometry import Polygon
+    quad = Polygon([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], [1, 0, 0], [0, 0, 1])
+    tri = Polygon([[0, 0, 1], [0, 1, 1], [1, 0, 1]], [0, 1, 0], [0, 0, -1])
+    with pytest.raises(ValueError, match="vertex counts"):
+        DirectionalRadiosityFast.from_polygon([quad, tri], 0.5)
