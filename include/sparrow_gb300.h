@@ -517,6 +517,25 @@ int sp_kang_directional_receiver(int n, const double* centers, const double* nor
                                  double speed_of_sound, double sampling_rate, int n_dirs, const int32_t* dir_idx,
                                  double* out, int* err, void* stream);
 
+/* The Kang closed forms of form_factor/kang.py on arbitrary axis-aligned
+ * patches (centres, normals (n, 3); sizes (n, size_cols), size_cols 2 or 3,
+ * Polygon.size).  Replaces kang.py:12-169 `patch2patch_ff_kang`: ff (n_pairs)
+ * of the listed (source, receiver) pairs (pairs (n_pairs, 2)). */
+int sp_kang_pair_form_factors(long long n_pairs, const int32_t* pairs, int n, const double* centers,
+                              const double* normals, const double* sizes, int size_cols, double* ff, void* stream);
+
+/* Replaces kang.py:171-262 `_source2patch_energy_kang`: energy (n, nb) and
+ * distance (n) of each patch from the point source src (3); attenuation
+ * (nb) may be NULL (no air attenuation).  sizes (n, 3).  `err` receives 3
+ * for a patch whose normal is not along an axis. */
+int sp_kang_point_source(int n, const double* src, const double* centers, const double* normals, const double* sizes,
+                         int nb, const double* attenuation, double* energy, double* distance, int* err,
+                         void* stream);
+
+/* Replaces kang.py:264-277 `_patch2receiver_energy_kang`: factor (n) of each
+ * patch for its patch-to-receiver vector (vectors (n, 3)). */
+int sp_kang_point_receiver(int n, const double* vectors, const double* normals, double* factor, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

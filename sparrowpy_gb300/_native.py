@@ -141,6 +141,9 @@ _SIGS = {
     "sp_kang_directional_exchange": (I, [I, I, I, I, I, P, P, P, P, P, I, P, P, P, LL, LL, D, D, I, P, P, P, SZ, P,
                                          P]),
     "sp_kang_directional_receiver": (I, [I, P, P, I, I, I, P, I, P, P, D, D, I, P, P, P, P]),
+    "sp_kang_pair_form_factors": (I, [LL, P, I, P, P, P, I, P, P]),
+    "sp_kang_point_source": (I, [I, P, P, P, P, I, P, P, P, P, P]),
+    "sp_kang_point_receiver": (I, [I, P, P, P, P]),
 }
 
 

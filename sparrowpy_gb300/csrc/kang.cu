@@ -241,6 +241,117 @@ __global__ void k_kang_receiver(int n, const double* __restrict__ centers, const
     *o = xadd(*o, resp);
 }
 
+// form_factor/kang.py:12-169 `patch2patch_ff_kang`: one listed (source,
+// receiver) pair per thread over arbitrary axis-aligned patches; sizes is
+// (n, size_cols), size_cols 2 or 3 as the reference's patches_size.
+__global__ void k_ff_kang_pairs(long long n_pairs, const int32_t* __restrict__ pairs, const double* __restrict__ ctr,
+                                const double* __restrict__ nrm, const double* __restrict__ size, int size_cols,
+                                double* __restrict__ ff) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    const int i = pairs[2 * q], j = pairs[2 * q + 1];
+    const double* sc = ctr + 3 * i;
+    const double* sn = nrm + 3 * i;
+    const double* rc = ctr + 3 * j;
+    const double* rn = nrm + 3 * j;
+    const double* sz = size + (size_t)size_cols * i;
+    const double dot = xadd(xadd(xmul(rn[0], sn[0]), xmul(rn[1], sn[1])), xmul(rn[2], sn[2]));
+    double out = 0.0;
+    if (dot == 0.0) {  // orthogonal (kang.py:44-120)
+        int s_lo, s_hi;  // the source's in-plane axes, as the set idx_source
+        double dl, dd_l, dd_m;
+        if (fabs(sn[0]) > 1e-5) {
+            s_lo = 1, s_hi = 2, dl = sc[2], dd_l = sz[2], dd_m = sz[1];
+        } else if (fabs(sn[1]) > 1e-5) {
+            s_lo = 0, s_hi = 2, dl = sc[2], dd_l = sz[2], dd_m = sz[0];
+        } else {  // |sn[2]| > 1e-5, checked by the host
+            s_lo = 0, s_hi = 1, dl = sc[1], dd_l = sz[1], dd_m = sz[0];
+        }
+        const bool has0 = s_lo == 0, has1 = s_lo == 1 || s_hi == 1;
+        int il, is, ir;
+        if (fabs(rn[0]) > 1e-5)
+            il = has1 ? 1 : 2, is = 0, ir = has1 ? 2 : 1;
+        else if (fabs(rn[1]) > 1e-5)
+            il = has0 ? 0 : 2, is = 1, ir = has0 ? 2 : 0;
+        else
+            il = has0 ? 0 : 1, is = 2, ir = has0 ? 1 : 0;
+        const double dm = fabs(xsub(sc[is], rc[is]));
+        dl = sc[il];
+        const double dlp = rc[il];
+        const double dnp = fabs(xsub(sc[ir], rc[ir]));
+        const double hm = xmul(0.5, dd_m), hl = xmul(0.5, dd_l);
+        const double A = xdiv(xsub(dm, hm), __dsqrt_rn(xadd(xadd(sq(xsub(dl, dlp)), sq(xsub(dm, hm))), sq(dnp))));
+        const double B = xdiv(xadd(dm, hm), __dsqrt_rn(xadd(xadd(sq(xsub(dl, dlp)), sq(xadd(dm, hm))), sq(dnp))));
+        const double one = atan(fabs(xdiv(xsub(xsub(dl, hl), dlp), dnp)));
+        const double two = atan(fabs(xdiv(xsub(xadd(dl, hl), dlp), dnp)));
+        const double k = fabs(xsub(dl, dlp)) < 1e-12 ? -1.0 : 1.0;
+        const double theta = fabs(xsub(one, xmul(k, two)));
+        out = xmul(xmul(xdiv(1.0, 2 * SP_PI), fabs(xsub(sq(A), sq(B)))), theta);
+    } else {  // parallel (kang.py:122-166), axes by the receiver's normal
+        int a, m, b, cl, cn;
+        if (fabs(rn[0]) > 1e-5)
+            a = 1, m = 0, b = 2, cl = 1, cn = size_cols > 2 ? 2 : 1;
+        else if (fabs(rn[1]) > 1e-5)
+            a = 0, m = 1, b = 2, cl = 0, cn = size_cols > 2 ? 2 : 1;
+        else
+            a = 1, m = 2, b = 0, cl = 1, cn = 0;
+        const double d = __dsqrt_rn(xadd(xadd(sq(xsub(rc[a], sc[a])), sq(xsub(rc[b], sc[b]))), sq(xsub(rc[m], sc[m]))));
+        out = xdiv(xmul(xmul(sz[cl], sz[cn]), sq(xsub(rc[m], sc[m]))), xmul(SP_PI, pow(d, 4.0)));
+    }
+    ff[q] = out;
+}
+
+// form_factor/kang.py:171-262 `_source2patch_energy_kang`: one patch per
+// thread; energy (n, nb) = |sin_phi_delta - sin_phi| beta / (4 pi), times
+// exp(-att_b d) when att is given; distance (n) in the patch's frame.
+__global__ void k_kang_point_source(int n, const double* __restrict__ src, const double* __restrict__ ctr,
+                                    const double* __restrict__ nrm, const double* __restrict__ size, int nb,
+                                    const double* __restrict__ att, double* __restrict__ energy,
+                                    double* __restrict__ distance, int* __restrict__ err) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double s[3] = {src[0], src[1], src[2]};
+    double r[3] = {ctr[3 * j], ctr[3 * j + 1], ctr[3 * j + 2]};
+    const double* nj = nrm + 3 * j;
+    int ax, idx[3];
+    if (fabs(nj[2]) > 0.99) {
+        ax = 2, idx[0] = 0, idx[1] = 1, idx[2] = 2;
+    } else if (fabs(nj[1]) > 0.99) {
+        ax = 1, idx[0] = 2, idx[1] = 0, idx[2] = 1;
+    } else if (fabs(nj[0]) > 0.99) {
+        ax = 0, idx[0] = 1, idx[1] = 2, idx[2] = 0;
+    } else {
+        atomicCAS(err, 0, 3);  // not aligned with an axis
+        return;
+    }
+    const double off = r[ax];
+    s[ax] = fabs(xsub(s[ax], off));
+    r[ax] = fabs(xsub(r[ax], off));
+    const double* sz = size + 3 * j;
+    double dphi, beta;
+    kang_init_geom(r[idx[0]], r[idx[1]], r[idx[2]], sz[idx[0]], sz[idx[1]], s[idx[0]], s[idx[1]], s[idx[2]], &dphi,
+                   &beta);
+    const double d = __dsqrt_rn(xadd(xadd(sq(xsub(r[idx[0]], s[idx[0]])), sq(xsub(r[idx[1]], s[idx[1]]))),
+                                     sq(xsub(r[idx[2]], s[idx[2]]))));
+    distance[j] = d;
+    const double e = xdiv(xmul(dphi, beta), 4 * SP_PI);
+    for (int b = 0; b < nb; ++b) energy[(size_t)j * nb + b] = att ? xmul(e, exp(xmul(-att[b], d))) : e;
+}
+
+// form_factor/kang.py:264-277 `_patch2receiver_energy_kang`: one patch per
+// thread; factor = |n . |v|| / R / (pi R^2) for the patch-to-receiver vector v.
+__global__ void k_kang_point_receiver(int n, const double* __restrict__ vec, const double* __restrict__ nrm,
+                                      double* __restrict__ factor) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* v = vec + 3 * i;
+    const double* ni = nrm + 3 * i;
+    const double R = __dsqrt_rn(xadd(xadd(sq(v[0]), sq(v[1])), sq(v[2])));
+    const double cos_xi =
+        xdiv(fabs(xadd(xadd(xmul(ni[0], fabs(v[0])), xmul(ni[1], fabs(v[1]))), xmul(ni[2], fabs(v[2])))), R);
+    factor[i] = xdiv(cos_xi, xmul(SP_PI, sq(R)));
+}
+
 // Launchers shared by the plain and the directional entry points.
 template <bool kDir>
 int kang_init(int n, const double* centers, const double* sizes, const double* normal, const double* src,
@@ -382,6 +493,36 @@ int sp_kang_directional_receiver(int n, const double* centers, const double* nor
                                  double* out, int* err, void* stream) {
     return kang_receiver<true>(n, centers, normal, nb, n_orders, nt, E, max_order, receiver, attenuation,
                                speed_of_sound, sampling_rate, n_dirs, dir_idx, out, err, stream);
+}
+
+int sp_kang_pair_form_factors(long long n_pairs, const int32_t* pairs, int n, const double* centers,
+                              const double* normals, const double* sizes, int size_cols, double* ff, void* stream) {
+    if (n_pairs < 0 || n < 0 || (size_cols != 2 && size_cols != 3)) return SP_ERR_ARG;
+    if (n_pairs == 0) return SP_OK;
+    if (!pairs || !centers || !normals || !sizes || !ff) return SP_ERR_ARG;
+    k_ff_kang_pairs<<<sp_blocks(n_pairs, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(n_pairs, pairs, centers,
+                                                                                             normals, sizes, size_cols, ff);
+    return sp_check_launch();
+}
+
+int sp_kang_point_source(int n, const double* src, const double* centers, const double* normals, const double* sizes,
+                         int nb, const double* attenuation, double* energy, double* distance, int* err,
+                         void* stream) {
+    if (n < 0 || nb < 1) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!src || !centers || !normals || !sizes || !energy || !distance || !err) return SP_ERR_ARG;
+    k_kang_point_source<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(
+        n, src, centers, normals, sizes, nb, attenuation, energy, distance, err);
+    return sp_check_launch();
+}
+
+int sp_kang_point_receiver(int n, const double* vectors, const double* normals, double* factor, void* stream) {
+    if (n < 0) return SP_ERR_ARG;
+    if (n == 0) return SP_OK;
+    if (!vectors || !normals || !factor) return SP_ERR_ARG;
+    k_kang_point_receiver<<<sp_blocks(n, 128), 128, 0, sp_counted((cudaStream_t)stream)>>>(n, vectors, normals,
+                                                                                              factor);
+    return sp_check_launch();
 }
 
 }  // extern "C"
