@@ -102,8 +102,11 @@ def _patch2receiver_energy_universal(receiver_pos, patches_points, receiver_visi
     rcv, c, p = (_dev(np.asarray(receiver_pos, float).reshape(3), torch.float64), _dev(ctr, torch.float64),
                  _dev(pts, torch.float64))
     v = _dev(vis.astype(np.uint8), torch.uint8)
-    nat.call("sp_receiver_factors", _ptr(rcv), n, _ptr(c), _ptr(p), nv, _ptr(v), _ptr(_dev(np.zeros(n), torch.int32)),
-             1, _ptr(_dev(np.array([[[0.0, 0.0, 1.0]]]), torch.float64)), _ptr(rfac), _ptr(ridx), _ptr(dist),
-             _stream())
+    # every device array is held in a local until the results are read: a temporary freed before the launch
+    # could hand its memory to the next allocation, whose copy would then overwrite it
+    wall = _dev(np.zeros(n), torch.int32)
+    dirs = _dev(np.array([[[0.0, 0.0, 1.0]]]), torch.float64)
+    nat.call("sp_receiver_factors", _ptr(rcv), n, _ptr(c), _ptr(p), nv, _ptr(v), _ptr(wall), 1, _ptr(dirs),
+             _ptr(rfac), _ptr(ridx), _ptr(dist), _stream())
     out[vis] = rfac.cpu().numpy()[vis]
     return out

@@ -161,7 +161,8 @@ class PatchesKang(Polygon):
             return
         g = self._geometry()
         rc, rn, rw = (_dev(np.concatenate(x)) for x in (cols_c, cols_n, cols_w))
-        nat.call("sp_kang_form_factors", n, _ptr(g["centers"]), _ptr(g["normal"]), _ptr(_dev(self.center)), n_r,
+        wc = _dev(self.center)  # held until the call has been enqueued and the result read
+        nat.call("sp_kang_form_factors", n, _ptr(g["centers"]), _ptr(g["normal"]), _ptr(wc), n_r,
                  _ptr(rc), _ptr(rn), _ptr(rw), float(self.max_size), _ptr(self._ff), _stream())
 
     def get_form_factor(self, patches_list, source_path_id, receiver_wall_id, receiver_patch_id):
