@@ -74,12 +74,15 @@ def test_gpu_universal_point_factors(gold):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method", ["universal", "kang"])
+@pytest.mark.parametrize("method", ["universal"])
 @pytest.mark.parametrize("src", [[2., 0, 0], [2., 2., 0], [2., 0., 2.]])
 @pytest.mark.parametrize("rec", [[1., 0., 0], [2., -2., 0], [2., 0., -2.]])
 def test_gpu_reciprocity_point_source_patch_receiver(src, rec, method):
     """tests/test_multisource.py:140-213: swapping source and receiver around one 2 x 2 m patch gives the same
-    source-energy times receiver-factor product (6 decimals, the reference's assert_array_almost_equal)."""
+    source-energy times receiver-factor product (6 decimals, the reference's assert_array_almost_equal).
+
+    The reference runs it with its default method="universal" only; its Kang branch is not reciprocal here
+    (the reference's own Kang functions give 0.0210 against 0.0141 for the first case, as these do)."""
     from sparrowpy_gb300.form_factor import kang, universal
     from sparrowpy_gb300.geometry import Polygon
     wall = Polygon([[0, -1, -1], [0, -1, 1], [0, 1, 1], [0, 1, -1]], [0, 0, 1], [1, 0, 0])
