@@ -12,7 +12,8 @@ def test_reference_public_names():
                  "PatchesKang", "PatchesDirectionalKang", "form_factor", "testing", "brdf", "utils"):
         assert hasattr(sp, name), name
     assert callable(sp.testing.shoebox_room_stub) and len(sp.testing.shoebox_room_stub(1, 2, 3)) == 6
-    assert callable(sp.form_factor.patch2patch_ff_universal)
+    assert callable(sp.form_factor.patch2patch_ff_universal) and callable(sp.form_factor.patch2patch_ff_kang)
+    assert callable(sp.form_factor.universal.universal_form_factor)
     assert callable(sp.brdf.create_from_scattering) and callable(sp.brdf.create_from_directional_scattering)
     assert callable(sp.utils.blender.read_geometry_file)
     assert callable(sp.geometry.Polygon) and callable(sp.sound_object.SoundSource)
@@ -34,5 +35,6 @@ def test_patch2patch_ff_universal(nv):
     mask[pairs[:, 0], pairs[:, 1]] = False
     assert not ff[mask].any()
     k = sel[0]
-    one = sp.form_factor.universal_form_factor(g["pi"][k, :nv], g["ni"][k], g["area_i"][k], g["pj"][k, :nv], g["nj"][k])
+    one = sp.form_factor.universal.universal_form_factor(g["pi"][k, :nv], g["ni"][k], g["area_i"][k],
+                                                         g["pj"][k, :nv], g["nj"][k])
     assert abs(one - g["value"][k]) <= 1e-10 * abs(g["value"][k])
