@@ -6,7 +6,10 @@ import torch
 
 
 def dev(a, dtype=torch.float64):
-    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device="cuda")
+    a = np.ascontiguousarray(a)
+    if not a.flags.writeable:  # e.g. a broadcast view: torch wants memory it may write
+        a = a.copy()
+    return torch.as_tensor(a, dtype=dtype, device="cuda")
 
 
 def ptr(t):
