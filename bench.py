@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Benchmark: milliseconds per solve (bake + exchange) of the street-canyon workload.
 
-Workload (default ``--config cfg3``): two 100 x 20 m facades 15 m apart and a
+Workload (default ``--config street_canyon_5939``): two 100 x 20 m facades 15 m apart and a
 100 x 15 m ground, 1 m patches, 40 seeded box occluders (5939 patches, one
 wall per patch), 8 octave bands, 32 directions, per-patch/per-band
 absorption U[0.01, 0.3], scattering 0.3, 1 source and 8 receivers, 1 ms x
@@ -54,17 +54,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--config", default="cfg3")
+    ap.add_argument("--config", default="street_canyon_5939")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--max-order", type=int, default=None, help="override the workload's reflection order")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU comparison solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-fwd-bwd", action="store_true", help="skip the gradient (forward + backward) leg")
-    ap.add_argument("--no-configs", action="store_true", help="skip the cfg1 / cfg2 legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the shoebox_126 / shoebox_2016 legs")
     ap.add_argument("--no-kahan", action="store_true", help="skip the plain-sum solves that time the Kahan cost")
     ap.add_argument("--batch-rooms", type=int, default=256,
-                    help="seeded shoebox rooms for the batch leg (cfg5: 256; 0: skip)")
+                    help="seeded shoebox rooms for the batch leg (256 by default; 0: skip)")
     ap.add_argument("--leg", default=None, choices=["general", "batch"],
                     help="print only one leg as one JSON line (profiling runs)")
     ap.add_argument("--general-patch", type=float, default=0.25,
@@ -255,8 +255,8 @@ def cpu_baseline(cfg, rows_per_thread=1, exchange_rows=8):
     return total * 1e3, threads, desc
 
 
-def cpu_full_solve_cfg1():
-    """One complete oracle solve of the 126-patch shoebox (cfg1), timed, no extrapolation.
+def cpu_full_solve_shoebox_126():
+    """One complete oracle solve of the 126-patch shoebox, timed, no extrapolation.
 
     Bake (visibility and form factors on every host thread, as the
     reference's parallel numba loops), source energy, the 20 exchange orders
@@ -266,7 +266,7 @@ def cpu_full_solve_cfg1():
     from oracle import oracle as orc
     from oracle.scene import scene_from_radiosity
     from sparrowpy_gb300 import scenes
-    cfg = scenes.config("cfg1", precision="fp64")
+    cfg = scenes.config("shoebox_126", precision="fp64")
     sc = scene_from_radiosity(cfg["radiosity"])
     threads = orc.num_threads()
     src, rcv = cfg["source"], cfg["receivers"]
@@ -283,7 +283,7 @@ def cpu_full_solve_cfg1():
     t2 = time.perf_counter()
     mono = orc.collect(sc, bk, etot, rcv, cfg["c"], cfg["dt"])
     t3 = time.perf_counter()
-    desc = (f"complete oracle FP64 solve of cfg1 (126 patches, {bk['src'].size} directed pairs, 16 directions, "
+    desc = (f"complete oracle FP64 solve of the 126-patch shoebox ({bk['src'].size} directed pairs, 16 directions, "
             f"1 band, T={nt}, order {cfg['max_order']}): bake + source {1e3 * (t1 - t0):.0f} ms on {threads} threads, "
             f"exchange {1e3 * (t2 - t1):.0f} ms on 1 thread, collection {1e3 * (t3 - t2):.0f} ms")
     return 1e3 * (t2 - t0), threads, desc, mono
@@ -327,8 +327,10 @@ def workload_config(name, cfg, world):
     nt = int(round(cfg["duration"] / cfg["dt"]))
     nb = len(r._frequencies)
     nd = r._brdf_outgoing_directions[0].cartesian.reshape(-1, 3).shape[0]
-    desc = {"cfg3": "street canyon: 100 x 20 m facades 15 m apart + 100 x 15 m ground, 1 m patches, 40 box occluders",
-            "canyon_small": "street canyon: 30 x 20 m facades 15 m apart + ground, 1 m patches, 10 box occluders"}
+    desc = {"street_canyon_5939": "street canyon: 100 x 20 m facades 15 m apart + 100 x 15 m ground, 1 m patches, "
+                                  "40 box occluders",
+            "street_canyon_1759": "street canyon: 30 x 20 m facades 15 m apart + ground, 1 m patches, "
+                                  "10 box occluders"}
     return {"workload": f"{desc.get(name, name)}; {r.n_patches} patches, {nb} bands, {nd} directions, "
                         f"{nt} x {cfg['dt'] * 1e3:g} ms bins, reflection order {cfg['max_order']}, 1 source",
             "name": name, "patches": r.n_patches, "bands": nb, "directions": nd, "bins": nt,
@@ -496,8 +498,8 @@ def run_gpu(args):
         r._bake = None
         torch.cuda.empty_cache()
         try:
-            cfg1_cpu = None if args.no_cpu else cpu_full_solve_cfg1()
-            configs = config_legs(cfg1_cpu)
+            shoebox_126_cpu = None if args.no_cpu else cpu_full_solve_shoebox_126()
+            configs = config_legs(shoebox_126_cpu)
         except Exception as exc:  # the config legs must not hide the solve result
             configs = {"error": f"{type(exc).__name__}: {exc}"}
 
@@ -521,8 +523,8 @@ def run_gpu(args):
         try:
             ms_cpu, cores, desc = cpu_baseline(cfg, rows_per_thread=2)
             cpu = {"value": ms_cpu, "unit": "ms/solve", "cores": cores, "kind": "port", "sample": desc}
-            if configs and "cfg1" in configs and "cpu_measured" in configs["cfg1"]:
-                cpu["measured_cfg1"] = configs["cfg1"]["cpu_measured"]
+            if configs and "shoebox_126" in configs and "cpu_measured" in configs["shoebox_126"]:
+                cpu["measured_shoebox_126"] = configs["shoebox_126"]["cpu_measured"]
         except Exception as exc:  # the CPU leg must not hide the GPU result
             cpu = {"value": None, "unit": "ms/solve", "cores": None, "kind": "port", "sample": f"failed: {exc}"}
 
@@ -619,19 +621,19 @@ def _triangle_leg(cfg):
     return out
 
 
-def config_legs(cpu_cfg1=None):
-    """cfg1 and cfg2 at FP32 and FP64 on the GPU, with their errors and the FP64 energy check.
+def config_legs(cpu_shoebox_126=None):
+    """shoebox_126 and shoebox_2016 at FP32 and FP64 on the GPU, with their errors and the FP64 energy check.
 
-    cfg1 (126 patches) is also solved completely by the oracle on the host
-    (cpu_cfg1: the result of cpu_full_solve_cfg1), which gives the error
-    against the FP64 oracle and a measured CPU/GPU ratio; cfg2 (2016 patches)
+    shoebox_126 (126 patches) is also solved completely by the oracle on the host
+    (cpu_shoebox_126: the result of cpu_full_solve_shoebox_126), which gives the error
+    against the FP64 oracle and a measured CPU/GPU ratio; shoebox_2016 (2016 patches)
     is too large for a complete oracle solve, so its FP32 error is stated
     against the FP64 GPU solve (itself oracle-checked at 1e-10 on smaller
     scenes).
     """
     import torch
     out = {}
-    for name in ("cfg1", "cfg2"):
+    for name in ("shoebox_126", "shoebox_2016"):
         leg = {}
         ms32, m32, r32 = _gpu_solve_timed(name, "fp32")
         eb32 = r32.energy_balance()
@@ -648,10 +650,10 @@ def config_legs(cpu_cfg1=None):
                                  "check_ms": eb32["ms"],
                                  "meaning": "per-band FP64 sum of E_total against the time-free energy budget of "
                                             "the orders; nothing is delayed past this histogram"})
-        if name == "cfg2":
+        if name == "shoebox_2016":
             leg["triangles"] = _triangle_leg(name)
-        if name == "cfg1" and cpu_cfg1 is not None:
-            cpu_ms, cores, desc, mono_ref = cpu_cfg1
+        if name == "shoebox_126" and cpu_shoebox_126 is not None:
+            cpu_ms, cores, desc, mono_ref = cpu_shoebox_126
             leg.update(receiver_rel_l2_fp32_vs_oracle=float(np.linalg.norm(m32 - mono_ref) / np.linalg.norm(mono_ref)),
                        receiver_rel_l2_fp64_vs_oracle=float(np.linalg.norm(m64 - mono_ref) / np.linalg.norm(mono_ref)),
                        cpu_measured={"ms": cpu_ms, "cores": cores, "sample": desc},
@@ -662,7 +664,7 @@ def config_legs(cpu_cfg1=None):
 
 # ------------------------------------------------------------ general BRDF
 def general_brdf_leg(orders=50, dense_orders=5, patch_size=0.25):
-    """A table without diffuse-plus-mirror structure on every wall: cfg2's geometry and histogram.
+    """A table without diffuse-plus-mirror structure on every wall: the 2016-patch shoebox's geometry and histogram.
 
     5 x 6 x 3 m shoebox at 0.25 m (2016 patches), one seeded random positive
     64 x 64 x 6 table (as create_from_directional_scattering tables are
@@ -685,7 +687,7 @@ def general_brdf_leg(orders=50, dense_orders=5, patch_size=0.25):
         r.set_wall_brdf(np.arange(r.n_walls), FrequencyData(tab, np.asarray(r._frequencies, float)), dirs, dirs)
         return r
 
-    out = {"workload": f"cfg2's 5 x 6 x 3 m shoebox at {patch_size} m patches, a seeded random positive 64 x 64 x 6 "
+    out = {"workload": f"the 5 x 6 x 3 m shoebox at {patch_size} m patches, a seeded random positive 64 x 64 x 6 "
                        "BRDF table on every wall, 6 bands, T=2000, FP32"}
     monos = {}
     for name, algo, tc, k in (("general_tensor_cores", "general", True, orders),
@@ -725,8 +727,8 @@ def fwd_bwd_config4(steps=2, fd_params=64, seed=4, fp64_reference=True):
         adjoint), against which every one of the 24,192 FP32 gradients is
         compared;
       * central differences (h = 1e-4) of the FP64 forward on `fd_params`
-        seeded random parameters, on the same materials model over config
-        1's geometry (the 5 x 6 x 3 m room at 1 m patches, 126 patches, same
+        seeded random parameters, on the same materials model over the
+        126-patch shoebox (the 5 x 6 x 3 m room at 1 m patches, same
         bands, directions, histogram and order): 128 FP64 solves there take
         seconds, where the 2016-patch room's would take about 15 minutes.
     """
@@ -795,15 +797,15 @@ def fwd_bwd_config4(steps=2, fd_params=64, seed=4, fp64_reference=True):
             "rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
             "max_rel_err_where_grad_above_1e-3_max": float((np.abs(g32 - g64)[big] / np.abs(g64)[big]).max())}
     if fd_params > 0:
-        out["fd_check"] = fd_check_cfg1_geometry(fd_params, seed=seed + 1)
+        out["fd_check"] = fd_check_shoebox_126_geometry(fd_params, seed=seed + 1)
     return out
 
 
-def fd_check_cfg1_geometry(n_params, seed=5, h=1e-4):
+def fd_check_shoebox_126_geometry(n_params, seed=5, h=1e-4):
     """FP32 and FP64 adjoint gradients against central differences of the FP64 forward (h = 1e-4).
 
-    Per-patch materials over config 1's geometry (5 x 6 x 3 m, 1 m patches,
-    126 patches), 6 bands, 64 directions, T = 2000, order 50; `n_params`
+    Per-patch materials over the 126-patch shoebox (5 x 6 x 3 m, 1 m
+    patches), 6 bands, 64 directions, T = 2000, order 50; `n_params`
     seeded random (absorption or scattering, patch, band) entries.
     """
     import torch
@@ -843,7 +845,7 @@ def fd_check_cfg1_geometry(n_params, seed=5, h=1e-4):
     a64 = np.array([e["adjoint_fp64"] for e in entries])
     a32 = np.array([e["adjoint_fp32"] for e in entries])
     scale = np.abs(fd).max()
-    return {"workload": "per-patch materials over cfg1's geometry (5x6x3 m, 1 m patches: 126 patches), 6 bands, "
+    return {"workload": "per-patch materials over the 126-patch shoebox (5x6x3 m, 1 m patches), 6 bands, "
                         "64 directions, T=2000, order 50", "h": h, "params": int(n_params),
             "max_rel_err_fp64_adjoint": float(np.max(np.abs(a64 - fd) / np.maximum(np.abs(fd), 1e-300))),
             "max_err_over_scale_fp64_adjoint": float(np.abs(a64 - fd).max() / scale),
@@ -854,7 +856,7 @@ def fd_check_cfg1_geometry(n_params, seed=5, h=1e-4):
 
 # ------------------------------------------------------------------- batch
 def batch_rooms(n_rooms, seed=5, rank=0, world=1, compare_rooms=16, fp64_sample=4):
-    """cfg5: seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, T = 1000, order 30,
+    """The batch of seeded shoebox rooms (dims U[3, 20] m, 0.5 m patches, 6 bands, 32 directions, T = 1000, order 30,
     1 source + 4 receivers each), each memory-sized wave's exchange orders in one persistent launch.
 
     Rank r of N takes rooms r, r + N, ...; the job's time is the slowest
@@ -920,14 +922,14 @@ def run_reference(args):
         if k >= args.warmup:
             times.append(ms)
     v = float(np.mean(times))
-    cfg1_ms, cfg1_cores, cfg1_desc, _ = cpu_full_solve_cfg1()
+    s126_ms, s126_cores, s126_desc, _ = cpu_full_solve_shoebox_126()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms/solve", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded street-canyon geometry and materials (no dataset)",
             "config": workload_config(args.config, cfg, world),
             "cpu_baseline": {"value": v, "unit": "ms/solve", "cores": cores, "kind": "port", "sample": desc,
-                             "measured_cfg1": {"ms": cfg1_ms, "cores": cfg1_cores, "sample": cfg1_desc}},
+                             "measured_shoebox_126": {"ms": s126_ms, "cores": s126_cores, "sample": s126_desc}},
             "e2e": {"value": v, "unit": "ms/solve", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

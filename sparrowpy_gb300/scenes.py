@@ -184,20 +184,20 @@ def rotated_room(patch_size=0.5, n_dirs=8, n_bins=2, seed=3, precision="fp32", d
 
 # Workload table: name -> builder kwargs and acoustic setup
 def config(name, precision="fp32"):
-    if name == "cfg1":
+    if name == "shoebox_126":
         r = shoebox(1.0, n_dirs=16, n_bins=1, scattering=1.0, absorption=0.1, precision=precision)
         return dict(radiosity=r, source=np.array([2.0, 2.0, 1.5]), receivers=np.array([[3.0, 4.0, 1.5]]),
                     c=343.0, dt=1e-3, duration=1.0, max_order=20)
-    if name == "cfg2":
+    if name == "shoebox_2016":
         r = shoebox(0.25, n_dirs=64, n_bins=6, scattering=0.3, per_patch=True, alpha_range=(0.02, 0.6), seed=2,
                     precision=precision)
         return dict(radiosity=r, source=np.array([2.0, 2.0, 1.5]), receivers=np.array([[3.0, 4.0, 1.5]]),
                     c=343.0, dt=1e-3, duration=2.0, max_order=50)
-    if name == "cfg3":
+    if name == "street_canyon_5939":
         r = street_canyon(seed=3, precision=precision)
         src, rcv = street_canyon_setup(seed=3)
         return dict(radiosity=r, source=src, receivers=rcv, c=343.0, dt=1e-3, duration=2.0, max_order=50)
-    if name == "canyon_small":
+    if name == "street_canyon_1759":
         # the street canyon at 30 m length, 10 occluders and 2 bands (same
         # directions, patch size and histogram length): a profiling case
         # whose histograms stay near 1 GB each

@@ -97,8 +97,8 @@ def _cube_materials(r, dirs=None):
     return r, setup, (dirs, dirs, 0.5, np.array([0.1, 0.15, 0.2, 0.3]), freqs)
 
 
-def cfg1_scene():
-    c = scenes.config('cfg1')
+def shoebox_126_scene():
+    c = scenes.config('shoebox_126')
     r = c.pop('radiosity')
     dirs = hemisphere_directions(16)
     return r, c, (dirs, dirs, 1.0, np.array([0.1]), np.array([63.0]))
@@ -109,7 +109,7 @@ def rot_scene():
     return r, dict(source=src, receivers=rcv, c=343.0, dt=1e-3, duration=0.15, max_order=4), None
 
 
-SCENES = {'cube': cube_scene, 'cfg1': cfg1_scene, 'rot': rot_scene, 'tri': tri_scene}
+SCENES = {'cube': cube_scene, 'shoebox_126': shoebox_126_scene, 'rot': rot_scene, 'tri': tri_scene}
 
 
 def run_reference(mods, sc, setup, brdf_inputs):

@@ -74,7 +74,7 @@ def test_canyon_two_orders_match_oracle_rows():
     import torch
     from sparrowpy_gb300 import scenes
     from sparrowpy_gb300.coords import Coordinates
-    cfg = scenes.config("cfg3", precision="fp32")
+    cfg = scenes.config("street_canyon_5939", precision="fp32")
     r = cfg["radiosity"]
     c, dt = cfg["c"], cfg["dt"]
     nt = int(cfg["duration"] / dt)

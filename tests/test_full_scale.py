@@ -103,7 +103,7 @@ def test_canyon_fp32_solve_matches_fp64():
     from sparrowpy_gb300.coords import Coordinates
 
     def run(precision):
-        c = scenes.config("cfg3", precision=precision)
+        c = scenes.config("street_canyon_5939", precision=precision)
         r = c["radiosity"]
         r.bake_geometry()
         r.init_source_energy(Coordinates(*c["source"]))

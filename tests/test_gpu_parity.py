@@ -13,7 +13,7 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-SCENES = ["cube", "cfg1", "rot", "tri"]
+SCENES = ["cube", "shoebox_126", "rot", "tri"]
 
 
 def _solve(g, precision, algorithm="auto"):

@@ -10,12 +10,12 @@ from sparrowpy_gb300.coords import Coordinates, FrequencyData
 from oracle.scene import scene_from_radiosity
 
 
-@pytest.mark.parametrize("name", ["cube", "cfg1"])
+@pytest.mark.parametrize("name", ["cube", "shoebox_126"])
 def test_patching_matches_reference(name):
     """geometry.py:290-410 `_process_patches` (golden patches from the reference run)."""
     g = load_golden(name)
     walls = g["walls_points"]
-    size = {"cube": 0.5, "cfg1": 1.0}[name]
+    size = {"cube": 0.5, "shoebox_126": 1.0}[name]
     pp, _, n, p2w = geometry.process_patches(walls, g["walls_normal"], size)
     np.testing.assert_array_equal(pp, g["patches_points"])
     np.testing.assert_array_equal(p2w, g["patch_to_wall_ids"])
@@ -23,7 +23,7 @@ def test_patching_matches_reference(name):
     np.testing.assert_allclose(geometry.calculate_area(pp), g["areas"], rtol=1e-15)
 
 
-@pytest.mark.parametrize("name", ["cube", "cfg1"])
+@pytest.mark.parametrize("name", ["cube", "shoebox_126"])
 def test_create_from_scattering_matches_reference(name):
     """brdf.py:8-130 run by the reference on the same directions."""
     g = load_golden(name)
@@ -39,8 +39,8 @@ def test_create_from_scattering_matches_reference(name):
 
 def test_scene_inputs_reproducible():
     """The host builders regenerate the stored golden inputs."""
-    g = load_golden("cfg1")
-    r = scenes.config("cfg1")["radiosity"]
+    g = load_golden("shoebox_126")
+    r = scenes.config("shoebox_126")["radiosity"]
     sc = scene_from_radiosity(r)
     np.testing.assert_allclose(sc["dirs_in"], g["dirs_in"], atol=1e-14)
     np.testing.assert_allclose(sc["dirs_out"], g["dirs_out"], atol=1e-14)

@@ -11,7 +11,7 @@ import pytest
 from conftest import acoustics, load_golden, rel_l2, scene_from_golden
 from oracle import oracle as orc
 
-SCENES = ["cube", "cfg1", "rot", "tri"]
+SCENES = ["cube", "shoebox_126", "rot", "tri"]
 
 
 @pytest.fixture(scope="module", params=SCENES)

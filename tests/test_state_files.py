@@ -126,7 +126,7 @@ def test_reference_layout_file_solves_like_the_original(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cfg1", "rot"])
+@pytest.mark.parametrize("name", ["shoebox_126", "rot"])
 def test_resume_from_state_file_without_bake(name, tmp_path):
     from sparrowpy_gb300 import DirectionalRadiosityFast
     from sparrowpy_gb300.coords import Coordinates

@@ -28,7 +28,7 @@ def test_static_visibility_matches_workspace_entry_point():
     import torch
     from sparrowpy_gb300 import _native as nat
     stream = torch.cuda.current_stream().cuda_stream
-    for name in ("cfg1", "rot", "cube"):  # different sizes in a row reuse the one scratch array
+    for name in ("shoebox_126", "rot", "cube"):  # different sizes in a row reuse the one scratch array
         g = load_golden(name)
         r = radiosity_from_golden(g, "fp64")
         d = r._geometry()
