@@ -19,8 +19,11 @@ Checked against real files (sparrowpy's SOFA test data): superblocks of
 versions 0 and 2, version-2 object headers, dense link and attribute
 storage, chunked data under version-1 B-trees with shuffle and deflate,
 fixed-length string attributes.  Version-1 object headers, symbol-table
-groups, variable-length strings, compact layouts and the version-4 chunk
-indexes follow the specification with no such file at hand to check them.
+groups, variable-length strings, compact layouts and multi-chunk data with
+padded edge chunks are checked against files that a small writer of the
+same specification produces (the test suite's hdf5_earliest.py), not
+against files of the HDF5 library; the version-4 chunk indexes (single
+chunk, implicit, fixed array) follow the specification unchecked.
 
 Only what the radiosity path needs is exposed: ``File(path)`` with
 ``datasets()`` (name -> numpy array, read on demand) and ``attrs`` of the
