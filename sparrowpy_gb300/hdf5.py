@@ -22,8 +22,8 @@ fixed-length string attributes.  Version-1 object headers, symbol-table
 groups, variable-length strings, compact layouts and multi-chunk data with
 padded edge chunks are checked against files that a small writer of the
 same specification produces (the test suite's hdf5_earliest.py), not
-against files of the HDF5 library; the version-4 chunk indexes (single
-chunk, implicit, fixed array) follow the specification unchecked.
+against files of the HDF5 library; so are the version-4 chunk indexes
+(single chunk, implicit, fixed array).
 
 Only what the radiosity path needs is exposed: ``File(path)`` with
 ``datasets()`` (name -> numpy array, read on demand) and ``attrs`` of the

@@ -9,7 +9,9 @@ layout, following the published file format specification, so that
 tests/test_hdf5_layouts.py can read it back with sparrowpy_gb300.hdf5:
 
 * datasets: contiguous, compact, or chunked (version-1 B-tree of chunks,
-  optional shuffle + deflate, edge chunks padded as HDF5 stores them);
+  optional shuffle + deflate, edge chunks padded as HDF5 stores them), and
+  chunked with a version-4 layout message (single-chunk, implicit or
+  fixed-array index);
 * types: little-endian float64, int32, fixed-length strings and
   variable-length strings (global heap);
 * attributes on the root group and on datasets.
@@ -89,6 +91,9 @@ class Writer:
         a = a.astype("<f8" if kind == "f8" else "<i4")
         msgs = [(0x01, _space_msg(a.shape)), (0x03, _dtype_msg(kind))]
         esz = a.dtype.itemsize
+        if layout.startswith("v4-"):
+            return self._header(msgs + self._v4_layout(a, layout[3:], chunks, filters, esz) +
+                                [self._attr_msg(k, v) for k, v in (attrs or {}).items()])
         if layout == "compact":
             raw = a.tobytes()
             msgs.append((0x08, struct.pack("<BBH", 3, 0, len(raw)) + raw))
@@ -124,6 +129,50 @@ class Writer:
         for name, value in (attrs or {}).items():
             msgs.append(self._attr_msg(name, value))
         return self._header(msgs)
+
+    def _v4_layout(self, a, index, chunks, filters, esz):
+        """Layout message version 4 with a single-chunk, implicit or fixed-array chunk index (checksums are
+        written as zeros: the reader does not check them)."""
+        chunks = tuple(a.shape) if index == "single" else tuple(chunks)
+        grid = [-(-a.shape[i] // chunks[i]) for i in range(a.ndim)]
+        stored = []
+        for idx in np.ndindex(*grid):
+            block = np.zeros(chunks, dtype=a.dtype)
+            src = tuple(slice(i * c, min((i + 1) * c, s)) for i, c, s in zip(idx, chunks, a.shape))
+            block[tuple(slice(0, sl.stop - sl.start) for sl in src)] = a[src]
+            raw = block.tobytes()
+            if filters:
+                raw = zlib.compress(np.frombuffer(raw, np.uint8).reshape(-1, esz).T.tobytes())
+            stored.append(raw)
+        dims = b"".join(struct.pack("<I", c) for c in chunks + (esz,))
+        flags = 0x02 if (filters and index == "single") else 0
+        head = struct.pack("<BBBBB", 4, 2, flags, a.ndim + 1, 4) + dims
+        msgs = []
+        if index == "single":
+            addr = self._alloc(stored[0])
+            info = (struct.pack("<QI", len(stored[0]), 0) if filters else b"") + struct.pack("<Q", addr)
+            msgs.append((0x08, head + bytes([1]) + info))
+        elif index == "implicit":
+            assert not filters
+            addr = self._alloc(b"".join(stored))
+            msgs.append((0x08, head + bytes([2]) + struct.pack("<Q", addr)))
+        else:  # fixed array: client 1 (filtered) holds address, 4-byte size and mask; client 0 the address
+            addrs = [self._alloc(raw) for raw in stored]
+            client, esize = (1, 16) if filters else (0, 8)
+            hdr_addr = len(self.buf)
+            dblock_addr = hdr_addr + 32
+            hdr = b"FAHD" + struct.pack("<BBBBQQ", 0, client, esize, 10, len(stored), dblock_addr) + b"\x00" * 4
+            self._alloc(hdr)
+            assert len(self.buf) == dblock_addr
+            elems = b"".join(struct.pack("<QII", ad, len(raw), 0) if filters else struct.pack("<Q", ad)
+                             for ad, raw in zip(addrs, stored))
+            self._alloc(b"FADB" + struct.pack("<BBQ", 0, client, hdr_addr) + elems + b"\x00" * 4)
+            msgs.append((0x08, head + bytes([3, 10]) + struct.pack("<Q", hdr_addr)))
+        if filters:
+            shuffle = struct.pack("<HHHH", 2, 0, 0, 1) + struct.pack("<I", esz) + b"\x00" * 4
+            deflate = struct.pack("<HHHH", 1, 0, 0, 1) + struct.pack("<I", 6) + b"\x00" * 4
+            msgs.append((0x0B, struct.pack("<BB6x", 1, 2) + shuffle + deflate))
+        return msgs
 
     def finish(self, path, links, root_attrs=None):
         """Write the root group (symbol table of `links`: name -> header address) and the file."""

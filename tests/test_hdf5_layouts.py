@@ -94,3 +94,22 @@ def test_malformed_file_raises(tmp_path):
     bad.write_bytes(b"not hdf5")
     with pytest.raises(ValueError):
         hdf5.File(bad)
+
+
+def test_version4_chunk_indexes(tmp_path):
+    """Layout messages of version 4 (files of newer HDF5 releases): single-chunk (plain and filtered),
+    implicit and fixed-array (plain and filtered) chunk indexes."""
+    rng = np.random.default_rng(7)
+    a = rng.normal(size=(5, 7))
+    w = Writer()
+    links = {"single": w.dataset(a, "v4-single"), "single_z": w.dataset(a, "v4-single", filters=True),
+             "implicit": w.dataset(a, "v4-implicit", chunks=(2, 3)),
+             "fixed": w.dataset(a, "v4-fixed", chunks=(2, 3)),
+             "fixed_z": w.dataset(a, "v4-fixed", chunks=(2, 3), filters=True),
+             "ints": w.dataset(np.arange(35, dtype=np.int32).reshape(5, 7), "v4-fixed", chunks=(3, 4))}
+    path = tmp_path / "v4.h5"
+    w.finish(path, links)
+    ds = hdf5.File(path).datasets()
+    for name in ("single", "single_z", "implicit", "fixed", "fixed_z"):
+        npt.assert_array_equal(ds[name].read(), a, err_msg=name)
+    npt.assert_array_equal(ds["ints"].read(), np.arange(35).reshape(5, 7))
