@@ -137,10 +137,17 @@ class Coordinates:
         return Coordinates.from_cartesian(self._pts - _cart(other))
 
     def find_nearest(self, points):
-        """Index of the nearest point (Euclidean) for every query point."""
+        """Index of the nearest point (Euclidean) for every query point, and its distance.
+
+        As pyfar's find_nearest, a k-d tree (scipy's cKDTree) answers the
+        query, so that exact ties resolve the same way.
+        """
+        from scipy.spatial import cKDTree
         q = _cart(points).reshape(-1, 3)
-        d = np.sum((self._pts.reshape(-1, 3)[None, :, :] - q[:, None, :]) ** 2, axis=-1)
-        return (np.argmin(d, axis=1),), np.sqrt(np.min(d, axis=1))
+        if q.shape[0] == 0 or self.csize == 0:
+            return (np.zeros(q.shape[0], dtype=int),), np.full(q.shape[0], np.inf)
+        dist, idx = cKDTree(self._pts.reshape(-1, 3)).query(q)
+        return (np.asarray(idx, dtype=int),), np.asarray(dist)
 
 
 def sph2cart(azimuth, colatitude, radius):

@@ -69,8 +69,8 @@ class DirectivityMS:
     def get_directivity(self, source_pos, source_view, source_up, target_position, i_freq):
         """Directivity value of the sampled direction nearest to the target (sound_object.py:42-73)."""
         az, el = _get_metrics(source_pos, source_view, source_up, target_position)
-        find = Coordinates.from_spherical_colatitude(np.atleast_1d(az) / 180 * np.pi,
-                                                     np.pi / 2 - np.atleast_1d(el) / 180 * np.pi, 1)
+        find = Coordinates.from_spherical_elevation(np.atleast_1d(az) / 180 * np.pi,
+                                                    np.atleast_1d(el) / 180 * np.pi, 1)
         index, _ = self.receivers.find_nearest(find)
         return np.asarray(self.data.freq)[index[0], i_freq]
 
