@@ -329,8 +329,17 @@ def _write_state(obj, filename, compress):
     far.write(filename, flat, compress=compress)
 
 
+def _none(x):
+    return None if isinstance(x, str) and x == 'None' else x
+
+
 def _read_state(filename, keys):
     v = far.read(filename)
+    if 'patches' in v and 'n_patch_walls' not in v:
+        # the reference's layout: pyfar.io.write(**to_dict()), the walls as a list of dicts
+        d = {k: _none(x) for k, x in v.items() if k != 'patches'}
+        d['patches'] = [{k: _none(x) for k, x in p.items()} for p in v['patches']]
+        return d
     patches = []
     for i in range(int(v['n_patch_walls'])):
         p = {k: v.get(f'patch{i}_{k}') for k in keys}

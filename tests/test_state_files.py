@@ -150,3 +150,34 @@ def test_resume_from_state_file_without_bake(name, tmp_path):
     r3.calculate_energy_exchange(c, dt, duration, k, recalculate=True)  # no bake_geometry()
     np.testing.assert_array_equal(r3.collect_energy_receiver_mono(receivers).time, mono)
     np.testing.assert_array_equal(r3._visibility_matrix, g["V"])
+
+
+def test_kang_objects_read_from_the_reference_layout(tmp_path):
+    """RadiosityKang / DirectionalRadiosityKang.from_read on a file in the reference's layout
+    (pyfar.io.write(**to_dict()): the walls as a list of dicts), written by the restated encoder; walls not
+    yet run (no energy matrices), so no device work."""
+    from sparrowpy_gb300.coords import Coordinates, FrequencyData
+    from sparrowpy_gb300.geometry import shoebox_room_stub
+    from sparrowpy_gb300.kang import DirectionalRadiosityKang, PatchesDirectionalKang, RadiosityKang
+    walls = shoebox_room_stub(2, 1.5, 1)
+    radi = RadiosityKang(walls, 0.5, 2, 0.1, speed_of_sound=343.0, sampling_rate=1000)
+    d = radi.to_dict()
+    path = tmp_path / "kang.far"
+    _pyfar_style_write(path, d)
+    back = RadiosityKang.from_read(path)
+    assert (back.patch_size, back.max_order_k, back.ir_length_s) == (0.5, 2, 0.1)
+    for a, b in zip(radi.patch_list, back.patch_list, strict=True):
+        np.testing.assert_array_equal(a.pts, b.pts)
+        assert a.wall_id == b.wall_id and b.E_matrix is None
+        np.testing.assert_array_equal(a.other_wall_ids, b.other_wall_ids)
+    g = np.linspace(0.1, 1.0, 6)
+    dirs = Coordinates.from_cartesian(np.stack([np.sin(g), np.zeros(6), np.cos(g)], 1), weights=np.full(6, 1 / 6))
+    data = FrequencyData(np.random.default_rng(1).uniform(0, 1, (6, 6, 2)), [500.0, 1000.0])
+    dwalls = [PatchesDirectionalKang(w, 0.5, [j for j in range(6) if j != i], i, data, dirs, dirs)
+              for i, w in enumerate(walls)]
+    drad = DirectionalRadiosityKang(dwalls, 0.5, 2, 0.1, None, speed_of_sound=343.0)
+    _pyfar_style_write(tmp_path / "dkang.far", drad.to_dict())
+    dback = DirectionalRadiosityKang.from_read(tmp_path / "dkang.far")
+    for a, b in zip(drad.patch_list, dback.patch_list, strict=True):
+        np.testing.assert_array_equal(a.directivity_data.freq, b.directivity_data.freq)
+        assert a.directivity_sources == b.directivity_sources
