@@ -16,11 +16,7 @@ import numpy as np
 import torch
 
 from .. import _native as nat
-from ._dev import dev as _dev_any, ptr as _ptr, stream as _stream
-
-
-def _dev(a, dtype):
-    return _dev_any(a, dtype)
+from ._dev import dev as _dev, ptr as _ptr, stream as _stream
 
 
 def patch2patch_ff_universal(patches_points, patches_normals, patches_areas, visible_patches):
